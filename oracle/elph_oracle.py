@@ -1,0 +1,430 @@
+"""CPU restatement of LetzElPhC's per-q electron-phonon matrix-element path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA path is
+compared against (tests/, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py``).  Nothing in the product imports it.
+
+It restates, in numpy FP64, the reference's G-space algorithm for one q-point
+(``compute_and_write_elphq``, src/elph/compute_elph_matq.c:20-234):
+
+* ``elph_local``        src/dvloc/compute_Vbare_loc.c:17-353
+* ``add_elph_nonlocal`` src/nonloc/Vbare_nloc.c:35-577 (+ sum_VNL_KKp.c:8-58)
+* ``elph_q_rotate``     src/symmetries/elphq_expand.c:16-73
+
+FFTW is replaced by numpy's pocketfft: the reference's FFT is a pruned,
+slab-distributed 3-D complex DFT (src/fft/*.c); pruning changes nothing but
+rounding, so the full 3-D transform is used here.  Constants follow
+src/common/constants.h (truncated pi = 3.1415927).
+
+Parity of this restatement is pinned against the reference itself: the
+reference's own hot-path C sources are compiled unmodified against small
+single-rank MPI / FFTW / CBLAS / netCDF shims (oracle/Makefile) and the two
+are compared on the golden systems of tests/golden/ (tests/test_oracle_vs_ref.py).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+ELPH_PI = 3.1415927
+ELPH_EPS = 1e-5
+ELPH_EPS6 = 1e-6
+ELPH_E2 = 2.0
+
+
+# ---------------------------------------------------------------- 3x3 helpers
+
+def mat_vec3(M, v, trans=False):
+    """MatVec3f, src/common/numerical_func.c:226-241 (explicit left-to-right sums)."""
+    M = np.asarray(M, float).reshape(9)
+    if trans:
+        return np.array([M[0] * v[0] + M[3] * v[1] + M[6] * v[2],
+                         M[1] * v[0] + M[4] * v[1] + M[7] * v[2],
+                         M[2] * v[0] + M[5] * v[1] + M[8] * v[2]])
+    return np.array([M[0] * v[0] + M[1] * v[1] + M[2] * v[2],
+                     M[3] * v[0] + M[4] * v[1] + M[5] * v[2],
+                     M[6] * v[0] + M[7] * v[1] + M[8] * v[2]])
+
+
+def det3x3(m):
+    m = np.asarray(m, float).reshape(9)
+    return (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6])
+            + m[2] * (m[7] * m[3] - m[4] * m[6]))
+
+
+def find_kidx_in_list(klist, kpt):
+    """src/common/numerical_func.c:471-497."""
+    d = klist - kpt[None, :]
+    d = d - np.rint(d)
+    s = np.sqrt((d * d).sum(axis=1))
+    hit = np.nonzero(s < ELPH_EPS)[0]
+    return int(hit[0]) if len(hit) else -1
+
+
+def get_kplusq_idxs(kpts_crys, q):
+    """src/common/numerical_func.c:500-524."""
+    out = np.empty(len(kpts_crys), np.int64)
+    for i, k in enumerate(kpts_crys):
+        out[i] = find_kidx_in_list(kpts_crys, k + q)
+        if out[i] < 0:
+            raise ValueError("K+Q point cannot be found in kgrid")
+    return out
+
+
+# ------------------------------------------------------------ wfc symmetry ops
+
+def rotate_gvecs(G, S, alat, G0=None):
+    """rotateGvecs(inverse=False, crystal=True), src/wfc/rotate_Gvecs.c:15-81:
+    G_crys = (alat^T S) G, plus the crystal coordinates of G0."""
+    sym_temp = alat.T @ S
+    out = G @ sym_temp.T
+    if G0 is not None:
+        out = out + mat_vec3(alat, G0, True)[None, :]
+    return out
+
+
+def sort_pw(gfloat, sets):
+    """Sort_pw + Sorted_gvecs_idxs, src/wfc/sortpw.c:95-315, src/wfc/gsort.c:16-128:
+    rint the crystal coordinates and order by x, then y, then z."""
+    gi = np.rint(gfloat).astype(np.int64)
+    order = np.lexsort((gi[:, 2], gi[:, 1], gi[:, 0]))
+    return gi[order], sets[..., order]
+
+
+def su2mat(sym, nspinor, invert, time_rev):
+    """SU2mat, src/wfc/su2mat.c:16-117 (Euler angles, -i sigma_y for time reversal)."""
+    if nspinor == 1:
+        return np.array([1.0 + 0j, 0, 0, 1])
+    det = det3x3(sym)
+    s = np.asarray(sym, float).reshape(9) / det
+    if abs(s[6] + 1) < ELPH_EPS:
+        alpha, beta, delta = 0.0, ELPH_PI / 2.0, math.atan2(s[1], s[2])
+    elif abs(s[6] - 1) < ELPH_EPS:
+        alpha, beta, delta = 0.0, -ELPH_PI / 2.0, math.atan2(-s[1], -s[2])
+    else:
+        beta = -math.asin(s[6])
+        alpha = math.atan2(s[3] / math.cos(beta), s[0] / math.cos(beta))
+        delta = math.atan2(s[7] / math.cos(beta), s[8] / math.cos(beta))
+    alpha, beta, delta = alpha / 2, beta / 2, delta / 2
+    p0 = np.array([1, 0, 0, 1], complex)
+    px = np.array([0, 1, 1, 0], complex)
+    py = np.array([0, -1j, 1j, 0], complex)
+    pz = np.array([1, 0, 0, -1], complex)
+    sd = math.cos(delta) * p0 - 1j * math.sin(delta) * px
+    sb = math.cos(beta) * p0 - 1j * math.sin(beta) * py
+    sa = math.cos(alpha) * p0 - 1j * math.sin(alpha) * pz
+
+    def mm(a, b):
+        return np.array([a[0] * b[0] + a[1] * b[2], a[0] * b[1] + a[1] * b[3],
+                         a[2] * b[0] + a[3] * b[2], a[2] * b[1] + a[3] * b[3]])
+    u = mm(sa, mm(sb, sd))
+    if time_rev:
+        a1, b1, c1, d1 = u
+        u = np.array([-c1, -d1, a1, b1])
+    if invert:
+        u = np.array([np.conj(u[0]), np.conj(u[2]), np.conj(u[1]), np.conj(u[3])])
+    return u
+
+
+def su2rotate(su2, wfc):
+    """src/wfc/su2rotate.c:13-41; wfc (..., nspinor, npw)."""
+    if wfc.shape[-2] != 2:
+        return wfc
+    up = wfc[..., 0, :]
+    dw = wfc[..., 1, :]
+    out = np.empty_like(wfc)
+    out[..., 0, :] = up * su2[0] + dw * su2[1]
+    out[..., 1, :] = up * su2[2] + dw * su2[3]
+    return out
+
+
+def apply_trans_wfc(tau, kvec, gvecs, wfc, conjugate=False):
+    """src/wfc/trans_wfc.c:15-52: c(G) e^{-i 2pi k.tau} e^{-i 2pi G.tau}."""
+    kphase = np.exp(-1j * 2 * ELPH_PI * float(kvec[0] * tau[0] + kvec[1] * tau[1] + kvec[2] * tau[2]))
+    gdot = gvecs[:, 0] * tau[0] + gvecs[:, 1] * tau[1] + gvecs[:, 2] * tau[2]
+    ph = kphase * np.exp(-1j * 2 * ELPH_PI * gdot)
+    out = wfc * ph
+    return np.conj(out) if conjugate else out
+
+
+# ------------------------------------------------------------------ FFTs
+
+def box_index(gint, fft_dims):
+    Nx, Ny, Nz = fft_dims
+    return ((gint[:, 0] % Nx) * Ny + (gint[:, 1] % Ny)) * Nz + (gint[:, 2] % Nz)
+
+
+def invfft3d(gint, wfcG, fft_dims, conjugate):
+    """invfft3D, src/fft/bwdfft.c:13-120: sphere -> box (conj if asked), then
+    the unnormalised backward DFT.  wfcG (nsets, npw) -> (nsets, Nx, Ny, Nz)."""
+    Nx, Ny, Nz = fft_dims
+    N = Nx * Ny * Nz
+    box = np.zeros((wfcG.shape[0], N), complex)
+    box[:, box_index(gint, fft_dims)] = np.conj(wfcG) if conjugate else wfcG
+    box = box.reshape(-1, Nx, Ny, Nz)
+    return np.fft.ifftn(box, axes=(1, 2, 3)) * N
+
+
+def fft_convolution3d(gint, nspinor, nmag, Vr, psir, fft_dims):
+    """fft_convolution3D, src/fft/convolution.c:13-189: FFT[dV psi] * 1/N on the
+    sphere.  Vr (nmag_avail, Nx, Ny, Nz), psir (nbnd, nspinor, Nx, Ny, Nz)
+    -> (nbnd, nspinor, npw)."""
+    if nspinor == 1:
+        nmag = 1
+    Nx, Ny, Nz = fft_dims
+    N = Nx * Ny * Nz
+    idx = box_index(gint, fft_dims)
+    out = np.empty((psir.shape[0], nspinor, len(gint)), complex)
+    for isp in range(nspinor):
+        if nmag == 1:
+            prod = psir[:, isp] * Vr[0][None]
+        else:
+            d0 = Vr[2 * isp]
+            d1 = Vr[2 * isp + 1]
+            prod = psir[:, 0] * d0[None] + psir[:, 1] * d1[None]
+        f = np.fft.fftn(prod, axes=(1, 2, 3)).reshape(prod.shape[0], N)
+        out[:, isp] = f[:, idx] * (1.0 / N)
+    return out
+
+
+# -------------------------------------------------------------- local part
+
+def elph_local(qpt, s, ikq, ik, kqsym, ksym, dVlocr):
+    """elphLocal, src/dvloc/compute_Vbare_loc.c:17-353.
+    dVlocr (nmodes, nmag, Nx, Ny, Nz) -> g (nmodes, nspin, nb_k, nb_kq)."""
+    nspin, nb, nspinor, nmag = s.nspin, s.nbnds, s.nspinor, s.nmag
+    lat = s.alat
+    blat = s.blat
+    wfc_kq, Gkq = s.wfc[ikq], s.gvec[ikq]
+    wfc_k, Gk = s.wfc[ik], s.gvec[ik]
+    kqvec, kvec = s.kibz[ikq], s.kibz[ik]
+    symkq, symk = s.sym_R[kqsym], s.sym_R[ksym]
+    taukq, tauk = s.sym_tau[kqsym], s.sym_tau[ksym]
+    trkq, trk = bool(s.sym_trev[kqsym]), bool(s.sym_trev[ksym])
+
+    tempSkq = mat_vec3(symkq, kqvec)                       # :103
+    tempSk = mat_vec3(symk, kvec)                          # :104
+    kvecSk = mat_vec3(lat, tempSk, True)                   # :106
+    kvecSkq = kvecSk + np.asarray(qpt, float)              # :108-111
+    tempSkq = tempSkq - tempSk                             # :114-117
+    qcart = mat_vec3(blat, qpt) / (2 * ELPH_PI)            # :120-125
+    taukq_crys = mat_vec3(blat, taukq, True) / (2 * ELPH_PI)
+    tauk_crys = mat_vec3(blat, tauk, True) / (2 * ELPH_PI)
+    ulm = tempSkq - qcart                                  # :141-144
+
+    gSkq = rotate_gvecs(Gkq, symkq, lat, ulm)              # :146
+    gSk = rotate_gvecs(Gk, symk, lat, None)                # :147
+    su2kq = su2mat(symkq, nspinor, False, trkq)
+    su2k = su2mat(symk, nspinor, False, trk)
+
+    gkq_i, wkq = sort_pw(gSkq, wfc_kq)                     # :170-176
+    gk_i, wk = sort_pw(gSk, wfc_k)
+
+    # k+q: su2 + fractional translation (:197-205)
+    wkq = su2rotate(su2kq, wkq)
+    wkq = apply_trans_wfc(taukq_crys, kvecSkq, gkq_i.astype(float), wkq)
+    # k: su2 + translation + (conj) inverse FFT (:223-241)
+    wk = su2rotate(su2k, wk)
+    wk = apply_trans_wfc(tauk_crys, kvecSk, gk_i.astype(float), wk)
+    Nx, Ny, Nz = s.fft_dims
+    psir = invfft3d(gk_i, wk.reshape(-1, len(gk_i)), s.fft_dims, trk)
+    psir = psir.reshape(nspin, nb, nspinor, Nx, Ny, Nz)
+
+    if nmag == 2 and (nspin != 2 or nspinor != 1):
+        raise ValueError("Incompatible dvscf")
+    out = np.zeros((s.nmodes, nspin, nb, nb), complex)
+    for iv in range(s.nmodes):
+        for isp in range(nspin):
+            Vr = dVlocr[iv, isp:] if nmag == 2 else dVlocr[iv]
+            dvpsi = fft_convolution3d(gkq_i, nspinor, nmag, Vr, psir[isp], s.fft_dims)
+            A = dvpsi.reshape(nb, -1)
+            B = wkq[isp].reshape(nb, -1)
+            out[iv, isp] = A @ (B.T if trkq else np.conj(B).T)   # 'T' / 'C' (:312-326)
+    return out
+
+
+# ----------------------------------------------------------- nonlocal part
+
+def _factorial(n):
+    return math.gamma(n + 1)
+
+
+def legendre(l, m, x):
+    """Associated Legendre without Condon-Shortley, src/common/numerical_func.c:29-94."""
+    if l == 0 and m == 0:
+        return 1.0
+    if l < 0:
+        return legendre(-l - 1, m, x)
+    if abs(m) > l:
+        return 0.0
+    if m < 0:
+        return legendre(l, -m, x) * (-1.0) ** (-m) * _factorial(l + m) / _factorial(l - m)
+    val = 1.0
+    sq = math.sqrt(1 - x * x)
+    for im in range(1, m + 1):
+        val *= (2 * im - 1) * sq
+    if l == m:
+        return val
+    vmm = val
+    val *= (2 * m + 1) * x
+    if l == m + 1:
+        return val
+    for im in range(m + 2, l + 1):
+        tmp = val
+        val = (2 * im - 1) * x * val - (im + m - 1) * vmm
+        val = val / (im - m)
+        vmm = tmp
+    return val
+
+
+def ylm(l, m, v):
+    """Real spherical harmonics (Blanco et al.), src/common/numerical_func.c:97-152."""
+    if l < 0:
+        return 0.0
+    norm = math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    if norm < ELPH_EPS6:
+        return 0.0 if l != 0 else 1.0 / math.sqrt(4 * ELPH_PI)
+    cost = v[2] / norm
+    phi = math.atan2(v[1], v[0])
+    if m > 0:
+        sh = math.sqrt(2) * math.cos(m * phi)
+    elif m < 0:
+        m = -m
+        sh = math.sqrt(2) * math.sin(m * phi)
+    else:
+        sh = 1.0
+    sh *= legendre(l, m, cost)
+    sh *= math.sqrt(_factorial(l - m) * (2 * l + 1) / (4 * ELPH_PI * _factorial(l + m)))
+    return sh
+
+
+def ylm_vec(l, m, V):
+    return np.array([ylm(l, m, v) for v in V])
+
+
+def sum_vnl_kkp(K, Kp, f, nspin, nb, nspinor, out):
+    """sum_VNL_KKp, src/nonloc/sum_VNL_KKp.c:8-58.
+    K, Kp (4, nspin, nb, nspinor); out (3, nspin, nb_k, nb_kq)."""
+    for ix in range(3):
+        for s1 in range(nspinor):
+            for s2 in range(nspinor):
+                fc = f[nspinor * s1 + s2]
+                # out[ix, is, ib1 (k), ib2 (kq)] += f (K[ix+1][ib2,s1] Kp[0][ib1,s2] + K[0][ib2,s1] Kp[ix+1][ib1,s2])
+                out[ix] += fc * (Kp[0, :, :, s2][:, :, None] * K[ix + 1, :, :, s1][:, None, :]
+                                 + Kp[ix + 1, :, :, s2][:, :, None] * K[0, :, :, s1][:, None, :])
+
+
+def add_elph_nonlocal(s, ikq, ik, kqsym, ksym, eigVec, elph):
+    """add_elphNonLocal, src/nonloc/Vbare_nloc.c:35-577.  Adds into elph
+    (nmodes, nspin, nb_k, nb_kq)."""
+    nspin, nb, nspinor = s.nspin, s.nbnds, s.nspinor
+    ntype, natom = s.ntype, s.natom
+    lmax = s.lmax
+    PP = s.PP_table
+    wK = s.wfc[ikq].copy()
+    wKp = s.wfc[ik].copy()
+    SK, SKp = s.sym_R[kqsym], s.sym_R[ksym]
+    tauK, tauKp = s.sym_tau[kqsym], s.sym_tau[ksym]
+    trK, trKp = bool(s.sym_trev[kqsym]), bool(s.sym_trev[ksym])
+    # rotate k+G (:148-168)
+    GK = (s.gvec[ikq] + s.kibz[ikq][None, :]) @ SK.T
+    GKp = (s.gvec[ik] + s.kibz[ik][None, :]) @ SKp.T
+    YK = {(l, m): ylm_vec(l, m, GK) for l in range(lmax + 1) for m in range(-l, l + 1)}
+    YKp = {(l, m): ylm_vec(l, m, GKp) for l in range(lmax + 1) for m in range(-l, l + 1)}
+    su2K = su2mat(SK, nspinor, False, trK)
+    su2Kp = su2mat(SKp, nspinor, False, trKp)
+    zero = np.zeros(3)
+    wK = apply_trans_wfc(tauK, zero, GK, su2rotate(su2K, wK))       # :227-235
+    wKp = apply_trans_wfc(tauKp, zero, GKp, su2rotate(su2Kp, wKp))  # :237-245
+    FK, FKp = s.Fk[ikq], s.Fk[ik]
+    nsets = nspin * nb * nspinor
+    BK = wK.reshape(nsets, -1)
+    BKp = wKp.reshape(nsets, -1)
+    buf = np.zeros((natom, 3, nspin, nb, nb), complex)
+    for ia in range(natom):
+        it = s.atom_type[ia]
+        tau = s.atom_pos[ia]
+        betaK, betaKp, channels = [], [], []
+        for lidx in range(s.nltimesj):
+            l = int(np.rint(PP[lidx, it, 0] - 1))
+            if l < 0:
+                continue
+            sign = s.Fsign[lidx, it]
+            dotK = GK[:, 0] * tau[0] + GK[:, 1] * tau[1] + GK[:, 2] * tau[2]
+            dotKp = GKp[:, 0] * tau[0] + GKp[:, 1] * tau[1] + GKp[:, 2] * tau[2]
+            for im in range(2 * l + 1):
+                b0 = FK[lidx, it] * np.exp(-1j * 2 * ELPH_PI * dotK) * YK[(l, im - l)]
+                betaK.append(np.stack([b0, b0 * GK[:, 0] * sign, b0 * GK[:, 1] * sign, b0 * GK[:, 2] * sign]))
+            for im in range(2 * l + 1):
+                b0 = FKp[lidx, it] * np.exp(1j * 2 * ELPH_PI * dotKp) * YKp[(l, im - l)]
+                betaKp.append(np.stack([b0, -b0 * GKp[:, 0] * sign, -b0 * GKp[:, 1] * sign, -b0 * GKp[:, 2] * sign]))
+            channels.append((lidx, l))
+        betaK = np.array(betaK)      # (nproj, 4, npwK)
+        betaKp = np.array(betaKp)
+        bandK = betaK @ (BK.T if trK else np.conj(BK).T)       # :412-414 ('C' or 'T')
+        bandKp = betaKp @ (np.conj(BKp).T if trKp else BKp.T)  # :416-418 ('T' or 'C')
+        bandK = bandK.reshape(-1, 4, nspin, nb, nspinor)
+        bandKp = bandKp.reshape(-1, 4, nspin, nb, nspinor)
+        ilc = 0
+        for (lidx, l) in channels:
+            j = int(np.rint(PP[lidx, it, 1]))
+            soc_fac = 1.0
+            if j != 0 and not s.is_soc_present:
+                soc_fac = (j + 1.0) / (4.0 * l + 2.0)
+            fc = None
+            if s.fCoeff is not None:
+                fc = s.fCoeff[s.ntype * lidx + it]
+            for im1 in range(2 * l + 1):
+                for im2 in range(2 * l + 1):
+                    if fc is None and im1 != im2:
+                        continue
+                    if fc is None:
+                        f = np.array([soc_fac, 0, 0, soc_fac], complex)
+                    else:
+                        f = fc[im1, im2].reshape(-1)
+                    sum_vnl_kkp(bandK[ilc + im1], bandKp[ilc + im2], f, nspin, nb, nspinor, buf[ia])
+            ilc += 2 * l + 1
+    pre = -2 * ELPH_PI * 1j * ELPH_E2
+    elph += pre * np.einsum("vj,jsmn->vsmn", eigVec.reshape(s.nmodes, natom * 3),
+                            buf.reshape(natom * 3, nspin, nb, nb))
+    return elph
+
+
+# -------------------------------------------------------------- q stage
+
+def compute_elphq(s, iq, eigVec=None, dVscfq=None, non_loc=True, kminusq=False, k_list=None):
+    """compute_and_write_elphq for one iBZ q, src/elph/compute_elph_matq.c:20-234.
+    Returns g (nk, nmodes, nspin, nb, nb) for the full-BZ k indices of
+    ``k_list`` (all of them by default)."""
+    qpt = np.asarray(s.qpts[iq], float)
+    eigVec = s.eigVec[iq] if eigVec is None else eigVec
+    dVscfq = s.dVscf[iq] if dVscfq is None else dVscfq
+    qt = -qpt if kminusq else qpt
+    kpq = get_kplusq_idxs(s.kbz_crys, qt)
+    ks = range(s.nk_bz) if k_list is None else k_list
+    out = np.zeros((len(ks), s.nmodes, s.nspin, s.nbnds, s.nbnds), complex)
+    for ii, i in enumerate(ks):
+        idx_k, idx_kq = i, int(kpq[i])
+        if kminusq:
+            idx_k, idx_kq = idx_kq, idx_k
+        ik, ksym = s.kmap[idx_k]
+        ikq, kqsym = s.kmap[idx_kq]
+        g = elph_local(qpt, s, ikq, ik, kqsym, ksym, dVscfq)
+        if non_loc:
+            add_elph_nonlocal(s, ikq, ik, kqsym, ksym, eigVec, g)
+        out[ii] = g
+    return out
+
+
+def elph_q_rotate(Dl, g, Dr, tim_rev):
+    """elph_q_rotate, src/symmetries/elphq_expand.c:16-73.
+    g (nmodes, nspin, nb, nb); D (nspin, nb, nb)."""
+    out = np.empty_like(g)
+    for isp in range(g.shape[1]):
+        for iv in range(g.shape[0]):
+            gq = g[iv, isp]
+            A = np.conj(gq).T if tim_rev else gq.T
+            tmp = A @ np.conj(Dr[isp]).T
+            out[iv, isp] = tmp.T @ Dl[isp].T
+    return out

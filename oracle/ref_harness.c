@@ -1,0 +1,272 @@
+/* Oracle harness around the reference's own per-q stage.
+ *
+ * Loads a synthetic system written by letzelphc_gb300/synth.py:write_system,
+ * fills the reference's boundary structs (struct WFC / Lattice / Pseudo /
+ * Phonon / ELPH_MPI_Comms, src/common/dtypes.h) and calls the UNMODIFIED
+ * compute_and_write_elphq (src/elph/compute_elph_matq.c:20) once per q, the
+ * way elph_driver does (src/elph/elph_driver.c:303-306), with every q its own
+ * star.  The netCDF writes of elph_mat are captured in memory and written out
+ * as complex128 (nq, nk_BZ, nmodes, nspin, nb, nb).
+ *
+ * usage: lelph_ref <system.bin> <g_out.bin> [rotate <D_in.bin> <g_rot_out.bin>]
+ *
+ * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
+#include <complex.h>
+#include <stdbool.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "common/ELPH_timers.h"
+#include "common/dtypes.h"
+#include "elph/elph.h"
+#include "netcdf.h"
+#include "symmetries/symmetries.h"
+
+struct rec
+{
+    char name[32];
+    int code;
+    unsigned ndim;
+    long long dims[8];
+    void* data;
+    size_t nbytes;
+};
+
+static struct rec recs[4096];
+static int nrec = 0;
+
+static void die(const char* m)
+{
+    fprintf(stderr, "lelph_ref: %s\n", m);
+    exit(2);
+}
+
+static void load(const char* path)
+{
+    FILE* f = fopen(path, "rb");
+    if (!f) die("cannot open system file");
+    char magic[8];
+    if (fread(magic, 1, 8, f) != 8 || memcmp(magic, "LELPHSYS", 8)) die("bad magic");
+    for (;;)
+    {
+        struct rec r;
+        memset(&r, 0, sizeof(r));
+        if (fread(r.name, 1, 32, f) != 32) die("truncated");
+        if (!strcmp(r.name, "END")) break;
+        if (fread(&r.code, 4, 1, f) != 1 || fread(&r.ndim, 4, 1, f) != 1) die("truncated");
+        if (r.ndim > 8) die("ndim");
+        if (fread(r.dims, 8, r.ndim, f) != r.ndim) die("truncated");
+        size_t n = 1;
+        for (unsigned i = 0; i < r.ndim; ++i) n *= (size_t)r.dims[i];
+        size_t es = r.code == 0 ? 8 : (r.code == 1 ? 4 : 16);
+        r.nbytes = n * es;
+        r.data = malloc(r.nbytes ? r.nbytes : 1);
+        if (fread(r.data, 1, r.nbytes, f) != r.nbytes) die("truncated data");
+        if (nrec >= 4096) die("too many records");
+        recs[nrec++] = r;
+    }
+    fclose(f);
+}
+
+static struct rec* get(const char* name, int required)
+{
+    for (int i = 0; i < nrec; ++i)
+        if (!strcmp(recs[i].name, name)) return &recs[i];
+    if (required)
+    {
+        fprintf(stderr, "missing record %s\n", name);
+        exit(2);
+    }
+    return NULL;
+}
+
+/* elph_mat slices land here: (nq, nk, nmodes, nspin, nb, nb) */
+static double _Complex* g_all = NULL;
+static size_t g_slice = 0;
+static size_t g_nk = 0;
+/* Dmats served to nc_get_vara: (nsym, nk, nspin, nb, nb) */
+static double _Complex* dmats = NULL;
+static size_t dmat_slice = 0, dmat_nk = 0;
+
+int nc_put_vara(int ncid, int varid, const size_t* startp, const size_t* countp, const void* op)
+{
+    (void)ncid; (void)varid; (void)countp;
+    memcpy(g_all + (startp[0] * g_nk + startp[1]) * g_slice, op, sizeof(double _Complex) * g_slice);
+    return 0;
+}
+
+int nc_get_vara(int ncid, int varid, const size_t* startp, const size_t* countp, void* ip)
+{
+    (void)ncid; (void)varid; (void)countp;
+    if (!dmats) return 1;
+    memcpy(ip, dmats + (startp[0] * dmat_nk + startp[1]) * dmat_slice, sizeof(double _Complex) * dmat_slice);
+    return 0;
+}
+
+const char* nc_strerror(int e)
+{
+    (void)e;
+    return "oracle netCDF stand-in error";
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 3) die("usage: lelph_ref <system.bin> <g_out.bin> [rotate <D.bin> <out.bin>]");
+    load(argv[1]);
+    init_ELPH_clocks();
+    const int* h = (const int*)get("header", 1)->data;
+    int natom = h[0], ntype = h[1], nsym = h[2], timerev = h[3], nspin = h[4], nspinor = h[5], nbnds = h[6];
+    int nmag = h[7], nmodes = h[8], nkibz = h[9], nkbz = h[10];
+    int Nx = h[11], Ny = h[12], Nz = h[13], nltimesj = h[14], lmax = h[15], soc = h[16], nq = h[17];
+    int kminusq = h[18], non_loc = h[19];
+    char dimension = (char)h[20];
+
+    struct Lattice lat;
+    memset(&lat, 0, sizeof(lat));
+    lat.natom = natom;
+    lat.nsym = nsym;
+    lat.timerev = timerev;
+    lat.nspin = nspin;
+    lat.nspinor = nspinor;
+    lat.total_bands = nbnds;
+    lat.start_band = 1;
+    lat.end_band = nbnds;
+    lat.nbnds = nbnds;
+    lat.dimension = dimension;
+    lat.nmag = nmag;
+    lat.nmodes = nmodes;
+    lat.nkpts_iBZ = nkibz;
+    lat.nkpts_BZ = nkbz;
+    lat.fft_dims[0] = Nx;
+    lat.fft_dims[1] = Ny;
+    lat.fft_dims[2] = Nz;
+    lat.nfftz_loc = Nz;
+    lat.nfftz_loc_shift = 0;
+    memcpy(lat.alat_vec, get("alat", 1)->data, 9 * sizeof(double));
+    memcpy(lat.blat_vec, get("blat", 1)->data, 9 * sizeof(double));
+    lat.volume = 0;
+    lat.atomic_pos = get("atom_pos", 1)->data;
+    lat.atom_type = get("atom_type", 1)->data;
+    lat.kpt_iredBZ = get("kibz", 1)->data;
+    lat.kpt_fullBZ_crys = get("kbz_crys", 1)->data;
+    lat.kpt_fullBZ = malloc(sizeof(double) * 3 * (size_t)nkbz);
+    for (int i = 0; i < nkbz; ++i)
+        for (int x = 0; x < 3; ++x)
+        {
+            double s = 0;
+            for (int j = 0; j < 3; ++j) s += lat.blat_vec[3 * x + j] * lat.kpt_fullBZ_crys[3 * i + j];
+            lat.kpt_fullBZ[3 * i + x] = s / (2 * 3.1415927);
+        }
+    lat.kmap = get("kmap", 1)->data;
+    lat.is_soc_present = soc != 0;
+    lat.syms = malloc(sizeof(struct symmetry) * (size_t)nsym);
+    const double* R = get("sym_R", 1)->data;
+    const double* T = get("sym_tau", 1)->data;
+    const int* TR = get("sym_trev", 1)->data;
+    for (int i = 0; i < nsym; ++i)
+    {
+        memcpy(lat.syms[i].Rmat, R + 9 * i, 9 * sizeof(double));
+        memcpy(lat.syms[i].tau, T + 3 * i, 3 * sizeof(double));
+        lat.syms[i].time_rev = TR[i] != 0;
+    }
+
+    struct WFC* wfcs = calloc((size_t)nkibz, sizeof(struct WFC));
+    long long npw_max = 0;
+    for (int ik = 0; ik < nkibz; ++ik)
+    {
+        char nm[32];
+        snprintf(nm, 32, "gvec%d", ik);
+        struct rec* g = get(nm, 1);
+        snprintf(nm, 32, "wfc%d", ik);
+        struct rec* w = get(nm, 1);
+        snprintf(nm, 32, "Fk%d", ik);
+        struct rec* fk = get(nm, 1);
+        wfcs[ik].gvec = g->data;
+        wfcs[ik].wfc = w->data;
+        wfcs[ik].Fk = fk->data;
+        wfcs[ik].npw_total = g->dims[0];
+        wfcs[ik].npw_loc = g->dims[0];
+        if (g->dims[0] > npw_max) npw_max = g->dims[0];
+    }
+    lat.npw_max = npw_max;
+
+    struct Pseudo ps;
+    memset(&ps, 0, sizeof(ps));
+    ps.PP_table = get("PP_table", 1)->data;
+    ps.Fsign = get("Fsign", 1)->data;
+    ps.nltimesj = nltimesj;
+    ps.ntype = ntype;
+    ps.lmax = lmax;
+    ps.fCoeff = NULL;
+    if (soc && nspinor == 2)
+    {
+        ps.fCoeff = calloc((size_t)(nltimesj * ntype), sizeof(double _Complex*));
+        for (int i = 0; i < nltimesj * ntype; ++i)
+        {
+            char nm[32];
+            snprintf(nm, 32, "fCoeff%d", i);
+            struct rec* r = get(nm, 0);
+            ps.fCoeff[i] = r ? r->data : NULL;
+        }
+    }
+
+    struct Phonon ph;
+    memset(&ph, 0, sizeof(ph));
+    ph.nq_iBZ = nq;
+    ph.nq_BZ = nq;
+    ph.nq_iBZ_loc = nq;
+    ph.qpts_iBZ = get("qpts", 1)->data;
+    ph.qpts_BZ = ph.qpts_iBZ;
+    ph.nph_sym = nsym;
+    ph.ph_syms = lat.syms;
+    ph.qmap = malloc(sizeof(int) * 2 * (size_t)nq);
+    ph.nqstar = malloc(sizeof(ND_int) * (size_t)nq);
+    for (int i = 0; i < nq; ++i)
+    {
+        ph.qmap[2 * i] = i;
+        ph.qmap[2 * i + 1] = 0;
+        ph.nqstar[i] = 1;
+    }
+
+    struct ELPH_MPI_Comms comm;
+    memset(&comm, 0, sizeof(comm));
+    comm.commW = comm.commQ = comm.commK = comm.commR = comm.commRq = MPI_COMM_WORLD;
+    comm.nqpools = comm.nkpools = 1;
+    comm.commW_size = comm.commQ_size = comm.commK_size = comm.commR_size = comm.commRq_size = 1;
+
+    g_slice = (size_t)nmodes * nspin * nbnds * nbnds;
+    g_nk = (size_t)nkbz;
+    g_all = calloc((size_t)nq * g_nk * g_slice, sizeof(double _Complex));
+    double _Complex* eig = get("eigVec", 1)->data;
+    double _Complex* dv = get("dVscf", 1)->data;
+    size_t nfft = (size_t)Nx * Ny * Nz;
+    for (int iq = 0; iq < nq; ++iq)
+    {
+        compute_and_write_elphq(wfcs, &lat, &ps, &ph, iq, eig + (size_t)iq * nmodes * nmodes,
+                                dv + (size_t)iq * nmodes * nmag * nfft, 0, 0, 0, 0, non_loc != 0,
+                                kminusq != 0, &comm);
+    }
+    FILE* fo = fopen(argv[2], "wb");
+    if (!fo) die("cannot write output");
+    fwrite(g_all, sizeof(double _Complex), (size_t)nq * g_nk * g_slice, fo);
+    fclose(fo);
+
+    if (argc >= 6 && !strcmp(argv[3], "rotate"))
+    {
+        /* elph_q_rotate on (g, Dl, Dr, time_rev) records of a separate file */
+        nrec = 0;
+        load(argv[4]);
+        struct rec* gq = get("g", 1);
+        struct rec* dl = get("Dl", 1);
+        struct rec* dr = get("Dr", 1);
+        const int* tr = get("trev", 1)->data;
+        double _Complex* out = malloc(gq->nbytes);
+        elph_q_rotate(dl->data, gq->data, dr->data, &lat, tr[0] != 0, out);
+        FILE* fr = fopen(argv[5], "wb");
+        fwrite(out, 1, gq->nbytes, fr);
+        fclose(fr);
+    }
+    return 0;
+}

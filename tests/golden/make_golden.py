@@ -1,0 +1,88 @@
+"""Generate the golden fixtures of tests/golden/ from the compiled reference.
+
+Each fixture is a small seeded synthetic system (regenerated bit-for-bit by
+letzelphc_gb300.synth.make_system from the spec stored in the fixture) and
+the elph matrix elements that the reference's own per-q stage
+(compute_and_write_elphq, src/elph/compute_elph_matq.c:20, FP64 build)
+produced for it, run through oracle/_ref/lelph_ref (oracle/Makefile).
+A second fixture pins elph_q_rotate (src/symmetries/elphq_expand.c:16).
+
+Run from the repo root after ``make -C oracle``:
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from letzelphc_gb300 import synth  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "lelph_ref")
+
+# name -> (base config, overrides, kminusq, non_loc)
+GOLDEN = {
+    "c0": ("c0", {}, False, True),
+    "c0_local": ("c0", {}, False, False),
+    "zb_tr": ("c0", {"kind": "zincblende", "timerev": True, "nbnds": 6}, False, True),
+    "zb_tr_kmq": ("c0", {"kind": "zincblende", "timerev": True, "nbnds": 6}, True, True),
+    "lsda": ("c0", {"nspin": 2, "nbnds": 4, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}, False, True),
+    "soc_tr": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True,
+                      "ls": (0, 1, 2), "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (4, 4, 4),
+                      "qpts": [(0.25, 0.25, 0)]}, False, True),
+    "spinor_nosoc": ("c0", {"nspinor": 2, "nmag": 1, "nbnds": 4, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)],
+                            "ls": (0, 1, 2)}, False, True),
+    "l12_small": ("c1", {"nbnds": 6, "kgrid": (2, 2, 2), "npw": 300, "fft": (24, 24, 24),
+                         "qpts": [(0.5, 0, 0), (0.5, 0.5, 0.5)]}, False, True),
+}
+
+
+def run(name, base, ov, kmq, nl, tmp):
+    s = synth.make_system(base, dict(ov))
+    sysf = os.path.join(tmp, name + ".bin")
+    gf = os.path.join(tmp, name + "_g.bin")
+    synth.write_system(s, sysf, kminusq=kmq, non_loc=nl)
+    subprocess.run([REF, sysf, gf], check=True)
+    g = synth.read_g(gf, s, len(s.qpts))
+    spec = json.dumps({"base": base, "overrides": ov, "kminusq": kmq, "non_loc": nl})
+    np.savez(os.path.join(ROOT, "tests", "golden", name + ".npz"), g=g, spec=np.array(spec),
+             wfc_sum=np.array([np.abs(w).sum() for w in s.wfc]), dv_sum=np.abs(s.dVscf).sum())
+    print(name, g.shape, float(np.abs(g).max()))
+
+
+def rotate_fixture(tmp):
+    s = synth.make_system("c0", {"nbnds": 5})
+    rng = np.random.default_rng(7)
+    nm, ns, nb = s.nmodes, s.nspin, s.nbnds
+    g = rng.standard_normal((nm, ns, nb, nb)) + 1j * rng.standard_normal((nm, ns, nb, nb))
+    Dl = rng.standard_normal((ns, nb, nb)) + 1j * rng.standard_normal((ns, nb, nb))
+    Dr = rng.standard_normal((ns, nb, nb)) + 1j * rng.standard_normal((ns, nb, nb))
+    out = {}
+    for trev in (0, 1):
+        sysf = os.path.join(tmp, "rot_sys.bin")
+        synth.write_system(s, sysf)
+        df = os.path.join(tmp, "rot_in.bin")
+        with open(df, "wb") as f:
+            f.write(b"LELPHSYS")
+            synth._rec(f, "g", g)
+            synth._rec(f, "Dl", Dl)
+            synth._rec(f, "Dr", Dr)
+            synth._rec(f, "trev", np.array([trev], np.int32))
+            f.write(b"END\0" + b"\0" * 28)
+        of = os.path.join(tmp, "rot_out.bin")
+        subprocess.run([REF, sysf, os.path.join(tmp, "ignore.bin"), "rotate", df, of], check=True)
+        out[trev] = np.fromfile(of, np.complex128).reshape(g.shape)
+    np.savez(os.path.join(ROOT, "tests", "golden", "q_rotate.npz"), g=g, Dl=Dl, Dr=Dr,
+             out_notr=out[0], out_tr=out[1])
+    print("q_rotate", g.shape)
+
+
+if __name__ == "__main__":
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (base, ov, kmq, nl) in GOLDEN.items():
+            run(name, base, ov, kmq, nl, tmp)
+        rotate_fixture(tmp)

@@ -1,0 +1,23 @@
+"""Helpers to load the golden fixtures (tests/golden/*.npz) and rebuild the
+synthetic system each was generated from."""
+import json
+import os
+
+import numpy as np
+
+from letzelphc_gb300 import synth
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NAMES = ["c0", "c0_local", "zb_tr", "zb_tr_kmq", "lsda", "soc_tr", "spinor_nosoc", "l12_small"]
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    spec = json.loads(str(z["spec"]))
+    ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls") else v)
+          for k, v in spec["overrides"].items()}
+    s = synth.make_system(spec["base"], ov)
+    # the regenerated inputs must be the ones the fixture was made from
+    assert np.allclose([np.abs(w).sum() for w in s.wfc], z["wfc_sum"], rtol=1e-12)
+    assert np.isclose(np.abs(s.dVscf).sum(), float(z["dv_sum"]), rtol=1e-12)
+    return s, z["g"], bool(spec["kminusq"]), bool(spec["non_loc"])

@@ -1,0 +1,35 @@
+"""The CPU restatement (oracle/elph_oracle.py) against the reference's own
+output (tests/golden/, made by the compiled reference, FP64 build)."""
+import numpy as np
+import pytest
+
+import elph_oracle as O
+from golden_util import NAMES, load
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference(name):
+    s, g_ref, kmq, nl = load(name)
+    g = np.array([O.compute_elphq(s, iq, non_loc=nl, kminusq=kmq) for iq in range(len(s.qpts))])
+    err = np.abs(g - g_ref).max() / np.abs(g_ref).max()
+    assert err < 1e-12, err
+
+
+def test_q_rotate_matches_reference():
+    import os
+    from golden_util import GOLDEN_DIR
+    z = np.load(os.path.join(GOLDEN_DIR, "q_rotate.npz"))
+    for trev, key in ((False, "out_notr"), (True, "out_tr")):
+        out = O.elph_q_rotate(z["Dl"], z["g"], z["Dr"], trev)
+        assert np.abs(out - z[key]).max() < 1e-12 * np.abs(z[key]).max()
+
+
+def test_synthetic_generator_shapes():
+    from letzelphc_gb300 import synth
+    s = synth.make_system("c0")
+    assert s.nk_bz == 64 and s.nk_ibz == 8 and len(s.sym_R) == 48
+    assert 360 <= s.npw.min() and s.npw.max() <= 440
+    # bz_expand's kmap reproduces every full-BZ point from its iBZ point
+    for i, (ik, isym) in enumerate(s.kmap):
+        k = s.alat.T @ (s.sym_R[isym] @ s.kibz[ik])
+        assert np.allclose(k, s.kbz_crys[i])
