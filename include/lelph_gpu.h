@@ -1,0 +1,154 @@
+/*
+ * lelph_gpu.h -- C ABI of the GB300 electron-phonon matrix-element stage.
+ *
+ * Drop-in for the per-q stage of LetzElPhC:
+ *   void compute_and_write_elphq(struct WFC* wfcs, struct Lattice* lattice,
+ *        struct Pseudo* pseudo, struct Phonon* phonon, const ND_int iqpt,
+ *        ELPH_cmplx* eigVec, ELPH_cmplx* dVscfq, const int ncid_elph,
+ *        const int varid_elph, const int ncid_dmat, const int varid_dmat,
+ *        const bool non_loc, const bool kminusq, const struct ELPH_MPI_Comms* Comm)
+ *   (src/elph/elph.h:10-17, src/elph/compute_elph_matq.c:20-234)
+ * together with its inner units elphLocal (src/dvloc/dvloc.h:16-18) and
+ * add_elphNonLocal (src/nonloc/Vnonloc.h:8-11).
+ *
+ * Plain pointers and sizes only.  Complex numbers are interleaved (re, im)
+ * doubles unless stated.  The library copies every input to the device; the
+ * caller owns all host buffers.  Functions return LELPH_GPU_OK (0) or a
+ * negative status and never abort the process (the reference aborts through
+ * error_msg -> MPI_Abort, src/common/error.c:8-21; a caller that wants that
+ * behaviour maps a nonzero status to error_msg).  One context per host
+ * thread; a context is not re-entrant.  Calls are synchronous: on return the
+ * outputs are in the caller's buffer.
+ */
+#ifndef LELPH_GPU_H
+#define LELPH_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LELPH_GPU_OK 0
+#define LELPH_GPU_ERR_INVALID (-1)     /* bad argument or inconsistent sizes */
+#define LELPH_GPU_ERR_ALLOC (-2)       /* device or host allocation failed */
+#define LELPH_GPU_ERR_CUDA (-3)        /* CUDA runtime/driver error */
+#define LELPH_GPU_ERR_TIMEOUT (-4)     /* a device-side wait ran out (kernel bailed out) */
+#define LELPH_GPU_ERR_GEOMETRY (-5)    /* k+q not on the grid, non-integral symmetry, box too small */
+#define LELPH_GPU_ERR_STATE (-6)       /* call order (e.g. run on an empty q slot) */
+#define LELPH_GPU_ERR_UNSUPPORTED (-7) /* size outside what this build handles */
+
+/* arithmetic of the path */
+#define LELPH_GPU_FP64 0       /* FP64 throughout (the plain form) */
+#define LELPH_GPU_MIXED_F16 1  /* FP32 FFTs, split-f16 (hi,lo) tensor-core sandwich, FP64 phases/reduction */
+#define LELPH_GPU_MIXED_BF16 2 /* as above with split-bf16 */
+
+/* element type of matrix-element outputs */
+#define LELPH_GPU_OUT_C128 0 /* double complex (reference built with -DCOMPILE_ELPH_DOUBLE) */
+#define LELPH_GPU_OUT_C64 1  /* float complex (reference default build, src/elphC.h:24-31) */
+
+typedef struct lelph_gpu lelph_gpu;
+
+/* The contents of struct Lattice / WFC / Pseudo (src/common/dtypes.h:80-266)
+ * that the per-q stage reads.  Layouts are the reference's. */
+typedef struct lelph_gpu_desc
+{
+    /* struct Lattice */
+    int natom, nsym, timerev, nspin, nspinor, nbnds, nmag, nmodes;
+    int nkpts_iBZ, nkpts_BZ;
+    int fft_dims[3];
+    const double* alat_vec;        /* [9]  a_i = alat[:, i], row-major */
+    const double* blat_vec;        /* [9]  b_i = blat[:, i], includes 2 pi */
+    const double* atomic_pos;      /* [natom*3] cartesian */
+    const int* atom_type;          /* [natom] */
+    const double* kpt_iredBZ;      /* [nkpts_iBZ*3] cartesian, no 2 pi */
+    const double* kpt_fullBZ_crys; /* [nkpts_BZ*3] crystal */
+    const int* kmap;               /* [nkpts_BZ*2] (iBZ k, symmetry) */
+    const double* sym_Rmat;        /* [nsym*9] cartesian, row-major */
+    const double* sym_tau;         /* [nsym*3] cartesian fractional translations */
+    const int* sym_time_rev;       /* [nsym] */
+    int is_soc_present;
+    /* struct WFC, one per iBZ k-point */
+    const int* npw;                /* [nkpts_iBZ] plane waves of each k */
+    const double* const* gvec;     /* [ik] -> [npw*3] cartesian, no 2 pi */
+    const double* const* wfc;      /* [ik] -> (nspin, nbnds, nspinor, npw) complex */
+    const double* const* Fk;       /* [ik] -> (nltimesj, ntype, npw) KB form factors */
+    /* struct Pseudo */
+    int ntype, nltimesj, lmax;
+    const double* PP_table;        /* (nltimesj, ntype, 3): l+1, 2j, spin */
+    const double* Fsign;           /* (nltimesj, ntype) */
+    const double* const* fCoeff;   /* [lidx*ntype+itype] -> (2l+1,2l+1,nspinor,nspinor) complex, or NULL */
+    /* library options */
+    int precision;                 /* LELPH_GPU_FP64 / LELPH_GPU_MIXED_F16 / LELPH_GPU_MIXED_BF16 */
+    int device;                    /* CUDA device ordinal */
+} lelph_gpu_desc;
+
+typedef struct lelph_gpu_stats
+{
+    long long kernel_launches;   /* kernels launched by this context so far */
+    long long local_launches;    /* launches of the local-sandwich kernel */
+    double local_ms;             /* device time of those launches (profiling on) */
+    double prepare_ms;           /* device time of the q-independent stage (profiling on) */
+    double finish_ms;            /* device time of the finish kernel (profiling on) */
+    long long pairs_done;        /* (k, q) pairs computed */
+    size_t device_bytes;         /* device memory held by the context */
+} lelph_gpu_stats;
+
+/* Create a context: validates the inputs, derives the integer symmetry maps,
+ * uploads wavefunctions, form factors and projector tables.
+ * Replaces the per-call setup of elphLocal / add_elphNonLocal
+ * (src/dvloc/compute_Vbare_loc.c:93-205, src/nonloc/Vbare_nloc.c:96-245). */
+int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out);
+
+/* Replace the plane-wave coefficients of every iBZ k-point
+ * ([ik] -> (nspin, nbnds, nspinor, npw) complex); invalidates lelph_gpu_prepare. */
+int lelph_gpu_set_wavefunctions(lelph_gpu* h, const double* const* wfc);
+
+/* q-independent work: unfold every full-BZ wavefunction (rotation, SU(2),
+ * fractional translation, time reversal), inverse-FFT it to the grid and
+ * project it on the KB projectors.  Runs implicitly on first use. */
+int lelph_gpu_prepare(lelph_gpu* h);
+
+/* Load one q-point into a slot: q in crystal coordinates, eigVec
+ * (nmodes, 3*natom) complex, dVscf (nmodes, nmag, Nx, Ny, Nz) complex -- the
+ * dVscfq / eigVec arguments of compute_and_write_elphq. */
+int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec, const double* dVscf);
+
+/* Matrix elements for n (q slot, full-BZ k) items, flags as in
+ * compute_and_write_elphq (non_loc, kminusq).  g_out (host) receives
+ * (n, nmodes, nspin, nbnds_k, nbnds_k+q) complex of out_type -- the
+ * elph_mat[q][k] slice layout (src/elph/elph_driver.c:164-187). */
+int lelph_gpu_run(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq, int out_type,
+                  void* g_out);
+
+/* Same, output left in device memory (g_out_dev, same layout). */
+int lelph_gpu_run_device(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
+                         int out_type, void* g_out_dev);
+
+/* compute_and_write_elphq for one iBZ q without the netCDF writes: every
+ * full-BZ k, output (nkpts_BZ, nmodes, nspin, nbnds, nbnds) complex double. */
+int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, const double* dVscfq,
+                            int non_loc, int kminusq, double* elph_out);
+
+/* elph_q_rotate (src/symmetries/elphq_expand.c:16-73): g_Sq = (g^{T|C} D_r^H)^T D_l^T
+ * per (mode, spin); g, out (nmodes, nspin, nb, nb), D (nspin, nb, nb) complex. */
+int lelph_gpu_elph_q_rotate(lelph_gpu* h, const double* Dmats_l, const double* elph_q, const double* Dmats_r,
+                            int time_rev, double* elph_Sq);
+
+/* Rotated (and umklapp-shifted) Miller indices of full-BZ k-point kbz, as the
+ * device computes them: out[npw*3].  Parity check of the integer maps of
+ * rotateGvecs + Sort_pw (src/wfc/rotate_Gvecs.c:15-81, src/wfc/sortpw.c:95-315). */
+int lelph_gpu_debug_gvec_map(lelph_gpu* h, int kbz, const int ulm[3], int* out);
+
+int lelph_gpu_set_profiling(lelph_gpu* h, int on);
+int lelph_gpu_stats_get(lelph_gpu* h, lelph_gpu_stats* s);
+/* the CUDA stream (cudaStream_t) every kernel of the context runs on */
+void* lelph_gpu_stream(lelph_gpu* h);
+const char* lelph_gpu_strerror(int status);
+const char* lelph_gpu_last_error(lelph_gpu* h);
+void lelph_gpu_destroy(lelph_gpu* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,490 @@
+// Wavefunction unfolding and batched 3-D FFTs for the electron-phonon path.
+//
+// * k_scatter: sphere -> box for every (full-BZ k, spin, band, spinor).  The
+//   symmetry-rotated Miller index is integer arithmetic (W n, W the integer
+//   action of the symmetry on the reciprocal lattice), so the plane-wave ->
+//   box map is exact; it replaces rotateGvecs + rint + Sort_pw
+//   (src/wfc/rotate_Gvecs.c:15-81, src/wfc/sortpw.c:95-315) and the
+//   sphere->box step of invfft3D (src/fft/bwdfft.c:45-69).  SU(2) rotation
+//   (src/wfc/su2rotate.c:13-41), the FP64 fractional-translation phase with
+//   the truncated pi (src/wfc/trans_wfc.c:15-52) and the time-reversal conj
+//   are applied on the fly.
+// * k_fft_contig / k_fft_strided: batched 1-D Stockham passes (radix 2,3,4,5)
+//   in shared memory, replacing the FFTW plans of src/fft/planner.c and the
+//   slab transposes of src/fft/transpose.c.  Unnormalised, sign +1 is
+//   FFTW_BACKWARD.
+// * k_fft_x_split: the last (x) pass of the mixed form, whose epilogue writes
+//   psi(r) straight into the split-precision tensor-core operand layout.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lelph_common.cuh"
+#include "lelph_internal.h"
+
+// ------------------------------------------------------------- butterflies
+
+template <typename T2>
+__device__ __forceinline__ T2 mul_i(T2 a, int sign)  // multiply by sign * i
+{
+    T2 r;
+    r.x = -sign * a.y;
+    r.y = sign * a.x;
+    return r;
+}
+
+template <typename T2, typename T>
+__device__ __forceinline__ void dft2(T2* v)
+{
+    T2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+
+template <typename T2, typename T>
+__device__ __forceinline__ void dft4(T2* v, int sign)
+{
+    T2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    T2 s13 = cadd(v[1], v[3]), d13 = mul_i(csub(v[1], v[3]), sign);
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+}
+
+template <typename T2, typename T>
+__device__ __forceinline__ void dft3(T2* v, int sign)
+{
+    const T c = (T)-0.5;
+    const T s = (T)(sign * 0.86602540378443864676);  // sin(2 pi / 3)
+    T2 a = cadd(v[1], v[2]);
+    T2 d = csub(v[1], v[2]);
+    T2 t1;
+    t1.x = v[0].x + c * a.x;
+    t1.y = v[0].y + c * a.y;
+    T2 t2;  // i s d
+    t2.x = -s * d.y;
+    t2.y = s * d.x;
+    v[0] = cadd(v[0], a);
+    v[1] = cadd(t1, t2);
+    v[2] = csub(t1, t2);
+}
+
+template <typename T2, typename T>
+__device__ __forceinline__ void dft5(T2* v, int sign)
+{
+    const T c1 = (T)0.30901699437494742410;   // cos(2 pi / 5)
+    const T c2 = (T)-0.80901699437494742410;  // cos(4 pi / 5)
+    const T s1 = (T)(sign * 0.95105651629515357212);  // sin(2 pi / 5)
+    const T s2 = (T)(sign * 0.58778525229247312917);  // sin(4 pi / 5)
+    T2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+    T2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    T2 x0 = v[0];
+    T2 r1, r2, i1, i2;
+    r1.x = x0.x + c1 * a1.x + c2 * a2.x;
+    r1.y = x0.y + c1 * a1.y + c2 * a2.y;
+    r2.x = x0.x + c2 * a1.x + c1 * a2.x;
+    r2.y = x0.y + c2 * a1.y + c1 * a2.y;
+    // i (s1 b1 + s2 b2) and i (s2 b1 - s1 b2)
+    T2 u, w;
+    u.x = s1 * b1.x + s2 * b2.x;
+    u.y = s1 * b1.y + s2 * b2.y;
+    w.x = s2 * b1.x - s1 * b2.x;
+    w.y = s2 * b1.y - s1 * b2.y;
+    i1.x = -u.y;
+    i1.y = u.x;
+    i2.x = -w.y;
+    i2.y = w.x;
+    v[0] = cadd(x0, cadd(a1, a2));
+    v[1] = cadd(r1, i1);
+    v[4] = csub(r1, i1);
+    v[2] = cadd(r2, i2);
+    v[3] = csub(r2, i2);
+}
+
+// One Stockham pass of radix R over nlines lines held in shared memory;
+// element e of line l lives at buf[l*ls + e*es].
+template <typename T2, typename T, int R>
+__device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int L,
+                                              int Ns, int es, int ls, const T2* tw, int sign)
+{
+    const int LR = L / R;
+    const int nwork = nlines * LR;
+    const int tstride = L / (Ns * R);
+    for (int w = threadIdx.x; w < nwork; w += blockDim.x)
+    {
+        int line = w / LR;
+        int j = w - line * LR;
+        int k = j % Ns;
+        const T2* s = src + (size_t)line * ls;
+        T2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = s[(size_t)(j + r * LR) * es];
+        if (k != 0)
+        {
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+            {
+                T2 t = tw[r * k * tstride];
+                if (sign < 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        if (R == 2) dft2<T2, T>(v);
+        if (R == 3) dft3<T2, T>(v, sign);
+        if (R == 4) dft4<T2, T>(v, sign);
+        if (R == 5) dft5<T2, T>(v, sign);
+        T2* d = dst + (size_t)line * ls;
+        int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) d[(size_t)(base + r * Ns) * es] = v[r];
+    }
+}
+
+// Runs all passes; returns the buffer holding the result.
+template <typename T2, typename T>
+__device__ T2* fft_smem(T2* a, T2* b, int nlines, int es, int ls, const FftPlan1D& p, const T2* tw, int sign)
+{
+    int Ns = 1;
+    for (int st = 0; st < p.nstage; ++st)
+    {
+        int R = p.radix[st];
+        if (R == 4) stockham_pass<T2, T, 4>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
+        else if (R == 2) stockham_pass<T2, T, 2>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
+        else if (R == 3) stockham_pass<T2, T, 3>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
+        else stockham_pass<T2, T, 5>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
+        __syncthreads();
+        T2* t = a;
+        a = b;
+        b = t;
+        Ns *= R;
+    }
+    return a;
+}
+
+// ---------------------------------------------------- contiguous-line pass
+
+template <typename T2, typename T>
+__global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long long nlines, FftPlan1D p,
+                                                    const T2* __restrict__ tw, int sign, int lpc)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* a = reinterpret_cast<T2*>(smraw);
+    T2* b = a + (size_t)lpc * p.L;
+    T2* tws = b + (size_t)lpc * p.L;
+    for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
+    long long l0 = (long long)blockIdx.x * lpc;
+    int nl = (int)min((long long)lpc, nlines - l0);
+    T2* g = data + l0 * p.L;
+    int n = nl * p.L;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = g[i];
+    __syncthreads();
+    T2* r = fft_smem<T2, T>(a, b, nl, 1, p.L, p, tws, sign);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) g[i] = r[i];
+}
+
+// ------------------------------------------------------- strided-line pass
+// data viewed as [nouter][L][inner]; one CTA = one outer index and a chunk
+// of `ich` inner positions, loaded as an [L][ich] tile (coalesced in inner).
+
+template <typename T2, typename T>
+__global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long long nouter, int inner, int ich,
+                                                     int nchunk, FftPlan1D p, const T2* __restrict__ tw, int sign)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* a = reinterpret_cast<T2*>(smraw);
+    T2* b = a + (size_t)ich * p.L;
+    T2* tws = b + (size_t)ich * p.L;
+    for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
+    long long o = blockIdx.x / nchunk;
+    int c = blockIdx.x - (int)(o * nchunk);
+    int i0 = c * ich;
+    int ic = min(ich, inner - i0);
+    T2* g = data + (size_t)o * p.L * inner + i0;
+    int n = p.L * ic;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    {
+        int l = idx / ic, i = idx - l * ic;
+        a[l * ic + i] = g[(size_t)l * inner + i];
+    }
+    __syncthreads();
+    T2* r = fft_smem<T2, T>(a, b, ic, ic, 1, p, tws, sign);
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    {
+        int l = idx / ic, i = idx - l * ic;
+        g[(size_t)l * inner + i] = r[l * ic + i];
+    }
+}
+
+// x pass of the mixed form: boxes (nbox = nk*nspin*nb*nspinor) of FP32
+// complex; result psi(r) * band_scale is split into (hi, lo) 16-bit floats and
+// written to the operand layout
+//   Bsplit[((kbz*nspin + s)*2 + hl)*(2*nbp) + row][2*kc + {0,1}],  kc = spinor*N + r
+// row n < nbp holds (Re, Im) of band n, row nbp + n holds (-Im, Re).
+template <int BF16>
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo)
+{
+    if (BF16)
+    {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        float2 hf = __bfloat1622float2(h);
+        __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+        hi = *reinterpret_cast<uint32_t*>(&h);
+        lo = *reinterpret_cast<uint32_t*>(&l);
+    }
+    else
+    {
+        __half2 h = __floats2half2_rn(a, b);
+        float2 hf = __half22float2(h);
+        __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+        hi = *reinterpret_cast<uint32_t*>(&h);
+        lo = *reinterpret_cast<uint32_t*>(&l);
+    }
+}
+
+template <int BF16>
+__global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ boxes, int nbox, int k0, int ich,
+                                                     int nchunk, FftPlan1D p, const float2* __restrict__ tw,
+                                                     int sign, GeomDev gd, const float* __restrict__ band_scale,
+                                                     uint16_t* __restrict__ Bsplit)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* a = reinterpret_cast<float2*>(smraw);
+    float2* b = a + (size_t)ich * p.L;
+    float2* tws = b + (size_t)ich * p.L;
+    for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
+    const int inner = gd.Ny * gd.Nz;
+    const long long N = (long long)gd.Nx * inner;
+    int o = blockIdx.x / nchunk;
+    int c = blockIdx.x - o * nchunk;
+    int i0 = c * ich;
+    int ic = min(ich, inner - i0);
+    const float2* g = boxes + (size_t)o * N + i0;
+    int n = p.L * ic;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    {
+        int l = idx / ic, i = idx - l * ic;
+        a[l * ic + i] = g[(size_t)l * inner + i];
+    }
+    __syncthreads();
+    float2* r = fft_smem<float2, float>(a, b, ic, ic, 1, p, tws, sign);
+    // box o -> (kslot, spin, band, spinor)
+    int sp = o % gd.nspinor;
+    int t = o / gd.nspinor;
+    int band = t % gd.nbnds;
+    t /= gd.nbnds;
+    int spin = t % gd.nspin;
+    int kslot = t / gd.nspin;
+    int kbz = k0 + kslot;
+    float sc = band_scale[((size_t)kbz * gd.nspin + spin) * gd.nbnds + band];
+    const long long Kr = 2LL * gd.nspinor * N;
+    const int nrow = 2 * gd.nbp;
+    size_t base_hi = ((size_t)(kbz * gd.nspin + spin) * 2 + 0) * nrow * Kr;
+    size_t base_lo = ((size_t)(kbz * gd.nspin + spin) * 2 + 1) * nrow * Kr;
+    uint32_t* Bw = reinterpret_cast<uint32_t*>(Bsplit);
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    {
+        int l = idx / ic, i = idx - l * ic;
+        float2 v = r[l * ic + i];
+        v.x *= sc;
+        v.y *= sc;
+        long long kc = (long long)sp * N + (long long)l * inner + i0 + i;
+        uint32_t h0, l0, h1, l1;
+        split2<BF16>(v.x, v.y, h0, l0);
+        split2<BF16>(-v.y, v.x, h1, l1);
+        size_t e_nat = ((size_t)band * Kr + 2 * kc) >> 1;
+        size_t e_rot = ((size_t)(gd.nbp + band) * Kr + 2 * kc) >> 1;
+        Bw[(base_hi >> 1) + e_nat] = h0;
+        Bw[(base_lo >> 1) + e_nat] = l0;
+        Bw[(base_hi >> 1) + e_rot] = h1;
+        Bw[(base_lo >> 1) + e_rot] = l1;
+    }
+}
+
+// ------------------------------------------------------------- scatter
+
+template <typename T2>
+__global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __restrict__ ks,
+                                                 const int* __restrict__ miller, const long long* __restrict__ pw_off,
+                                                 const int* __restrict__ npw_arr, const double2* __restrict__ coef,
+                                                 const long long* __restrict__ coef_off, GeomDev gd,
+                                                 T2* __restrict__ boxes, double2* __restrict__ chat,
+                                                 const long long* __restrict__ chat_off)
+{
+    const int kslot = blockIdx.y;
+    const int set = blockIdx.z;  // spin * nbnds + band
+    const int kbz = k0 + kslot;
+    const KPointSym s = ks[kbz];
+    const int npw = npw_arr[s.ik];
+    const int* mil = miller + 3 * pw_off[s.ik];
+    const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
+    const double2* c = coef + coef_off[s.ik] + (size_t)set * gd.nspinor * npw;
+    double2* ch = chat + chat_off[kbz] + (size_t)set * gd.nspinor * npw;
+    T2* bx = boxes + ((size_t)kslot * gd.nspin * gd.nbnds + set) * gd.nspinor * N;
+    const double2 kph = make_double2(s.kphase[0], s.kphase[1]);
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < npw; g += gridDim.x * blockDim.x)
+    {
+        int n0 = mil[3 * g], n1 = mil[3 * g + 1], n2 = mil[3 * g + 2];
+        int G0 = s.W[0] * n0 + s.W[1] * n1 + s.W[2] * n2;
+        int G1 = s.W[3] * n0 + s.W[4] * n1 + s.W[5] * n2;
+        int G2 = s.W[6] * n0 + s.W[7] * n1 + s.W[8] * n2;
+        // e^{-i 2 pi G.tau} (the reference: cexp(-I*2*ELPH_PI*dot)); then kphase * gphase
+        double dot = (double)G0 * s.tau_crys[0] + (double)G1 * s.tau_crys[1] + (double)G2 * s.tau_crys[2];
+        double sn, cs;
+        sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
+        double2 ph = cmul(kph, make_double2(cs, -sn));
+        double2 v[2];
+        if (gd.nspinor == 2)
+        {
+            double2 up = c[g], dw = c[npw + g];
+            double2 u0 = make_double2(s.su2[0], s.su2[1]), u1 = make_double2(s.su2[2], s.su2[3]);
+            double2 u2 = make_double2(s.su2[4], s.su2[5]), u3 = make_double2(s.su2[6], s.su2[7]);
+            v[0] = cadd(cmul(up, u0), cmul(dw, u1));
+            v[1] = cadd(cmul(up, u2), cmul(dw, u3));
+        }
+        else
+        {
+            v[0] = c[g];
+        }
+        int ix = G0 % gd.Nx;
+        if (ix < 0) ix += gd.Nx;
+        int iy = G1 % gd.Ny;
+        if (iy < 0) iy += gd.Ny;
+        int iz = G2 % gd.Nz;
+        if (iz < 0) iz += gd.Nz;
+        size_t bidx = ((size_t)ix * gd.Ny + iy) * gd.Nz + iz;
+        for (int sp = 0; sp < gd.nspinor; ++sp)
+        {
+            double2 w = cmul(v[sp], ph);
+            if (s.trev) w.y = -w.y;
+            ch[(size_t)sp * npw + g] = w;
+            if (bx) bx[(size_t)sp * N + bidx] = mk2<T2>(w.x, w.y);
+        }
+    }
+}
+
+__global__ void k_gmap(const KPointSym* __restrict__ ks, int kbz, const int* __restrict__ miller,
+                       const long long* __restrict__ pw_off, const int* __restrict__ npw_arr, GeomDev gd,
+                       const int* __restrict__ ulm, int* __restrict__ out)
+{
+    const KPointSym s = ks[kbz];
+    const int npw = npw_arr[s.ik];
+    const int* mil = miller + 3 * pw_off[s.ik];
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < npw; g += gridDim.x * blockDim.x)
+    {
+        int n0 = mil[3 * g], n1 = mil[3 * g + 1], n2 = mil[3 * g + 2];
+        int G0 = s.W[0] * n0 + s.W[1] * n1 + s.W[2] * n2 + ulm[0];
+        int G1 = s.W[3] * n0 + s.W[4] * n1 + s.W[5] * n2 + ulm[1];
+        int G2 = s.W[6] * n0 + s.W[7] * n1 + s.W[8] * n2 + ulm[2];
+        out[3 * g] = G0;
+        out[3 * g + 1] = G1;
+        out[3 * g + 2] = G2;
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+static int ich_for(int L, int inner, int elems)
+{
+    int ich = elems / L;
+    ich = ich >= 32 ? (ich / 16) * 16 : (ich < 1 ? 1 : ich);
+    if (ich > inner) ich = inner;
+    return ich;
+}
+
+template <typename T2, typename T>
+static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st)
+{
+    const int elems = sizeof(T) == 8 ? 2048 : 4096;
+    int lpc = elems / p.L;
+    if (lpc < 1) lpc = 1;
+    size_t smem = (size_t)(2 * lpc * p.L + p.L) * sizeof(T2);
+    static bool attr_set = false;
+    if (!attr_set)
+    {
+        cudaFuncSetAttribute(k_fft_contig<T2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    long long nb = (nlines + lpc - 1) / lpc;
+    k_fft_contig<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nlines, p, tw, sign, lpc);
+}
+
+template <typename T2, typename T>
+static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1D& p, const T2* tw, int sign,
+                           cudaStream_t st)
+{
+    const int elems = sizeof(T) == 8 ? 2048 : 4096;
+    int ich = ich_for(p.L, inner, elems);
+    int nchunk = (inner + ich - 1) / ich;
+    size_t smem = (size_t)(2 * ich * p.L + p.L) * sizeof(T2);
+    static bool attr_set = false;
+    if (!attr_set)
+    {
+        cudaFuncSetAttribute(k_fft_strided<T2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    long long nb = nouter * nchunk;
+    k_fft_strided<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign);
+}
+
+void lelph_launch_fft_contig_d(double2* data, long long nlines, const FftPlan1D& p, const double2* tw, int sign,
+                               cudaStream_t st)
+{
+    launch_contig<double2, double>(data, nlines, p, tw, sign, st);
+}
+void lelph_launch_fft_contig_f(float2* data, long long nlines, const FftPlan1D& p, const float2* tw, int sign,
+                               cudaStream_t st)
+{
+    launch_contig<float2, float>(data, nlines, p, tw, sign, st);
+}
+void lelph_launch_fft_strided_d(double2* data, long long nouter, int inner, const FftPlan1D& p, const double2* tw,
+                                int sign, cudaStream_t st)
+{
+    launch_strided<double2, double>(data, nouter, inner, p, tw, sign, st);
+}
+void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const FftPlan1D& p, const float2* tw,
+                                int sign, cudaStream_t st)
+{
+    launch_strided<float2, float>(data, nouter, inner, p, tw, sign, st);
+}
+
+void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
+                                 int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
+                                 cudaStream_t st)
+{
+    const int inner = g.Ny * g.Nz;
+    int ich = ich_for(p.L, inner, 4096);
+    int nchunk = (inner + ich - 1) / ich;
+    size_t smem = (size_t)(2 * ich * p.L + p.L) * sizeof(float2);
+    long long nbox = (long long)nbox_k * g.nspin * g.nbnds * g.nspinor;
+    static bool attr_set = false;
+    if (!attr_set)
+    {
+        cudaFuncSetAttribute(k_fft_x_split<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_fft_x_split<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    unsigned nb = (unsigned)(nbox * nchunk);
+    if (ab_bf16)
+        k_fft_x_split<1><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit);
+    else
+        k_fft_x_split<0><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit);
+}
+
+void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
+                          const int* npw, const double2* coef, const long long* coef_off, const GeomDev& g,
+                          int box_fp64, void* boxes, double2* chat, const long long* chat_off, cudaStream_t st)
+{
+    dim3 grid(4, nk, g.nspin * g.nbnds);
+    if (box_fp64)
+        k_scatter<double2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
+                                                 (double2*)boxes, chat, chat_off);
+    else
+        k_scatter<float2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
+                                                (float2*)boxes, chat, chat_off);
+}
+
+void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,
+                       const GeomDev& g, const int* ulm, int* out, cudaStream_t st)
+{
+    k_gmap<<<16, 256, 0, st>>>(ks, kbz, miller, pw_off, npw, g, ulm, out);
+}

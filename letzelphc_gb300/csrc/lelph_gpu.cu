@@ -1,0 +1,1109 @@
+// Host side of the C ABI declared in include/lelph_gpu.h.
+//
+// Owns the device state of one context: the iBZ wavefunctions and form
+// factors, the unfolded full-BZ wavefunctions on the FFT grid (FP64 boxes for
+// the plain form, split 16-bit tensor-core operands for the mixed form), the
+// KB projections, the q slots (dV_scf, eigVec) and the run workspaces.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lelph_gpu.h"
+#include "lelph_common.cuh"
+#include "lelph_internal.h"
+
+namespace
+{
+const double PI_T = 3.1415927;  // src/common/constants.h:11
+const double EPS_K = 1e-5;      // ELPH_EPS, src/common/constants.h:9
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t n = 0;
+};
+}  // namespace
+
+struct QSlot
+{
+    bool set = false;
+    double q[3];
+};
+
+struct lelph_gpu
+{
+    lelph_gpu_desc d;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool profiling = false;
+    std::string err;
+    lelph_gpu_stats stats;
+    GeomDev g;
+    int nltimesj = 0, ntype = 0;
+    int nproj_max = 0;
+    int ab_bf16 = 0;
+    bool mixed = false;
+    bool prepared = false;
+    // host copies
+    std::vector<double> alat, blat, kibz, kbz_crys, symR, symtau, atom_pos, PP, Fsign;
+    std::vector<int> kmap, symtr, atom_type, npw;
+    std::vector<long long> pw_off, coef_off, fk_off, chat_off;
+    std::vector<KPointSym> ksym;
+    std::vector<float> band_scale;  // (nk_bz, nspin, nb)
+    std::vector<int> miller;        // concatenated (npw*3)
+    std::vector<QSlot> qslots;
+    long long total_pw = 0;
+    // device buffers
+    std::vector<DevBuf*> owned;
+    DevBuf d_miller, d_pwoff, d_npw, d_coef, d_coefoff, d_gvec, d_fk, d_fkoff, d_ksym, d_chat, d_chatoff;
+    DevBuf d_psi64, d_boxes32, d_bsplit, d_band_scale, d_proj;
+    DevBuf d_atype, d_apos, d_pp, d_fsign, d_fcoef, d_fcoefoff;
+    DevBuf d_tw64[3], d_tw32[3];
+    DevBuf d_dv64, d_dv32, d_dvstage, d_eig, d_mode_scale, d_maxabs;
+    DevBuf d_pairs, d_glocal, d_partials, d_gout, d_status, d_tmp;
+    FftPlan1D plan[3];
+    CUtensorMap tmapB, tmapA;
+    int nslots_alloc = 0;
+    int chunk_pts = 0, nchunks = 0;
+};
+
+namespace
+{
+int fail(lelph_gpu* h, int code, const std::string& msg)
+{
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CUDA_TRY(h, call)                                                                                  \
+    do                                                                                                     \
+    {                                                                                                      \
+        cudaError_t e__ = (call);                                                                          \
+        if (e__ != cudaSuccess)                                                                            \
+            return fail((h), e__ == cudaErrorMemoryAllocation ? LELPH_GPU_ERR_ALLOC : LELPH_GPU_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e__));                              \
+    } while (0)
+
+int ensure(lelph_gpu* h, DevBuf& b, size_t bytes)
+{
+    if (b.n >= bytes && b.p) return LELPH_GPU_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        return fail(h, LELPH_GPU_ERR_ALLOC, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    b.n = bytes;
+    return LELPH_GPU_OK;
+}
+
+int upload(lelph_gpu* h, DevBuf& b, const void* src, size_t bytes)
+{
+    int rc = ensure(h, b, bytes);
+    if (rc) return rc;
+    if (bytes) CUDA_TRY(h, cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, h->st));
+    return LELPH_GPU_OK;
+}
+
+void mat_vec3(const double* M, const double* v, bool trans, double* out)
+{
+    if (trans)
+    {
+        out[0] = M[0] * v[0] + M[3] * v[1] + M[6] * v[2];
+        out[1] = M[1] * v[0] + M[4] * v[1] + M[7] * v[2];
+        out[2] = M[2] * v[0] + M[5] * v[1] + M[8] * v[2];
+    }
+    else
+    {
+        out[0] = M[0] * v[0] + M[1] * v[1] + M[2] * v[2];
+        out[1] = M[3] * v[0] + M[4] * v[1] + M[5] * v[2];
+        out[2] = M[6] * v[0] + M[7] * v[1] + M[8] * v[2];
+    }
+}
+
+double det3(const double* m)
+{
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+           m[2] * (m[7] * m[3] - m[4] * m[6]);
+}
+
+// SU(2) matrix of a rotation (Euler angles), -i sigma_y for time reversal:
+// the construction of SU2mat, src/wfc/su2mat.c:16-117
+bool su2mat(const double* sym_in, int nspinor, bool time_rev, std::complex<double>* u)
+{
+    typedef std::complex<double> C;
+    if (nspinor == 1)
+    {
+        u[0] = 1.0;
+        u[1] = u[2] = 0.0;
+        u[3] = 1.0;
+        return true;
+    }
+    double det = det3(sym_in);
+    if (std::fabs(std::fabs(det) - 1) > 1e-4) return false;
+    double s[9];
+    for (int i = 0; i < 9; ++i) s[i] = sym_in[i] / det;
+    double alpha, beta, delta;
+    if (std::fabs(s[6] + 1) < EPS_K)
+    {
+        alpha = 0;
+        beta = PI_T / 2.0;
+        delta = std::atan2(s[1], s[2]);
+    }
+    else if (std::fabs(s[6] - 1) < EPS_K)
+    {
+        alpha = 0;
+        beta = -PI_T / 2.0;
+        delta = std::atan2(-s[1], -s[2]);
+    }
+    else
+    {
+        beta = -std::asin(s[6]);
+        alpha = std::atan2(s[3] / std::cos(beta), s[0] / std::cos(beta));
+        delta = std::atan2(s[7] / std::cos(beta), s[8] / std::cos(beta));
+    }
+    alpha /= 2;
+    beta /= 2;
+    delta /= 2;
+    const C I(0, 1);
+    C p0[4] = {1, 0, 0, 1}, px[4] = {0, 1, 1, 0}, py[4] = {0, -I, I, 0}, pz[4] = {1, 0, 0, -1};
+    C sd[4], sb[4], sa[4], t[4];
+    for (int i = 0; i < 4; ++i)
+    {
+        sd[i] = std::cos(delta) * p0[i] - I * std::sin(delta) * px[i];
+        sb[i] = std::cos(beta) * p0[i] - I * std::sin(beta) * py[i];
+        sa[i] = std::cos(alpha) * p0[i] - I * std::sin(alpha) * pz[i];
+    }
+    auto mm = [](const C* a, const C* b, C* o) {
+        o[0] = a[0] * b[0] + a[1] * b[2];
+        o[1] = a[0] * b[1] + a[1] * b[3];
+        o[2] = a[2] * b[0] + a[3] * b[2];
+        o[3] = a[2] * b[1] + a[3] * b[3];
+    };
+    mm(sb, sd, t);
+    mm(sa, t, u);
+    if (time_rev)
+    {
+        C a1 = u[0], b1 = u[1], c1 = u[2], d1 = u[3];
+        u[0] = -c1;
+        u[1] = -d1;
+        u[2] = a1;
+        u[3] = b1;
+    }
+    return true;
+}
+
+bool plan_1d(int L, FftPlan1D& p)
+{
+    p.L = L;
+    p.nstage = 0;
+    int n = L;
+    while (n % 4 == 0 && p.nstage < LELPH_MAX_RADIX_STAGES)
+    {
+        p.radix[p.nstage++] = 4;
+        n /= 4;
+    }
+    const int rs[3] = {2, 3, 5};
+    for (int r : rs)
+        while (n % r == 0 && p.nstage < LELPH_MAX_RADIX_STAGES)
+        {
+            p.radix[p.nstage++] = r;
+            n /= r;
+        }
+    return n == 1;
+}
+
+float pow2_scale(double bound, double target)
+{
+    if (!(bound > 0)) return 1.0f;
+    int e = (int)std::floor(std::log2(target / bound));
+    if (e > 100) e = 100;
+    if (e < -100) e = -100;
+    return std::ldexp(1.0f, e);
+}
+
+// -------------------------------------------------------------- small kernels
+
+__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+// max over r (and spin rows s) of sum_{s'} |dV^{s s'}(r)| per mode -> atomicMax on float bits
+__global__ void k_dv_maxabs(const double2* __restrict__ dv, int nmodes, int nmag, long long N,
+                            unsigned* __restrict__ maxbits)
+{
+    const int nu = blockIdx.y;
+    const double2* d = dv + (size_t)nu * nmag * N;
+    float m = 0.f;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x)
+    {
+        double v;
+        if (nmag == 4)
+        {
+            double a0 = hypot(d[r].x, d[r].y) + hypot(d[N + r].x, d[N + r].y);
+            double a1 = hypot(d[2 * N + r].x, d[2 * N + r].y) + hypot(d[3 * N + r].x, d[3 * N + r].y);
+            v = fmax(a0, a1);
+        }
+        else
+        {
+            v = 0;
+            for (int c = 0; c < nmag; ++c) v = fmax(v, hypot(d[c * N + r].x, d[c * N + r].y));
+        }
+        m = fmaxf(m, (float)v);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&maxbits[nu], __float_as_uint(m));
+}
+
+__global__ void k_mode_scale(const unsigned* __restrict__ maxbits, int nmodes, float* __restrict__ scale)
+{
+    int nu = threadIdx.x;
+    if (nu < nmodes)
+    {
+        float m = __uint_as_float(maxbits[nu]) * 1.0001f;
+        // |dV s_nu| <= 2: together with |psi s_m| <= 2^14 the operand stays below 2^15
+        int e = m > 0.f ? (int)floorf(log2f(2.0f / m)) : 0;
+        scale[nu] = ldexpf(1.0f, e);
+    }
+}
+
+// tmp[a][b] = sum_c op(g)[a][c] conj(Dr[b][c]), op(g)[a][c] = g[c][a] (conj if trev)
+__global__ void k_qrot1(const double2* g, const double2* Dr, int nb, int nspin, int trev, double2* tmp)
+{
+    int mode = blockIdx.y, s = blockIdx.z;
+    const double2* gq = g + ((size_t)mode * nspin + s) * nb * nb;
+    const double2* D = Dr + (size_t)s * nb * nb;
+    double2* t = tmp + ((size_t)mode * nspin + s) * nb * nb;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * nb; e += gridDim.x * blockDim.x)
+    {
+        int a = e / nb, b = e - a * nb;
+        double2 acc = make_double2(0, 0);
+        for (int c = 0; c < nb; ++c)
+        {
+            double2 x = gq[(size_t)c * nb + a];
+            if (trev) x.y = -x.y;
+            acc = cadd(acc, cmul(x, cconj(D[(size_t)b * nb + c])));
+        }
+        t[e] = acc;
+    }
+}
+
+// out[i][j] = sum_k tmp[k][i] Dl[j][k]
+__global__ void k_qrot2(const double2* tmp, const double2* Dl, int nb, int nspin, double2* out)
+{
+    int mode = blockIdx.y, s = blockIdx.z;
+    const double2* t = tmp + ((size_t)mode * nspin + s) * nb * nb;
+    const double2* D = Dl + (size_t)s * nb * nb;
+    double2* o = out + ((size_t)mode * nspin + s) * nb * nb;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb * nb; e += gridDim.x * blockDim.x)
+    {
+        int i = e / nb, j = e - i * nb;
+        double2 acc = make_double2(0, 0);
+        for (int k = 0; k < nb; ++k) acc = cadd(acc, cmul(t[(size_t)k * nb + i], D[(size_t)j * nb + k]));
+        o[e] = acc;
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn)
+    {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+int make_tmap(lelph_gpu* h, CUtensorMap* m, void* base, unsigned long long inner, unsigned long long rows,
+              unsigned box_rows, bool swz)
+{
+    auto enc = get_encode();
+    if (!enc) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {inner, rows};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    return LELPH_GPU_OK;
+}
+
+int find_k(const lelph_gpu* h, const double* kpt)
+{
+    const int nk = h->d.nkpts_BZ;
+    for (int i = 0; i < nk; ++i)
+    {
+        double s = 0;
+        for (int x = 0; x < 3; ++x)
+        {
+            double dd = h->kbz_crys[3 * i + x] - kpt[x];
+            dd -= std::rint(dd);
+            s += dd * dd;
+        }
+        if (std::sqrt(s) < EPS_K) return i;
+    }
+    return -1;
+}
+
+int check_status(lelph_gpu* h)
+{
+    unsigned st = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    if (st & LELPH_DEV_ERR_TIMEOUT) return fail(h, LELPH_GPU_ERR_TIMEOUT, "a device-side wait ran out");
+    if (st) return fail(h, LELPH_GPU_ERR_CUDA, "device status " + std::to_string(st));
+    return LELPH_GPU_OK;
+}
+
+void tstart(lelph_gpu* h)
+{
+    if (h->profiling) cudaEventRecord(h->ev0, h->st);
+}
+double tstop(lelph_gpu* h)
+{
+    if (!h->profiling) return 0.0;
+    cudaEventRecord(h->ev1, h->st);
+    cudaEventSynchronize(h->ev1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    return ms;
+}
+
+NonlocalDesc nl_desc(lelph_gpu* h)
+{
+    NonlocalDesc nl;
+    nl.natom = h->d.natom;
+    nl.ntype = h->ntype;
+    nl.nltimesj = h->nltimesj;
+    nl.lmax = h->d.lmax;
+    nl.nproj_max = h->nproj_max;
+    nl.is_soc = h->d.is_soc_present;
+    nl.atom_type = (const int*)h->d_atype.p;
+    nl.atom_pos = (const double*)h->d_apos.p;
+    nl.PP_table = (const double*)h->d_pp.p;
+    nl.Fsign = (const double*)h->d_fsign.p;
+    nl.fcoef = h->d_fcoef.n > 16 ? (const double*)h->d_fcoef.p : nullptr;
+    nl.fcoef_off = (const int*)h->d_fcoefoff.p;
+    return nl;
+}
+}  // namespace
+
+// ====================================================================== API
+
+extern "C" const char* lelph_gpu_strerror(int s)
+{
+    switch (s)
+    {
+        case LELPH_GPU_OK: return "ok";
+        case LELPH_GPU_ERR_INVALID: return "invalid argument";
+        case LELPH_GPU_ERR_ALLOC: return "allocation failed";
+        case LELPH_GPU_ERR_CUDA: return "CUDA error";
+        case LELPH_GPU_ERR_TIMEOUT: return "device wait timed out";
+        case LELPH_GPU_ERR_GEOMETRY: return "inconsistent geometry (k+q, symmetry or FFT box)";
+        case LELPH_GPU_ERR_STATE: return "call order";
+        case LELPH_GPU_ERR_UNSUPPORTED: return "unsupported size";
+        default: return "unknown status";
+    }
+}
+
+extern "C" const char* lelph_gpu_last_error(lelph_gpu* h) { return h ? h->err.c_str() : "null context"; }
+
+extern "C" void* lelph_gpu_stream(lelph_gpu* h) { return h ? (void*)h->st : nullptr; }
+
+extern "C" int lelph_gpu_set_profiling(lelph_gpu* h, int on)
+{
+    if (!h) return LELPH_GPU_ERR_INVALID;
+    h->profiling = on != 0;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_stats_get(lelph_gpu* h, lelph_gpu_stats* s)
+{
+    if (!h || !s) return LELPH_GPU_ERR_INVALID;
+    *s = h->stats;
+    size_t tot = 0;
+    for (DevBuf* b : h->owned) tot += b->n;
+    s->device_bytes = tot;
+    return LELPH_GPU_OK;
+}
+
+extern "C" void lelph_gpu_destroy(lelph_gpu* h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (DevBuf* b : h->owned)
+        if (b->p) cudaFree(b->p);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+}
+
+static int upload_wfc(lelph_gpu* h, const double* const* wfc)
+{
+    const lelph_gpu_desc& d = h->d;
+    const int nsets = d.nspin * d.nbnds * d.nspinor;
+    for (int ik = 0; ik < d.nkpts_iBZ; ++ik)
+    {
+        if (!wfc[ik]) return fail(h, LELPH_GPU_ERR_INVALID, "null wavefunction pointer");
+        size_t bytes = sizeof(double2) * (size_t)nsets * h->npw[ik];
+        CUDA_TRY(h, cudaMemcpyAsync((char*)h->d_coef.p + sizeof(double2) * h->coef_off[ik], wfc[ik], bytes,
+                                    cudaMemcpyHostToDevice, h->st));
+    }
+    // power-of-two operand scales: |psi_b(r)| <= sum_G sum_s |c_b,s(G)| (L1 bound)
+    const int nb = d.nbnds;
+    std::vector<float> sc_ibz((size_t)d.nkpts_iBZ * d.nspin * nb);
+    for (int ik = 0; ik < d.nkpts_iBZ; ++ik)
+        for (int s = 0; s < d.nspin; ++s)
+            for (int b = 0; b < nb; ++b)
+            {
+                const double* c = wfc[ik] + 2 * ((size_t)(s * nb + b) * d.nspinor * h->npw[ik]);
+                double l1 = 0;
+                for (long long i = 0; i < (long long)d.nspinor * h->npw[ik]; ++i) l1 += std::hypot(c[2 * i], c[2 * i + 1]);
+                sc_ibz[((size_t)ik * d.nspin + s) * nb + b] = pow2_scale(l1 * 1.0001, 16384.0);
+            }
+    h->band_scale.resize((size_t)d.nkpts_BZ * d.nspin * nb);
+    for (int i = 0; i < d.nkpts_BZ; ++i)
+        for (int s = 0; s < d.nspin; ++s)
+            for (int b = 0; b < nb; ++b)
+                h->band_scale[((size_t)i * d.nspin + s) * nb + b] = sc_ibz[((size_t)h->ksym[i].ik * d.nspin + s) * nb + b];
+    int rc = upload(h, h->d_band_scale, h->band_scale.data(), sizeof(float) * h->band_scale.size());
+    if (rc) return rc;
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    h->prepared = false;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
+{
+    if (!desc || !out) return LELPH_GPU_ERR_INVALID;
+    *out = nullptr;
+    lelph_gpu* h = new (std::nothrow) lelph_gpu();
+    if (!h) return LELPH_GPU_ERR_ALLOC;
+    memset(&h->stats, 0, sizeof(h->stats));
+    h->d = *desc;
+    const lelph_gpu_desc& d = h->d;
+    auto bad = [&](int code, const std::string& m) {
+        fprintf(stderr, "lelph_gpu_create: %s\n", m.c_str());
+        lelph_gpu_destroy(h);
+        return code;
+    };
+    if (d.natom <= 0 || d.nsym <= 0 || d.nbnds <= 0 || d.nkpts_iBZ <= 0 || d.nkpts_BZ <= 0 || d.ntype <= 0 ||
+        d.nltimesj < 0 || d.lmax < 0 || d.lmax > 3)
+        return bad(LELPH_GPU_ERR_INVALID, "non-positive size");
+    if (d.nspin < 1 || d.nspin > 2 || d.nspinor < 1 || d.nspinor > 2) return bad(LELPH_GPU_ERR_INVALID, "nspin/nspinor");
+    if (!(d.nmag == 1 || d.nmag == 2 || d.nmag == 4)) return bad(LELPH_GPU_ERR_INVALID, "nmag");
+    if (d.nmag == 2 && (d.nspin != 2 || d.nspinor != 1)) return bad(LELPH_GPU_ERR_INVALID, "Incompatible dvscf");
+    if (d.nmag == 4 && d.nspinor != 2) return bad(LELPH_GPU_ERR_INVALID, "nmag 4 needs spinors");
+    if (d.nspin == 2 && d.nmag != 2) return bad(LELPH_GPU_ERR_INVALID, "nspin 2 needs nmag 2");
+    if (d.nmodes != 3 * d.natom) return bad(LELPH_GPU_ERR_INVALID, "nmodes != 3 natom");
+    if (3 * d.natom > 48) return bad(LELPH_GPU_ERR_UNSUPPORTED, "more than 16 atoms");
+    if (!d.alat_vec || !d.blat_vec || !d.atomic_pos || !d.atom_type || !d.kpt_iredBZ || !d.kpt_fullBZ_crys ||
+        !d.kmap || !d.sym_Rmat || !d.sym_tau || !d.sym_time_rev || !d.npw || !d.gvec || !d.wfc || !d.Fk ||
+        !d.PP_table || !d.Fsign)
+        return bad(LELPH_GPU_ERR_INVALID, "null input pointer");
+    if (d.precision < 0 || d.precision > 2) return bad(LELPH_GPU_ERR_INVALID, "precision");
+    h->mixed = d.precision != LELPH_GPU_FP64;
+    h->ab_bf16 = d.precision == LELPH_GPU_MIXED_BF16;
+    h->device = d.device;
+    for (int x = 0; x < 3; ++x)
+    {
+        if (d.fft_dims[x] <= 0 || !plan_1d(d.fft_dims[x], h->plan[x]))
+            return bad(LELPH_GPU_ERR_UNSUPPORTED, "FFT dimension must factor into 2, 3, 5");
+    }
+    const long long N = (long long)d.fft_dims[0] * d.fft_dims[1] * d.fft_dims[2];
+    h->g.Nx = d.fft_dims[0];
+    h->g.Ny = d.fft_dims[1];
+    h->g.Nz = d.fft_dims[2];
+    h->g.nspin = d.nspin;
+    h->g.nspinor = d.nspinor;
+    h->g.nbnds = d.nbnds;
+    h->g.nbp = (d.nbnds + 7) / 8 * 8;
+    h->g.nmag = d.nmag;
+    h->g.nmodes = d.nmodes;
+    if (h->mixed)
+    {
+        if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
+        if (2 * h->g.nbp > 256) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 128 bands");
+        if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
+    }
+    h->ntype = d.ntype;
+    h->nltimesj = d.nltimesj;
+    // host copies
+    h->alat.assign(d.alat_vec, d.alat_vec + 9);
+    h->blat.assign(d.blat_vec, d.blat_vec + 9);
+    h->kibz.assign(d.kpt_iredBZ, d.kpt_iredBZ + 3 * d.nkpts_iBZ);
+    h->kbz_crys.assign(d.kpt_fullBZ_crys, d.kpt_fullBZ_crys + 3 * d.nkpts_BZ);
+    h->kmap.assign(d.kmap, d.kmap + 2 * d.nkpts_BZ);
+    h->symR.assign(d.sym_Rmat, d.sym_Rmat + 9 * d.nsym);
+    h->symtau.assign(d.sym_tau, d.sym_tau + 3 * d.nsym);
+    h->symtr.assign(d.sym_time_rev, d.sym_time_rev + d.nsym);
+    h->atom_pos.assign(d.atomic_pos, d.atomic_pos + 3 * d.natom);
+    h->atom_type.assign(d.atom_type, d.atom_type + d.natom);
+    h->PP.assign(d.PP_table, d.PP_table + 3 * d.nltimesj * d.ntype);
+    h->Fsign.assign(d.Fsign, d.Fsign + d.nltimesj * d.ntype);
+    h->npw.assign(d.npw, d.npw + d.nkpts_iBZ);
+    for (int a = 0; a < d.natom; ++a)
+        if (h->atom_type[a] < 0 || h->atom_type[a] >= d.ntype) return bad(LELPH_GPU_ERR_INVALID, "atom_type");
+    // projectors per type
+    h->nproj_max = 0;
+    for (int t = 0; t < d.ntype; ++t)
+    {
+        int np = 0;
+        for (int l = 0; l < d.nltimesj; ++l)
+        {
+            int ll = (int)std::rint(h->PP[3 * (l * d.ntype + t)] - 1);
+            if (ll > 3) return bad(LELPH_GPU_ERR_UNSUPPORTED, "l > 3");
+            if (ll >= 0) np += 2 * ll + 1;
+        }
+        h->nproj_max = std::max(h->nproj_max, np);
+    }
+    if (h->nproj_max > 24) return bad(LELPH_GPU_ERR_UNSUPPORTED, "more than 24 projectors per atom");
+    if (h->nproj_max == 0) h->nproj_max = 1;
+    // Miller indices of every iBZ plane wave: n = rint(alat^T G)
+    h->pw_off.resize(d.nkpts_iBZ);
+    h->coef_off.resize(d.nkpts_iBZ);
+    h->fk_off.resize(d.nkpts_iBZ);
+    long long tot = 0, ctot = 0, ftot = 0;
+    const int nsets = d.nspin * d.nbnds * d.nspinor;
+    for (int ik = 0; ik < d.nkpts_iBZ; ++ik)
+    {
+        if (h->npw[ik] <= 0 || !d.gvec[ik] || !d.Fk[ik]) return bad(LELPH_GPU_ERR_INVALID, "npw / gvec / Fk");
+        h->pw_off[ik] = tot;
+        h->coef_off[ik] = ctot;
+        h->fk_off[ik] = ftot;
+        tot += h->npw[ik];
+        ctot += (long long)nsets * h->npw[ik];
+        ftot += (long long)d.nltimesj * d.ntype * h->npw[ik];
+    }
+    h->total_pw = tot;
+    h->miller.resize(3 * tot);
+    std::vector<double> gall(3 * tot), fall(ftot);
+    for (int ik = 0; ik < d.nkpts_iBZ; ++ik)
+    {
+        for (int g = 0; g < h->npw[ik]; ++g)
+        {
+            double c[3];
+            mat_vec3(d.alat_vec, d.gvec[ik] + 3 * g, true, c);
+            for (int x = 0; x < 3; ++x)
+            {
+                double r = std::rint(c[x]);
+                if (std::fabs(c[x] - r) > 1e-4) return bad(LELPH_GPU_ERR_GEOMETRY, "G vector not on the reciprocal lattice");
+                h->miller[3 * (h->pw_off[ik] + g) + x] = (int)r;
+                gall[3 * (h->pw_off[ik] + g) + x] = d.gvec[ik][3 * g + x];
+            }
+        }
+        memcpy(fall.data() + h->fk_off[ik], d.Fk[ik], sizeof(double) * d.nltimesj * d.ntype * h->npw[ik]);
+    }
+    // per full-BZ k symmetry data
+    double B[9];
+    for (int i = 0; i < 9; ++i) B[i] = d.blat_vec[i] / (2 * PI_T);
+    h->ksym.resize(d.nkpts_BZ);
+    std::vector<int> maxabs(3, 0);
+    for (int i = 0; i < d.nkpts_BZ; ++i)
+    {
+        KPointSym& ks = h->ksym[i];
+        memset(&ks, 0, sizeof(ks));
+        ks.ik = h->kmap[2 * i];
+        ks.isym = h->kmap[2 * i + 1];
+        if (ks.ik < 0 || ks.ik >= d.nkpts_iBZ || ks.isym < 0 || ks.isym >= d.nsym)
+            return bad(LELPH_GPU_ERR_INVALID, "kmap out of range");
+        const double* R = &h->symR[9 * ks.isym];
+        const double* tau = &h->symtau[3 * ks.isym];
+        ks.trev = h->symtr[ks.isym] != 0;
+        memcpy(ks.R, R, sizeof(ks.R));
+        memcpy(ks.tau_cart, tau, sizeof(ks.tau_cart));
+        // W = alat^T R A^{-T},  A^{-T} = blat / (2 pi)
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+            {
+                double acc = 0;
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) acc += d.alat_vec[3 * k + r] * R[3 * k + l] * B[3 * l + c];
+                double w = std::rint(acc);
+                if (std::fabs(acc - w) > 1e-6) return bad(LELPH_GPU_ERR_GEOMETRY, "symmetry not integral on the reciprocal lattice");
+                ks.W[3 * r + c] = (int)w;
+            }
+        double tc[3];
+        mat_vec3(d.blat_vec, tau, true, tc);
+        for (int x = 0; x < 3; ++x) ks.tau_crys[x] = tc[x] / (2 * PI_T);
+        double kr[3], kc[3];
+        mat_vec3(R, &h->kibz[3 * ks.ik], false, kr);
+        mat_vec3(d.alat_vec, kr, true, kc);
+        double dot = kc[0] * ks.tau_crys[0] + kc[1] * ks.tau_crys[1] + kc[2] * ks.tau_crys[2];
+        std::complex<double> kp = std::exp(std::complex<double>(0, -2 * PI_T * dot));
+        ks.kphase[0] = kp.real();
+        ks.kphase[1] = kp.imag();
+        memcpy(ks.kcart, &h->kibz[3 * ks.ik], sizeof(ks.kcart));
+        std::complex<double> u[4];
+        if (!su2mat(R, d.nspinor, ks.trev, u)) return bad(LELPH_GPU_ERR_GEOMETRY, "Wrong symmetric matrices");
+        for (int e = 0; e < 4; ++e)
+        {
+            ks.su2[2 * e] = u[e].real();
+            ks.su2[2 * e + 1] = u[e].imag();
+        }
+        // box fit of the rotated sphere (one extra unit for the umklapp shift)
+        for (int g = 0; g < h->npw[ks.ik]; ++g)
+        {
+            const int* n = &h->miller[3 * (h->pw_off[ks.ik] + g)];
+            for (int r = 0; r < 3; ++r)
+            {
+                int v = std::abs(ks.W[3 * r] * n[0] + ks.W[3 * r + 1] * n[1] + ks.W[3 * r + 2] * n[2]) + 1;
+                maxabs[r] = std::max(maxabs[r], v);
+            }
+        }
+    }
+    for (int r = 0; r < 3; ++r)
+        if (2 * maxabs[r] >= d.fft_dims[r]) return bad(LELPH_GPU_ERR_GEOMETRY, "FFT box too small for the plane-wave sphere");
+    // chat offsets per full-BZ k
+    h->chat_off.resize(d.nkpts_BZ);
+    long long chtot = 0;
+    for (int i = 0; i < d.nkpts_BZ; ++i)
+    {
+        h->chat_off[i] = chtot;
+        chtot += (long long)nsets * h->npw[h->ksym[i].ik];
+    }
+
+    // ---- device
+    if (cudaSetDevice(h->device) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "cudaSetDevice");
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "stream");
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    DevBuf* bufs[] = {&h->d_miller, &h->d_pwoff, &h->d_npw, &h->d_coef, &h->d_coefoff, &h->d_gvec, &h->d_fk,
+                      &h->d_fkoff, &h->d_ksym, &h->d_chat, &h->d_chatoff, &h->d_psi64, &h->d_boxes32, &h->d_bsplit,
+                      &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
+                      &h->d_fcoefoff, &h->d_tw64[0], &h->d_tw64[1], &h->d_tw64[2], &h->d_tw32[0], &h->d_tw32[1],
+                      &h->d_tw32[2], &h->d_dv64, &h->d_dv32, &h->d_dvstage, &h->d_eig, &h->d_mode_scale,
+                      &h->d_maxabs, &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp};
+    for (DevBuf* b : bufs) h->owned.push_back(b);
+    int rc = 0;
+#define UP(buf, ptr, bytes)                              \
+    do                                                   \
+    {                                                    \
+        rc = upload(h, buf, ptr, bytes);                 \
+        if (rc) return bad(rc, h->err);                  \
+    } while (0)
+    UP(h->d_miller, h->miller.data(), sizeof(int) * h->miller.size());
+    UP(h->d_pwoff, h->pw_off.data(), sizeof(long long) * h->pw_off.size());
+    UP(h->d_npw, h->npw.data(), sizeof(int) * h->npw.size());
+    UP(h->d_coefoff, h->coef_off.data(), sizeof(long long) * h->coef_off.size());
+    UP(h->d_gvec, gall.data(), sizeof(double) * gall.size());
+    UP(h->d_fk, fall.data(), sizeof(double) * fall.size());
+    UP(h->d_fkoff, h->fk_off.data(), sizeof(long long) * h->fk_off.size());
+    UP(h->d_ksym, h->ksym.data(), sizeof(KPointSym) * h->ksym.size());
+    UP(h->d_chatoff, h->chat_off.data(), sizeof(long long) * h->chat_off.size());
+    UP(h->d_atype, h->atom_type.data(), sizeof(int) * h->atom_type.size());
+    UP(h->d_apos, h->atom_pos.data(), sizeof(double) * h->atom_pos.size());
+    UP(h->d_pp, h->PP.data(), sizeof(double) * h->PP.size());
+    UP(h->d_fsign, h->Fsign.data(), sizeof(double) * h->Fsign.size());
+    // fCoeff packing: offsets in complex units, -1 where absent
+    {
+        std::vector<int> off(std::max(1, d.nltimesj * d.ntype), -1);
+        std::vector<double> pack;
+        if (d.fCoeff)
+        {
+            for (int i = 0; i < d.nltimesj * d.ntype; ++i)
+            {
+                if (!d.fCoeff[i]) continue;
+                int lidx = i / d.ntype, t = i % d.ntype;
+                int l = (int)std::rint(h->PP[3 * (lidx * d.ntype + t)] - 1);
+                if (l < 0) continue;
+                size_t n = (size_t)(2 * l + 1) * (2 * l + 1) * d.nspinor * d.nspinor;
+                off[i] = (int)(pack.size() / 2);
+                pack.insert(pack.end(), d.fCoeff[i], d.fCoeff[i] + 2 * n);
+            }
+        }
+        if (pack.empty()) pack.assign(2, 0.0);
+        UP(h->d_fcoef, pack.data(), sizeof(double) * pack.size());
+        if (pack.size() == 2) h->d_fcoef.n = 16;  // marks "no coefficients"
+        UP(h->d_fcoefoff, off.data(), sizeof(int) * off.size());
+    }
+    // twiddles e^{+2 pi i t / L}
+    for (int x = 0; x < 3; ++x)
+    {
+        int L = d.fft_dims[x];
+        std::vector<double2> t64(L);
+        std::vector<float2> t32(L);
+        for (int t = 0; t < L; ++t)
+        {
+            long double ang = 6.283185307179586476925286766559005768L * (long double)t / (long double)L;
+            t64[t] = make_double2((double)cosl(ang), (double)sinl(ang));
+            t32[t] = make_float2((float)cosl(ang), (float)sinl(ang));
+        }
+        UP(h->d_tw64[x], t64.data(), sizeof(double2) * L);
+        UP(h->d_tw32[x], t32.data(), sizeof(float2) * L);
+    }
+    rc = ensure(h, h->d_coef, sizeof(double2) * (size_t)ctot);
+    if (rc) return bad(rc, h->err);
+    rc = ensure(h, h->d_chat, sizeof(double2) * (size_t)chtot);
+    if (rc) return bad(rc, h->err);
+    rc = ensure(h, h->d_proj, sizeof(double2) * (size_t)d.nkpts_BZ * d.natom * h->nproj_max * 4 * nsets);
+    if (rc) return bad(rc, h->err);
+    rc = ensure(h, h->d_status, 64);
+    if (rc) return bad(rc, h->err);
+    if (cudaMemsetAsync(h->d_status.p, 0, 64, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
+    if (h->mixed)
+    {
+        const size_t Kr = 2 * (size_t)d.nspinor * N;
+        const size_t rows = (size_t)d.nkpts_BZ * d.nspin * 2 * 2 * h->g.nbp;
+        rc = ensure(h, h->d_bsplit, sizeof(uint16_t) * Kr * rows);
+        if (rc) return bad(rc, h->err);
+        if (cudaMemsetAsync(h->d_bsplit.p, 0, h->d_bsplit.n, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
+        rc = make_tmap(h, &h->tmapB, h->d_bsplit.p, Kr, rows, 2 * h->g.nbp, true);
+        if (rc) return bad(rc, h->err);
+        rc = make_tmap(h, &h->tmapA, h->d_bsplit.p, Kr, rows, h->g.nbp, false);
+        if (rc) return bad(rc, h->err);
+        // K chunk per CTA: a multiple of 32 grid points dividing nspinor*N, near 4096
+        long long Ktot = (long long)d.nspinor * N;
+        long long units = Ktot / TC_KPTS_HOST;
+        long long best = 1;
+        for (long long c = 1; c <= units; ++c)
+            if (units % c == 0 && c * TC_KPTS_HOST <= 4096) best = c;
+        h->chunk_pts = (int)(best * TC_KPTS_HOST);
+        h->nchunks = (int)(Ktot / h->chunk_pts);
+    }
+    rc = upload_wfc(h, d.wfc);
+    if (rc) return bad(rc, h->err);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "sync");
+    *out = h;
+    return LELPH_GPU_OK;
+#undef UP
+}
+
+extern "C" int lelph_gpu_set_wavefunctions(lelph_gpu* h, const double* const* wfc)
+{
+    if (!h || !wfc) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    return upload_wfc(h, wfc);
+}
+
+extern "C" int lelph_gpu_prepare(lelph_gpu* h)
+{
+    if (!h) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    const long long N = (long long)g.Nx * g.Ny * g.Nz;
+    const int nbox_per_k = d.nspin * d.nbnds * d.nspinor;
+    tstart(h);
+    int rc;
+    if (!h->mixed)
+    {
+        size_t bytes = sizeof(double2) * (size_t)d.nkpts_BZ * nbox_per_k * N;
+        rc = ensure(h, h->d_psi64, bytes);
+        if (rc) return rc;
+        CUDA_TRY(h, cudaMemsetAsync(h->d_psi64.p, 0, bytes, h->st));
+        lelph_launch_scatter(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
+                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double2*)h->d_coef.p,
+                             (const long long*)h->d_coefoff.p, g, 1, h->d_psi64.p, (double2*)h->d_chat.p,
+                             (const long long*)h->d_chatoff.p, h->st);
+        const long long nbox = (long long)d.nkpts_BZ * nbox_per_k;
+        double2* psi = (double2*)h->d_psi64.p;
+        lelph_launch_fft_contig_d(psi, nbox * g.Nx * g.Ny, h->plan[2], (const double2*)h->d_tw64[2].p, +1, h->st);
+        lelph_launch_fft_strided_d(psi, nbox * g.Nx, g.Nz, h->plan[1], (const double2*)h->d_tw64[1].p, +1, h->st);
+        lelph_launch_fft_strided_d(psi, nbox, g.Ny * g.Nz, h->plan[0], (const double2*)h->d_tw64[0].p, +1, h->st);
+        h->stats.kernel_launches += 4;
+    }
+    else
+    {
+        // FP32 boxes in chunks of k-points (<= ~4 GB of boxes)
+        const size_t per_k = sizeof(float2) * (size_t)nbox_per_k * N;
+        int nkc = (int)std::max<size_t>(1, std::min<size_t>((size_t)d.nkpts_BZ, (4ull << 30) / per_k));
+        rc = ensure(h, h->d_boxes32, per_k * nkc);
+        if (rc) return rc;
+        for (int k0 = 0; k0 < d.nkpts_BZ; k0 += nkc)
+        {
+            int nk = std::min(nkc, d.nkpts_BZ - k0);
+            CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
+            lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
+                                 (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double2*)h->d_coef.p,
+                                 (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p, (double2*)h->d_chat.p,
+                                 (const long long*)h->d_chatoff.p, h->st);
+            const long long nbox = (long long)nk * nbox_per_k;
+            float2* bx = (float2*)h->d_boxes32.p;
+            lelph_launch_fft_contig_f(bx, nbox * g.Nx * g.Ny, h->plan[2], (const float2*)h->d_tw32[2].p, +1, h->st);
+            lelph_launch_fft_strided_f(bx, nbox * g.Nx, g.Nz, h->plan[1], (const float2*)h->d_tw32[1].p, +1, h->st);
+            lelph_launch_fft_x_to_split(bx, nk, k0, h->plan[0], (const float2*)h->d_tw32[0].p, +1, g,
+                                        (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p, h->st);
+            h->stats.kernel_launches += 4;
+        }
+    }
+    NonlocalDesc nl = nl_desc(h);
+    lelph_launch_projections(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
+                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double*)h->d_fk.p,
+                             (const long long*)h->d_fkoff.p, (const double2*)h->d_chat.p,
+                             (const long long*)h->d_chatoff.p, nl, g, h->mixed ? 1 : 0, (double2*)h->d_proj.p, h->st);
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    h->stats.prepare_ms += tstop(h);
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    h->prepared = true;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                               const double* dVscf)
+{
+    if (!h || slot < 0 || !qpt_crys || !eigVec || !dVscf) return LELPH_GPU_ERR_INVALID;
+    if (slot > 4096) return fail(h, LELPH_GPU_ERR_INVALID, "slot index too large");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const lelph_gpu_desc& d = h->d;
+    const long long N = (long long)h->g.Nx * h->g.Ny * h->g.Nz;
+    const size_t dvn = (size_t)d.nmodes * d.nmag * N;
+    if (slot >= h->nslots_alloc)
+    {
+        // grow the slot arrays, keeping the loaded slots
+        int ns = std::max(slot + 1, 2 * h->nslots_alloc);
+        DevBuf nd64, nd32, neig, nsc;
+        int rc;
+        if (!h->mixed)
+        {
+            rc = ensure(h, nd64, sizeof(double2) * dvn * ns);
+            if (rc) return rc;
+            if (h->d_dv64.p) CUDA_TRY(h, cudaMemcpyAsync(nd64.p, h->d_dv64.p, sizeof(double2) * dvn * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
+        }
+        else
+        {
+            rc = ensure(h, nd32, sizeof(float2) * dvn * ns);
+            if (rc) return rc;
+            if (h->d_dv32.p) CUDA_TRY(h, cudaMemcpyAsync(nd32.p, h->d_dv32.p, sizeof(float2) * dvn * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
+        }
+        rc = ensure(h, neig, sizeof(double2) * d.nmodes * d.nmodes * ns);
+        if (rc) return rc;
+        rc = ensure(h, nsc, sizeof(float) * d.nmodes * ns);
+        if (rc) return rc;
+        if (h->d_eig.p) CUDA_TRY(h, cudaMemcpyAsync(neig.p, h->d_eig.p, sizeof(double2) * d.nmodes * d.nmodes * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
+        if (h->d_mode_scale.p) CUDA_TRY(h, cudaMemcpyAsync(nsc.p, h->d_mode_scale.p, sizeof(float) * d.nmodes * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
+        CUDA_TRY(h, cudaStreamSynchronize(h->st));
+        for (DevBuf* b : {&h->d_dv64, &h->d_dv32, &h->d_eig, &h->d_mode_scale})
+            if (b->p) cudaFree(b->p);
+        h->d_dv64 = nd64;
+        h->d_dv32 = nd32;
+        h->d_eig = neig;
+        h->d_mode_scale = nsc;
+        h->nslots_alloc = ns;
+        h->qslots.resize(ns);
+    }
+    QSlot& q = h->qslots[slot];
+    memcpy(q.q, qpt_crys, sizeof(q.q));
+    CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_eig.p + (size_t)slot * d.nmodes * d.nmodes, eigVec,
+                                sizeof(double2) * d.nmodes * d.nmodes, cudaMemcpyHostToDevice, h->st));
+    if (!h->mixed)
+    {
+        CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_dv64.p + (size_t)slot * dvn, dVscf, sizeof(double2) * dvn,
+                                    cudaMemcpyHostToDevice, h->st));
+    }
+    else
+    {
+        int rc = ensure(h, h->d_dvstage, sizeof(double2) * dvn);
+        if (rc) return rc;
+        rc = ensure(h, h->d_maxabs, sizeof(unsigned) * d.nmodes);
+        if (rc) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_dvstage.p, dVscf, sizeof(double2) * dvn, cudaMemcpyHostToDevice, h->st));
+        CUDA_TRY(h, cudaMemsetAsync(h->d_maxabs.p, 0, sizeof(unsigned) * d.nmodes, h->st));
+        k_dv_convert<<<1024, 256, 0, h->st>>>((const double2*)h->d_dvstage.p, (float2*)h->d_dv32.p + (size_t)slot * dvn,
+                                              (long long)dvn);
+        k_dv_maxabs<<<dim3(64, d.nmodes), 256, 0, h->st>>>((const double2*)h->d_dvstage.p, d.nmodes, d.nmag, N,
+                                                          (unsigned*)h->d_maxabs.p);
+        k_mode_scale<<<1, 64, 0, h->st>>>((const unsigned*)h->d_maxabs.p, d.nmodes,
+                                          (float*)h->d_mode_scale.p + (size_t)slot * d.nmodes);
+        h->stats.kernel_launches += 3;
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    q.set = true;
+    return LELPH_GPU_OK;
+}
+
+static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq, int out_type,
+                    void* g_out, bool out_device)
+{
+    if (!h || n < 0 || (n > 0 && (!qslot || !kbz || !g_out))) return LELPH_GPU_ERR_INVALID;
+    if (out_type != LELPH_GPU_OUT_C128 && out_type != LELPH_GPU_OUT_C64) return fail(h, LELPH_GPU_ERR_INVALID, "out_type");
+    if (n == 0) return LELPH_GPU_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    if (!h->prepared)
+    {
+        int rc = lelph_gpu_prepare(h);
+        if (rc) return rc;
+    }
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    // pairs (src/elph/compute_elph_matq.c:65-128)
+    std::vector<PairInfo> pairs(n);
+    for (int i = 0; i < n; ++i)
+    {
+        if (qslot[i] < 0 || qslot[i] >= (int)h->qslots.size() || !h->qslots[qslot[i]].set)
+            return fail(h, LELPH_GPU_ERR_STATE, "q slot not loaded");
+        if (kbz[i] < 0 || kbz[i] >= d.nkpts_BZ) return fail(h, LELPH_GPU_ERR_INVALID, "k index out of range");
+        const double* q = h->qslots[qslot[i]].q;
+        double qt[3], kq[3];
+        for (int x = 0; x < 3; ++x) qt[x] = kminusq ? -q[x] : q[x];
+        for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * kbz[i] + x] + qt[x];
+        int ikq = find_k(h, kq);
+        if (ikq < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
+        int idx_k = kbz[i], idx_kq = ikq;
+        if (kminusq) std::swap(idx_k, idx_kq);
+        PairInfo& P = pairs[i];
+        P.kbz_k = idx_k;
+        P.kbz_kq = idx_kq;
+        P.qslot = qslot[i];
+        // umklapp G0 = S_kq k_kq - S_k k - q (src/dvloc/compute_Vbare_loc.c:93-144)
+        const KPointSym& sk = h->ksym[idx_k];
+        const KPointSym& skq = h->ksym[idx_kq];
+        double tkq[3], tk[3], qc[3], ulm[3], uc[3];
+        mat_vec3(skq.R, &h->kibz[3 * skq.ik], false, tkq);
+        mat_vec3(sk.R, &h->kibz[3 * sk.ik], false, tk);
+        mat_vec3(h->blat.data(), q, false, qc);
+        for (int x = 0; x < 3; ++x) ulm[x] = (tkq[x] - tk[x]) - qc[x] / (2 * PI_T);
+        mat_vec3(h->alat.data(), ulm, true, uc);
+        for (int x = 0; x < 3; ++x)
+        {
+            double r = std::rint(uc[x]);
+            if (std::fabs(uc[x] - r) > 1e-3) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
+            P.ulm[x] = (int)r;
+        }
+    }
+    int rc = upload(h, h->d_pairs, pairs.data(), sizeof(PairInfo) * n);
+    if (rc) return rc;
+    const size_t gsz = (size_t)d.nmodes * d.nspin * d.nbnds * d.nbnds;
+    const size_t esz = out_type == LELPH_GPU_OUT_C64 ? sizeof(float2) : sizeof(double2);
+    void* gdev = g_out;
+    if (!out_device)
+    {
+        rc = ensure(h, h->d_gout, esz * gsz * n);
+        if (rc) return rc;
+        gdev = h->d_gout.p;
+    }
+    NonlocalDesc nl = nl_desc(h);
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+    const int nrows = d.nmodes * d.nbnds;
+    // batch the pairs so the local workspace stays bounded (~4 GB)
+    size_t per_pair;
+    if (!h->mixed) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
+    else per_pair = sizeof(float) * (size_t)d.nspin * ((nrows + 127) / 128) * h->nchunks * 128 * 2 * g.nbp;
+    int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, (4ull << 30) / per_pair));
+    rc = ensure(h, h->mixed ? h->d_partials : h->d_glocal, per_pair * batch);
+    if (rc) return rc;
+    for (int p0 = 0; p0 < n; p0 += batch)
+    {
+        int nb = std::min(batch, n - p0);
+        const PairInfo* dp = (const PairInfo*)h->d_pairs.p + p0;
+        tstart(h);
+        if (!h->mixed)
+            lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_dv64.p, g,
+                                    (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
+        else
+            lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapA, (const float2*)h->d_dv32.p,
+                                  (const float*)h->d_mode_scale.p, g, h->ab_bf16, h->chunk_pts, h->nchunks,
+                                  (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st);
+        h->stats.local_ms += tstop(h);
+        h->stats.local_launches += 1;
+        tstart(h);
+        lelph_launch_finish(dp, nb, h->mixed ? 0 : 1, (const double2*)h->d_glocal.p, (const float*)h->d_partials.p,
+                            h->nchunks, (const float*)h->d_mode_scale.p, (const float*)h->d_band_scale.p,
+                            (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
+                            out_type == LELPH_GPU_OUT_C64, (char*)gdev + esz * gsz * p0, h->st);
+        h->stats.finish_ms += tstop(h);
+        h->stats.kernel_launches += 2;
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    if (!out_device) CUDA_TRY(h, cudaMemcpyAsync(g_out, gdev, esz * gsz * n, cudaMemcpyDeviceToHost, h->st));
+    rc = check_status(h);
+    if (rc) return rc;
+    h->stats.pairs_done += n;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_run(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
+                             int out_type, void* g_out)
+{
+    return run_impl(h, n, qslot, kbz, non_loc, kminusq, out_type, g_out, false);
+}
+
+extern "C" int lelph_gpu_run_device(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
+                                    int out_type, void* g_out_dev)
+{
+    return run_impl(h, n, qslot, kbz, non_loc, kminusq, out_type, g_out_dev, true);
+}
+
+extern "C" int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec,
+                                       const double* dVscfq, int non_loc, int kminusq, double* elph_out)
+{
+    if (!h) return LELPH_GPU_ERR_INVALID;
+    int rc = lelph_gpu_set_q(h, 0, qpt_crys, eigVec, dVscfq);
+    if (rc) return rc;
+    std::vector<int> qs(h->d.nkpts_BZ, 0), ks(h->d.nkpts_BZ);
+    for (int i = 0; i < h->d.nkpts_BZ; ++i) ks[i] = i;
+    return lelph_gpu_run(h, h->d.nkpts_BZ, qs.data(), ks.data(), non_loc, kminusq, LELPH_GPU_OUT_C128, elph_out);
+}
+
+extern "C" int lelph_gpu_elph_q_rotate(lelph_gpu* h, const double* Dl, const double* g, const double* Dr,
+                                       int time_rev, double* out)
+{
+    if (!h || !Dl || !g || !Dr || !out) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const int nb = h->d.nbnds, ns = h->d.nspin, nm = h->d.nmodes;
+    const size_t gs = (size_t)nm * ns * nb * nb, ds = (size_t)ns * nb * nb;
+    int rc = ensure(h, h->d_tmp, sizeof(double2) * (3 * gs + 2 * ds));
+    if (rc) return rc;
+    double2* dg = (double2*)h->d_tmp.p;
+    double2* dt = dg + gs;
+    double2* dout = dt + gs;
+    double2* ddl = dout + gs;
+    double2* ddr = ddl + ds;
+    CUDA_TRY(h, cudaMemcpyAsync(dg, g, sizeof(double2) * gs, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(ddl, Dl, sizeof(double2) * ds, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(ddr, Dr, sizeof(double2) * ds, cudaMemcpyHostToDevice, h->st));
+    dim3 grid((nb * nb + 255) / 256, nm, ns);
+    k_qrot1<<<grid, 256, 0, h->st>>>(dg, ddr, nb, ns, time_rev != 0, dt);
+    k_qrot2<<<grid, 256, 0, h->st>>>(dt, ddl, nb, ns, dout);
+    h->stats.kernel_launches += 2;
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(out, dout, sizeof(double2) * gs, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_debug_gvec_map(lelph_gpu* h, int kbz, const int ulm[3], int* out)
+{
+    if (!h || !out || kbz < 0 || kbz >= h->d.nkpts_BZ) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    int npw = h->npw[h->ksym[kbz].ik];
+    int rc = ensure(h, h->d_tmp, sizeof(int) * (3 * (size_t)npw + 4));
+    if (rc) return rc;
+    int u[3] = {ulm ? ulm[0] : 0, ulm ? ulm[1] : 0, ulm ? ulm[2] : 0};
+    int* dt = (int*)h->d_tmp.p;
+    CUDA_TRY(h, cudaMemcpyAsync(dt, u, sizeof(u), cudaMemcpyHostToDevice, h->st));
+    lelph_launch_gmap((const KPointSym*)h->d_ksym.p, kbz, (const int*)h->d_miller.p, (const long long*)h->d_pwoff.p,
+                      (const int*)h->d_npw.p, h->g, dt, dt + 4, h->st);
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(out, dt + 4, sizeof(int) * 3 * npw, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}

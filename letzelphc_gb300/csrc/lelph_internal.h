@@ -1,0 +1,97 @@
+// Internal launch interface shared by the .cu translation units of the
+// electron-phonon library (not part of the public C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define LELPH_MAX_RADIX_STAGES 12
+#define TC_KPTS_HOST 32  // grid points per pipeline stage of the tensor-core sandwich
+
+// One 1-D transform length L = prod(radix[0..nstage)), radices in {2,3,4,5}.
+struct FftPlan1D
+{
+    int L;
+    int nstage;
+    int radix[LELPH_MAX_RADIX_STAGES];
+};
+
+// Per full-BZ k-point symmetry data (host-computed, FP64).
+struct KPointSym
+{
+    int ik;          // iBZ index
+    int isym;        // symmetry index
+    int trev;        // time-reversal symmetry
+    int W[9];        // integer action on Miller indices (row-major)
+    double R[9];     // cartesian rotation (row-major, v' = R v)
+    double tau_crys[3];
+    double tau_cart[3];
+    double kphase[2];  // exp(-i 2 pi kvec_crys . tau_crys), kvec_crys = alat^T R k_iBZ
+    double kcart[3];   // k_iBZ (cart)
+    double su2[8];     // 2x2 complex spinor rotation (re, im interleaved)
+};
+
+// One (k, k+q) pair of a run.
+struct PairInfo
+{
+    int kbz_k;   // full-BZ index of the k wavefunction
+    int kbz_kq;  // full-BZ index of the k+q wavefunction
+    int ulm[3];  // umklapp G0 (crystal) applied to the k+q wavefunction
+    int qslot;   // q slot (dV, eigVec)
+};
+
+struct GeomDev
+{
+    int Nx, Ny, Nz;
+    int nspin, nspinor, nbnds, nbp, nmag, nmodes;
+};
+
+// FFT (fft_gather.cu)
+void lelph_launch_fft_contig_d(double2* data, long long nlines, const FftPlan1D& p, const double2* tw, int sign,
+                               cudaStream_t st);
+void lelph_launch_fft_contig_f(float2* data, long long nlines, const FftPlan1D& p, const float2* tw, int sign,
+                               cudaStream_t st);
+void lelph_launch_fft_strided_d(double2* data, long long nouter, int inner, const FftPlan1D& p, const double2* tw,
+                                int sign, cudaStream_t st);
+void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const FftPlan1D& p, const float2* tw,
+                                int sign, cudaStream_t st);
+// x-pass of the mixed form writing the split tensor-core operand directly
+void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
+                                 int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
+                                 cudaStream_t st);
+
+// sphere -> box scatter with su2, fractional-translation phase and conj
+void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
+                          const int* npw, const double2* coef, const long long* coef_off, const GeomDev& g,
+                          int box_fp64, void* boxes, double2* chat, const long long* chat_off, cudaStream_t st);
+
+// debugging / parity: box index of each rotated plane wave of one full-BZ k
+void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,
+                       const GeomDev& g, const int* ulm, int* out, cudaStream_t st);
+
+// local sandwich (sandwich.cu)
+void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* psi, const double2* dV,
+                             const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st);
+int lelph_local_tc_smem_bytes(const GeomDev& g);
+void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
+                           const float2* dV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
+                           int nchunks, float* partials, unsigned* status, cudaStream_t st);
+
+// nonlocal + finish (nonlocal.cu)
+struct NonlocalDesc
+{
+    int natom, ntype, nltimesj, lmax, nproj_max, is_soc;
+    const int* atom_type;    // natom
+    const double* atom_pos;  // natom*3 cart
+    const double* PP_table;  // nltimesj*ntype*3
+    const double* Fsign;     // nltimesj*ntype
+    const double* fcoef;     // packed (see host), may be null
+    const int* fcoef_off;    // per lidx*ntype+itype, -1 if none
+};
+void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const double* gvec, const long long* pw_off,
+                              const int* npw, const double* Fk, const long long* fk_off, const double2* chat,
+                              const long long* chat_off, const NonlocalDesc& nl, const GeomDev& g, int f32acc,
+                              double2* proj, cudaStream_t st);
+void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const double2* glocal,
+                         const float* partials, int nchunks, const float* mode_scale, const float* band_scale,
+                         const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,
+                         const GeomDev& g, int out_c64, void* gout, cudaStream_t st);

@@ -1,0 +1,529 @@
+// Local dV sandwich <psi_{m,k+q} | dV_nu | psi_{n,k}> in real space.
+//
+// The reference forms dV*psi_k on the FFT box, transforms it forward, keeps
+// the k+q sphere and contracts with the k+q coefficients
+// (src/dvloc/compute_Vbare_loc.c:286-341, src/fft/convolution.c:13-189).
+// With psi(r) the unnormalised inverse transform of the zero-padded sphere,
+// Parseval turns that into one contraction over the grid:
+//   g[nu][m][n] = (1/N) sum_{s,r} conj(psi_kq,n,s(r) e^{i 2pi G0.r})
+//                                 * sum_s' dV_nu^{s s'}(r) psi_k,m,s'(r)
+// (G0 the umklapp shift of the k+q wavefunction), i.e. a complex GEMM with
+// M = (mode, band of k), N = band of k+q, K = (spinor, grid point), whose A
+// operand is generated on the fly from dV and psi_k.
+//
+// * k_local_fp64: the plain form, FP64 SIMT.
+// * k_local_tc:   the mixed form on the 5th-generation tensor cores: psi(r)
+//   in FP32, split into 16-bit (hi, lo) pairs, three products
+//   A_hi B_hi + A_hi B_lo + A_lo B_hi accumulated in FP32 in tensor memory per
+//   K chunk; chunks are reduced in FP64 by the finish kernel.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lelph_common.cuh"
+#include "lelph_internal.h"
+
+// e^{-i 2 pi G0.r / N} for grid point r (exact integer reduction)
+__device__ __forceinline__ long long ulm_num(const int* ulm, int r, const GeomDev& g)
+{
+    const long long NyNz = (long long)g.Ny * g.Nz;
+    int ix = r / (int)NyNz;
+    int rem = r - ix * (int)NyNz;
+    int iy = rem / g.Nz;
+    int iz = rem - iy * g.Nz;
+    long long N = (long long)g.Nx * NyNz;
+    long long tx = ((long long)ulm[0] * ix) % g.Nx;
+    long long ty = ((long long)ulm[1] * iy) % g.Ny;
+    long long tz = ((long long)ulm[2] * iz) % g.Nz;
+    long long num = tx * NyNz + ty * (long long)g.Nx * g.Nz + tz * (long long)g.Nx * g.Ny;
+    num %= N;
+    if (num < 0) num += N;
+    if (2 * num > N) num -= N;
+    return num;
+}
+
+__device__ __forceinline__ double2 ulm_phase_d(const int* ulm, int r, const GeomDev& g)
+{
+    long long num = ulm_num(ulm, r, g);
+    double N = (double)g.Nx * g.Ny * g.Nz;
+    double s, c;
+    sincospi(2.0 * (double)num / N, &s, &c);
+    return make_double2(c, -s);
+}
+
+__device__ __forceinline__ float2 ulm_phase_f(const int* ulm, int r, const GeomDev& g)
+{
+    long long num = ulm_num(ulm, r, g);
+    float N = (float)g.Nx * (float)g.Ny * (float)g.Nz;
+    float s, c;
+    sincospif(2.0f * (float)num / N, &s, &c);
+    return make_float2(c, -s);
+}
+
+// ================================================================ FP64 form
+
+#define F64_TM 64
+#define F64_TN 32
+#define F64_KP 16
+
+// grid: (ceil(nrows/64), ceil(nb/32), npairs*nspin); 256 threads
+__global__ void __launch_bounds__(256) k_local_fp64(const PairInfo* __restrict__ pairs,
+                                                    const double2* __restrict__ psi, const double2* __restrict__ dV,
+                                                    GeomDev gd, double2* __restrict__ glocal)
+{
+    __shared__ double2 As[F64_TM][F64_KP + 1];
+    __shared__ double2 Bs[F64_TN][F64_KP + 1];
+    __shared__ int ulm_s[3];
+    const int zp = blockIdx.z;
+    const int pair = zp / gd.nspin;
+    const int spin = zp - pair * gd.nspin;
+    const PairInfo P = pairs[pair];
+    if (threadIdx.x < 3) ulm_s[threadIdx.x] = P.ulm[threadIdx.x];
+    const int nrows = gd.nmodes * gd.nbnds;
+    const int row0 = blockIdx.x * F64_TM;
+    const int col0 = blockIdx.y * F64_TN;
+    const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
+    const long long Ktot = (long long)gd.nspinor * N;
+    const size_t box = (size_t)N;
+    // psi layout [kbz][spin][band][spinor][r]
+    const double2* psik = psi + ((size_t)P.kbz_k * gd.nspin + spin) * gd.nbnds * gd.nspinor * box;
+    const double2* psikq = psi + ((size_t)P.kbz_kq * gd.nspin + spin) * gd.nbnds * gd.nspinor * box;
+    const double2* dvq = dV + (size_t)P.qslot * gd.nmodes * gd.nmag * box;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double2 acc[4][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) acc[i][j] = make_double2(0.0, 0.0);
+    __syncthreads();
+    for (long long k0 = 0; k0 < Ktot; k0 += F64_KP)
+    {
+        // A tile: 64 rows x 16 points
+        for (int e = threadIdx.x; e < F64_TM * F64_KP; e += blockDim.x)
+        {
+            int rr = e / F64_KP, p = e - rr * F64_KP;
+            int row = row0 + rr;
+            long long kc = k0 + p;
+            double2 a = make_double2(0.0, 0.0);
+            if (row < nrows && kc < Ktot)
+            {
+                int nu = row / gd.nbnds, m = row - nu * gd.nbnds;
+                int s = (int)(kc / N);
+                int r = (int)(kc - (long long)s * N);
+                const double2* dvn = dvq + (size_t)nu * gd.nmag * box;
+                const double2* pm = psik + (size_t)m * gd.nspinor * box;
+                if (gd.nmag == 4)
+                {
+                    a = cadd(cmul(dvn[(size_t)(2 * s) * box + r], pm[r]),
+                             cmul(dvn[(size_t)(2 * s + 1) * box + r], pm[box + r]));
+                }
+                else
+                {
+                    int comp = (gd.nmag == 2) ? spin : 0;
+                    a = cmul(dvn[(size_t)comp * box + r], pm[(size_t)s * box + r]);
+                }
+                a = cmul(a, ulm_phase_d(ulm_s, r, gd));
+            }
+            As[rr][p] = a;
+        }
+        for (int e = threadIdx.x; e < F64_TN * F64_KP; e += blockDim.x)
+        {
+            int cc = e / F64_KP, p = e - cc * F64_KP;
+            int n = col0 + cc;
+            long long kc = k0 + p;
+            double2 b = make_double2(0.0, 0.0);
+            if (n < gd.nbnds && kc < Ktot)
+            {
+                int s = (int)(kc / N);
+                int r = (int)(kc - (long long)s * N);
+                b = cconj(psikq[((size_t)n * gd.nspinor + s) * box + r]);
+            }
+            Bs[cc][p] = b;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int p = 0; p < F64_KP; ++p)
+        {
+            double2 av[4], bv[2];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = As[ty * 4 + i][p];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) bv[j] = Bs[tx * 2 + j][p];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                {
+                    acc[i][j].x = fma(av[i].x, bv[j].x, acc[i][j].x);
+                    acc[i][j].x = fma(-av[i].y, bv[j].y, acc[i][j].x);
+                    acc[i][j].y = fma(av[i].x, bv[j].y, acc[i][j].y);
+                    acc[i][j].y = fma(av[i].y, bv[j].x, acc[i][j].y);
+                }
+        }
+        __syncthreads();
+    }
+    const double invN = 1.0 / (double)N;
+    double2* go = glocal + (size_t)zp * nrows * gd.nbnds;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+        {
+            int row = row0 + ty * 4 + i, n = col0 + tx * 2 + j;
+            if (row < nrows && n < gd.nbnds)
+                go[(size_t)row * gd.nbnds + n] = make_double2(acc[i][j].x * invN, acc[i][j].y * invN);
+        }
+}
+
+void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* psi, const double2* dV,
+                             const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st)
+{
+    (void)status;
+    int nrows = g.nmodes * g.nbnds;
+    dim3 grid((nrows + F64_TM - 1) / F64_TM, (g.nbnds + F64_TN - 1) / F64_TN, npairs * g.nspin);
+    k_local_fp64<<<grid, 256, 0, st>>>(pairs, psi, dV, g, glocal);
+}
+
+// ============================================================= mixed form
+//
+// Warp roles (320 threads): warp 0 issues TMA, warp 1 owns tensor memory and
+// issues the MMAs, warps 2-9 build the A operand; warps 2-5 then drain the
+// accumulator (warp w reads TMEM lanes 32*(w%4)..+31).
+
+#define TC_NST_MAX 4
+#define TC_SMEM_LIMIT (227 * 1024)
+#define TC_KPTS 32  // complex grid points per pipeline stage (64 16-bit K elements = 128 B rows)
+#define TC_THREADS 320
+
+struct TcSmemLayout
+{
+    uint32_t a_hi, a_lo, b_hi, b_lo, p_hi, p_lo;  // offsets of stage 0
+    uint32_t a_bytes, b_bytes, p_bytes;           // per stage per half
+    uint32_t stage_bytes;
+    uint32_t nst;
+    uint32_t bar_off, total;
+};
+
+__host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
+{
+    TcSmemLayout L;
+    const uint32_t NT = 2 * g.nbp;
+    const uint32_t nsp = (g.nmag == 4) ? 2 : 1;
+    L.a_bytes = 128 * 128;
+    L.b_bytes = NT * 128;
+    L.p_bytes = nsp * g.nbp * 128;
+    L.a_hi = 0;
+    L.a_lo = L.a_hi + L.a_bytes;
+    L.b_hi = L.a_lo + L.a_bytes;
+    L.b_lo = L.b_hi + L.b_bytes;
+    L.p_hi = L.b_lo + L.b_bytes;
+    L.p_lo = L.p_hi + L.p_bytes;
+    L.stage_bytes = (L.p_lo + L.p_bytes + 1023) / 1024 * 1024;
+    L.nst = (TC_SMEM_LIMIT - 2048) / L.stage_bytes;
+    if (L.nst > TC_NST_MAX) L.nst = TC_NST_MAX;
+    L.bar_off = L.nst * L.stage_bytes;
+    L.total = L.bar_off + 256 + 1024;  // barriers + alignment slack
+    return L;
+}
+
+int lelph_local_tc_smem_bytes(const GeomDev& g) { return (int)tc_layout(g).total; }
+
+template <int BF16>
+__device__ __forceinline__ void split_store(uint8_t* a_hi, uint8_t* a_lo, uint32_t off, float re, float im)
+{
+    uint32_t h, l;
+    if (BF16)
+    {
+        __nv_bfloat162 hv = __floats2bfloat162_rn(re, im);
+        float2 hf = __bfloat1622float2(hv);
+        __nv_bfloat162 lv = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+        h = *reinterpret_cast<uint32_t*>(&hv);
+        l = *reinterpret_cast<uint32_t*>(&lv);
+    }
+    else
+    {
+        __half2 hv = __floats2half2_rn(re, im);
+        float2 hf = __half22float2(hv);
+        __half2 lv = __floats2half2_rn(re - hf.x, im - hf.y);
+        h = *reinterpret_cast<uint32_t*>(&hv);
+        l = *reinterpret_cast<uint32_t*>(&lv);
+    }
+    *reinterpret_cast<uint32_t*>(a_hi + off) = h;
+    *reinterpret_cast<uint32_t*>(a_lo + off) = l;
+}
+
+template <int BF16>
+__device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* lo, uint32_t off)
+{
+    uint32_t h = *reinterpret_cast<const uint32_t*>(hi + off);
+    uint32_t l = *reinterpret_cast<const uint32_t*>(lo + off);
+    float2 a, b;
+    if (BF16)
+    {
+        a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&h));
+        b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&l));
+    }
+    else
+    {
+        a = __half22float2(*reinterpret_cast<__half2*>(&h));
+        b = __half22float2(*reinterpret_cast<__half2*>(&l));
+    }
+    return make_float2(a.x + b.x, a.y + b.y);
+}
+
+// grid: (nchunks, mtiles, npairs*nspin)
+template <int BF16>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapA,
+               const PairInfo* __restrict__ pairs, const float2* __restrict__ dV,
+               const float* __restrict__ mode_scale, GeomDev gd, int chunk_pts, int nchunks,
+               float* __restrict__ partials, unsigned* __restrict__ status)
+{
+    extern __shared__ __align__(1024) uint8_t smraw[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    const TcSmemLayout L = tc_layout(gd);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
+    uint64_t* aready = full + TC_NST_MAX;
+    uint64_t* empty = aready + TC_NST_MAX;
+    uint64_t* accum = empty + TC_NST_MAX;
+    const int NST = (int)L.nst;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = blockIdx.x, mt = blockIdx.y, zp = blockIdx.z;
+    const int pair = zp / gd.nspin, spin = zp - pair * gd.nspin;
+    const PairInfo P = pairs[pair];
+    const int NT = 2 * gd.nbp;
+    const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
+    const int nstage = chunk_pts / TC_KPTS;
+    const int nsp = (gd.nmag == 4) ? 2 : 1;
+    const uint32_t ncols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < NST; ++s)
+        {
+            mbar_init(&full[s], 1);
+            mbar_init(&aready[s], 8);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, ncols);
+    // zero the A operand buffers once (rows past the last (mode, band) stay 0)
+    for (int s = 0; s < NST; ++s)
+    {
+        uint32_t* a = reinterpret_cast<uint32_t*>(sm + s * L.stage_bytes + L.a_hi);
+        for (int i = threadIdx.x; i < (int)(2 * L.a_bytes / 4); i += blockDim.x) a[i] = 0u;
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0)
+    {
+        if (lane == 0)
+        {
+            prefetch_tmap(&tmapB);
+            prefetch_tmap(&tmapA);
+            const int rowB_hi = ((P.kbz_kq * gd.nspin + spin) * 2 + 0) * NT;
+            const int rowB_lo = rowB_hi + NT;
+            const int rowP_hi = ((P.kbz_k * gd.nspin + spin) * 2 + 0) * NT;
+            const int rowP_lo = rowP_hi + NT;
+            const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes;
+            for (int it = 0; it < nstage; ++it)
+            {
+                const int s = it % NST;
+                const uint32_t ph = (uint32_t)(it / NST) & 1u;
+                if (!mbar_wait_bounded(&empty[s], ph ^ 1u))
+                {
+                    *abort_flag = 1;
+                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                    break;
+                }
+                if (*abort_flag) break;
+                uint8_t* st = sm + s * L.stage_bytes;
+                const long long kc = (long long)chunk * chunk_pts + (long long)it * TC_KPTS;
+                const int sp = (int)(kc / N);
+                const long long r0 = kc - (long long)sp * N;
+                mbar_arrive_expect_tx(&full[s], bytes);
+                tma_load_2d(st + L.b_hi, &tmapB, &full[s], (int)(2 * kc), rowB_hi);
+                tma_load_2d(st + L.b_lo, &tmapB, &full[s], (int)(2 * kc), rowB_lo);
+                for (int q = 0; q < nsp; ++q)
+                {
+                    const int spp = (gd.nmag == 4) ? q : sp;
+                    const int x = (int)(2 * ((long long)spp * N + r0));
+                    tma_load_2d(st + L.p_hi + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_hi);
+                    tma_load_2d(st + L.p_lo + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_lo);
+                }
+            }
+            // let every issued copy land before the CTA can retire
+            for (int it = (nstage > NST ? nstage - NST : 0); it < nstage; ++it)
+                mbar_wait_bounded(&full[it % NST], (uint32_t)(it / NST) & 1u);
+        }
+    }
+    else if (warp == 1)
+    {
+        if (lane == 0)
+        {
+            const uint32_t idesc = umma_idesc_f16(BF16 ? 1u : 0u, 128u, (uint32_t)NT);
+            for (int it = 0; it < nstage; ++it)
+            {
+                const int s = it % NST;
+                const uint32_t ph = (uint32_t)(it / NST) & 1u;
+                if (!mbar_wait_bounded(&full[s], ph) || !mbar_wait_bounded(&aready[s], ph))
+                {
+                    *abort_flag = 1;
+                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                    break;
+                }
+                if (*abort_flag) break;
+                tc_fence_after();
+                const uint32_t base = smem_u32(sm + s * L.stage_bytes);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const uint64_t ah = umma_desc_sw128(base + L.a_hi + 32 * k);
+                    const uint64_t al = umma_desc_sw128(base + L.a_lo + 32 * k);
+                    const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
+                    const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
+                    umma_f16(tmem, ah, bh, idesc, (it > 0 || k > 0) ? 1u : 0u);
+                    umma_f16(tmem, ah, bl, idesc, 1u);
+                    umma_f16(tmem, al, bh, idesc, 1u);
+                }
+                umma_commit(&empty[s]);
+            }
+            umma_commit(accum);
+        }
+    }
+    else
+    {
+        // ---------------- A producers: warps 2..9, lane = grid point in stage
+        const int pw = warp - 2;  // 0..7
+        const int nrows = gd.nmodes * gd.nbnds;
+        const int row0 = mt * 128;
+        const int nu_lo = row0 / gd.nbnds;
+        const int nu_hi = min(gd.nmodes - 1, (row0 + 127) / gd.nbnds);
+        const float2* dvq = dV + (size_t)P.qslot * gd.nmodes * gd.nmag * N;
+        const float* msc = mode_scale + (size_t)P.qslot * gd.nmodes;
+        for (int it = 0; it < nstage; ++it)
+        {
+            const int s = it % NST;
+            const uint32_t ph = (uint32_t)(it / NST) & 1u;
+            bool ok = mbar_wait_bounded(&empty[s], ph ^ 1u) && mbar_wait_bounded(&full[s], ph);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok && lane == 0)
+            {
+                *abort_flag = 1;
+                atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+            }
+            if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;
+            uint8_t* st = sm + s * L.stage_bytes;
+            const long long kc = (long long)chunk * chunk_pts + (long long)it * TC_KPTS;
+            const int sp = (int)(kc / N);
+            const int r = (int)(kc - (long long)sp * N) + lane;
+            const float2 phs = ulm_phase_f(P.ulm, r, gd);
+            // swizzled byte offset of (row, point lane) inside a 128-row tile
+            const uint32_t chunk16 = (uint32_t)(lane >> 2), within = (uint32_t)(lane & 3) * 4;
+            for (int m = pw; m < gd.nbnds; m += 8)
+            {
+                float2 psi0 = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)m * 128 + 4 * lane);
+                float2 psi1 = make_float2(0.f, 0.f);
+                if (gd.nmag == 4)
+                    psi1 = load_split<BF16>(st + L.p_hi + gd.nbp * 128, st + L.p_lo + gd.nbp * 128,
+                                            (uint32_t)m * 128 + 4 * lane);
+                for (int nu = nu_lo; nu <= nu_hi; ++nu)
+                {
+                    const int row = nu * gd.nbnds + m - row0;
+                    if (row < 0 || row >= 128 || row + row0 >= nrows) continue;
+                    const float2* dvn = dvq + (size_t)nu * gd.nmag * N;
+                    float2 a;
+                    if (gd.nmag == 4)
+                    {
+                        float2 d0 = dvn[(size_t)(2 * sp) * N + r];
+                        float2 d1 = dvn[(size_t)(2 * sp + 1) * N + r];
+                        a = cadd(cmul(d0, psi0), cmul(d1, psi1));
+                    }
+                    else
+                    {
+                        const int comp = (gd.nmag == 2) ? spin : 0;
+                        a = cmul(dvn[(size_t)comp * N + r], psi0);
+                    }
+                    a = cmul(a, phs);
+                    const float sc = msc[nu];
+                    const uint32_t off = (uint32_t)(row >> 3) * 1024 + (uint32_t)(row & 7) * 128 +
+                                         ((chunk16 ^ (uint32_t)(row & 7)) << 4) + within;
+                    split_store<BF16>(st + L.a_hi, st + L.a_lo, off, a.x * sc, a.y * sc);
+                }
+            }
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&aready[s]);
+        }
+        // ---------------- epilogue: warps 2..5 drain the accumulator
+        if (warp < 6)
+        {
+            const int q = warp & 3;
+            bool ok = (*abort_flag == 0) && mbar_wait_bounded(accum, 0);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok && lane == 0 && *abort_flag == 0)
+            {
+                *abort_flag = 1;
+                atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+            }
+            tc_fence_after();
+            if (ok)
+            {
+                const int row = q * 32 + lane;
+                const int mtiles = gridDim.y;
+                float* out = partials + ((((size_t)zp * mtiles + mt) * nchunks + chunk) * 128 + row) * NT;
+                for (int c = 0; c < NT; c += 16)
+                {
+                    float v[16];
+                    tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
+                    float4* o4 = reinterpret_cast<float4*>(out + c);
+                    o4[0] = make_float4(v[0], v[1], v[2], v[3]);
+                    o4[1] = make_float4(v[4], v[5], v[6], v[7]);
+                    o4[2] = make_float4(v[8], v[9], v[10], v[11]);
+                    o4[3] = make_float4(v[12], v[13], v[14], v[15]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+    {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
+                           const float2* dV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
+                           int nchunks, float* partials, unsigned* status, cudaStream_t st)
+{
+    const int nrows = g.nmodes * g.nbnds;
+    const int mtiles = (nrows + 127) / 128;
+    dim3 grid(nchunks, mtiles, npairs * g.nspin);
+    const int smem = lelph_local_tc_smem_bytes(g);
+    const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
+    const CUtensorMap* tA = static_cast<const CUtensorMap*>(tmapA);
+    if (ab_bf16)
+    {
+        cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_local_tc<1><<<grid, TC_THREADS, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+                                                      partials, status);
+    }
+    else
+    {
+        cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        k_local_tc<0><<<grid, TC_THREADS, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+                                                      partials, status);
+    }
+}

@@ -1,0 +1,262 @@
+"""Python host binding of the C ABI in include/lelph_gpu.h (ctypes).
+
+Mirrors the reference's per-q stage: ``compute_elphq`` corresponds to
+``compute_and_write_elphq`` (src/elph/compute_elph_matq.c:20-234) with the
+same argument meaning (q in crystal units, eigVec (nmodes, 3*natom), dVscfq
+(nmodes, nmag, Nx, Ny, Nz), ``non_loc``, ``kminusq``) and returns the
+elph_mat[q] slice (nk_BZ, nmodes, nspin, nb_k, nb_k+q) instead of writing it
+through netCDF.  There is no CPU fallback: without the compiled library every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liblelph_gpu.so")
+
+FP64, MIXED_F16, MIXED_BF16 = 0, 1, 2
+OUT_C128, OUT_C64 = 0, 1
+PRECISIONS = {"fp64": FP64, "mixed": MIXED_F16, "mixed_f16": MIXED_F16, "mixed_bf16": MIXED_BF16}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("natom", C.c_int), ("nsym", C.c_int), ("timerev", C.c_int), ("nspin", C.c_int), ("nspinor", C.c_int),
+        ("nbnds", C.c_int), ("nmag", C.c_int), ("nmodes", C.c_int),
+        ("nkpts_iBZ", C.c_int), ("nkpts_BZ", C.c_int),
+        ("fft_dims", C.c_int * 3),
+        ("alat_vec", _dp), ("blat_vec", _dp), ("atomic_pos", _dp), ("atom_type", _ip),
+        ("kpt_iredBZ", _dp), ("kpt_fullBZ_crys", _dp), ("kmap", _ip),
+        ("sym_Rmat", _dp), ("sym_tau", _dp), ("sym_time_rev", _ip),
+        ("is_soc_present", C.c_int),
+        ("npw", _ip), ("gvec", C.POINTER(_dp)), ("wfc", C.POINTER(_dp)), ("Fk", C.POINTER(_dp)),
+        ("ntype", C.c_int), ("nltimesj", C.c_int), ("lmax", C.c_int),
+        ("PP_table", _dp), ("Fsign", _dp), ("fCoeff", C.POINTER(_dp)),
+        ("precision", C.c_int), ("device", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("kernel_launches", C.c_longlong), ("local_launches", C.c_longlong), ("local_ms", C.c_double),
+        ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
+        ("device_bytes", C.c_size_t),
+    ]
+
+
+EXPORTS = [
+    "lelph_gpu_create", "lelph_gpu_set_wavefunctions", "lelph_gpu_prepare", "lelph_gpu_set_q", "lelph_gpu_run",
+    "lelph_gpu_run_device", "lelph_gpu_compute_elphq", "lelph_gpu_elph_q_rotate", "lelph_gpu_debug_gvec_map",
+    "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
+    "lelph_gpu_last_error", "lelph_gpu_destroy",
+]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load liblelph_gpu.so and declare the C signatures.  Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library {path} is missing: run __graft_entry__.build() first")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.lelph_gpu_create.argtypes = [C.POINTER(Desc), C.POINTER(vp)]
+    L.lelph_gpu_set_wavefunctions.argtypes = [vp, C.POINTER(_dp)]
+    L.lelph_gpu_prepare.argtypes = [vp]
+    L.lelph_gpu_set_q.argtypes = [vp, C.c_int, _dp, _dp, _dp]
+    L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
+    L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
+    L.lelph_gpu_compute_elphq.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp]
+    L.lelph_gpu_elph_q_rotate.argtypes = [vp, _dp, _dp, _dp, C.c_int, _dp]
+    L.lelph_gpu_debug_gvec_map.argtypes = [vp, C.c_int, _ip, _ip]
+    L.lelph_gpu_set_profiling.argtypes = [vp, C.c_int]
+    L.lelph_gpu_stats_get.argtypes = [vp, C.POINTER(Stats)]
+    L.lelph_gpu_stream.argtypes = [vp]
+    L.lelph_gpu_stream.restype = vp
+    L.lelph_gpu_strerror.argtypes = [C.c_int]
+    L.lelph_gpu_strerror.restype = C.c_char_p
+    L.lelph_gpu_last_error.argtypes = [vp]
+    L.lelph_gpu_last_error.restype = C.c_char_p
+    L.lelph_gpu_destroy.argtypes = [vp]
+    L.lelph_gpu_destroy.restype = None
+    for name in EXPORTS:
+        if name not in ("lelph_gpu_stream", "lelph_gpu_strerror", "lelph_gpu_last_error", "lelph_gpu_destroy"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+class LelphError(RuntimeError):
+    def __init__(self, status, detail):
+        super().__init__(f"lelph_gpu status {status}: {detail}")
+        self.status = status
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+class LelphGPU:
+    """One device context holding a system (the reference's Lattice, WFC[],
+    Pseudo) and any number of q slots."""
+
+    def __init__(self, s, precision="fp64", device=0):
+        L = load_library()
+        self._L = L
+        self._keep = []
+        d = Desc()
+        keep = self._keep
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(x, dtype=dt)
+            keep.append(a)
+            return a
+
+        d.natom, d.nsym, d.timerev = s.natom, len(s.sym_R), int(s.timerev)
+        d.nspin, d.nspinor, d.nbnds, d.nmag, d.nmodes = s.nspin, s.nspinor, s.nbnds, s.nmag, s.nmodes
+        d.nkpts_iBZ, d.nkpts_BZ = s.nk_ibz, s.nk_bz
+        d.fft_dims[:] = list(s.fft_dims)
+        d.alat_vec = _ptr(arr(s.alat, np.float64))
+        d.blat_vec = _ptr(arr(s.blat, np.float64))
+        d.atomic_pos = _ptr(arr(s.atom_pos, np.float64))
+        d.atom_type = _ptr(arr(s.atom_type, np.int32), _ip)
+        d.kpt_iredBZ = _ptr(arr(s.kibz, np.float64))
+        d.kpt_fullBZ_crys = _ptr(arr(s.kbz_crys, np.float64))
+        d.kmap = _ptr(arr(s.kmap, np.int32), _ip)
+        d.sym_Rmat = _ptr(arr(s.sym_R, np.float64))
+        d.sym_tau = _ptr(arr(s.sym_tau, np.float64))
+        d.sym_time_rev = _ptr(arr(s.sym_trev, np.int32), _ip)
+        d.is_soc_present = int(s.is_soc_present)
+        d.npw = _ptr(arr([len(g) for g in s.gvec], np.int32), _ip)
+        gv = (_dp * s.nk_ibz)(*[_ptr(arr(g, np.float64)) for g in s.gvec])
+        fk = (_dp * s.nk_ibz)(*[_ptr(arr(f, np.float64)) for f in s.Fk])
+        keep += [gv, fk]
+        d.gvec, d.Fk = gv, fk
+        self._wfc_arrays = [arr(w, np.complex128) for w in s.wfc]
+        wf = (_dp * s.nk_ibz)(*[_ptr(w) for w in self._wfc_arrays])
+        keep.append(wf)
+        d.wfc = wf
+        d.ntype, d.nltimesj, d.lmax = s.ntype, s.nltimesj, s.lmax
+        d.PP_table = _ptr(arr(s.PP_table, np.float64))
+        d.Fsign = _ptr(arr(s.Fsign, np.float64))
+        if s.fCoeff is not None:
+            fc = (_dp * len(s.fCoeff))(*[(_ptr(arr(f, np.complex128)) if f is not None else _dp()) for f in s.fCoeff])
+            keep.append(fc)
+            d.fCoeff = fc
+        else:
+            d.fCoeff = C.POINTER(_dp)()
+        d.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        d.device = device
+        h = C.c_void_p()
+        rc = L.lelph_gpu_create(C.byref(d), C.byref(h))
+        if rc != 0:
+            raise LelphError(rc, L.lelph_gpu_strerror(rc).decode())
+        self.h = h
+        self.sys = s
+        self.precision = precision
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LelphError(rc, self._L.lelph_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.lelph_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- reference-shaped entry points
+    def set_wavefunctions(self, wfc_list):
+        arrs = [np.ascontiguousarray(w, dtype=np.complex128) for w in wfc_list]
+        ptrs = (_dp * len(arrs))(*[_ptr(a) for a in arrs])
+        self._check(self._L.lelph_gpu_set_wavefunctions(self.h, ptrs))
+
+    def prepare(self):
+        self._check(self._L.lelph_gpu_prepare(self.h))
+
+    def set_q(self, slot, qpt, eigVec, dVscf):
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        v = np.ascontiguousarray(dVscf, dtype=np.complex128)
+        self._check(self._L.lelph_gpu_set_q(self.h, slot, _ptr(q), _ptr(e), _ptr(v)))
+
+    def run(self, qslots, kbz, non_loc=True, kminusq=False, out=OUT_C128, g_out=None):
+        qs = np.ascontiguousarray(qslots, dtype=np.int32)
+        ks = np.ascontiguousarray(kbz, dtype=np.int32)
+        s = self.sys
+        shape = (len(ks), s.nmodes, s.nspin, s.nbnds, s.nbnds)
+        if g_out is None:
+            g_out = np.empty(shape, dtype=np.complex64 if out == OUT_C64 else np.complex128)
+        self._check(self._L.lelph_gpu_run(self.h, len(ks), _ptr(qs, _ip), _ptr(ks, _ip), int(non_loc), int(kminusq),
+                                          out, g_out.ctypes.data_as(C.c_void_p)))
+        return g_out
+
+    def run_device(self, qslots, kbz, dev_ptr, non_loc=True, kminusq=False, out=OUT_C128):
+        qs = np.ascontiguousarray(qslots, dtype=np.int32)
+        ks = np.ascontiguousarray(kbz, dtype=np.int32)
+        self._check(self._L.lelph_gpu_run_device(self.h, len(ks), _ptr(qs, _ip), _ptr(ks, _ip), int(non_loc),
+                                                 int(kminusq), out, C.c_void_p(dev_ptr)))
+
+    def compute_elphq(self, qpt, eigVec, dVscfq, non_loc=True, kminusq=False):
+        """compute_and_write_elphq for one q: (nk_BZ, nmodes, nspin, nb, nb) complex128."""
+        s = self.sys
+        out = np.empty((s.nk_bz, s.nmodes, s.nspin, s.nbnds, s.nbnds), np.complex128)
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        v = np.ascontiguousarray(dVscfq, dtype=np.complex128)
+        self._check(self._L.lelph_gpu_compute_elphq(self.h, _ptr(q), _ptr(e), _ptr(v), int(non_loc), int(kminusq),
+                                                    _ptr(out)))
+        return out
+
+    def elph_q_rotate(self, Dl, g, Dr, time_rev):
+        g = np.ascontiguousarray(g, dtype=np.complex128)
+        out = np.empty_like(g)
+        Dl = np.ascontiguousarray(Dl, dtype=np.complex128)
+        Dr = np.ascontiguousarray(Dr, dtype=np.complex128)
+        self._check(self._L.lelph_gpu_elph_q_rotate(self.h, _ptr(Dl), _ptr(g), _ptr(Dr), int(time_rev), _ptr(out)))
+        return out
+
+    def gvec_map(self, kbz, ulm=(0, 0, 0)):
+        npw = len(self.sys.gvec[self.sys.kmap[kbz][0]])
+        out = np.empty((npw, 3), np.int32)
+        u = np.ascontiguousarray(ulm, dtype=np.int32)
+        self._check(self._L.lelph_gpu_debug_gvec_map(self.h, kbz, _ptr(u, _ip), _ptr(out, _ip)))
+        return out
+
+    def set_profiling(self, on=True):
+        self._check(self._L.lelph_gpu_set_profiling(self.h, int(on)))
+
+    def stats(self):
+        st = Stats()
+        self._check(self._L.lelph_gpu_stats_get(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+    def stream(self):
+        return self._L.lelph_gpu_stream(self.h)
+
+
+def compute_elphq(s, iq, precision="fp64", non_loc=True, kminusq=False):
+    """One-shot convenience: the reference's per-q stage on the GPU."""
+    with LelphGPU(s, precision) as ctx:
+        return ctx.compute_elphq(s.qpts[iq], s.eigVec[iq], s.dVscf[iq], non_loc=non_loc, kminusq=kminusq)
