@@ -548,7 +548,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     if (h->mixed)
     {
         if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
-        if (2 * h->g.nbp > 256) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 128 bands");
+        if (2 * h->g.nbp > 128) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
         if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
     }
     h->ntype = d.ntype;
@@ -784,6 +784,12 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         for (long long c = 1; c <= units; ++c)
             if (units % c == 0 && c * TC_KPTS_HOST <= 4096) best = c;
         h->chunk_pts = (int)(best * TC_KPTS_HOST);
+        // tuning override: LELPH_TC_CHUNK = grid points per K chunk (multiple of 32 dividing nspinor*N)
+        if (const char* e = getenv("LELPH_TC_CHUNK"))
+        {
+            long long c = atoll(e);
+            if (c > 0 && c % TC_KPTS_HOST == 0 && Ktot % c == 0) h->chunk_pts = (int)c;
+        }
         h->nchunks = (int)(Ktot / h->chunk_pts);
     }
     rc = upload_wfc(h, d.wfc);

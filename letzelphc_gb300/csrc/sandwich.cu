@@ -186,14 +186,15 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 
 // ============================================================= mixed form
 //
-// Warp roles (320 threads): warp 0 issues TMA, warp 1 owns tensor memory and
-// issues the MMAs, warps 2-9 build the A operand; warps 2-5 then drain the
-// accumulator (warp w reads TMEM lanes 32*(w%4)..+31).
+// Warp roles: warp 0 issues TMA, warp 1 owns tensor memory and issues the
+// MMAs, warps 2-9 build the A operand, warps 10.. drain the accumulators
+// (warp w reads TMEM lanes 32*(w%4)..+31, one 64-column half each).
 
 #define TC_NST_MAX 4
 #define TC_SMEM_LIMIT (227 * 1024)
 #define TC_KPTS 32  // complex grid points per pipeline stage (64 16-bit K elements = 128 B rows)
-#define TC_THREADS 320
+#define TC_GROUP 2         // pipeline stages chained into one TMEM accumulator before it is drained
+#define TC_MAX_THREADS 576 // 10 role warps + up to 8 drain warps
 
 struct TcSmemLayout
 {
@@ -271,9 +272,16 @@ __device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* l
     return make_float2(a.x + b.x, a.y + b.y);
 }
 
-// grid: (nchunks, mtiles, npairs*nspin)
+// grid: (nchunks, mtiles, npairs*nspin); 32*(10 + ndrain) threads.
+//
+// The tensor-core accumulator loses low-order bits on every accumulation
+// (its error grows linearly with the number of MMAs chained into one FP32
+// accumulator), so accumulation chains are kept to TC_GROUP pipeline stages:
+// the MMA warp alternates between two TMEM accumulators, and the drain warps
+// add each finished accumulator into round-to-nearest FP32 registers, which
+// are written out per K chunk and reduced in FP64 by the finish kernel.
 template <int BF16>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapA,
                const PairInfo* __restrict__ pairs, const float2* __restrict__ dV,
                const float* __restrict__ mode_scale, GeomDev gd, int chunk_pts, int nchunks,
@@ -285,9 +293,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
     uint64_t* aready = full + TC_NST_MAX;
     uint64_t* empty = aready + TC_NST_MAX;
-    uint64_t* accum = empty + TC_NST_MAX;
+    uint64_t* accf = empty + TC_NST_MAX;  // [2] accumulator b complete (MMA -> drain)
+    uint64_t* acce = accf + 2;            // [2] accumulator b drained (drain -> MMA)
     const int NST = (int)L.nst;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -297,8 +306,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int NT = 2 * gd.nbp;
     const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
     const int nstage = chunk_pts / TC_KPTS;
+    const int ngroup = (nstage + TC_GROUP - 1) / TC_GROUP;
     const int nsp = (gd.nmag == 4) ? 2 : 1;
-    const uint32_t ncols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+    const int ndrain = 4 * ((NT + 63) / 64);
+    const uint32_t ncols = 2 * NT <= 32 ? 32 : (2 * NT <= 64 ? 64 : (2 * NT <= 128 ? 128 : 256));
 
     if (threadIdx.x == 0)
     {
@@ -308,7 +319,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&aready[s], 8);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accum, 1);
+        for (int b = 0; b < 2; ++b)
+        {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], ndrain);
+        }
         *abort_flag = 0;
         fence_barrier_init();
     }
@@ -336,6 +351,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int rowP_hi = ((P.kbz_k * gd.nspin + spin) * 2 + 0) * NT;
             const int rowP_lo = rowP_hi + NT;
             const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes;
+            int issued = 0;
             for (int it = 0; it < nstage; ++it)
             {
                 const int s = it % NST;
@@ -361,9 +377,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     tma_load_2d(st + L.p_hi + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_hi);
                     tma_load_2d(st + L.p_lo + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_lo);
                 }
+                issued = it + 1;
             }
             // let every issued copy land before the CTA can retire
-            for (int it = (nstage > NST ? nstage - NST : 0); it < nstage; ++it)
+            for (int it = (issued > NST ? issued - NST : 0); it < issued; ++it)
                 mbar_wait_bounded(&full[it % NST], (uint32_t)(it / NST) & 1u);
         }
     }
@@ -376,7 +393,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             {
                 const int s = it % NST;
                 const uint32_t ph = (uint32_t)(it / NST) & 1u;
-                if (!mbar_wait_bounded(&full[s], ph) || !mbar_wait_bounded(&aready[s], ph))
+                const int grp = it / TC_GROUP;
+                const int b = grp & 1;
+                const bool first = (it % TC_GROUP) == 0;
+                const bool last = (it % TC_GROUP) == TC_GROUP - 1 || it == nstage - 1;
+                bool ok = true;
+                if (first) ok = mbar_wait_bounded(&acce[b], (uint32_t)((grp >> 1) & 1) ^ 1u);
+                ok = ok && mbar_wait_bounded(&full[s], ph) && mbar_wait_bounded(&aready[s], ph);
+                if (!ok)
                 {
                     *abort_flag = 1;
                     atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
@@ -385,6 +409,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (*abort_flag) break;
                 tc_fence_after();
                 const uint32_t base = smem_u32(sm + s * L.stage_bytes);
+                const uint32_t dacc = tmem + (uint32_t)(b * NT);
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                 {
@@ -392,16 +417,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const uint64_t al = umma_desc_sw128(base + L.a_lo + 32 * k);
                     const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
                     const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
-                    umma_f16(tmem, ah, bh, idesc, (it > 0 || k > 0) ? 1u : 0u);
-                    umma_f16(tmem, ah, bl, idesc, 1u);
-                    umma_f16(tmem, al, bh, idesc, 1u);
+                    umma_f16(dacc, ah, bh, idesc, (first && k == 0) ? 0u : 1u);
+                    umma_f16(dacc, ah, bl, idesc, 1u);
+                    umma_f16(dacc, al, bh, idesc, 1u);
                 }
                 umma_commit(&empty[s]);
+                if (last) umma_commit(&accf[b]);
             }
-            umma_commit(accum);
         }
     }
-    else
+    else if (warp < 10)
     {
         // ---------------- A producers: warps 2..9, lane = grid point in stage
         const int pw = warp - 2;  // 0..7
@@ -465,34 +490,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(&aready[s]);
         }
-        // ---------------- epilogue: warps 2..5 drain the accumulator
-        if (warp < 6)
+    }
+    else if (warp < 10 + ndrain)
+    {
+        // ---------------- drain warps: TMEM lane quadrant warp%4, 64-column half
+        const int dw = warp - 10;
+        const int q = warp & 3;
+        const int c0 = (dw >> 2) * 64;
+        const int nc = min(64, NT - c0);
+        float acc[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+        bool good = true;
+        for (int grp = 0; grp < ngroup; ++grp)
         {
-            const int q = warp & 3;
-            bool ok = (*abort_flag == 0) && mbar_wait_bounded(accum, 0);
+            const int b = grp & 1;
+            bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], (uint32_t)(grp >> 1) & 1u);
             ok = __all_sync(0xffffffffu, ok);
-            if (!ok && lane == 0 && *abort_flag == 0)
+            if (!ok)
             {
-                *abort_flag = 1;
-                atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                if (lane == 0 && *abort_flag == 0)
+                {
+                    *abort_flag = 1;
+                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                }
+                good = false;
+                break;
             }
             tc_fence_after();
-            if (ok)
+            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NT + c0);
+#pragma unroll
+            for (int c = 0; c < 64; c += 16)
             {
-                const int row = q * 32 + lane;
-                const int mtiles = gridDim.y;
-                float* out = partials + ((((size_t)zp * mtiles + mt) * nchunks + chunk) * 128 + row) * NT;
-                for (int c = 0; c < NT; c += 16)
+                if (c < nc)
                 {
                     float v[16];
-                    tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
-                    float4* o4 = reinterpret_cast<float4*>(out + c);
-                    o4[0] = make_float4(v[0], v[1], v[2], v[3]);
-                    o4[1] = make_float4(v[4], v[5], v[6], v[7]);
-                    o4[2] = make_float4(v[8], v[9], v[10], v[11]);
-                    o4[3] = make_float4(v[12], v[13], v[14], v[15]);
+                    tmem_ld16(ta + (uint32_t)c, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[b]);
+        }
+        if (good)
+        {
+            const int row = q * 32 + lane;
+            const int mtiles = gridDim.y;
+            float* out = partials + ((((size_t)zp * mtiles + mt) * nchunks + chunk) * 128 + row) * NT + c0;
+#pragma unroll
+            for (int c = 0; c < 64; c += 4)
+                if (c < nc) *reinterpret_cast<float4*>(out + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
         }
     }
     tc_fence_before();
@@ -512,18 +561,19 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     const int mtiles = (nrows + 127) / 128;
     dim3 grid(nchunks, mtiles, npairs * g.nspin);
     const int smem = lelph_local_tc_smem_bytes(g);
+    const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tA = static_cast<const CUtensorMap*>(tmapA);
     if (ab_bf16)
     {
         cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<1><<<grid, TC_THREADS, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
                                                       partials, status);
     }
     else
     {
         cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<0><<<grid, TC_THREADS, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
                                                       partials, status);
     }
 }
