@@ -1,0 +1,457 @@
+#!/usr/bin/env python
+"""Throughput of the per-q electron-phonon matrix-element stage on GB300.
+
+Metric: g elements per second (elements g_mn^nu(k,q) of ndb.elph) for the
+4-atom cell workload: 48^3 grid, npw ~2500, 8x8x8 k (512 full-BZ points
+unfolded from 35 irreducible), 8 q-points, 12 modes, 32 bands, KB projectors
+l = 0,1, kernel dfpt (local + nonlocal).  One step = every (k, q) pair of the
+batch (4096 pairs, 5.03e7 g elements), starting from the iBZ plane-wave
+coefficients and dV_scf resident in HBM: unfold + FFT all full-BZ
+wavefunctions, project on the KB projectors, sandwich every pair.
+
+* value / ms_per_step: device-resident step, mixed form (FP32 FFTs,
+  split-f16 tensor-core sandwich, FP64 phases and chunk reduction).
+* e2e: the same step through the C ABI with host buffers: every step copies
+  the coefficients and the 8 dV_scf from pinned host memory and reads g back
+  (complex64, the reference's default output type).
+* fp64: the plain FP64 form on a sample of pairs (its full-BZ preparation
+  plus sampled pairs, scaled to the batch), and the mixed-vs-FP64 errors.
+* roofline: the local-sandwich kernel (tensor bound) against the measured
+  bf16 dense peak.
+* cpu_baseline: the CPU oracle (numpy restatement of the reference's
+  G-space algorithm) on a sample of pairs, one core.
+
+`--impl reference` times the reference's CPU path instead (the oracle port,
+all host cores, a bounded sample of pairs per step).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "g elements/s per GB300, mixed vs FP64 form, at |g| rel err <= 1e-5 vs FP64"
+WORKLOAD = "4-atom cell, 48^3 grid, npw~2500, 8x8x8 k, 8 q, 12 modes, 32 bands, KB l=0..1"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="mixed_f16")
+    p.add_argument("--fp64-pairs", type=int, default=64)
+    p.add_argument("--cpu-pairs", type=int, default=3)
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--profile-case", type=int, default=0,
+                   help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ ranks
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def shard_qpoints(rank, world):
+    """q-points of this rank: rank 0 takes the workload's 8 q; other ranks
+    take further irreducible q of the 8x8x8 grid (no data exchanged)."""
+    from letzelphc_gb300 import synth
+    base = synth.CONFIGS["c1"]["qpts"]
+    if rank == 0:
+        return base
+    A, _, _, _ = synth._structure("l12", synth.CONFIGS["c1"]["a"])
+    s = synth.make_system("c0", {"kind": "l12", "a": synth.CONFIGS["c1"]["a"], "kgrid": (2, 2, 2),
+                                 "qpts": [(0, 0, 0)], "nbnds": 1, "npw": 20, "fft": (24, 24, 24)})
+    qirr = synth.reduce_grid((8, 8, 8), s.sym_R, A)
+    idx = [(8 * rank + i) % len(qirr) for i in range(8)]
+    return [tuple(qirr[i]) for i in idx]
+
+
+class Dist:
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            backend = "nccl" if os.environ.get("LELPH_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+
+# ------------------------------------------------------------- clocks
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        self.out = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ helpers
+
+def g_elems(s, npairs):
+    return npairs * s.nmodes * s.nspin * s.nbnds * s.nbnds
+
+
+def tensor_flops_per_pair(s):
+    """Tensor-core work of the local sandwich per (k, q) pair: three real
+    GEMMs (hi*hi, hi*lo, lo*hi) of (nmodes*nbnds) x (2*nbp) x (2*nspinor*N)."""
+    N = int(np.prod(s.fft_dims))
+    nbp = (s.nbnds + 7) // 8 * 8
+    M = s.nmodes * s.nbnds
+    return 3 * 2.0 * M * (2 * nbp) * (2 * s.nspinor * N) * s.nspin
+
+
+def err_stats(g, ref):
+    a, b = np.abs(g), np.abs(ref)
+    e = np.abs(a - b) / np.maximum(b, 1e-6 * b.max())
+    return {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e))),
+            "norm": float(np.linalg.norm((g - ref).ravel()) / np.linalg.norm(ref.ravel()))}
+
+
+def cpu_port_sample(s, pairs):
+    """Time the oracle on a list of (iq, k) pairs; returns (seconds, g elements)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import elph_oracle as O
+    t0 = time.perf_counter()
+    for iq, k in pairs:
+        O.compute_elphq(s, iq, k_list=[k])
+    return time.perf_counter() - t0, g_elems(s, len(pairs))
+
+
+def _port_worker(args):
+    iq, k = args
+    s = _port_worker.s
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import elph_oracle as O
+    O.compute_elphq(s, iq, k_list=[k])
+    return 1
+
+
+def _port_init():
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from letzelphc_gb300 import synth
+    _port_worker.s = synth.make_system("c1")
+
+
+# ---------------------------------------------------------- reference arm
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    from letzelphc_gb300 import synth
+    s = synth.make_system("c1")
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    rng = np.random.default_rng(0)
+    with ctx.Pool(cores, initializer=_port_init) as pool:
+        def step(n):
+            pairs = [(int(rng.integers(len(s.qpts))), int(rng.integers(s.nk_bz))) for _ in range(n)]
+            t0 = time.perf_counter()
+            pool.map(_port_worker, pairs, chunksize=1)
+            return time.perf_counter() - t0, g_elems(s, n)
+        for _ in range(args.warmup):
+            step(cores)
+        ts, es = [], []
+        for _ in range(args.steps):
+            t, e = step(cores)
+            ts.append(t)
+            es.append(e)
+    value = sum(es) / sum(ts)
+    line = {"metric": METRIC, "value": value, "unit": "g_elements/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(ts) / len(ts), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, c1 shapes)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"{cores} random (k,q) pairs per step",
+                       "reference_build": "oracle port: the reference's compiled sources are not available on "
+                                          "this host (built for x86 from the reference tree)"},
+            "cpu_baseline": {"value": value, "unit": "g_elements/s", "cores": cores, "kind": "port",
+                             "sample": f"{cores} (k,q) pairs per step, {args.steps} steps"},
+            "e2e": {"value": value, "unit": "g_elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# -------------------------------------------------------------- our arm
+
+def run_profile_case(args):
+    """A small slice of the workload for ncu captures (not a bench value)."""
+    import torch
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64
+    build_library()
+    # the workload's cell, grid, plane waves and bands on a 2x2x2 k grid: < 1 GB on the device
+    s = synth.make_system("c1", {"kgrid": (2, 2, 2), "qpts": [(0.5, 0.0, 0.0)]})
+    n = min(args.profile_case, s.nk_bz)
+    qs = np.zeros(n, np.int32)
+    ks = np.arange(n, dtype=np.int32)
+    with LelphGPU(s, args.precision) as ctx:
+        ctx.set_q(0, s.qpts[0], s.eigVec[0], s.dVscf[0])
+        gdev = torch.empty(n * s.nmodes * s.nbnds * s.nbnds * 2, dtype=torch.float32, device="cuda")
+        for _ in range(max(1, args.warmup)):
+            ctx.prepare()
+            ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+        torch.cuda.synchronize()
+        ctx.set_profiling(True)
+        p0 = ctx.stats()
+        ctx.prepare()
+        ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+        p1 = ctx.stats()
+    out = {"profile_case_pairs": n, "local_ms": p1["local_ms"] - p0["local_ms"],
+           "prepare_ms": p1["prepare_ms"] - p0["prepare_ms"], "finish_ms": p1["finish_ms"] - p0["finish_ms"],
+           "tensor_flops": tensor_flops_per_pair(s) * n}
+    out["local_tflops"] = out["tensor_flops"] / (out["local_ms"] * 1e-3) / 1e12
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = Dist(world)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64
+
+    build_library()
+    qpts = shard_qpoints(rank, world)
+    s = synth.make_system("c1", {"qpts": qpts})
+    nq, nk = len(s.qpts), s.nk_bz
+    npairs = nq * nk
+    qs = np.repeat(np.arange(nq), nk).astype(np.int32)
+    ks = np.tile(np.arange(nk), nq).astype(np.int32)
+    gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+    elems = g_elems(s, npairs)
+
+    ctx = LelphGPU(s, args.precision, device=local)
+    for iq in range(nq):
+        ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+    gdev = torch.empty(npairs * gsz * 2, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def step():
+        ctx.prepare()
+        ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    st0 = ctx.stats()
+    clocks = ClockSampler(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for e0, e1 in evs:
+        e0.record(stream)
+        step()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    dist.barrier()
+    clk = clocks.stop()
+    st1 = ctx.stats()
+    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms_step = dist.max(sum(ms) / len(ms))
+    launches = (st1["kernel_launches"] - st0["kernel_launches"]) // args.steps
+
+    # per-kernel device times (events around each launch on the library stream)
+    ctx.set_profiling(True)
+    p0 = ctx.stats()
+    step()
+    p1 = ctx.stats()
+    ctx.set_profiling(False)
+    local_ms = p1["local_ms"] - p0["local_ms"]
+    local_launches = p1["local_launches"] - p0["local_launches"]
+    prep_ms = p1["prepare_ms"] - p0["prepare_ms"]
+    fin_ms = p1["finish_ms"] - p0["finish_ms"]
+    flops = tensor_flops_per_pair(s) * npairs
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak = peaks.get("bf16_tflops_sustained") or 1700.0
+    achieved = flops / (local_ms * 1e-3) / 1e12 if local_ms > 0 else None
+    roofline = {"kernel": "k_local_tc (split-f16 tcgen05 sandwich)", "bound": "tensor",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback",
+                "flops_per_launch": flops / max(1, local_launches), "launches": local_launches,
+                "avg_launch_ms": local_ms / max(1, local_launches),
+                "traffic": None, "step_share": local_ms / (local_ms + prep_ms + fin_ms),
+                "prepare_ms": prep_ms, "finish_ms": fin_ms}
+
+    # ------------------------------------------------ end to end (host buffers)
+    wfc_pin = [torch.empty(w.shape, dtype=torch.complex128, pin_memory=True) for w in s.wfc]
+    for t, w in zip(wfc_pin, s.wfc):
+        t.numpy()[...] = w
+    dv_pin = torch.empty(s.dVscf.shape, dtype=torch.complex128, pin_memory=True)
+    dv_pin.numpy()[...] = s.dVscf
+    g_pin = torch.empty((npairs, s.nmodes, s.nspin, s.nbnds, s.nbnds), dtype=torch.complex64, pin_memory=True)
+    wnp = [t.numpy() for t in wfc_pin]
+    dvnp = dv_pin.numpy()
+    gnp = g_pin.numpy()
+    h2d = sum(w.nbytes for w in wnp) + dvnp.nbytes + s.eigVec.nbytes
+    d2h = gnp.nbytes
+
+    def e2e_step():
+        ctx.set_wavefunctions(wnp)
+        for iq in range(nq):
+            ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], dvnp[iq])
+        ctx.run(qs, ks, out=OUT_C64, g_out=gnp)
+
+    for _ in range(2):
+        e2e_step()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_step_ms = dist.max(sum(e2e_ms) / len(e2e_ms))
+    g_mixed = gnp.copy()
+
+    # ------------------------------------------------ FP64 form on a sample
+    fp64 = None
+    if not args.no_fp64 and rank == 0:
+        rng = np.random.default_rng(1)
+        sel = np.sort(rng.choice(npairs, size=min(args.fp64_pairs, npairs), replace=False))
+        with LelphGPU(s, "fp64", device=local) as c64:
+            for iq in range(nq):
+                c64.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+            c64.prepare()
+            c64.run(qs[sel[:2]], ks[sel[:2]])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            c64.prepare()
+            torch.cuda.synchronize()
+            t_prep = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            g64 = c64.run(qs[sel], ks[sel])
+            torch.cuda.synchronize()
+            t_pairs = time.perf_counter() - t0
+        t_batch = t_prep + t_pairs * npairs / len(sel)
+        fp64_rate = elems / t_batch
+        err = err_stats(g_mixed[sel].astype(np.complex128), g64)
+        fp64 = {"value": fp64_rate, "unit": "g_elements/s", "ms_per_step_est": 1e3 * t_batch,
+                "sample": f"full-BZ preparation + {len(sel)} of {npairs} pairs, pair time scaled to the batch",
+                "mixed_over_fp64": (elems / (ms_step * 1e-3)) / fp64_rate,
+                "mixed_error_vs_fp64": err,
+                "error_definition": "e_i = ||g_mixed|-|g_fp64|| / max(|g_fp64|, 1e-6 max|g_fp64|); "
+                                    "norm = ||g_mixed - g_fp64||_2 / ||g_fp64||_2 (mixed output in complex64)"}
+
+    # ------------------------------------------------ CPU baseline (oracle port)
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        pairs = [(i % nq, (37 * i + 5) % nk) for i in range(args.cpu_pairs)]
+        t, e = cpu_port_sample(s, pairs)
+        cpu = {"value": e / t, "unit": "g_elements/s", "cores": 1, "kind": "port",
+               "sample": f"{len(pairs)} (k,q) pairs of the workload, numpy restatement, one core"}
+
+    value = world * elems / (ms_step * 1e-3)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "g_elements/s", "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f16x3 split on tensor cores, f32 FFT, f64 phases",
+                "data": "synthetic (seeded; no public dataset)",
+                "config": {"workload": WORKLOAD, "pairs_per_step": npairs, "g_elements_per_step": elems,
+                           "precision": args.precision, "parallelism": f"q-sharded x{world}",
+                           "l2": "inputs larger than L2 (split operands 29 GB)"},
+                "e2e": {"value": world * elems / (e2e_step_ms * 1e-3), "unit": "g_elements/s",
+                        "ms_per_step": e2e_step_ms, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "fp64_form": fp64,
+                "cpu_baseline": cpu, "wall_s_timed": t_wall}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile_case:
+        return run_profile_case(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

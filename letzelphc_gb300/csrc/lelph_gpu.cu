@@ -72,7 +72,8 @@ struct lelph_gpu
     DevBuf d_dv64, d_dv32, d_dvstage, d_eig, d_mode_scale, d_maxabs;
     DevBuf d_pairs, d_glocal, d_partials, d_gout, d_status, d_tmp;
     FftPlan1D plan[3];
-    CUtensorMap tmapB, tmapA;
+    CUtensorMap tmapB, tmapA, tmapV;
+    void* tmapV_base = nullptr;
     int nslots_alloc = 0;
     int chunk_pts = 0, nchunks = 0;
 };
@@ -238,10 +239,14 @@ float pow2_scale(double bound, double target)
 
 // -------------------------------------------------------------- small kernels
 
-__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, long long n)
+__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, long long n,
+                             long long per_mode, const float* __restrict__ scale)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+    {
+        const double sc = (double)scale[i / per_mode];
+        out[i] = make_float2((float)(in[i].x * sc), (float)(in[i].y * sc));
+    }
 }
 
 // max over r (and spin rows s) of sum_{s'} |dV^{s s'}(r)| per mode -> atomicMax on float bits
@@ -336,17 +341,19 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode()
 }
 
 int make_tmap(lelph_gpu* h, CUtensorMap* m, void* base, unsigned long long inner, unsigned long long rows,
-              unsigned box_rows, bool swz)
+              unsigned box_rows, bool swz, bool f32 = false)
 {
     auto enc = get_encode();
     if (!enc) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    const unsigned long long es_bytes = f32 ? 4 : 2;
     cuuint64_t dims[2] = {inner, rows};
-    cuuint64_t strides[1] = {inner * 2};
+    cuuint64_t strides[1] = {inner * es_bytes};
     cuuint32_t box[2] = {64, box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base, dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = enc(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base, dims, strides,
+                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
     return LELPH_GPU_OK;
 }
@@ -545,6 +552,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->g.nbp = (d.nbnds + 7) / 8 * 8;
     h->g.nmag = d.nmag;
     h->g.nmodes = d.nmodes;
+    h->g.mt_modes = std::min(d.nmodes, std::max(1, 128 / d.nbnds));
     if (h->mixed)
     {
         if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
@@ -779,7 +787,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         if (rc) return bad(rc, h->err);
         // K chunk per CTA: a multiple of 32 grid points dividing nspinor*N, near 4096
         long long Ktot = (long long)d.nspinor * N;
-        long long units = Ktot / TC_KPTS_HOST;
+        long long units = N / TC_KPTS_HOST;  // chunks divide N so a chunk stays within one spinor component
         long long best = 1;
         for (long long c = 1; c <= units; ++c)
             if (units % c == 0 && c * TC_KPTS_HOST <= 4096) best = c;
@@ -788,7 +796,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         if (const char* e = getenv("LELPH_TC_CHUNK"))
         {
             long long c = atoll(e);
-            if (c > 0 && c % TC_KPTS_HOST == 0 && Ktot % c == 0) h->chunk_pts = (int)c;
+            if (c > 0 && c % TC_KPTS_HOST == 0 && N % c == 0) h->chunk_pts = (int)c;
         }
         h->nchunks = (int)(Ktot / h->chunk_pts);
     }
@@ -931,12 +939,14 @@ extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3],
         if (rc) return rc;
         CUDA_TRY(h, cudaMemcpyAsync(h->d_dvstage.p, dVscf, sizeof(double2) * dvn, cudaMemcpyHostToDevice, h->st));
         CUDA_TRY(h, cudaMemsetAsync(h->d_maxabs.p, 0, sizeof(unsigned) * d.nmodes, h->st));
-        k_dv_convert<<<1024, 256, 0, h->st>>>((const double2*)h->d_dvstage.p, (float2*)h->d_dv32.p + (size_t)slot * dvn,
-                                              (long long)dvn);
         k_dv_maxabs<<<dim3(64, d.nmodes), 256, 0, h->st>>>((const double2*)h->d_dvstage.p, d.nmodes, d.nmag, N,
                                                           (unsigned*)h->d_maxabs.p);
         k_mode_scale<<<1, 64, 0, h->st>>>((const unsigned*)h->d_maxabs.p, d.nmodes,
                                           (float*)h->d_mode_scale.p + (size_t)slot * d.nmodes);
+        // FP32 copy of dV_scf scaled by the mode's power-of-two operand scale
+        k_dv_convert<<<1024, 256, 0, h->st>>>((const double2*)h->d_dvstage.p, (float2*)h->d_dv32.p + (size_t)slot * dvn,
+                                              (long long)dvn, (long long)d.nmag * N,
+                                              (const float*)h->d_mode_scale.p + (size_t)slot * d.nmodes);
         h->stats.kernel_launches += 3;
         CUDA_TRY(h, cudaGetLastError());
     }
@@ -1006,6 +1016,15 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         gdev = h->d_gout.p;
     }
     NonlocalDesc nl = nl_desc(h);
+    if (h->mixed && h->tmapV_base != h->d_dv32.p)
+    {
+        // dV_scf of every slot as a 2-D FP32 tensor: rows (slot, mode, component), 2N floats each
+        const long long N = (long long)g.Nx * g.Ny * g.Nz;
+        rc = make_tmap(h, &h->tmapV, h->d_dv32.p, 2ull * N, (unsigned long long)h->nslots_alloc * d.nmodes * d.nmag,
+                       (unsigned)(g.mt_modes * d.nmag), false, true);
+        if (rc) return rc;
+        h->tmapV_base = h->d_dv32.p;
+    }
     CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
     const int nrows = d.nmodes * d.nbnds;
     // batch the pairs so the local workspace stays bounded (~4 GB)
@@ -1024,7 +1043,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
             lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_dv64.p, g,
                                     (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
         else
-            lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapA, (const float2*)h->d_dv32.p,
+            lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapA, &h->tmapV,
                                   (const float*)h->d_mode_scale.p, g, h->ab_bf16, h->chunk_pts, h->nchunks,
                                   (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st);
         h->stats.local_ms += tstop(h);

@@ -43,6 +43,7 @@ struct GeomDev
 {
     int Nx, Ny, Nz;
     int nspin, nspinor, nbnds, nbp, nmag, nmodes;
+    int mt_modes;  // whole modes per 128-row tile of the tensor-core sandwich: min(nmodes, max(1, 128/nbnds))
 };
 
 // FFT (fft_gather.cu)
@@ -72,8 +73,9 @@ void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const lo
 void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* psi, const double2* dV,
                              const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st);
 int lelph_local_tc_smem_bytes(const GeomDev& g);
+int lelph_local_tc_tile_modes(const GeomDev& g);
 void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
-                           const float2* dV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
+                           const void* tmapV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
                            int nchunks, float* partials, unsigned* status, cudaStream_t st);
 
 // nonlocal + finish (nonlocal.cu)

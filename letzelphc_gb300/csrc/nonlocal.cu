@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
     }
     const double invN = 1.0 / ((double)gd.Nx * gd.Ny * gd.Nz);
     const int nrows = gd.nmodes * nb;
-    const int mtiles = (nrows + 127) / 128;
+    const int mtiles = (gd.nmodes + gd.mt_modes - 1) / gd.mt_modes;
     const int NT = 2 * gd.nbp;
     // pre-factor -2 pi i e2 (src/nonloc/Vbare_nloc.c:547)
     const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
         }
         else
         {
-            int mt = row >> 7, rr = row & 127;
+            int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
             const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
             double re = 0.0, im = 0.0;
             for (int c = 0; c < nchunks; ++c)

@@ -23,28 +23,31 @@
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
 
-// e^{-i 2 pi G0.r / N} for grid point r (exact integer reduction)
-__device__ __forceinline__ long long ulm_num(const int* ulm, int r, const GeomDev& g)
+// e^{-i 2 pi G0.r / N} for grid point r: exact integer reduction of
+// G0x ix/Nx + G0y iy/Ny + G0z iz/Nz to num/N, num in (-N/2, N/2]  (N < 2^31/3)
+__device__ __forceinline__ int ulm_num(const int* ulm, int r, const GeomDev& g)
 {
-    const long long NyNz = (long long)g.Ny * g.Nz;
-    int ix = r / (int)NyNz;
-    int rem = r - ix * (int)NyNz;
-    int iy = rem / g.Nz;
-    int iz = rem - iy * g.Nz;
-    long long N = (long long)g.Nx * NyNz;
-    long long tx = ((long long)ulm[0] * ix) % g.Nx;
-    long long ty = ((long long)ulm[1] * iy) % g.Ny;
-    long long tz = ((long long)ulm[2] * iz) % g.Nz;
-    long long num = tx * NyNz + ty * (long long)g.Nx * g.Nz + tz * (long long)g.Nx * g.Ny;
+    const int NyNz = g.Ny * g.Nz;
+    const int ix = r / NyNz;
+    const int rem = r - ix * NyNz;
+    const int iy = rem / g.Nz;
+    const int iz = rem - iy * g.Nz;
+    const int N = g.Nx * NyNz;
+    int tx = (ulm[0] * ix) % g.Nx;
+    int ty = (ulm[1] * iy) % g.Ny;
+    int tz = (ulm[2] * iz) % g.Nz;
+    if (tx < 0) tx += g.Nx;
+    if (ty < 0) ty += g.Ny;
+    if (tz < 0) tz += g.Nz;
+    int num = tx * NyNz + ty * (g.Nx * g.Nz) + tz * (g.Nx * g.Ny);
     num %= N;
-    if (num < 0) num += N;
     if (2 * num > N) num -= N;
     return num;
 }
 
 __device__ __forceinline__ double2 ulm_phase_d(const int* ulm, int r, const GeomDev& g)
 {
-    long long num = ulm_num(ulm, r, g);
+    int num = ulm_num(ulm, r, g);
     double N = (double)g.Nx * g.Ny * g.Nz;
     double s, c;
     sincospi(2.0 * (double)num / N, &s, &c);
@@ -53,7 +56,7 @@ __device__ __forceinline__ double2 ulm_phase_d(const int* ulm, int r, const Geom
 
 __device__ __forceinline__ float2 ulm_phase_f(const int* ulm, int r, const GeomDev& g)
 {
-    long long num = ulm_num(ulm, r, g);
+    int num = ulm_num(ulm, r, g);
     float N = (float)g.Nx * (float)g.Ny * (float)g.Nz;
     float s, c;
     sincospif(2.0f * (float)num / N, &s, &c);
@@ -198,12 +201,15 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 
 struct TcSmemLayout
 {
-    uint32_t a_hi, a_lo, b_hi, b_lo, p_hi, p_lo;  // offsets of stage 0
-    uint32_t a_bytes, b_bytes, p_bytes;           // per stage per half
+    uint32_t a_hi, a_lo, b_hi, b_lo, p_hi, p_lo, dv;  // offsets of stage 0
+    uint32_t a_bytes, b_bytes, p_bytes, dv_bytes;     // per stage per half
     uint32_t stage_bytes;
     uint32_t nst;
-    uint32_t bar_off, total;
+    uint32_t bar_off, tab_off, total;
 };
+
+// whole modes per 128-row tile of (mode, band) rows
+__host__ __device__ inline int tc_tile_modes(const GeomDev& g) { return g.mt_modes; }
 
 __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
 {
@@ -219,15 +225,19 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     L.b_lo = L.b_hi + L.b_bytes;
     L.p_hi = L.b_lo + L.b_bytes;
     L.p_lo = L.p_hi + L.p_bytes;
-    L.stage_bytes = (L.p_lo + L.p_bytes + 1023) / 1024 * 1024;
-    L.nst = (TC_SMEM_LIMIT - 2048) / L.stage_bytes;
+    L.dv = L.p_lo + L.p_bytes;
+    L.dv_bytes = tc_tile_modes(g) * g.nmag * TC_KPTS * 8;
+    L.stage_bytes = (L.dv + L.dv_bytes + 1023) / 1024 * 1024;
+    L.nst = (TC_SMEM_LIMIT - 2048 - (g.Nx + g.Ny + g.Nz) * 8) / L.stage_bytes;
     if (L.nst > TC_NST_MAX) L.nst = TC_NST_MAX;
     L.bar_off = L.nst * L.stage_bytes;
-    L.total = L.bar_off + 256 + 1024;  // barriers + alignment slack
+    L.tab_off = L.bar_off + 256;  // umklapp phase tables: Nx + Ny + Nz complex floats
+    L.total = L.tab_off + (g.Nx + g.Ny + g.Nz) * 8 + 1024;  // + alignment slack
     return L;
 }
 
 int lelph_local_tc_smem_bytes(const GeomDev& g) { return (int)tc_layout(g).total; }
+int lelph_local_tc_tile_modes(const GeomDev& g) { return tc_tile_modes(g); }
 
 template <int BF16>
 __device__ __forceinline__ void split_store(uint8_t* a_hi, uint8_t* a_lo, uint32_t off, float re, float im)
@@ -272,6 +282,32 @@ __device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* l
     return make_float2(a.x + b.x, a.y + b.y);
 }
 
+// A operand for one pipeline stage, fast path: nb % 8 == 0, one magnetic
+// component per row.  Warp pw owns bands m = pw + 8j (j < BPW = nb/8); row
+// (ml, m) = ml*nb + m keeps the swizzle phase of a band fixed, so each product
+// costs one complex multiply, one (hi, lo) split and two shared stores.
+template <int BF16, int BPW>
+__device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L, const float2* dvs, float2 phs,
+                                             int MTa, int comp, int nmag, int nbnds, int pw, int lane,
+                                             const uint32_t* off0)
+{
+    float2 psi[BPW];
+#pragma unroll
+    for (int j = 0; j < BPW; ++j)
+        psi[j] = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)(pw + 8 * j) * 128 + 4 * lane);
+    const uint32_t mstride = (uint32_t)(nbnds >> 3) * 1024u;
+    for (int ml = 0; ml < MTa; ++ml)
+    {
+        const float2 dvp = cmul(dvs[(ml * nmag + comp) * TC_KPTS + lane], phs);
+#pragma unroll
+        for (int j = 0; j < BPW; ++j)
+        {
+            const float2 a = cmul(dvp, psi[j]);
+            split_store<BF16>(st + L.a_hi, st + L.a_lo, off0[j] + (uint32_t)ml * mstride, a.x, a.y);
+        }
+    }
+}
+
 // grid: (nchunks, mtiles, npairs*nspin); 32*(10 + ndrain) threads.
 //
 // The tensor-core accumulator loses low-order bits on every accumulation
@@ -283,7 +319,7 @@ __device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* l
 template <int BF16>
 __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapA,
-               const PairInfo* __restrict__ pairs, const float2* __restrict__ dV,
+               const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs,
                const float* __restrict__ mode_scale, GeomDev gd, int chunk_pts, int nchunks,
                float* __restrict__ partials, unsigned* __restrict__ status)
 {
@@ -295,8 +331,9 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     uint64_t* empty = aready + TC_NST_MAX;
     uint64_t* accf = empty + TC_NST_MAX;  // [2] accumulator b complete (MMA -> drain)
     uint64_t* acce = accf + 2;            // [2] accumulator b drained (drain -> MMA)
+    uint64_t* dvbar = acce + 2;           // [NST] scaled dV tile written (producers -> producers)
     const int NST = (int)L.nst;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(dvbar + TC_NST_MAX);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -318,6 +355,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             mbar_init(&full[s], 1);
             mbar_init(&aready[s], 8);
             mbar_init(&empty[s], 1);
+            mbar_init(&dvbar[s], 8);
         }
         for (int b = 0; b < 2; ++b)
         {
@@ -346,11 +384,13 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         {
             prefetch_tmap(&tmapB);
             prefetch_tmap(&tmapA);
+            prefetch_tmap(&tmapV);
             const int rowB_hi = ((P.kbz_kq * gd.nspin + spin) * 2 + 0) * NT;
             const int rowB_lo = rowB_hi + NT;
             const int rowP_hi = ((P.kbz_k * gd.nspin + spin) * 2 + 0) * NT;
             const int rowP_lo = rowP_hi + NT;
-            const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes;
+            const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes + L.dv_bytes;
+            const int rowV = (P.qslot * gd.nmodes + mt * gd.mt_modes) * gd.nmag;
             int issued = 0;
             for (int it = 0; it < nstage; ++it)
             {
@@ -377,6 +417,8 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     tma_load_2d(st + L.p_hi + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_hi);
                     tma_load_2d(st + L.p_lo + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_lo);
                 }
+                // dV_nu(r) of the tile's modes, all magnetic components: rows (nu, comp) x 32 points
+                tma_load_2d(st + L.dv, &tmapV, &full[s], (int)(2 * r0), rowV);
                 issued = it + 1;
             }
             // let every issued copy land before the CTA can retire
@@ -430,12 +472,46 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     {
         // ---------------- A producers: warps 2..9, lane = grid point in stage
         const int pw = warp - 2;  // 0..7
-        const int nrows = gd.nmodes * gd.nbnds;
-        const int row0 = mt * 128;
-        const int nu_lo = row0 / gd.nbnds;
-        const int nu_hi = min(gd.nmodes - 1, (row0 + 127) / gd.nbnds);
-        const float2* dvq = dV + (size_t)P.qslot * gd.nmodes * gd.nmag * N;
-        const float* msc = mode_scale + (size_t)P.qslot * gd.nmodes;
+        const int MT = gd.mt_modes;
+        const int nu0 = mt * MT;
+        const int MTa = min(MT, gd.nmodes - nu0);  // modes present in this tile
+        // umklapp phase tables e^{-i 2pi G0_x ix / Nx} etc., exact integer reduction, FP64 -> FP32
+        float2* tab = reinterpret_cast<float2*>(sm + L.tab_off);
+        {
+            const int ntab = gd.Nx + gd.Ny + gd.Nz;
+            for (int t = threadIdx.x - 64; t < ntab; t += 256)
+            {
+                int ax = t < gd.Nx ? 0 : (t < gd.Nx + gd.Ny ? 1 : 2);
+                int i = t - (ax == 0 ? 0 : (ax == 1 ? gd.Nx : gd.Nx + gd.Ny));
+                int n = ax == 0 ? gd.Nx : (ax == 1 ? gd.Ny : gd.Nz);
+                int num = (P.ulm[ax] * i) % n;
+                if (num < 0) num += n;
+                double sn, cs;
+                sincospi(2.0 * (double)num / (double)n, &sn, &cs);
+                tab[t] = make_float2((float)cs, (float)-sn);
+            }
+            // producers only: bounded-free named barrier is safe here (no early exit above)
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+        }
+        const float2* tabx = tab;
+        const float2* taby = tab + gd.Nx;
+        const float2* tabz = tab + gd.Nx + gd.Ny;
+        const int NyNz = gd.Ny * gd.Nz;
+        const float inv_nynz = 1.0f / (float)NyNz, inv_nz = 1.0f / (float)gd.Nz;
+        const bool fast = (gd.nbnds % 8 == 0) && (gd.nmag != 4) && gd.nbnds <= 64;
+        const uint32_t chunk16 = (uint32_t)(lane >> 2), within = (uint32_t)(lane & 3) * 4;
+        const int bpw = gd.nbnds >> 3;
+        uint32_t off0[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const uint32_t m = (uint32_t)(pw + 8 * j);
+            off0[j] = (m >> 3) * 1024 + (m & 7) * 128 + ((chunk16 ^ (m & 7)) << 4) + within;
+        }
+        // a K chunk never straddles spinor components (chunk_pts divides N)
+        const long long kc0 = (long long)chunk * chunk_pts;
+        const int sp = (int)(kc0 / N);
+        const int rbase = (int)(kc0 - (long long)sp * N);
         for (int it = 0; it < nstage; ++it)
         {
             const int s = it % NST;
@@ -449,41 +525,52 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             }
             if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;
             uint8_t* st = sm + s * L.stage_bytes;
-            const long long kc = (long long)chunk * chunk_pts + (long long)it * TC_KPTS;
-            const int sp = (int)(kc / N);
-            const int r = (int)(kc - (long long)sp * N) + lane;
-            const float2 phs = ulm_phase_f(P.ulm, r, gd);
-            // swizzled byte offset of (row, point lane) inside a 128-row tile
-            const uint32_t chunk16 = (uint32_t)(lane >> 2), within = (uint32_t)(lane & 3) * 4;
-            for (int m = pw; m < gd.nbnds; m += 8)
+            const int r = rbase + it * TC_KPTS + lane;
+            // grid indices of r without integer division (exact: r < 2^24, margins >= 0.5/NyNz)
+            const int ix = __float2int_rz(((float)r + 0.5f) * inv_nynz);
+            const int rem = r - ix * NyNz;
+            const int iy = __float2int_rz(((float)rem + 0.5f) * inv_nz);
+            const int iz = rem - iy * gd.Nz;
+            const float2 phs = cmul(cmul(tabx[ix], taby[iy]), tabz[iz]);
+            const float2* dvs = reinterpret_cast<const float2*>(st + L.dv);
+            if (fast)
             {
-                float2 psi0 = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)m * 128 + 4 * lane);
-                float2 psi1 = make_float2(0.f, 0.f);
-                if (gd.nmag == 4)
-                    psi1 = load_split<BF16>(st + L.p_hi + gd.nbp * 128, st + L.p_lo + gd.nbp * 128,
-                                            (uint32_t)m * 128 + 4 * lane);
-                for (int nu = nu_lo; nu <= nu_hi; ++nu)
+                const int comp = (gd.nmag == 2) ? spin : 0;
+                switch (bpw)
                 {
-                    const int row = nu * gd.nbnds + m - row0;
-                    if (row < 0 || row >= 128 || row + row0 >= nrows) continue;
-                    const float2* dvn = dvq + (size_t)nu * gd.nmag * N;
-                    float2 a;
+                    case 1: produce_fast<BF16, 1>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 2: produce_fast<BF16, 2>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 3: produce_fast<BF16, 3>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 4: produce_fast<BF16, 4>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 5: produce_fast<BF16, 5>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 6: produce_fast<BF16, 6>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 7: produce_fast<BF16, 7>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    default: produce_fast<BF16, 8>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                }
+            }
+            else
+            {
+                for (int m = pw; m < gd.nbnds; m += 8)
+                {
+                    float2 psi0 = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)m * 128 + 4 * lane);
+                    float2 psi1 = make_float2(0.f, 0.f);
                     if (gd.nmag == 4)
+                        psi1 = load_split<BF16>(st + L.p_hi + gd.nbp * 128, st + L.p_lo + gd.nbp * 128,
+                                                (uint32_t)m * 128 + 4 * lane);
+                    for (int ml = 0; ml < MTa; ++ml)
                     {
-                        float2 d0 = dvn[(size_t)(2 * sp) * N + r];
-                        float2 d1 = dvn[(size_t)(2 * sp + 1) * N + r];
-                        a = cadd(cmul(d0, psi0), cmul(d1, psi1));
+                        const int row = ml * gd.nbnds + m;
+                        const float2* dvn = dvs + ml * gd.nmag * TC_KPTS + lane;
+                        float2 a;
+                        if (gd.nmag == 4)
+                            a = cadd(cmul(dvn[(2 * sp) * TC_KPTS], psi0), cmul(dvn[(2 * sp + 1) * TC_KPTS], psi1));
+                        else
+                            a = cmul(dvn[((gd.nmag == 2) ? spin : 0) * TC_KPTS], psi0);
+                        a = cmul(a, phs);
+                        const uint32_t off = (uint32_t)(row >> 3) * 1024 + (uint32_t)(row & 7) * 128 +
+                                             ((chunk16 ^ (uint32_t)(row & 7)) << 4) + within;
+                        split_store<BF16>(st + L.a_hi, st + L.a_lo, off, a.x, a.y);
                     }
-                    else
-                    {
-                        const int comp = (gd.nmag == 2) ? spin : 0;
-                        a = cmul(dvn[(size_t)comp * N + r], psi0);
-                    }
-                    a = cmul(a, phs);
-                    const float sc = msc[nu];
-                    const uint32_t off = (uint32_t)(row >> 3) * 1024 + (uint32_t)(row & 7) * 128 +
-                                         ((chunk16 ^ (uint32_t)(row & 7)) << 4) + within;
-                    split_store<BF16>(st + L.a_hi, st + L.a_lo, off, a.x * sc, a.y * sc);
                 }
             }
             fence_proxy_async_smem();
@@ -554,26 +641,26 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
 }
 
 void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
-                           const float2* dV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
+                           const void* tmapV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
                            int nchunks, float* partials, unsigned* status, cudaStream_t st)
 {
-    const int nrows = g.nmodes * g.nbnds;
-    const int mtiles = (nrows + 127) / 128;
+    const int mtiles = (g.nmodes + g.mt_modes - 1) / g.mt_modes;
     dim3 grid(nchunks, mtiles, npairs * g.nspin);
     const int smem = lelph_local_tc_smem_bytes(g);
     const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tA = static_cast<const CUtensorMap*>(tmapA);
+    const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (ab_bf16)
     {
         cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tA, *tV, pairs, mode_scale, g, chunk_pts, nchunks,
                                                       partials, status);
     }
     else
     {
         cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tA, pairs, dV, mode_scale, g, chunk_pts, nchunks,
+        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tA, *tV, pairs, mode_scale, g, chunk_pts, nchunks,
                                                       partials, status);
     }
 }
