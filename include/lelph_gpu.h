@@ -125,6 +125,28 @@ int lelph_gpu_run(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non
 int lelph_gpu_run_device(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
                          int out_type, void* g_out_dev);
 
+/* Allocation-free variant of lelph_gpu_run_device (no counterpart in the
+ * reference).  For callers that cannot allocate device memory once set-up is
+ * done: a host code whose device memory is entirely owned by another pool or
+ * framework, or a service loop that must not meet an allocation failure or the
+ * latency of cudaMalloc in the middle of a run.  The call makes no cudaMalloc,
+ * cudaFree or other device-allocating call (and no host heap allocation on
+ * its success path): its working storage (the
+ * pair table and the local-sandwich partial sums) is a 64 MiB file-scope
+ * static device array that every GPU loading the library holds until exit.
+ * The context must already be prepared (lelph_gpu_prepare) and its q slots
+ * loaded; g_out_dev is a caller-owned device buffer laid out as in
+ * lelph_gpu_run.  Items are processed in batches that fit the array; a size
+ * whose single (k, q) pair needs more than the array returns
+ * LELPH_GPU_ERR_UNSUPPORTED.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) with that device current, so that first call should
+ * come before any stream capture.  All calls share the one array and every
+ * call overwrites what it uses, so calls that overlap on the GPU (several
+ * contexts or threads at once on one device) race and must be serialised by
+ * the caller. */
+int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
+                                 int out_type, void* g_out_dev);
+
 /* compute_and_write_elphq for one iBZ q without the netCDF writes: every
  * full-BZ k, output (nkpts_BZ, nmodes, nspin, nbnds, nbnds) complex double. */
 int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, const double* dVscfq,

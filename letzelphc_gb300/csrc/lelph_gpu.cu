@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1130,5 +1131,151 @@ extern "C" int lelph_gpu_debug_gvec_map(lelph_gpu* h, int kbz, const int ulm[3],
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpyAsync(out, dt + 4, sizeof(int) * 3 * npw, cudaMemcpyDeviceToHost, h->st));
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}
+
+// ============================================ allocation-free variant of run
+
+// Callers that cannot allocate device memory once set-up is over -- a host
+// code whose device memory is all owned by another pool or framework, or a
+// service loop that must not meet an allocation failure (or the latency of
+// cudaMalloc) in the middle of a run -- can compute matrix elements through
+// lelph_gpu_run_device_noalloc.  Its only working storage is this file-scope
+// array: the (k, k+q) pair table in the first LELPH_NOALLOC_PAIR_BYTES and the
+// local-sandwich partial sums (mixed form) or FP64 local blocks (plain form)
+// after it.  Every GPU that loads the library holds the array until exit.
+#define LELPH_NOALLOC_BYTES (64ull << 20)
+#define LELPH_NOALLOC_PAIR_BYTES (256ull << 10)
+static __device__ __align__(256) unsigned char lelph_noalloc_scratch[LELPH_NOALLOC_BYTES];
+
+namespace
+{
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+// Device address of the scratch array on h->device, looked up once per device
+// with that device current (the first call on a device does this set-up).
+int noalloc_scratch(lelph_gpu* h, unsigned char** out)
+{
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (h->device < 0 || h->device >= 256) return fail(h, LELPH_GPU_ERR_INVALID, "device ordinal");
+    if (!g_noalloc_addr[h->device])
+    {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, lelph_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(h, LELPH_GPU_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_addr[h->device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[h->device]);
+    return LELPH_GPU_OK;
+}
+
+// (k, k+q) pair of one item: k+q search and umklapp vector, as run does it
+int noalloc_pair(lelph_gpu* h, int qs, int k, int kminusq, PairInfo& P)
+{
+    const lelph_gpu_desc& d = h->d;
+    if (qs < 0 || qs >= (int)h->qslots.size() || !h->qslots[qs].set)
+        return fail(h, LELPH_GPU_ERR_STATE, "q slot not loaded");
+    if (k < 0 || k >= d.nkpts_BZ) return fail(h, LELPH_GPU_ERR_INVALID, "k index out of range");
+    const double* q = h->qslots[qs].q;
+    double kq[3];
+    for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * k + x] + (kminusq ? -q[x] : q[x]);
+    int ikq = find_k(h, kq);
+    if (ikq < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
+    int idx_k = k, idx_kq = ikq;
+    if (kminusq) std::swap(idx_k, idx_kq);
+    P.kbz_k = idx_k;
+    P.kbz_kq = idx_kq;
+    P.qslot = qs;
+    const KPointSym& sk = h->ksym[idx_k];
+    const KPointSym& skq = h->ksym[idx_kq];
+    double tkq[3], tk[3], qc[3], ulm[3], uc[3];
+    mat_vec3(skq.R, &h->kibz[3 * skq.ik], false, tkq);
+    mat_vec3(sk.R, &h->kibz[3 * sk.ik], false, tk);
+    mat_vec3(h->blat.data(), q, false, qc);
+    for (int x = 0; x < 3; ++x) ulm[x] = (tkq[x] - tk[x]) - qc[x] / (2 * PI_T);
+    mat_vec3(h->alat.data(), ulm, true, uc);
+    for (int x = 0; x < 3; ++x)
+    {
+        double r = std::rint(uc[x]);
+        if (std::fabs(uc[x] - r) > 1e-3) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
+        P.ulm[x] = (int)r;
+    }
+    return LELPH_GPU_OK;
+}
+}  // namespace
+
+extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc,
+                                            int kminusq, int out_type, void* g_out_dev)
+{
+    if (!h || n < 0 || (n > 0 && (!qslot || !kbz || !g_out_dev))) return LELPH_GPU_ERR_INVALID;
+    if (out_type != LELPH_GPU_OUT_C128 && out_type != LELPH_GPU_OUT_C64) return fail(h, LELPH_GPU_ERR_INVALID, "out_type");
+    if (n == 0) return LELPH_GPU_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    if (!h->prepared) return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_prepare must run before the allocation-free call");
+    unsigned char* scratch = nullptr;
+    int rc = noalloc_scratch(h, &scratch);
+    if (rc) return rc;
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    const int nrows = d.nmodes * d.nbnds;
+    const int mtiles = (d.nmodes + g.mt_modes - 1) / g.mt_modes;
+    size_t per_pair;
+    if (!h->mixed) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
+    else per_pair = sizeof(float) * (size_t)d.nspin * mtiles * h->nchunks * 128 * 2 * g.nbp;
+    const size_t room = LELPH_NOALLOC_BYTES - LELPH_NOALLOC_PAIR_BYTES;
+    if (per_pair > room)
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED,
+                    "one (k, q) pair needs " + std::to_string(per_pair) + " bytes of scratch; the static scratch of "
+                    "lelph_gpu_run_device_noalloc holds " + std::to_string(room));
+    const int max_pairs = (int)(LELPH_NOALLOC_PAIR_BYTES / sizeof(PairInfo));
+    const int batch = (int)std::min<size_t>({(size_t)n, room / per_pair, (size_t)max_pairs});
+    if (h->mixed && h->tmapV_base != h->d_dv32.p)
+    {
+        const long long N = (long long)g.Nx * g.Ny * g.Nz;
+        rc = make_tmap(h, &h->tmapV, h->d_dv32.p, 2ull * N, (unsigned long long)h->nslots_alloc * d.nmodes * d.nmag,
+                       (unsigned)(g.mt_modes * d.nmag), false, true);
+        if (rc) return rc;
+        h->tmapV_base = h->d_dv32.p;
+    }
+    PairInfo* dpairs = reinterpret_cast<PairInfo*>(scratch);
+    unsigned char* work = scratch + LELPH_NOALLOC_PAIR_BYTES;
+    const size_t gsz = (size_t)d.nmodes * d.nspin * d.nbnds * d.nbnds;
+    const size_t esz = out_type == LELPH_GPU_OUT_C64 ? sizeof(float2) : sizeof(double2);
+    NonlocalDesc nl = nl_desc(h);
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+    PairInfo stage[256];  // host staging on the stack: no heap allocation either
+    for (int p0 = 0; p0 < n; p0 += batch)
+    {
+        const int nb = std::min(batch, n - p0);
+        for (int c0 = 0; c0 < nb; c0 += 256)
+        {
+            const int nc = std::min(256, nb - c0);
+            for (int i = 0; i < nc; ++i)
+            {
+                rc = noalloc_pair(h, qslot[p0 + c0 + i], kbz[p0 + c0 + i], kminusq, stage[i]);
+                if (rc) return rc;
+            }
+            // pageable source: the call returns once the staging buffer has been consumed
+            CUDA_TRY(h, cudaMemcpyAsync(dpairs + c0, stage, sizeof(PairInfo) * nc, cudaMemcpyHostToDevice, h->st));
+        }
+        if (!h->mixed)
+            lelph_launch_local_fp64(dpairs, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_dv64.p, g,
+                                    (double2*)work, (unsigned*)h->d_status.p, h->st);
+        else
+            lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapA, &h->tmapV, (const float*)h->d_mode_scale.p, g,
+                                  h->ab_bf16, h->chunk_pts, h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st);
+        lelph_launch_finish(dpairs, nb, h->mixed ? 0 : 1, (const double2*)work, (const float*)work, h->nchunks,
+                            (const float*)h->d_mode_scale.p, (const float*)h->d_band_scale.p,
+                            (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
+                            out_type == LELPH_GPU_OUT_C64, (char*)g_out_dev + esz * gsz * p0, h->st);
+        h->stats.kernel_launches += 2;
+        h->stats.local_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    rc = check_status(h);
+    if (rc) return rc;
+    h->stats.pairs_done += n;
     return LELPH_GPU_OK;
 }

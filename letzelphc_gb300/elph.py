@@ -55,7 +55,7 @@ EXPORTS = [
     "lelph_gpu_create", "lelph_gpu_set_wavefunctions", "lelph_gpu_prepare", "lelph_gpu_set_q", "lelph_gpu_run",
     "lelph_gpu_run_device", "lelph_gpu_compute_elphq", "lelph_gpu_elph_q_rotate", "lelph_gpu_debug_gvec_map",
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
-    "lelph_gpu_last_error", "lelph_gpu_destroy",
+    "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
 ]
 
 _lib = None
@@ -76,6 +76,7 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_set_q.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
+    L.lelph_gpu_run_device_noalloc.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_compute_elphq.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp]
     L.lelph_gpu_elph_q_rotate.argtypes = [vp, _dp, _dp, _dp, C.c_int, _dp]
     L.lelph_gpu_debug_gvec_map.argtypes = [vp, C.c_int, _ip, _ip]
