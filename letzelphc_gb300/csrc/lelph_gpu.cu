@@ -38,6 +38,8 @@ struct QSlot
 {
     bool set = false;
     double q[3];
+    std::vector<int> ulms;  // distinct umklapp vectors (3 ints each) of every k+q and k-q pair of this q
+    int dmin[3];            // first G' - G1 of the window of differences this q needs
 };
 
 struct lelph_gpu
@@ -69,12 +71,20 @@ struct lelph_gpu
     DevBuf d_miller, d_pwoff, d_npw, d_coef, d_coefoff, d_gvec, d_fk, d_fkoff, d_ksym, d_chat, d_chatoff;
     DevBuf d_psi64, d_boxes32, d_bsplit, d_band_scale, d_proj;
     DevBuf d_atype, d_apos, d_pp, d_fsign, d_fcoef, d_fcoefoff;
-    DevBuf d_tw64[3], d_tw32[3];
-    DevBuf d_dv64, d_dv32, d_dvstage, d_eig, d_mode_scale, d_maxabs;
+    DevBuf d_tw64[3], d_tw32[3], d_twN[3];
+    DevBuf d_dvr, d_eig, d_maxabs;                 // per q slot: dV_scf on the reference box (FP64), eigVec
+    DevBuf d_win64, d_win32, d_winscale, d_wtmpN, d_wtmpM;  // dV windows on the product grid, per (slot, umklapp)
     DevBuf d_pairs, d_glocal, d_partials, d_gout, d_status, d_tmp;
-    FftPlan1D plan[3];
+    FftPlan1D plan[3];   // product grid (g.Nx, g.Ny, g.Nz)
+    FftPlan1D planN[3];  // the reference's FFT box
+    int Nbox[3] = {0, 0, 0};
+    double Rc[3] = {0, 0, 0};  // largest |k+G| component (crystal units) over every rotated sphere
+    std::vector<int> win_base;  // first window entry of each q slot
+    int nwin = 0;
+    bool windows_ok = false;
     CUtensorMap tmapB, tmapA, tmapV;
     void* tmapV_base = nullptr;
+    int tmapV_rows = 0;
     int nslots_alloc = 0;
     int chunk_pts = 0, nchunks = 0;
 };
@@ -279,7 +289,7 @@ __global__ void k_dv_maxabs(const double2* __restrict__ dv, int nmodes, int nmag
 
 __global__ void k_mode_scale(const unsigned* __restrict__ maxbits, int nmodes, float* __restrict__ scale)
 {
-    int nu = threadIdx.x;
+    int nu = blockIdx.x * blockDim.x + threadIdx.x;
     if (nu < nmodes)
     {
         float m = __uint_as_float(maxbits[nu]) * 1.0001f;
@@ -373,6 +383,36 @@ int find_k(const lelph_gpu* h, const double* kpt)
         }
         if (std::sqrt(s) < EPS_K) return i;
     }
+    return -1;
+}
+
+// umklapp G0 = S_kq k_kq - S_k k - q in crystal units for the pair
+// (idx_k, idx_kq) (src/dvloc/compute_Vbare_loc.c:93-144); nonzero if not integral
+int umklapp(const lelph_gpu* h, int idx_k, int idx_kq, const double* q, int* u)
+{
+    const KPointSym& sk = h->ksym[idx_k];
+    const KPointSym& skq = h->ksym[idx_kq];
+    double tkq[3], tk[3], qc[3], ulm[3], uc[3];
+    mat_vec3(skq.R, &h->kibz[3 * skq.ik], false, tkq);
+    mat_vec3(sk.R, &h->kibz[3 * sk.ik], false, tk);
+    mat_vec3(h->blat.data(), q, false, qc);
+    for (int x = 0; x < 3; ++x) ulm[x] = (tkq[x] - tk[x]) - qc[x] / (2 * PI_T);
+    mat_vec3(h->alat.data(), ulm, true, uc);
+    for (int x = 0; x < 3; ++x)
+    {
+        double r = std::rint(uc[x]);
+        if (std::fabs(uc[x] - r) > 1e-3) return 1;
+        u[x] = (int)r;
+    }
+    return 0;
+}
+
+// window entry of (q slot, umklapp vector), -1 if absent
+int window_of(const lelph_gpu* h, int slot, const int* u)
+{
+    const std::vector<int>& L = h->qslots[slot].ulms;
+    for (size_t e = 0; e < L.size(); e += 3)
+        if (L[e] == u[0] && L[e + 1] == u[1] && L[e + 2] == u[2]) return h->win_base[slot] + (int)(e / 3);
     return -1;
 }
 
@@ -540,13 +580,10 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->device = d.device;
     for (int x = 0; x < 3; ++x)
     {
-        if (d.fft_dims[x] <= 0 || !plan_1d(d.fft_dims[x], h->plan[x]))
+        if (d.fft_dims[x] <= 0 || !plan_1d(d.fft_dims[x], h->planN[x]))
             return bad(LELPH_GPU_ERR_UNSUPPORTED, "FFT dimension must factor into 2, 3, 5");
+        h->Nbox[x] = d.fft_dims[x];
     }
-    const long long N = (long long)d.fft_dims[0] * d.fft_dims[1] * d.fft_dims[2];
-    h->g.Nx = d.fft_dims[0];
-    h->g.Ny = d.fft_dims[1];
-    h->g.Nz = d.fft_dims[2];
     h->g.nspin = d.nspin;
     h->g.nspinor = d.nspinor;
     h->g.nbnds = d.nbnds;
@@ -554,12 +591,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->g.nmag = d.nmag;
     h->g.nmodes = d.nmodes;
     h->g.mt_modes = std::min(d.nmodes, std::max(1, 128 / d.nbnds));
-    if (h->mixed)
-    {
-        if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
-        if (2 * h->g.nbp > 128) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
-        if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
-    }
+    if (h->mixed && 2 * h->g.nbp > 128) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
     // host copies
@@ -632,7 +664,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     double B[9];
     for (int i = 0; i < 9; ++i) B[i] = d.blat_vec[i] / (2 * PI_T);
     h->ksym.resize(d.nkpts_BZ);
-    std::vector<int> maxabs(3, 0);
+    int ext[3] = {0, 0, 0};  // largest extent (max - min) of a rotated sphere on each axis
     for (int i = 0; i < d.nkpts_BZ; ++i)
     {
         KPointSym& ks = h->ksym[i];
@@ -675,19 +707,85 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
             ks.su2[2 * e] = u[e].real();
             ks.su2[2 * e + 1] = u[e].imag();
         }
-        // box fit of the rotated sphere (one extra unit for the umklapp shift)
+        // extent of the rotated sphere on each axis
+        int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
         for (int g = 0; g < h->npw[ks.ik]; ++g)
         {
             const int* n = &h->miller[3 * (h->pw_off[ks.ik] + g)];
             for (int r = 0; r < 3; ++r)
             {
-                int v = std::abs(ks.W[3 * r] * n[0] + ks.W[3 * r + 1] * n[1] + ks.W[3 * r + 2] * n[2]) + 1;
-                maxabs[r] = std::max(maxabs[r], v);
+                int v = ks.W[3 * r] * n[0] + ks.W[3 * r + 1] * n[1] + ks.W[3 * r + 2] * n[2];
+                lo[r] = std::min(lo[r], v);
+                hi[r] = std::max(hi[r], v);
+            }
+        }
+        for (int r = 0; r < 3; ++r) ext[r] = std::max(ext[r], hi[r] - lo[r]);
+        // |S(k+G)| in crystal units: S(k+G) = W n + alat^T R k
+        double krot[3];
+        mat_vec3(d.alat_vec, kr, true, krot);
+        for (int g = 0; g < h->npw[ks.ik]; ++g)
+        {
+            const int* n = &h->miller[3 * (h->pw_off[ks.ik] + g)];
+            for (int r = 0; r < 3; ++r)
+            {
+                double u = (double)(ks.W[3 * r] * n[0] + ks.W[3 * r + 1] * n[1] + ks.W[3 * r + 2] * n[2]) + krot[r];
+                h->Rc[r] = std::max(h->Rc[r], std::fabs(u));
             }
         }
     }
     for (int r = 0; r < 3; ++r)
-        if (2 * maxabs[r] >= d.fft_dims[r]) return bad(LELPH_GPU_ERR_GEOMETRY, "FFT box too small for the plane-wave sphere");
+        if (ext[r] >= d.fft_dims[r]) return bad(LELPH_GPU_ERR_GEOMETRY, "FFT box too small for the plane-wave sphere");
+    // Product grid.  For a pair, D = G' - G1 (k+q sphere, shift G0 included,
+    // minus k sphere) satisfies D + q = S'(k'+G') - S(k+G), so every component
+    // of D lies in [-q - 2Rc, -q + 2Rc]: floor(4 Rc) + 3 consecutive integers
+    // cover it for any q.  On a grid of at least that many points per axis the
+    // real-space sandwich with the dV window of each q (k_dv_window) gives the
+    // reference's sum over G exactly.  Smallest 2^a 3^b 5^c sizes, never above
+    // the reference's box (which is always exact); the mixed form also wants
+    // a multiple of 32 points.
+    {
+        auto friendly = [](int n) {
+            for (int p : {2, 3, 5})
+                while (n % p == 0) n /= p;
+            return n == 1;
+        };
+        std::vector<int> cand[3];
+        for (int r = 0; r < 3; ++r)
+        {
+            for (int n = (int)std::floor(4.0 * h->Rc[r] + 1e-9) + 3; n < d.fft_dims[r]; ++n)
+                if (friendly(n)) cand[r].push_back(n);
+            cand[r].push_back(d.fft_dims[r]);
+        }
+        long long best = -1;
+        int bm[3] = {d.fft_dims[0], d.fft_dims[1], d.fft_dims[2]};
+        for (int a : cand[0])
+            for (int b : cand[1])
+                for (int c : cand[2])
+                {
+                    long long p = (long long)a * b * c;
+                    if (h->mixed && p % TC_KPTS_HOST != 0) continue;
+                    if (best < 0 || p < best)
+                    {
+                        best = p;
+                        bm[0] = a;
+                        bm[1] = b;
+                        bm[2] = c;
+                    }
+                }
+        if (const char* e = getenv("LELPH_FULL_BOX"))
+            if (atoi(e) != 0) bm[0] = d.fft_dims[0], bm[1] = d.fft_dims[1], bm[2] = d.fft_dims[2];
+        h->g.Nx = bm[0];
+        h->g.Ny = bm[1];
+        h->g.Nz = bm[2];
+        for (int r = 0; r < 3; ++r)
+            if (!plan_1d(bm[r], h->plan[r])) return bad(LELPH_GPU_ERR_UNSUPPORTED, "product grid");
+    }
+    const long long N = (long long)h->g.Nx * h->g.Ny * h->g.Nz;
+    if (h->mixed)
+    {
+        if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
+        if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
+    }
     // chat offsets per full-BZ k
     h->chat_off.resize(d.nkpts_BZ);
     long long chtot = 0;
@@ -706,8 +804,9 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_fkoff, &h->d_ksym, &h->d_chat, &h->d_chatoff, &h->d_psi64, &h->d_boxes32, &h->d_bsplit,
                       &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
                       &h->d_fcoefoff, &h->d_tw64[0], &h->d_tw64[1], &h->d_tw64[2], &h->d_tw32[0], &h->d_tw32[1],
-                      &h->d_tw32[2], &h->d_dv64, &h->d_dv32, &h->d_dvstage, &h->d_eig, &h->d_mode_scale,
-                      &h->d_maxabs, &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp};
+                      &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
+                      &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
+                      &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -751,10 +850,10 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         if (pack.size() == 2) h->d_fcoef.n = 16;  // marks "no coefficients"
         UP(h->d_fcoefoff, off.data(), sizeof(int) * off.size());
     }
-    // twiddles e^{+2 pi i t / L}
-    for (int x = 0; x < 3; ++x)
+    // twiddles e^{+2 pi i t / L}: product grid (FP64, FP32) and reference box (FP64)
+    for (int x = 0; x < 6; ++x)
     {
-        int L = d.fft_dims[x];
+        int L = x < 3 ? (x == 0 ? h->g.Nx : (x == 1 ? h->g.Ny : h->g.Nz)) : d.fft_dims[x - 3];
         std::vector<double2> t64(L);
         std::vector<float2> t32(L);
         for (int t = 0; t < L; ++t)
@@ -763,8 +862,15 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
             t64[t] = make_double2((double)cosl(ang), (double)sinl(ang));
             t32[t] = make_float2((float)cosl(ang), (float)sinl(ang));
         }
-        UP(h->d_tw64[x], t64.data(), sizeof(double2) * L);
-        UP(h->d_tw32[x], t32.data(), sizeof(float2) * L);
+        if (x < 3)
+        {
+            UP(h->d_tw64[x], t64.data(), sizeof(double2) * L);
+            UP(h->d_tw32[x], t32.data(), sizeof(float2) * L);
+        }
+        else
+        {
+            UP(h->d_twN[x - 3], t64.data(), sizeof(double2) * L);
+        }
     }
     rc = ensure(h, h->d_coef, sizeof(double2) * (size_t)ctot);
     if (rc) return bad(rc, h->err);
@@ -815,6 +921,8 @@ extern "C" int lelph_gpu_set_wavefunctions(lelph_gpu* h, const double* const* wf
     CUDA_TRY(h, cudaSetDevice(h->device));
     return upload_wfc(h, wfc);
 }
+
+static int build_windows(lelph_gpu* h);
 
 extern "C" int lelph_gpu_prepare(lelph_gpu* h)
 {
@@ -874,10 +982,45 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
                              (const long long*)h->d_chatoff.p, nl, g, h->mixed ? 1 : 0, (double2*)h->d_proj.p, h->st);
     h->stats.kernel_launches += 1;
     CUDA_TRY(h, cudaGetLastError());
+    int wr = build_windows(h);
+    if (wr) return wr;
     h->stats.prepare_ms += tstop(h);
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->prepared = true;
     return LELPH_GPU_OK;
+}
+
+// dV on the product grid for one (q slot, umklapp G0): with dVhat the
+// normalised forward transform of dV on the reference box,
+//   dV_G0(r') = sum_d dVhat(d + G0) e^{i d.r'},  d over one period of the product grid
+// (signed representatives), so that (1/M) sum_r' dV_G0 psi_k conj(psi_kq) equals
+// the reference's sum_{G1,G'} c_k(G1) conj(c_kq(G')) dVhat(G' - G1) exactly.
+__global__ void k_dv_window(const double2* __restrict__ dvhat, int ncomp, int Nx, int Ny, int Nz,
+                            const int* __restrict__ ulms, int nu, int3 dmin, GeomDev g, double invN,
+                            double2* __restrict__ out)
+{
+    const long long M = (long long)g.Nx * g.Ny * g.Nz;
+    const int c = blockIdx.y;   // (mode, component)
+    const int u = blockIdx.z;   // umklapp index
+    const int ux = ulms[3 * u], uy = ulms[3 * u + 1], uz = ulms[3 * u + 2];
+    const double2* src = dvhat + (size_t)c * ((size_t)Nx * Ny * Nz);
+    double2* dst = out + ((size_t)u * ncomp + c) * M;
+    // grid residue x stands for the difference D' = G'' - G1 in [dmin - G0, dmin - G0 + M); value dVhat(D' + G0)
+    const int lx = dmin.x - ux, ly = dmin.y - uy, lz = dmin.z - uz;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x)
+    {
+        int x = (int)(r / ((long long)g.Ny * g.Nz));
+        int rem = (int)(r - (long long)x * g.Ny * g.Nz);
+        int y = rem / g.Nz, z = rem - (rem / g.Nz) * g.Nz;
+        int dx = lx + (((x - lx) % g.Nx) + g.Nx) % g.Nx;
+        int dy = ly + (((y - ly) % g.Ny) + g.Ny) % g.Ny;
+        int dz = lz + (((z - lz) % g.Nz) + g.Nz) % g.Nz;
+        int ix = ((dx + ux) % Nx + Nx) % Nx;
+        int iy = ((dy + uy) % Ny + Ny) % Ny;
+        int iz = ((dz + uz) % Nz + Nz) % Nz;
+        double2 v = src[((size_t)ix * Ny + iy) * Nz + iz];
+        dst[r] = make_double2(v.x * invN, v.y * invN);
+    }
 }
 
 extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
@@ -887,72 +1030,154 @@ extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3],
     if (slot > 4096) return fail(h, LELPH_GPU_ERR_INVALID, "slot index too large");
     CUDA_TRY(h, cudaSetDevice(h->device));
     const lelph_gpu_desc& d = h->d;
-    const long long N = (long long)h->g.Nx * h->g.Ny * h->g.Nz;
-    const size_t dvn = (size_t)d.nmodes * d.nmag * N;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    const size_t dvn = (size_t)d.nmodes * d.nmag * NN;
     if (slot >= h->nslots_alloc)
     {
         // grow the slot arrays, keeping the loaded slots
         int ns = std::max(slot + 1, 2 * h->nslots_alloc);
-        DevBuf nd64, nd32, neig, nsc;
-        int rc;
-        if (!h->mixed)
-        {
-            rc = ensure(h, nd64, sizeof(double2) * dvn * ns);
-            if (rc) return rc;
-            if (h->d_dv64.p) CUDA_TRY(h, cudaMemcpyAsync(nd64.p, h->d_dv64.p, sizeof(double2) * dvn * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
-        }
-        else
-        {
-            rc = ensure(h, nd32, sizeof(float2) * dvn * ns);
-            if (rc) return rc;
-            if (h->d_dv32.p) CUDA_TRY(h, cudaMemcpyAsync(nd32.p, h->d_dv32.p, sizeof(float2) * dvn * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
-        }
+        DevBuf ndv, neig;
+        int rc = ensure(h, ndv, sizeof(double2) * dvn * ns);
+        if (rc) return rc;
         rc = ensure(h, neig, sizeof(double2) * d.nmodes * d.nmodes * ns);
         if (rc) return rc;
-        rc = ensure(h, nsc, sizeof(float) * d.nmodes * ns);
-        if (rc) return rc;
-        if (h->d_eig.p) CUDA_TRY(h, cudaMemcpyAsync(neig.p, h->d_eig.p, sizeof(double2) * d.nmodes * d.nmodes * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
-        if (h->d_mode_scale.p) CUDA_TRY(h, cudaMemcpyAsync(nsc.p, h->d_mode_scale.p, sizeof(float) * d.nmodes * h->nslots_alloc, cudaMemcpyDeviceToDevice, h->st));
+        if (h->d_dvr.p)
+            CUDA_TRY(h, cudaMemcpyAsync(ndv.p, h->d_dvr.p, sizeof(double2) * dvn * h->nslots_alloc,
+                                        cudaMemcpyDeviceToDevice, h->st));
+        if (h->d_eig.p)
+            CUDA_TRY(h, cudaMemcpyAsync(neig.p, h->d_eig.p, sizeof(double2) * d.nmodes * d.nmodes * h->nslots_alloc,
+                                        cudaMemcpyDeviceToDevice, h->st));
         CUDA_TRY(h, cudaStreamSynchronize(h->st));
-        for (DevBuf* b : {&h->d_dv64, &h->d_dv32, &h->d_eig, &h->d_mode_scale})
+        for (DevBuf* b : {&h->d_dvr, &h->d_eig})
             if (b->p) cudaFree(b->p);
-        h->d_dv64 = nd64;
-        h->d_dv32 = nd32;
+        h->d_dvr = ndv;
         h->d_eig = neig;
-        h->d_mode_scale = nsc;
         h->nslots_alloc = ns;
         h->qslots.resize(ns);
     }
     QSlot& q = h->qslots[slot];
     memcpy(q.q, qpt_crys, sizeof(q.q));
+    for (int x = 0; x < 3; ++x) q.dmin[x] = (int)std::floor(-qpt_crys[x] - 2.0 * h->Rc[x] - 1e-9);
+    // every umklapp vector a k+q (or, yambo convention, k-q) pair of this q can need
+    q.ulms.clear();
+    for (int conv = 0; conv < 2; ++conv)
+        for (int k = 0; k < d.nkpts_BZ; ++k)
+        {
+            double kq[3];
+            for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * k + x] + (conv ? -qpt_crys[x] : qpt_crys[x]);
+            int o = find_k(h, kq);
+            if (o < 0) continue;  // the run reports non-commensurate grids
+            int ik = conv ? o : k, ikq = conv ? k : o;
+            int u[3];
+            if (umklapp(h, ik, ikq, qpt_crys, u)) continue;
+            bool seen = false;
+            for (size_t e = 0; e < q.ulms.size(); e += 3)
+                if (q.ulms[e] == u[0] && q.ulms[e + 1] == u[1] && q.ulms[e + 2] == u[2]) seen = true;
+            if (!seen) q.ulms.insert(q.ulms.end(), u, u + 3);
+        }
     CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_eig.p + (size_t)slot * d.nmodes * d.nmodes, eigVec,
                                 sizeof(double2) * d.nmodes * d.nmodes, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_dvr.p + (size_t)slot * dvn, dVscf, sizeof(double2) * dvn,
+                                cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    q.set = true;
+    h->windows_ok = false;
+    return LELPH_GPU_OK;
+}
+
+// dV windows of every loaded q slot on the product grid (FP64 plain form;
+// FP32 scaled by a per-mode power of two in the mixed form)
+static int build_windows(lelph_gpu* h)
+{
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    const long long M = (long long)g.Nx * g.Ny * g.Nz;
+    const int ncomp = d.nmodes * d.nmag;
+    h->win_base.assign(h->qslots.size(), -1);
+    int nwin = 0, umax = 0;
+    for (size_t s = 0; s < h->qslots.size(); ++s)
+        if (h->qslots[s].set)
+        {
+            h->win_base[s] = nwin;
+            int nu = (int)h->qslots[s].ulms.size() / 3;
+            nwin += nu;
+            umax = std::max(umax, nu);
+        }
+    h->nwin = nwin;
+    if (nwin == 0)
+    {
+        h->windows_ok = true;
+        return LELPH_GPU_OK;
+    }
+    int rc = ensure(h, h->d_wtmpN, sizeof(double2) * ncomp * NN);
+    if (rc) return rc;
+    rc = ensure(h, h->d_wtmpM, sizeof(double2) * (size_t)umax * ncomp * M);
+    if (rc) return rc;
+    rc = ensure(h, h->d_tmp, sizeof(int) * 3 * (size_t)umax + 16);
+    if (rc) return rc;
     if (!h->mixed)
     {
-        CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_dv64.p + (size_t)slot * dvn, dVscf, sizeof(double2) * dvn,
-                                    cudaMemcpyHostToDevice, h->st));
+        rc = ensure(h, h->d_win64, sizeof(double2) * (size_t)nwin * ncomp * M);
+        if (rc) return rc;
     }
     else
     {
-        int rc = ensure(h, h->d_dvstage, sizeof(double2) * dvn);
+        rc = ensure(h, h->d_win32, sizeof(float2) * (size_t)nwin * ncomp * M);
         if (rc) return rc;
-        rc = ensure(h, h->d_maxabs, sizeof(unsigned) * d.nmodes);
+        rc = ensure(h, h->d_winscale, sizeof(float) * (size_t)nwin * d.nmodes);
         if (rc) return rc;
-        CUDA_TRY(h, cudaMemcpyAsync(h->d_dvstage.p, dVscf, sizeof(double2) * dvn, cudaMemcpyHostToDevice, h->st));
-        CUDA_TRY(h, cudaMemsetAsync(h->d_maxabs.p, 0, sizeof(unsigned) * d.nmodes, h->st));
-        k_dv_maxabs<<<dim3(64, d.nmodes), 256, 0, h->st>>>((const double2*)h->d_dvstage.p, d.nmodes, d.nmag, N,
-                                                          (unsigned*)h->d_maxabs.p);
-        k_mode_scale<<<1, 64, 0, h->st>>>((const unsigned*)h->d_maxabs.p, d.nmodes,
-                                          (float*)h->d_mode_scale.p + (size_t)slot * d.nmodes);
-        // FP32 copy of dV_scf scaled by the mode's power-of-two operand scale
-        k_dv_convert<<<1024, 256, 0, h->st>>>((const double2*)h->d_dvstage.p, (float2*)h->d_dv32.p + (size_t)slot * dvn,
-                                              (long long)dvn, (long long)d.nmag * N,
-                                              (const float*)h->d_mode_scale.p + (size_t)slot * d.nmodes);
-        h->stats.kernel_launches += 3;
+        rc = ensure(h, h->d_maxabs, sizeof(unsigned) * (size_t)umax * d.nmodes);
+        if (rc) return rc;
+    }
+    for (size_t s = 0; s < h->qslots.size(); ++s)
+    {
+        if (!h->qslots[s].set) continue;
+        const int nu = (int)h->qslots[s].ulms.size() / 3;
+        if (nu == 0) continue;
+        double2* tN = (double2*)h->d_wtmpN.p;
+        double2* tM = (double2*)h->d_wtmpM.p;
+        CUDA_TRY(h, cudaMemcpyAsync(tN, (const double2*)h->d_dvr.p + (size_t)s * ncomp * NN,
+                                    sizeof(double2) * ncomp * NN, cudaMemcpyDeviceToDevice, h->st));
+        // forward transform on the reference box (FFTW_FORWARD, unnormalised)
+        lelph_launch_fft_contig_d(tN, (long long)ncomp * h->Nbox[0] * h->Nbox[1], h->planN[2],
+                                  (const double2*)h->d_twN[2].p, -1, h->st);
+        lelph_launch_fft_strided_d(tN, (long long)ncomp * h->Nbox[0], h->Nbox[2], h->planN[1],
+                                   (const double2*)h->d_twN[1].p, -1, h->st);
+        lelph_launch_fft_strided_d(tN, (long long)ncomp, h->Nbox[1] * h->Nbox[2], h->planN[0],
+                                   (const double2*)h->d_twN[0].p, -1, h->st);
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->qslots[s].ulms.data(), sizeof(int) * 3 * nu,
+                                    cudaMemcpyHostToDevice, h->st));
+        const int3 dm = make_int3(h->qslots[s].dmin[0], h->qslots[s].dmin[1], h->qslots[s].dmin[2]);
+        k_dv_window<<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
+                                                             (const int*)h->d_tmp.p, nu, dm, g, 1.0 / (double)NN, tM);
+        // inverse transform on the product grid
+        lelph_launch_fft_contig_d(tM, (long long)nu * ncomp * g.Nx * g.Ny, h->plan[2], (const double2*)h->d_tw64[2].p,
+                                  +1, h->st);
+        lelph_launch_fft_strided_d(tM, (long long)nu * ncomp * g.Nx, g.Nz, h->plan[1], (const double2*)h->d_tw64[1].p,
+                                   +1, h->st);
+        lelph_launch_fft_strided_d(tM, (long long)nu * ncomp, g.Ny * g.Nz, h->plan[0], (const double2*)h->d_tw64[0].p,
+                                   +1, h->st);
+        const size_t base = (size_t)h->win_base[s] * ncomp * M;
+        if (!h->mixed)
+        {
+            CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_win64.p + base, tM, sizeof(double2) * (size_t)nu * ncomp * M,
+                                        cudaMemcpyDeviceToDevice, h->st));
+        }
+        else
+        {
+            unsigned* mx = (unsigned*)h->d_maxabs.p;
+            float* sc = (float*)h->d_winscale.p + (size_t)h->win_base[s] * d.nmodes;
+            CUDA_TRY(h, cudaMemsetAsync(mx, 0, sizeof(unsigned) * nu * d.nmodes, h->st));
+            k_dv_maxabs<<<dim3(64, nu * d.nmodes), 256, 0, h->st>>>(tM, nu * d.nmodes, d.nmag, M, mx);
+            k_mode_scale<<<(nu * d.nmodes + 63) / 64, 64, 0, h->st>>>(mx, nu * d.nmodes, sc);
+            k_dv_convert<<<1024, 256, 0, h->st>>>(tM, (float2*)h->d_win32.p + base, (long long)nu * ncomp * M,
+                                                  (long long)d.nmag * M, sc);
+        }
+        h->stats.kernel_launches += h->mixed ? 10 : 7;
         CUDA_TRY(h, cudaGetLastError());
     }
-    CUDA_TRY(h, cudaStreamSynchronize(h->st));
-    q.set = true;
+    h->windows_ok = true;
     return LELPH_GPU_OK;
 }
 
@@ -966,6 +1191,11 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     if (!h->prepared)
     {
         int rc = lelph_gpu_prepare(h);
+        if (rc) return rc;
+    }
+    if (!h->windows_ok)
+    {
+        int rc = build_windows(h);
         if (rc) return rc;
     }
     const lelph_gpu_desc& d = h->d;
@@ -989,21 +1219,9 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         P.kbz_k = idx_k;
         P.kbz_kq = idx_kq;
         P.qslot = qslot[i];
-        // umklapp G0 = S_kq k_kq - S_k k - q (src/dvloc/compute_Vbare_loc.c:93-144)
-        const KPointSym& sk = h->ksym[idx_k];
-        const KPointSym& skq = h->ksym[idx_kq];
-        double tkq[3], tk[3], qc[3], ulm[3], uc[3];
-        mat_vec3(skq.R, &h->kibz[3 * skq.ik], false, tkq);
-        mat_vec3(sk.R, &h->kibz[3 * sk.ik], false, tk);
-        mat_vec3(h->blat.data(), q, false, qc);
-        for (int x = 0; x < 3; ++x) ulm[x] = (tkq[x] - tk[x]) - qc[x] / (2 * PI_T);
-        mat_vec3(h->alat.data(), ulm, true, uc);
-        for (int x = 0; x < 3; ++x)
-        {
-            double r = std::rint(uc[x]);
-            if (std::fabs(uc[x] - r) > 1e-3) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
-            P.ulm[x] = (int)r;
-        }
+        if (umklapp(h, idx_k, idx_kq, q, P.ulm)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
+        P.dvslot = window_of(h, qslot[i], P.ulm);
+        if (P.dvslot < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "umklapp vector outside the q slot's set");
     }
     int rc = upload(h, h->d_pairs, pairs.data(), sizeof(PairInfo) * n);
     if (rc) return rc;
@@ -1017,14 +1235,15 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         gdev = h->d_gout.p;
     }
     NonlocalDesc nl = nl_desc(h);
-    if (h->mixed && h->tmapV_base != h->d_dv32.p)
+    if (h->mixed && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
     {
-        // dV_scf of every slot as a 2-D FP32 tensor: rows (slot, mode, component), 2N floats each
-        const long long N = (long long)g.Nx * g.Ny * g.Nz;
-        rc = make_tmap(h, &h->tmapV, h->d_dv32.p, 2ull * N, (unsigned long long)h->nslots_alloc * d.nmodes * d.nmag,
+        // dV windows as a 2-D FP32 tensor: rows (window, mode, component), 2M floats each
+        const long long M = (long long)g.Nx * g.Ny * g.Nz;
+        rc = make_tmap(h, &h->tmapV, h->d_win32.p, 2ull * M, (unsigned long long)h->nwin * d.nmodes * d.nmag,
                        (unsigned)(g.mt_modes * d.nmag), false, true);
         if (rc) return rc;
-        h->tmapV_base = h->d_dv32.p;
+        h->tmapV_base = h->d_win32.p;
+        h->tmapV_rows = h->nwin;
     }
     CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
     const int nrows = d.nmodes * d.nbnds;
@@ -1041,17 +1260,17 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         const PairInfo* dp = (const PairInfo*)h->d_pairs.p + p0;
         tstart(h);
         if (!h->mixed)
-            lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_dv64.p, g,
+            lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_win64.p, g,
                                     (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
         else
             lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapA, &h->tmapV,
-                                  (const float*)h->d_mode_scale.p, g, h->ab_bf16, h->chunk_pts, h->nchunks,
+                                  (const float*)h->d_winscale.p, g, h->ab_bf16, h->chunk_pts, h->nchunks,
                                   (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st);
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
         tstart(h);
         lelph_launch_finish(dp, nb, h->mixed ? 0 : 1, (const double2*)h->d_glocal.p, (const float*)h->d_partials.p,
-                            h->nchunks, (const float*)h->d_mode_scale.p, (const float*)h->d_band_scale.p,
+                            h->nchunks, (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
                             out_type == LELPH_GPU_OUT_C64, (char*)gdev + esz * gsz * p0, h->st);
         h->stats.finish_ms += tstop(h);
@@ -1188,20 +1407,9 @@ int noalloc_pair(lelph_gpu* h, int qs, int k, int kminusq, PairInfo& P)
     P.kbz_k = idx_k;
     P.kbz_kq = idx_kq;
     P.qslot = qs;
-    const KPointSym& sk = h->ksym[idx_k];
-    const KPointSym& skq = h->ksym[idx_kq];
-    double tkq[3], tk[3], qc[3], ulm[3], uc[3];
-    mat_vec3(skq.R, &h->kibz[3 * skq.ik], false, tkq);
-    mat_vec3(sk.R, &h->kibz[3 * sk.ik], false, tk);
-    mat_vec3(h->blat.data(), q, false, qc);
-    for (int x = 0; x < 3; ++x) ulm[x] = (tkq[x] - tk[x]) - qc[x] / (2 * PI_T);
-    mat_vec3(h->alat.data(), ulm, true, uc);
-    for (int x = 0; x < 3; ++x)
-    {
-        double r = std::rint(uc[x]);
-        if (std::fabs(uc[x] - r) > 1e-3) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
-        P.ulm[x] = (int)r;
-    }
+    if (umklapp(h, idx_k, idx_kq, q, P.ulm)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
+    P.dvslot = window_of(h, qs, P.ulm);
+    if (P.dvslot < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "umklapp vector outside the q slot's set");
     return LELPH_GPU_OK;
 }
 }  // namespace
@@ -1213,7 +1421,8 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
     if (out_type != LELPH_GPU_OUT_C128 && out_type != LELPH_GPU_OUT_C64) return fail(h, LELPH_GPU_ERR_INVALID, "out_type");
     if (n == 0) return LELPH_GPU_OK;
     CUDA_TRY(h, cudaSetDevice(h->device));
-    if (!h->prepared) return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_prepare must run before the allocation-free call");
+    if (!h->prepared || !h->windows_ok)
+        return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_prepare must run (after the last set_q) before the allocation-free call");
     unsigned char* scratch = nullptr;
     int rc = noalloc_scratch(h, &scratch);
     if (rc) return rc;
@@ -1231,13 +1440,14 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
                     "lelph_gpu_run_device_noalloc holds " + std::to_string(room));
     const int max_pairs = (int)(LELPH_NOALLOC_PAIR_BYTES / sizeof(PairInfo));
     const int batch = (int)std::min<size_t>({(size_t)n, room / per_pair, (size_t)max_pairs});
-    if (h->mixed && h->tmapV_base != h->d_dv32.p)
+    if (h->mixed && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
     {
-        const long long N = (long long)g.Nx * g.Ny * g.Nz;
-        rc = make_tmap(h, &h->tmapV, h->d_dv32.p, 2ull * N, (unsigned long long)h->nslots_alloc * d.nmodes * d.nmag,
+        const long long M = (long long)g.Nx * g.Ny * g.Nz;
+        rc = make_tmap(h, &h->tmapV, h->d_win32.p, 2ull * M, (unsigned long long)h->nwin * d.nmodes * d.nmag,
                        (unsigned)(g.mt_modes * d.nmag), false, true);
         if (rc) return rc;
-        h->tmapV_base = h->d_dv32.p;
+        h->tmapV_base = h->d_win32.p;
+        h->tmapV_rows = h->nwin;
     }
     PairInfo* dpairs = reinterpret_cast<PairInfo*>(scratch);
     unsigned char* work = scratch + LELPH_NOALLOC_PAIR_BYTES;
@@ -1261,13 +1471,13 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
             CUDA_TRY(h, cudaMemcpyAsync(dpairs + c0, stage, sizeof(PairInfo) * nc, cudaMemcpyHostToDevice, h->st));
         }
         if (!h->mixed)
-            lelph_launch_local_fp64(dpairs, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_dv64.p, g,
+            lelph_launch_local_fp64(dpairs, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_win64.p, g,
                                     (double2*)work, (unsigned*)h->d_status.p, h->st);
         else
-            lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapA, &h->tmapV, (const float*)h->d_mode_scale.p, g,
+            lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapA, &h->tmapV, (const float*)h->d_winscale.p, g,
                                   h->ab_bf16, h->chunk_pts, h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st);
         lelph_launch_finish(dpairs, nb, h->mixed ? 0 : 1, (const double2*)work, (const float*)work, h->nchunks,
-                            (const float*)h->d_mode_scale.p, (const float*)h->d_band_scale.p,
+                            (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
                             out_type == LELPH_GPU_OUT_C64, (char*)g_out_dev + esz * gsz * p0, h->st);
         h->stats.kernel_launches += 2;

@@ -36,7 +36,8 @@ struct PairInfo
     int kbz_k;   // full-BZ index of the k wavefunction
     int kbz_kq;  // full-BZ index of the k+q wavefunction
     int ulm[3];  // umklapp G0 (crystal) applied to the k+q wavefunction
-    int qslot;   // q slot (dV, eigVec)
+    int qslot;   // q slot (eigVec)
+    int dvslot;  // dV window of (q slot, G0) on the product grid
 };
 
 struct GeomDev

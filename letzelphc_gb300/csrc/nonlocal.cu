@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
                 re += (double)pp[(size_t)c * 128 * NT + n];
                 im += (double)pp[(size_t)c * 128 * NT + gd.nbp + n];
             }
-            double sc = (double)mode_scale[(size_t)P.qslot * gd.nmodes + nu] *
+            double sc = (double)mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
                         (double)band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
                         (double)band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
             double f = invN / sc;

@@ -3,11 +3,13 @@
 // The reference forms dV*psi_k on the FFT box, transforms it forward, keeps
 // the k+q sphere and contracts with the k+q coefficients
 // (src/dvloc/compute_Vbare_loc.c:286-341, src/fft/convolution.c:13-189).
-// With psi(r) the unnormalised inverse transform of the zero-padded sphere,
-// Parseval turns that into one contraction over the grid:
-//   g[nu][m][n] = (1/N) sum_{s,r} conj(psi_kq,n,s(r) e^{i 2pi G0.r})
-//                                 * sum_s' dV_nu^{s s'}(r) psi_k,m,s'(r)
-// (G0 the umklapp shift of the k+q wavefunction), i.e. a complex GEMM with
+// With psi(r) the unnormalised inverse transform of the zero-padded sphere on
+// the product grid (M points) and dV_G0 the window of dV for the pair's
+// umklapp shift G0 (built on the host side, see k_dv_window), Parseval turns
+// that into one contraction over the grid:
+//   g[nu][m][n] = (1/M) sum_{s,r} conj(psi_kq,n,s(r))
+//                                 * sum_s' dV_G0,nu^{s s'}(r) psi_k,m,s'(r)
+// i.e. a complex GEMM with
 // M = (mode, band of k), N = band of k+q, K = (spinor, grid point), whose A
 // operand is generated on the fly from dV and psi_k.
 //
@@ -23,46 +25,6 @@
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
 
-// e^{-i 2 pi G0.r / N} for grid point r: exact integer reduction of
-// G0x ix/Nx + G0y iy/Ny + G0z iz/Nz to num/N, num in (-N/2, N/2]  (N < 2^31/3)
-__device__ __forceinline__ int ulm_num(const int* ulm, int r, const GeomDev& g)
-{
-    const int NyNz = g.Ny * g.Nz;
-    const int ix = r / NyNz;
-    const int rem = r - ix * NyNz;
-    const int iy = rem / g.Nz;
-    const int iz = rem - iy * g.Nz;
-    const int N = g.Nx * NyNz;
-    int tx = (ulm[0] * ix) % g.Nx;
-    int ty = (ulm[1] * iy) % g.Ny;
-    int tz = (ulm[2] * iz) % g.Nz;
-    if (tx < 0) tx += g.Nx;
-    if (ty < 0) ty += g.Ny;
-    if (tz < 0) tz += g.Nz;
-    int num = tx * NyNz + ty * (g.Nx * g.Nz) + tz * (g.Nx * g.Ny);
-    num %= N;
-    if (2 * num > N) num -= N;
-    return num;
-}
-
-__device__ __forceinline__ double2 ulm_phase_d(const int* ulm, int r, const GeomDev& g)
-{
-    int num = ulm_num(ulm, r, g);
-    double N = (double)g.Nx * g.Ny * g.Nz;
-    double s, c;
-    sincospi(2.0 * (double)num / N, &s, &c);
-    return make_double2(c, -s);
-}
-
-__device__ __forceinline__ float2 ulm_phase_f(const int* ulm, int r, const GeomDev& g)
-{
-    int num = ulm_num(ulm, r, g);
-    float N = (float)g.Nx * (float)g.Ny * (float)g.Nz;
-    float s, c;
-    sincospif(2.0f * (float)num / N, &s, &c);
-    return make_float2(c, -s);
-}
-
 // ================================================================ FP64 form
 
 #define F64_TM 64
@@ -76,12 +38,10 @@ __global__ void __launch_bounds__(256) k_local_fp64(const PairInfo* __restrict__
 {
     __shared__ double2 As[F64_TM][F64_KP + 1];
     __shared__ double2 Bs[F64_TN][F64_KP + 1];
-    __shared__ int ulm_s[3];
     const int zp = blockIdx.z;
     const int pair = zp / gd.nspin;
     const int spin = zp - pair * gd.nspin;
     const PairInfo P = pairs[pair];
-    if (threadIdx.x < 3) ulm_s[threadIdx.x] = P.ulm[threadIdx.x];
     const int nrows = gd.nmodes * gd.nbnds;
     const int row0 = blockIdx.x * F64_TM;
     const int col0 = blockIdx.y * F64_TN;
@@ -91,7 +51,7 @@ __global__ void __launch_bounds__(256) k_local_fp64(const PairInfo* __restrict__
     // psi layout [kbz][spin][band][spinor][r]
     const double2* psik = psi + ((size_t)P.kbz_k * gd.nspin + spin) * gd.nbnds * gd.nspinor * box;
     const double2* psikq = psi + ((size_t)P.kbz_kq * gd.nspin + spin) * gd.nbnds * gd.nspinor * box;
-    const double2* dvq = dV + (size_t)P.qslot * gd.nmodes * gd.nmag * box;
+    const double2* dvq = dV + (size_t)P.dvslot * gd.nmodes * gd.nmag * box;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     double2 acc[4][2];
 #pragma unroll
@@ -125,7 +85,6 @@ __global__ void __launch_bounds__(256) k_local_fp64(const PairInfo* __restrict__
                     int comp = (gd.nmag == 2) ? spin : 0;
                     a = cmul(dvn[(size_t)comp * box + r], pm[(size_t)s * box + r]);
                 }
-                a = cmul(a, ulm_phase_d(ulm_s, r, gd));
             }
             As[rr][p] = a;
         }
@@ -205,7 +164,7 @@ struct TcSmemLayout
     uint32_t a_bytes, b_bytes, p_bytes, dv_bytes;     // per stage per half
     uint32_t stage_bytes;
     uint32_t nst;
-    uint32_t bar_off, tab_off, total;
+    uint32_t bar_off, total;
 };
 
 // whole modes per 128-row tile of (mode, band) rows
@@ -228,11 +187,10 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     L.dv = L.p_lo + L.p_bytes;
     L.dv_bytes = tc_tile_modes(g) * g.nmag * TC_KPTS * 8;
     L.stage_bytes = (L.dv + L.dv_bytes + 1023) / 1024 * 1024;
-    L.nst = (TC_SMEM_LIMIT - 2048 - (g.Nx + g.Ny + g.Nz) * 8) / L.stage_bytes;
+    L.nst = (TC_SMEM_LIMIT - 2048) / L.stage_bytes;
     if (L.nst > TC_NST_MAX) L.nst = TC_NST_MAX;
     L.bar_off = L.nst * L.stage_bytes;
-    L.tab_off = L.bar_off + 256;  // umklapp phase tables: Nx + Ny + Nz complex floats
-    L.total = L.tab_off + (g.Nx + g.Ny + g.Nz) * 8 + 1024;  // + alignment slack
+    L.total = L.bar_off + 256 + 1024;  // barriers + alignment slack
     return L;
 }
 
@@ -287,8 +245,7 @@ __device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* l
 // (ml, m) = ml*nb + m keeps the swizzle phase of a band fixed, so each product
 // costs one complex multiply, one (hi, lo) split and two shared stores.
 template <int BF16, int BPW>
-__device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L, const float2* dvs, float2 phs,
-                                             int MTa, int comp, int nmag, int nbnds, int pw, int lane,
+__device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L, const float2* dvs, int MTa, int comp, int nmag, int nbnds, int pw, int lane,
                                              const uint32_t* off0)
 {
     float2 psi[BPW];
@@ -298,7 +255,7 @@ __device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L,
     const uint32_t mstride = (uint32_t)(nbnds >> 3) * 1024u;
     for (int ml = 0; ml < MTa; ++ml)
     {
-        const float2 dvp = cmul(dvs[(ml * nmag + comp) * TC_KPTS + lane], phs);
+        const float2 dvp = dvs[(ml * nmag + comp) * TC_KPTS + lane];
 #pragma unroll
         for (int j = 0; j < BPW; ++j)
         {
@@ -390,7 +347,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             const int rowP_hi = ((P.kbz_k * gd.nspin + spin) * 2 + 0) * NT;
             const int rowP_lo = rowP_hi + NT;
             const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes + L.dv_bytes;
-            const int rowV = (P.qslot * gd.nmodes + mt * gd.mt_modes) * gd.nmag;
+            const int rowV = (P.dvslot * gd.nmodes + mt * gd.mt_modes) * gd.nmag;
             int issued = 0;
             for (int it = 0; it < nstage; ++it)
             {
@@ -475,29 +432,6 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         const int MT = gd.mt_modes;
         const int nu0 = mt * MT;
         const int MTa = min(MT, gd.nmodes - nu0);  // modes present in this tile
-        // umklapp phase tables e^{-i 2pi G0_x ix / Nx} etc., exact integer reduction, FP64 -> FP32
-        float2* tab = reinterpret_cast<float2*>(sm + L.tab_off);
-        {
-            const int ntab = gd.Nx + gd.Ny + gd.Nz;
-            for (int t = threadIdx.x - 64; t < ntab; t += 256)
-            {
-                int ax = t < gd.Nx ? 0 : (t < gd.Nx + gd.Ny ? 1 : 2);
-                int i = t - (ax == 0 ? 0 : (ax == 1 ? gd.Nx : gd.Nx + gd.Ny));
-                int n = ax == 0 ? gd.Nx : (ax == 1 ? gd.Ny : gd.Nz);
-                int num = (P.ulm[ax] * i) % n;
-                if (num < 0) num += n;
-                double sn, cs;
-                sincospi(2.0 * (double)num / (double)n, &sn, &cs);
-                tab[t] = make_float2((float)cs, (float)-sn);
-            }
-            // producers only: bounded-free named barrier is safe here (no early exit above)
-            asm volatile("bar.sync 1, 256;" ::: "memory");
-        }
-        const float2* tabx = tab;
-        const float2* taby = tab + gd.Nx;
-        const float2* tabz = tab + gd.Nx + gd.Ny;
-        const int NyNz = gd.Ny * gd.Nz;
-        const float inv_nynz = 1.0f / (float)NyNz, inv_nz = 1.0f / (float)gd.Nz;
         const bool fast = (gd.nbnds % 8 == 0) && (gd.nmag != 4) && gd.nbnds <= 64;
         const uint32_t chunk16 = (uint32_t)(lane >> 2), within = (uint32_t)(lane & 3) * 4;
         const int bpw = gd.nbnds >> 3;
@@ -511,7 +445,6 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         // a K chunk never straddles spinor components (chunk_pts divides N)
         const long long kc0 = (long long)chunk * chunk_pts;
         const int sp = (int)(kc0 / N);
-        const int rbase = (int)(kc0 - (long long)sp * N);
         for (int it = 0; it < nstage; ++it)
         {
             const int s = it % NST;
@@ -525,27 +458,20 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             }
             if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;
             uint8_t* st = sm + s * L.stage_bytes;
-            const int r = rbase + it * TC_KPTS + lane;
-            // grid indices of r without integer division (exact: r < 2^24, margins >= 0.5/NyNz)
-            const int ix = __float2int_rz(((float)r + 0.5f) * inv_nynz);
-            const int rem = r - ix * NyNz;
-            const int iy = __float2int_rz(((float)rem + 0.5f) * inv_nz);
-            const int iz = rem - iy * gd.Nz;
-            const float2 phs = cmul(cmul(tabx[ix], taby[iy]), tabz[iz]);
             const float2* dvs = reinterpret_cast<const float2*>(st + L.dv);
             if (fast)
             {
                 const int comp = (gd.nmag == 2) ? spin : 0;
                 switch (bpw)
                 {
-                    case 1: produce_fast<BF16, 1>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 2: produce_fast<BF16, 2>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 3: produce_fast<BF16, 3>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 4: produce_fast<BF16, 4>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 5: produce_fast<BF16, 5>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 6: produce_fast<BF16, 6>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 7: produce_fast<BF16, 7>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    default: produce_fast<BF16, 8>(st, L, dvs, phs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 1: produce_fast<BF16, 1>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 2: produce_fast<BF16, 2>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 3: produce_fast<BF16, 3>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 4: produce_fast<BF16, 4>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 5: produce_fast<BF16, 5>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 6: produce_fast<BF16, 6>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    case 7: produce_fast<BF16, 7>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
+                    default: produce_fast<BF16, 8>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
                 }
             }
             else
@@ -566,7 +492,6 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                             a = cadd(cmul(dvn[(2 * sp) * TC_KPTS], psi0), cmul(dvn[(2 * sp + 1) * TC_KPTS], psi1));
                         else
                             a = cmul(dvn[((gd.nmag == 2) ? spin : 0) * TC_KPTS], psi0);
-                        a = cmul(a, phs);
                         const uint32_t off = (uint32_t)(row >> 3) * 1024 + (uint32_t)(row & 7) * 128 +
                                              ((chunk16 ^ (uint32_t)(row & 7)) << 4) + within;
                         split_store<BF16>(st + L.a_hi, st + L.a_lo, off, a.x, a.y);
