@@ -165,10 +165,12 @@ def g_elems(s, npairs):
     return npairs * s.nmodes * s.nspin * s.nbnds * s.nbnds
 
 
-def tensor_flops_per_pair(s):
+def tensor_flops_per_pair(s, grid=None):
     """Tensor-core work of the local sandwich per (k, q) pair: three real
-    GEMMs (hi*hi, hi*lo, lo*hi) of (nmodes*nbnds) x (2*nbp) x (2*nspinor*N)."""
-    N = int(np.prod(s.fft_dims))
+    GEMMs (hi*hi, hi*lo, lo*hi) of (nmodes*nbnds) x (2*nbp) x (2*nspinor*M),
+    M the points of the product grid the library chose (the reference's box
+    when not given)."""
+    N = int(np.prod(grid if grid is not None else s.fft_dims))
     nbp = (s.nbnds + 7) // 8 * 8
     M = s.nmodes * s.nbnds
     return 3 * 2.0 * M * (2 * nbp) * (2 * s.nspinor * N) * s.nspin
@@ -274,7 +276,7 @@ def run_profile_case(args):
         p1 = ctx.stats()
     out = {"profile_case_pairs": n, "local_ms": p1["local_ms"] - p0["local_ms"],
            "prepare_ms": p1["prepare_ms"] - p0["prepare_ms"], "finish_ms": p1["finish_ms"] - p0["finish_ms"],
-           "tensor_flops": tensor_flops_per_pair(s) * n}
+           "tensor_flops": tensor_flops_per_pair(s, p1["product_grid"]) * n, "product_grid": p1["product_grid"]}
     out["local_tflops"] = out["tensor_flops"] / (out["local_ms"] * 1e-3) / 1e12
     print(json.dumps(out), flush=True)
     return 0
@@ -341,7 +343,7 @@ def run_ours(args):
     local_launches = p1["local_launches"] - p0["local_launches"]
     prep_ms = p1["prepare_ms"] - p0["prepare_ms"]
     fin_ms = p1["finish_ms"] - p0["finish_ms"]
-    flops = tensor_flops_per_pair(s) * npairs
+    flops = tensor_flops_per_pair(s, p1["product_grid"]) * npairs
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
@@ -353,6 +355,7 @@ def run_ours(args):
                 "frac": (achieved / peak) if achieved else None,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback",
                 "flops_per_launch": flops / max(1, local_launches), "launches": local_launches,
+                "product_grid": list(p1["product_grid"]), "reference_box": list(s.fft_dims),
                 "avg_launch_ms": local_ms / max(1, local_launches),
                 "traffic": None, "step_share": local_ms / (local_ms + prep_ms + fin_ms),
                 "prepare_ms": prep_ms, "finish_ms": fin_ms}

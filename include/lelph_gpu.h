@@ -92,6 +92,8 @@ typedef struct lelph_gpu_stats
     double finish_ms;            /* device time of the finish kernel (profiling on) */
     long long pairs_done;        /* (k, q) pairs computed */
     size_t device_bytes;         /* device memory held by the context */
+    int product_grid[3];         /* grid of the real-space sandwich and wavefunction FFTs */
+    int chunk_points;            /* grid points per K chunk of the tensor-core sandwich (mixed form) */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

@@ -495,6 +495,10 @@ extern "C" int lelph_gpu_stats_get(lelph_gpu* h, lelph_gpu_stats* s)
     size_t tot = 0;
     for (DevBuf* b : h->owned) tot += b->n;
     s->device_bytes = tot;
+    s->product_grid[0] = h->g.Nx;
+    s->product_grid[1] = h->g.Ny;
+    s->product_grid[2] = h->g.Nz;
+    s->chunk_points = h->chunk_pts;
     return LELPH_GPU_OK;
 }
 

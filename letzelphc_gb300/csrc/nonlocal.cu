@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
 
@@ -60,13 +62,48 @@ __device__ __forceinline__ double ylm_real(int l, int m, double vx, double vy, d
     return sh;
 }
 
-#define PJ_G 32
+#define PJ_G 16
 #define PJ_MAXP 24
+#define PJ_ROWS 64   // (atom, projector, component) rows per block
+#define PJ_SETS 32   // coefficient sets per block
 
-// grid: (nk, natom, nsb * npb); 256 threads.  A block covers nset_b <= 64
-// consecutive coefficient sets (set-block sb) and 256/nset_b consecutive
-// (projector, component) pairs (px-block pb); one output per thread.
-// Pi layout: proj[(((kbz*natom + a)*nproj_max + p)*4 + x)*nsets + set],
+// Real spherical harmonics of all (l, m), l <= lmax, at K, written to y[l*l + l + m]:
+// cos(m phi), sin(m phi) by the angle-addition recurrence from cos(phi), sin(phi).
+__device__ __forceinline__ void ylm_all(int lmax, double vx, double vy, double vz, double* y)
+{
+    const double fact[8] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0};
+    const double norm = sqrt(vx * vx + vy * vy + vz * vz);
+    if (norm < 1e-6)
+    {
+        for (int i = 0; i < (lmax + 1) * (lmax + 1); ++i) y[i] = 0.0;
+        y[0] = 1.0 / sqrt(4 * LELPH_PI_T);
+        return;
+    }
+    const double cost = vz / norm;
+    const double rxy = sqrt(vx * vx + vy * vy);
+    const double c1 = rxy > 0.0 ? vx / rxy : 1.0, s1 = rxy > 0.0 ? vy / rxy : 0.0;
+    double cm = 1.0, sm = 0.0;  // cos(m phi), sin(m phi)
+    for (int m = 0; m <= lmax; ++m)
+    {
+        for (int l = m; l <= lmax; ++l)
+        {
+            double p = ylm_legendre(l, m, cost) * sqrt(fact[l - m] * (2 * l + 1) / (4 * LELPH_PI_T * fact[l + m]));
+            if (m == 0)
+                y[l * l + l] = p;
+            else
+            {
+                y[l * l + l + m] = sqrt(2.0) * cm * p;
+                y[l * l + l - m] = sqrt(2.0) * sm * p;
+            }
+        }
+        const double cn = cm * c1 - sm * s1, sn = sm * c1 + cm * s1;
+        cm = cn;
+        sm = sn;
+    }
+}
+
+// grid: (nk, row blocks, set blocks); 256 threads, 4 rows x 2 sets per thread.
+// Rows r = (atom*nproj_max + p)*4 + x; Pi layout proj[((kbz*rows_tot) + r)*nsets + set],
 // nsets = nspin*nbnds*nspinor, set = (spin*nbnds + band)*nspinor + spinor.
 template <int F32ACC>
 __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __restrict__ ks,
@@ -76,119 +113,182 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
                                                      const long long* __restrict__ fk_off,
                                                      const double2* __restrict__ chat,
                                                      const long long* __restrict__ chat_off, NonlocalDesc nl,
-                                                     GeomDev gd, int nset_b, int nsb, double2* __restrict__ proj)
+                                                     GeomDev gd, double2* __restrict__ proj)
 {
-    __shared__ double2 base_s[PJ_MAXP][PJ_G];  // F e^{-i 2pi K.tau_a} Y_lm(K) per projector
+    typedef typename cplx_of<typename std::conditional<F32ACC, float, double>::type>::type C2;
+    __shared__ double2 beta_s[PJ_ROWS][PJ_G + 1];
+    __shared__ double2 ch_s[PJ_G][PJ_SETS + 1];
+    __shared__ double ylm_s[16][PJ_G];
     __shared__ double kx_s[3][PJ_G];
-    __shared__ double2 ch_s[PJ_G][65];
-    __shared__ int plist[PJ_MAXP][3];  // (lidx, l, m)
-    __shared__ double psign[PJ_MAXP];
-    __shared__ int nproj_s;
+    __shared__ double2 ph_s[4][PJ_G];   // structure-factor phases of the (up to 4) atoms of the row block
+    __shared__ int rinfo[PJ_ROWS][4];  // atom slot, lm index, (lidx*ntype+type), x
+    __shared__ double rsign[PJ_ROWS];
     const int kbz = k0 + blockIdx.x;
-    const int a = blockIdx.y;
-    const int sb = blockIdx.z % nsb, pb = blockIdx.z / nsb;
     const KPointSym S = ks[kbz];
-    const int it = nl.atom_type[a];
     const int npw = npw_arr[S.ik];
     const int nsets = gd.nspin * gd.nbnds * gd.nspinor;
-    if (threadIdx.x == 0)
+    const int rows_tot = nl.natom * nl.nproj_max * 4;
+    const int r0 = blockIdx.y * PJ_ROWS;
+    const int s0 = blockIdx.z * PJ_SETS;
+    const int nr = min(PJ_ROWS, rows_tot - r0);
+    const int ns = min(PJ_SETS, nsets - s0);
+    const int a0 = r0 / (nl.nproj_max * 4);
+    if (threadIdx.x < PJ_ROWS)
     {
-        int np = 0;
-        for (int lidx = 0; lidx < nl.nltimesj; ++lidx)
+        const int r = r0 + threadIdx.x;
+        int info[4] = {-1, 0, 0, 0};
+        double sg = 1.0;
+        if (threadIdx.x < nr)
         {
-            int l = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3] - 1.0);
-            if (l < 0) continue;
-            for (int im = 0; im <= 2 * l && np < PJ_MAXP; ++im, ++np)
+            const int a = r / (nl.nproj_max * 4);
+            const int p = (r / 4) % nl.nproj_max;
+            const int x = r % 4;
+            const int it = nl.atom_type[a];
+            int np = 0;
+            for (int lidx = 0; lidx < nl.nltimesj; ++lidx)
             {
-                plist[np][0] = lidx;
-                plist[np][1] = l;
-                plist[np][2] = im - l;
-                psign[np] = nl.Fsign[lidx * nl.ntype + it];
+                int l = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3] - 1.0);
+                if (l < 0) continue;
+                if (p >= np && p < np + 2 * l + 1)
+                {
+                    info[0] = a - a0;
+                    info[1] = l * l + (p - np);  // lm index: l*l + l + m with m = (p-np) - l
+                    info[2] = lidx * nl.ntype + it;
+                    info[3] = x;
+                    sg = nl.Fsign[lidx * nl.ntype + it];
+                }
+                np += 2 * l + 1;
             }
         }
-        nproj_s = np;
+        for (int c = 0; c < 4; ++c) rinfo[threadIdx.x][c] = info[c];
+        rsign[threadIdx.x] = sg;
     }
-    __syncthreads();
-    const int nproj = nproj_s;
-    const int ppb = blockDim.x / nset_b;
-    const int set_l = threadIdx.x % nset_b;
-    const int px = pb * ppb + threadIdx.x / nset_b;
-    const int p = px >> 2, x = px & 3;
-    const int set0 = sb * nset_b;
-    const int set = set0 + set_l;
-    const int nset_here = min(nset_b, nsets - set0);
-    const bool active = (threadIdx.x / nset_b) < ppb && p < nproj && set < nsets;
+    const int tr = threadIdx.x / 16, tsx = threadIdx.x % 16;  // rows tr*4.., sets tsx*2..
+    C2 acc[4][2];
+    double2 acc64[4][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+        {
+            acc[i][j].x = 0;
+            acc[i][j].y = 0;
+            acc64[i][j] = make_double2(0.0, 0.0);
+        }
     const double* G = gvec + 3 * pw_off[S.ik];
     const double* F = Fk + fk_off[S.ik];
-    const double2* C = chat + chat_off[kbz];
-    const double tx = nl.atom_pos[3 * a], ty = nl.atom_pos[3 * a + 1], tz = nl.atom_pos[3 * a + 2];
-    double2 acc = make_double2(0.0, 0.0);
+    const double2* Cc = chat + chat_off[kbz];
+    const int natom_blk = min(4, nl.natom - a0);
     for (int g0 = 0; g0 < npw; g0 += PJ_G)
     {
         const int ng = min(PJ_G, npw - g0);
         __syncthreads();
-        if (threadIdx.x < ng)
+        if (threadIdx.x < PJ_G)
         {
-            int g = g0 + threadIdx.x;
-            // K = S (k + G), cartesian (src/nonloc/Vbare_nloc.c:148-168)
-            double v0 = S.kcart[0] + G[3 * g], v1 = S.kcart[1] + G[3 * g + 1], v2 = S.kcart[2] + G[3 * g + 2];
-            double K0 = S.R[0] * v0 + S.R[1] * v1 + S.R[2] * v2;
-            double K1 = S.R[3] * v0 + S.R[4] * v1 + S.R[5] * v2;
-            double K2 = S.R[6] * v0 + S.R[7] * v1 + S.R[8] * v2;
-            kx_s[0][threadIdx.x] = K0;
-            kx_s[1][threadIdx.x] = K1;
-            kx_s[2][threadIdx.x] = K2;
-            double dot = K0 * tx + K1 * ty + K2 * tz;
-            double sn, cs;
-            sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
-            for (int pp = 0; pp < nproj; ++pp)
+            const int t = threadIdx.x;
+            double y[16];
+            if (t < ng)
             {
-                int lidx = plist[pp][0], l = plist[pp][1], m = plist[pp][2];
-                double f = F[((size_t)lidx * nl.ntype + it) * npw + g];
-                double y = ylm_real(l, m, K0, K1, K2);
-                base_s[pp][threadIdx.x] = make_double2(f * cs * y, -f * sn * y);
+                const int g = g0 + t;
+                // K = S (k + G), cartesian (src/nonloc/Vbare_nloc.c:148-168)
+                double v0 = S.kcart[0] + G[3 * g], v1 = S.kcart[1] + G[3 * g + 1], v2 = S.kcart[2] + G[3 * g + 2];
+                double K0 = S.R[0] * v0 + S.R[1] * v1 + S.R[2] * v2;
+                double K1 = S.R[3] * v0 + S.R[4] * v1 + S.R[5] * v2;
+                double K2 = S.R[6] * v0 + S.R[7] * v1 + S.R[8] * v2;
+                kx_s[0][t] = K0;
+                kx_s[1][t] = K1;
+                kx_s[2][t] = K2;
+                ylm_all(nl.lmax, K0, K1, K2, y);
+                for (int i = 0; i < (nl.lmax + 1) * (nl.lmax + 1); ++i) ylm_s[i][t] = y[i];
+                for (int aa = 0; aa < natom_blk; ++aa)
+                {
+                    const double* tau = nl.atom_pos + 3 * (a0 + aa);
+                    double dot = K0 * tau[0] + K1 * tau[1] + K2 * tau[2];
+                    double sn, cs;
+                    sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
+                    ph_s[aa][t] = make_double2(cs, -sn);
+                }
             }
         }
-        for (int e = threadIdx.x; e < ng * nset_here; e += blockDim.x)
+        for (int e = threadIdx.x; e < ns * PJ_G; e += blockDim.x)
         {
-            int gg = e / nset_here, ss = e - gg * nset_here;
-            ch_s[gg][ss] = C[(size_t)(set0 + ss) * npw + g0 + gg];
+            const int ss = e / PJ_G, gg = e - ss * PJ_G;
+            ch_s[gg][ss] = gg < ng ? Cc[(size_t)(s0 + ss) * npw + g0 + gg] : make_double2(0.0, 0.0);
         }
         __syncthreads();
-        if (active)
+        // beta_x(G) = F e^{-i 2pi K.tau} Y_lm (1 | K_x sign)  (src/nonloc/Vbare_nloc.c:318-363)
+        for (int e = threadIdx.x; e < PJ_ROWS * PJ_G; e += blockDim.x)
         {
-            const double kk = (x > 0) ? psign[p] : 1.0;
-            if (F32ACC)
+            const int rr = e / PJ_G, gg = e - rr * PJ_G;
+            double2 b = make_double2(0.0, 0.0);
+            if (gg < ng && rinfo[rr][0] >= 0)
             {
-                float2 a32 = make_float2(0.f, 0.f);
-                for (int gg = 0; gg < ng; ++gg)
+                const double f = F[(size_t)rinfo[rr][2] * npw + g0 + gg];
+                const double2 ph = ph_s[rinfo[rr][0]][gg];
+                const double fy = f * ylm_s[rinfo[rr][1]][gg];
+                b = make_double2(fy * ph.x, fy * ph.y);
+                const int x = rinfo[rr][3];
+                if (x > 0)
                 {
-                    double2 b = base_s[p][gg];
-                    double w = (x > 0) ? kx_s[x - 1][gg] * kk : 1.0;
-                    float2 bf = make_float2((float)(b.x * w), (float)(b.y * w));
-                    double2 c = ch_s[gg][set_l];
-                    a32 = cadd(a32, cmul(bf, make_float2((float)c.x, (float)-c.y)));
-                }
-                acc.x += a32.x;
-                acc.y += a32.y;
-            }
-            else
-            {
-                for (int gg = 0; gg < ng; ++gg)
-                {
-                    double2 b = base_s[p][gg];
-                    if (x > 0)
-                    {
-                        double w = kx_s[x - 1][gg] * kk;
-                        b.x *= w;
-                        b.y *= w;
-                    }
-                    acc = cadd(acc, cmul(b, cconj(ch_s[gg][set_l])));
+                    const double w = kx_s[x - 1][gg] * rsign[rr];
+                    b.x *= w;
+                    b.y *= w;
                 }
             }
+            beta_s[rr][gg] = b;
+        }
+        __syncthreads();
+        // Pi += beta conj(c^) over the chunk
+#pragma unroll 4
+        for (int gg = 0; gg < PJ_G; ++gg)
+        {
+            C2 bv[4], cv[2];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+            {
+                double2 b = beta_s[tr * 4 + i][gg];
+                bv[i].x = b.x;
+                bv[i].y = b.y;
+            }
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+            {
+                double2 c = ch_s[gg][tsx * 2 + j];
+                cv[j].x = c.x;
+                cv[j].y = -c.y;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) acc[i][j] = cadd(acc[i][j], cmul(bv[i], cv[j]));
+        }
+        if (F32ACC)
+        {
+            // chunk sums in FP32, the running sum in FP64
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                {
+                    acc64[i][j].x += (double)acc[i][j].x;
+                    acc64[i][j].y += (double)acc[i][j].y;
+                    acc[i][j].x = 0;
+                    acc[i][j].y = 0;
+                }
         }
     }
-    if (active) proj[((((size_t)kbz * nl.natom + a) * nl.nproj_max + p) * 4 + x) * nsets + set] = acc;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+        {
+            const int rr = tr * 4 + i, ss = tsx * 2 + j;
+            if (rr < nr && ss < ns)
+            {
+                double2 v = F32ACC ? acc64[i][j] : make_double2((double)acc[i][j].x, (double)acc[i][j].y);
+                proj[((size_t)kbz * rows_tot + r0 + rr) * nsets + s0 + ss] = v;
+            }
+        }
 }
 
 void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const double* gvec, const long long* pw_off,
@@ -197,17 +297,14 @@ void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const d
                               double2* proj, cudaStream_t st)
 {
     const int nsets = g.nspin * g.nbnds * g.nspinor;
-    const int nset_b = nsets < 64 ? nsets : 64;
-    const int nsb = (nsets + nset_b - 1) / nset_b;
-    const int ppb = 256 / nset_b;
-    const int npb = (nl.nproj_max * 4 + ppb - 1) / ppb;
-    dim3 grid(nk, nl.natom, nsb * npb);
+    const int rows = nl.natom * nl.nproj_max * 4;
+    dim3 grid(nk, (rows + PJ_ROWS - 1) / PJ_ROWS, (nsets + PJ_SETS - 1) / PJ_SETS);
     if (f32acc)
         k_projections<1><<<grid, 256, 0, st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off, chat, chat_off, nl, g,
-                                               nset_b, nsb, proj);
+                                               proj);
     else
         k_projections<0><<<grid, 256, 0, st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off, chat, chat_off, nl, g,
-                                               nset_b, nsb, proj);
+                                               proj);
 }
 
 // ------------------------------------------------------------------ finish
@@ -345,11 +442,197 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
     }
 }
 
+// Finish, one block per (pair, spin): the two projection sets of the pair
+// (this spin) and the pair's eigVec live in shared memory; each thread owns
+// (m, n) elements and keeps the 3*natom displacement sums in registers.
+template <int NJ>
+__global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const PairInfo* __restrict__ pairs, int mode_fp64,
+                                                     const double2* __restrict__ glocal,
+                                                     const float* __restrict__ partials, int nchunks,
+                                                     const float* __restrict__ mode_scale,
+                                                     const float* __restrict__ band_scale,
+                                                     const double2* __restrict__ proj,
+                                                     const double2* __restrict__ eig, int non_loc, NonlocalDesc nl,
+                                                     GeomDev gd, int out_c64, void* __restrict__ gout)
+{
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int zp = blockIdx.x;
+    const int pair = zp / gd.nspin, spin = zp - pair * gd.nspin;
+    const PairInfo P = pairs[pair];
+    const int nb = gd.nbnds, ns = gd.nspinor;
+    const int nsets = gd.nspin * nb * ns;
+    const int sets = nb * ns;  // this spin's sets
+    const int rows = nl.natom * nl.nproj_max * 4;
+    const int nj = 3 * nl.natom;
+    double2* sK = reinterpret_cast<double2*>(fsm);           // [rows][sets]  role k+q
+    double2* sKp = sK + (size_t)rows * sets;                  // [rows][sets]  role k (raw Pi)
+    double2* sE = sKp + (size_t)rows * sets;                  // [nmodes][nj]
+    int* sch = reinterpret_cast<int*>(sE + (size_t)gd.nmodes * nj);  // channels: [type][8][4] = lidx, l, pbase, foff
+    double* ssoc = reinterpret_cast<double*>(sch + nl.ntype * 8 * 4);
+    if (non_loc)
+    {
+        const double2* PK = proj + (size_t)P.kbz_kq * rows * nsets + (size_t)spin * sets;
+        const double2* PKp = proj + (size_t)P.kbz_k * rows * nsets + (size_t)spin * sets;
+        for (int e = threadIdx.x; e < rows * sets; e += blockDim.x)
+        {
+            const int r = e / sets, c = e - r * sets;
+            sK[e] = PK[(size_t)r * nsets + c];
+            sKp[e] = PKp[(size_t)r * nsets + c];
+        }
+        const double2* E = eig + (size_t)P.qslot * gd.nmodes * gd.nmodes;
+        for (int e = threadIdx.x; e < gd.nmodes * nj; e += blockDim.x) sE[e] = E[(e / nj) * gd.nmodes + (e % nj)];
+        if (threadIdx.x < nl.ntype)
+        {
+            const int it = threadIdx.x;
+            int nc = 0, pb = 0;
+            for (int lidx = 0; lidx < nl.nltimesj && nc < 8; ++lidx)
+            {
+                int l = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3] - 1.0);
+                if (l < 0) continue;
+                int twoj = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3 + 1]);
+                int* ch = sch + (it * 8 + nc) * 4;
+                ch[0] = lidx;
+                ch[1] = l;
+                ch[2] = pb;
+                ch[3] = nl.fcoef ? nl.fcoef_off[lidx * nl.ntype + it] : -1;
+                ssoc[it * 8 + nc] = (twoj != 0 && !nl.is_soc) ? (twoj + 1.0) / (4.0 * l + 2.0) : 1.0;
+                pb += 2 * l + 1;
+                ++nc;
+            }
+            for (; nc < 8; ++nc) sch[(it * 8 + nc) * 4 + 1] = -1;
+        }
+        __syncthreads();
+    }
+    const double invN = 1.0 / ((double)gd.Nx * gd.Ny * gd.Nz);
+    const int mtiles = (gd.nmodes + gd.mt_modes - 1) / gd.mt_modes;
+    const int NT = 2 * gd.nbp;
+    const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
+    {
+        const int m = e / nb, n = e - m * nb;  // m: band of k, n: band of k+q
+        double2 out[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) out[j] = make_double2(0.0, 0.0);
+        if (non_loc)
+        {
+#pragma unroll
+            for (int j = 0; j < NJ; ++j)
+            {
+                if (j >= nj) continue;
+                const int a = j / 3, x = j - 3 * a;
+                const int it = nl.atom_type[a];
+                const int rb = a * nl.nproj_max * 4;
+                double2 acc = make_double2(0.0, 0.0);
+                for (int c = 0; c < 8; ++c)
+                {
+                    const int* ch = sch + (it * 8 + c) * 4;
+                    const int l = ch[1];
+                    if (l < 0) break;
+                    const int tl = 2 * l + 1, pb = ch[2], foff = ch[3];
+                    const double soc = ssoc[it * 8 + c];
+                    for (int im1 = 0; im1 < tl; ++im1)
+                        for (int im2 = 0; im2 < tl; ++im2)
+                        {
+                            if (foff < 0 && im1 != im2) continue;
+                            const int p1 = pb + im1, p2 = pb + im2;
+                            for (int s1 = 0; s1 < ns; ++s1)
+                                for (int s2 = 0; s2 < ns; ++s2)
+                                {
+                                    double2 f;
+                                    if (foff >= 0)
+                                    {
+                                        const double* fc = nl.fcoef + 2 * ((size_t)foff + (im1 * tl + im2) * ns * ns + s1 * ns + s2);
+                                        f = make_double2(fc[0], fc[1]);
+                                    }
+                                    else
+                                    {
+                                        if (s1 != s2) continue;
+                                        f = make_double2(soc, 0.0);
+                                    }
+                                    const double2 K0 = sK[(size_t)(rb + p1 * 4 + 0) * sets + n * ns + s1];
+                                    const double2 Kx = sK[(size_t)(rb + p1 * 4 + 1 + x) * sets + n * ns + s1];
+                                    const double2 Kp0 = cconj(sKp[(size_t)(rb + p2 * 4 + 0) * sets + m * ns + s2]);
+                                    double2 Kpx = sKp[(size_t)(rb + p2 * 4 + 1 + x) * sets + m * ns + s2];
+                                    Kpx = make_double2(-Kpx.x, Kpx.y);  // -conj
+                                    acc = cadd(acc, cmul(f, cadd(cmul(Kx, Kp0), cmul(K0, Kpx))));
+                                }
+                        }
+                }
+                out[j] = acc;
+            }
+        }
+        for (int nu = 0; nu < gd.nmodes; ++nu)
+        {
+            double2 v;
+            if (mode_fp64)
+            {
+                v = glocal[((size_t)zp * gd.nmodes * nb + nu * nb + m) * nb + n];
+            }
+            else
+            {
+                const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
+                const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
+                double re = 0.0, im = 0.0;
+                for (int c = 0; c < nchunks; ++c)
+                {
+                    re += (double)pp[(size_t)c * 128 * NT + n];
+                    im += (double)pp[(size_t)c * 128 * NT + gd.nbp + n];
+                }
+                const double sc = (double)mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
+                                  (double)band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
+                                  (double)band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
+                const double f = invN / sc;
+                v = make_double2(re * f, im * f);
+            }
+            if (non_loc)
+            {
+                double2 sacc = make_double2(0.0, 0.0);
+#pragma unroll
+                for (int j = 0; j < NJ; ++j)
+                    if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
+                v = cadd(v, cmul(pre, sacc));
+            }
+            const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
+            if (out_c64)
+                reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
+            else
+                reinterpret_cast<double2*>(gout)[oidx] = v;
+        }
+    }
+}
+
+static size_t finish_pair_smem(const NonlocalDesc& nl, const GeomDev& g)
+{
+    const size_t rows = (size_t)nl.natom * nl.nproj_max * 4;
+    const size_t sets = (size_t)g.nbnds * g.nspinor;
+    return 2 * rows * sets * sizeof(double2) + (size_t)g.nmodes * 3 * nl.natom * sizeof(double2) +
+           (size_t)nl.ntype * 8 * 4 * sizeof(int) + (size_t)nl.ntype * 8 * sizeof(double);
+}
+
 void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const double2* glocal,
                          const float* partials, int nchunks, const float* mode_scale, const float* band_scale,
                          const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,
                          const GeomDev& g, int out_c64, void* gout, cudaStream_t st)
 {
+    const size_t smem = finish_pair_smem(nl, g);
+    const int nj = 3 * nl.natom;
+    if (smem <= 160 * 1024 && nj <= 24)
+    {
+        static bool attr = false;
+        if (!attr)
+        {
+            cudaFuncSetAttribute(k_finish_pair<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(k_finish_pair<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            attr = true;
+        }
+        const int nz = npairs * g.nspin;
+#define FINL(NJ) k_finish_pair<NJ><<<nz, NJ <= 12 ? 256 : 128, smem, st>>>(pairs, mode_fp64, glocal, partials, nchunks, mode_scale, \
+                                                          band_scale, proj, eig, non_loc, nl, g, out_c64, gout)
+        if (nj <= 12) FINL(12);
+        else FINL(24);
+#undef FINL
+        return;
+    }
     dim3 grid((g.nbnds * g.nbnds + FIN_MN - 1) / FIN_MN, npairs * g.nspin);
     k_finish<<<grid, 256, 0, st>>>(pairs, mode_fp64, glocal, partials, nchunks, mode_scale, band_scale, proj, eig,
                                    non_loc, nl, g, out_c64, gout);

@@ -47,7 +47,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("kernel_launches", C.c_longlong), ("local_launches", C.c_longlong), ("local_ms", C.c_double),
         ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
-        ("device_bytes", C.c_size_t),
+        ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
     ]
 
 
@@ -251,7 +251,9 @@ class LelphGPU:
     def stats(self):
         st = Stats()
         self._check(self._L.lelph_gpu_stats_get(self.h, C.byref(st)))
-        return {f: getattr(st, f) for f, _ in Stats._fields_}
+        out = {f: getattr(st, f) for f, _ in Stats._fields_}
+        out["product_grid"] = tuple(out["product_grid"])
+        return out
 
     def stream(self):
         return self._L.lelph_gpu_stream(self.h)

@@ -35,9 +35,9 @@ def test_descriptor_layout_matches_c():
 #include <stddef.h>
 #include "lelph_gpu.h"
 int main(void){
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(lelph_gpu_desc), offsetof(lelph_gpu_desc, alat_vec),
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(lelph_gpu_desc), offsetof(lelph_gpu_desc, alat_vec),
          offsetof(lelph_gpu_desc, npw), offsetof(lelph_gpu_desc, ntype), offsetof(lelph_gpu_desc, precision),
-         sizeof(lelph_gpu_stats));
+         sizeof(lelph_gpu_stats), offsetof(lelph_gpu_stats, product_grid));
   return 0; }
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -48,7 +48,7 @@ int main(void){
         out = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     D = elph.Desc
     assert out == [ctypes.sizeof(D), D.alat_vec.offset, D.npw.offset, D.ntype.offset, D.precision.offset,
-                   ctypes.sizeof(elph.Stats)]
+                   ctypes.sizeof(elph.Stats), elph.Stats.product_grid.offset]
 
 
 def test_strerror_covers_status_codes():
