@@ -14,7 +14,8 @@
 //   slab transposes of src/fft/transpose.c.  Unnormalised, sign +1 is
 //   FFTW_BACKWARD.
 // * k_fft_x_split: the last (x) pass of the mixed form, whose epilogue writes
-//   psi(r) straight into the split-precision tensor-core operand layout.
+//   psi(r) straight into the split-precision tensor-core operand layout (the
+//   k+q role) and as FP32 (the k role, from which the A operand is formed).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -245,7 +246,7 @@ template <int BF16>
 __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ boxes, int nbox, int k0, int ich,
                                                      int nchunk, FftPlan1D p, const float2* __restrict__ tw,
                                                      int sign, GeomDev gd, const float* __restrict__ band_scale,
-                                                     uint16_t* __restrict__ Bsplit)
+                                                     uint16_t* __restrict__ Bsplit, float2* __restrict__ psi32)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* a = reinterpret_cast<float2*>(smraw);
@@ -276,10 +277,14 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     int kslot = t / gd.nspin;
     int kbz = k0 + kslot;
     float sc = band_scale[((size_t)kbz * gd.nspin + spin) * gd.nbnds + band];
-    const long long Kr = 2LL * gd.nspinor * N;
-    const int nrow = 2 * gd.nbp;
-    size_t base_hi = ((size_t)(kbz * gd.nspin + spin) * 2 + 0) * nrow * Kr;
-    size_t base_lo = ((size_t)(kbz * gd.nspin + spin) * 2 + 1) * nrow * Kr;
+    // tile-major operands: one 32-point K block of all rows of a (k, spin, hi|lo)
+    // group is contiguous (NT rows x 128 B), as is one 16-point block of the
+    // FP32 rows of a (k, spin) (nbp rows x 128 B)
+    const int NT = 2 * gd.nbp;
+    const size_t nkb = (size_t)gd.nspinor * N / 32;
+    const size_t npb = (size_t)gd.nspinor * N / 16;
+    const size_t rg_hi = (size_t)(kbz * gd.nspin + spin) * 2;
+    const size_t pg = (size_t)(kbz * gd.nspin + spin);
     uint32_t* Bw = reinterpret_cast<uint32_t*>(Bsplit);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
@@ -291,12 +296,14 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
         uint32_t h0, l0, h1, l1;
         split2<BF16>(v.x, v.y, h0, l0);
         split2<BF16>(-v.y, v.x, h1, l1);
-        size_t e_nat = ((size_t)band * Kr + 2 * kc) >> 1;
-        size_t e_rot = ((size_t)(gd.nbp + band) * Kr + 2 * kc) >> 1;
-        Bw[(base_hi >> 1) + e_nat] = h0;
-        Bw[(base_lo >> 1) + e_nat] = l0;
-        Bw[(base_hi >> 1) + e_rot] = h1;
-        Bw[(base_lo >> 1) + e_rot] = l1;
+        const size_t kb = (size_t)(kc >> 5), kw = (size_t)(kc & 31);
+        const size_t t_hi = (rg_hi * nkb + kb) * NT, t_lo = ((rg_hi + 1) * nkb + kb) * NT;
+        Bw[(t_hi + band) * 32 + kw] = h0;
+        Bw[(t_lo + band) * 32 + kw] = l0;
+        Bw[(t_hi + gd.nbp + band) * 32 + kw] = h1;
+        Bw[(t_lo + gd.nbp + band) * 32 + kw] = l1;
+        // FP32 copy of the scaled psi(r) (rows (kbz, spin, band))
+        psi32[((pg * npb + (size_t)(kc >> 4)) * gd.nbp + band) * 16 + (kc & 15)] = v;
     }
 }
 
@@ -449,7 +456,7 @@ void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const
 
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
-                                 cudaStream_t st)
+                                 float2* psi32, cudaStream_t st)
 {
     const int inner = g.Ny * g.Nz;
     int ich = ich_for(p.L, inner, 4096);
@@ -465,9 +472,11 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
     }
     unsigned nb = (unsigned)(nbox * nchunk);
     if (ab_bf16)
-        k_fft_x_split<1><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit);
+        k_fft_x_split<1><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
+                                                psi32);
     else
-        k_fft_x_split<0><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit);
+        k_fft_x_split<0><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
+                                                psi32);
 }
 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,

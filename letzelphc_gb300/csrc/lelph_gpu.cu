@@ -69,7 +69,7 @@ struct lelph_gpu
     // device buffers
     std::vector<DevBuf*> owned;
     DevBuf d_miller, d_pwoff, d_npw, d_coef, d_coefoff, d_gvec, d_fk, d_fkoff, d_ksym, d_chat, d_chatoff;
-    DevBuf d_psi64, d_boxes32, d_bsplit, d_band_scale, d_proj;
+    DevBuf d_psi64, d_boxes32, d_bsplit, d_psi32, d_band_scale, d_proj;
     DevBuf d_atype, d_apos, d_pp, d_fsign, d_fcoef, d_fcoefoff;
     DevBuf d_tw64[3], d_tw32[3], d_twN[3];
     DevBuf d_dvr, d_eig, d_maxabs;                 // per q slot: dV_scf on the reference box (FP64), eigVec
@@ -82,7 +82,7 @@ struct lelph_gpu
     std::vector<int> win_base;  // first window entry of each q slot
     int nwin = 0;
     bool windows_ok = false;
-    CUtensorMap tmapB, tmapA, tmapV;
+    CUtensorMap tmapB, tmapP, tmapV;
     void* tmapV_base = nullptr;
     int tmapV_rows = 0;
     int nslots_alloc = 0;
@@ -250,13 +250,24 @@ float pow2_scale(double bound, double target)
 
 // -------------------------------------------------------------- small kernels
 
-__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, long long n,
-                             long long per_mode, const float* __restrict__ scale)
+// scaled FP32 copy of nwin windows (rows (mode, component) of M points) into the
+// tile-major window array: 32-point blocks of all ncomp rows of a window contiguous
+__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, int nwin, int ncomp,
+                             long long M, int wbase, int nmag, const float* __restrict__ scale)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    const long long nkb = M / 32;
+    const long long n = (long long)nwin * ncomp * M;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n; o += (long long)gridDim.x * blockDim.x)
     {
-        const double sc = (double)scale[i / per_mode];
-        out[i] = make_float2((float)(in[i].x * sc), (float)(in[i].y * sc));
+        const int p = (int)(o & 31);
+        long long t = o >> 5;
+        const int row = (int)(t % ncomp);
+        t /= ncomp;
+        const long long kb = t % nkb;
+        const int w = (int)(t / nkb);
+        const double2 v = in[((size_t)w * ncomp + row) * M + kb * 32 + p];
+        const double sc = (double)scale[(size_t)w * (ncomp / nmag) + row / nmag];
+        out[(((size_t)(wbase + w) * nkb + kb) * ncomp + row) * 32 + p] = make_float2((float)(v.x * sc), (float)(v.y * sc));
     }
 }
 
@@ -352,16 +363,36 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode()
 }
 
 int make_tmap(lelph_gpu* h, CUtensorMap* m, void* base, unsigned long long inner, unsigned long long rows,
-              unsigned box_rows, bool swz, bool f32 = false)
+              unsigned box_rows, bool swz, bool f32 = false, unsigned box_inner = 64)
 {
     auto enc = get_encode();
     if (!enc) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     const unsigned long long es_bytes = f32 ? 4 : 2;
     cuuint64_t dims[2] = {inner, rows};
     cuuint64_t strides[1] = {inner * es_bytes};
-    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t box[2] = {box_inner, box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = enc(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, base, dims, strides,
+                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    return LELPH_GPU_OK;
+}
+
+// 3-D tile-major tensor: dims {inner, rows, blocks}, rows packed (stride inner
+// elements), blocks packed (stride rows * inner elements)
+int make_tmap3(lelph_gpu* h, CUtensorMap* m, void* base, bool f32, unsigned long long inner, unsigned long long rows,
+               unsigned long long blocks, unsigned box_rows, unsigned box_blocks, bool swz)
+{
+    auto enc = get_encode();
+    if (!enc) return fail(h, LELPH_GPU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    const unsigned long long es_bytes = f32 ? 4 : 2;
+    cuuint64_t dims[3] = {inner, rows, blocks};
+    cuuint64_t strides[2] = {inner * es_bytes, rows * inner * es_bytes};
+    cuuint32_t box[3] = {(cuuint32_t)inner, box_rows, box_blocks};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = enc(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, base, dims, strides,
                      box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                      swz ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -595,7 +626,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->g.nmag = d.nmag;
     h->g.nmodes = d.nmodes;
     h->g.mt_modes = std::min(d.nmodes, std::max(1, 128 / d.nbnds));
-    if (h->mixed && 2 * h->g.nbp > 128) return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
+    if (h->mixed && (2 * h->g.nbp > 128 || !lelph_local_tc_supported(h->g)))
+        return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
     // host copies
@@ -806,7 +838,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     cudaEventCreate(&h->ev1);
     DevBuf* bufs[] = {&h->d_miller, &h->d_pwoff, &h->d_npw, &h->d_coef, &h->d_coefoff, &h->d_gvec, &h->d_fk,
                       &h->d_fkoff, &h->d_ksym, &h->d_chat, &h->d_chatoff, &h->d_psi64, &h->d_boxes32, &h->d_bsplit,
-                      &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
+                      &h->d_psi32, &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
                       &h->d_fcoefoff, &h->d_tw64[0], &h->d_tw64[1], &h->d_tw64[2], &h->d_tw32[0], &h->d_tw32[1],
                       &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
@@ -892,9 +924,18 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         rc = ensure(h, h->d_bsplit, sizeof(uint16_t) * Kr * rows);
         if (rc) return bad(rc, h->err);
         if (cudaMemsetAsync(h->d_bsplit.p, 0, h->d_bsplit.n, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
-        rc = make_tmap(h, &h->tmapB, h->d_bsplit.p, Kr, rows, 2 * h->g.nbp, true);
+        // split rows, tile-major: blocks (k, spin, hi|lo, 32-point K block) of 2*nbp rows x 64 halves
+        rc = make_tmap3(h, &h->tmapB, h->d_bsplit.p, false, 64, 2 * h->g.nbp, rows / (2 * h->g.nbp) * (Kr / 64),
+                        2 * h->g.nbp, 1, true);
         if (rc) return bad(rc, h->err);
-        rc = make_tmap(h, &h->tmapA, h->d_bsplit.p, Kr, rows, h->g.nbp, false);
+        // FP32 psi(r) of the k role, tile-major: blocks (k, spin, 16-point block) of nbp rows x 32 floats,
+        // two blocks (one 32-point stage) per box, 128-byte swizzled
+        const size_t prow = (size_t)d.nkpts_BZ * d.nspin * h->g.nbp;
+        rc = ensure(h, h->d_psi32, sizeof(float) * Kr * prow);
+        if (rc) return bad(rc, h->err);
+        if (cudaMemsetAsync(h->d_psi32.p, 0, h->d_psi32.n, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
+        rc = make_tmap3(h, &h->tmapP, h->d_psi32.p, true, 32, h->g.nbp, (size_t)d.nkpts_BZ * d.nspin * (Kr / 32),
+                        h->g.nbp, 2, true);
         if (rc) return bad(rc, h->err);
         // K chunk per CTA: a multiple of 32 grid points dividing nspinor*N, near 4096
         long long Ktot = (long long)d.nspinor * N;
@@ -975,7 +1016,8 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
             lelph_launch_fft_contig_f(bx, nbox * g.Nx * g.Ny, h->plan[2], (const float2*)h->d_tw32[2].p, +1, h->st);
             lelph_launch_fft_strided_f(bx, nbox * g.Nx, g.Nz, h->plan[1], (const float2*)h->d_tw32[1].p, +1, h->st);
             lelph_launch_fft_x_to_split(bx, nk, k0, h->plan[0], (const float2*)h->d_tw32[0].p, +1, g,
-                                        (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p, h->st);
+                                        (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p,
+                                        (float2*)h->d_psi32.p, h->st);
             h->stats.kernel_launches += 4;
         }
     }
@@ -1175,8 +1217,8 @@ static int build_windows(lelph_gpu* h)
             CUDA_TRY(h, cudaMemsetAsync(mx, 0, sizeof(unsigned) * nu * d.nmodes, h->st));
             k_dv_maxabs<<<dim3(64, nu * d.nmodes), 256, 0, h->st>>>(tM, nu * d.nmodes, d.nmag, M, mx);
             k_mode_scale<<<(nu * d.nmodes + 63) / 64, 64, 0, h->st>>>(mx, nu * d.nmodes, sc);
-            k_dv_convert<<<1024, 256, 0, h->st>>>(tM, (float2*)h->d_win32.p + base, (long long)nu * ncomp * M,
-                                                  (long long)d.nmag * M, sc);
+            k_dv_convert<<<1024, 256, 0, h->st>>>(tM, (float2*)h->d_win32.p, nu, (int)ncomp, M, h->win_base[s],
+                                                  d.nmag, sc);
         }
         h->stats.kernel_launches += h->mixed ? 10 : 7;
         CUDA_TRY(h, cudaGetLastError());
@@ -1241,10 +1283,10 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     NonlocalDesc nl = nl_desc(h);
     if (h->mixed && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
     {
-        // dV windows as a 2-D FP32 tensor: rows (window, mode, component), 2M floats each
+        // dV windows, tile-major: blocks (window, 32-point block) of (mode, component) rows x 64 floats
         const long long M = (long long)g.Nx * g.Ny * g.Nz;
-        rc = make_tmap(h, &h->tmapV, h->d_win32.p, 2ull * M, (unsigned long long)h->nwin * d.nmodes * d.nmag,
-                       (unsigned)(g.mt_modes * d.nmag), false, true);
+        rc = make_tmap3(h, &h->tmapV, h->d_win32.p, true, 64, (unsigned long long)d.nmodes * d.nmag,
+                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag), 1, false);
         if (rc) return rc;
         h->tmapV_base = h->d_win32.p;
         h->tmapV_rows = h->nwin;
@@ -1267,8 +1309,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
             lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_win64.p, g,
                                     (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
         else
-            lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapA, &h->tmapV,
-                                  (const float*)h->d_winscale.p, g, h->ab_bf16, h->chunk_pts, h->nchunks,
+            lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapP, &h->tmapV, g, h->ab_bf16, h->chunk_pts, h->nchunks,
                                   (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st);
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
@@ -1447,8 +1488,8 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
     if (h->mixed && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
     {
         const long long M = (long long)g.Nx * g.Ny * g.Nz;
-        rc = make_tmap(h, &h->tmapV, h->d_win32.p, 2ull * M, (unsigned long long)h->nwin * d.nmodes * d.nmag,
-                       (unsigned)(g.mt_modes * d.nmag), false, true);
+        rc = make_tmap3(h, &h->tmapV, h->d_win32.p, true, 64, (unsigned long long)d.nmodes * d.nmag,
+                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag), 1, false);
         if (rc) return rc;
         h->tmapV_base = h->d_win32.p;
         h->tmapV_rows = h->nwin;
@@ -1478,8 +1519,8 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
             lelph_launch_local_fp64(dpairs, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_win64.p, g,
                                     (double2*)work, (unsigned*)h->d_status.p, h->st);
         else
-            lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapA, &h->tmapV, (const float*)h->d_winscale.p, g,
-                                  h->ab_bf16, h->chunk_pts, h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st);
+            lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapP, &h->tmapV, g, h->ab_bf16, h->chunk_pts,
+                                  h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st);
         lelph_launch_finish(dpairs, nb, h->mixed ? 0 : 1, (const double2*)work, (const float*)work, h->nchunks,
                             (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,

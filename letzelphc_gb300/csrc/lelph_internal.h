@@ -59,7 +59,7 @@ void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const
 // x-pass of the mixed form writing the split tensor-core operand directly
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
-                                 cudaStream_t st);
+                                 float2* psi32, cudaStream_t st);
 
 // sphere -> box scatter with su2, fractional-translation phase and conj
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
@@ -75,9 +75,10 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
                              const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st);
 int lelph_local_tc_smem_bytes(const GeomDev& g);
 int lelph_local_tc_tile_modes(const GeomDev& g);
-void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
-                           const void* tmapV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
-                           int nchunks, float* partials, unsigned* status, cudaStream_t st);
+int lelph_local_tc_supported(const GeomDev& g);
+void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapP,
+                           const void* tmapV, const GeomDev& g, int ab_bf16, int chunk_pts, int nchunks,
+                           float* partials, unsigned* status, cudaStream_t st);
 
 // nonlocal + finish (nonlocal.cu)
 struct NonlocalDesc

@@ -62,7 +62,6 @@ __device__ __forceinline__ double ylm_real(int l, int m, double vx, double vy, d
     return sh;
 }
 
-#define PJ_G 16
 #define PJ_MAXP 24
 #define PJ_ROWS 64   // (atom, projector, component) rows per block
 #define PJ_SETS 32   // coefficient sets per block
@@ -102,10 +101,24 @@ __device__ __forceinline__ void ylm_all(int lmax, double vx, double vy, double v
     }
 }
 
+template <typename T> struct PjCfg;
+template <> struct PjCfg<float> { static constexpr int G = 64; };
+template <> struct PjCfg<double> { static constexpr int G = 32; };
+
+template <typename T> static constexpr size_t pj_smem_bytes()
+{
+    typedef typename cplx_of<T>::type C2;
+    constexpr int G = PjCfg<T>::G;
+    return sizeof(C2) * (PJ_ROWS * (G + 1) + G * (PJ_SETS + 1) + 4 * G) + sizeof(T) * (16 * G + 3 * G);
+}
+
 // grid: (nk, row blocks, set blocks); 256 threads, 4 rows x 2 sets per thread.
 // Rows r = (atom*nproj_max + p)*4 + x; Pi layout proj[((kbz*rows_tot) + r)*nsets + set],
 // nsets = nspin*nbnds*nspinor, set = (spin*nbnds + band)*nspinor + spinor.
-template <int F32ACC>
+// T = float: beta, coefficients and products in FP32, each G chunk summed in
+// FP32 and the chunk sums in FP64; the K vectors, Y_lm and the structure-factor
+// phases e^{-i 2pi K.tau} are evaluated in FP64 in both forms.
+template <typename T>
 __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __restrict__ ks,
                                                      const double* __restrict__ gvec,
                                                      const long long* __restrict__ pw_off,
@@ -115,14 +128,17 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
                                                      const long long* __restrict__ chat_off, NonlocalDesc nl,
                                                      GeomDev gd, double2* __restrict__ proj)
 {
-    typedef typename cplx_of<typename std::conditional<F32ACC, float, double>::type>::type C2;
-    __shared__ double2 beta_s[PJ_ROWS][PJ_G + 1];
-    __shared__ double2 ch_s[PJ_G][PJ_SETS + 1];
-    __shared__ double ylm_s[16][PJ_G];
-    __shared__ double kx_s[3][PJ_G];
-    __shared__ double2 ph_s[4][PJ_G];   // structure-factor phases of the (up to 4) atoms of the row block
+    typedef typename cplx_of<T>::type C2;
+    constexpr int PG = PjCfg<T>::G;
+    constexpr int PARTS = 256 / PG;
+    extern __shared__ __align__(16) unsigned char pj_smem[];
+    C2* beta_s = reinterpret_cast<C2*>(pj_smem);   // [PJ_ROWS][PG + 1]
+    C2* ch_s = beta_s + PJ_ROWS * (PG + 1);          // [PG][PJ_SETS + 1]
+    C2* ph_s = ch_s + PG * (PJ_SETS + 1);            // [4][PG]
+    T* ylm_s = reinterpret_cast<T*>(ph_s + 4 * PG);  // [16][PG]
+    T* kx_s = ylm_s + 16 * PG;                       // [3][PG]
     __shared__ int rinfo[PJ_ROWS][4];  // atom slot, lm index, (lidx*ntype+type), x
-    __shared__ double rsign[PJ_ROWS];
+    __shared__ T rsign[PJ_ROWS];
     const int kbz = k0 + blockIdx.x;
     const KPointSym S = ks[kbz];
     const int npw = npw_arr[S.ik];
@@ -161,7 +177,7 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
             }
         }
         for (int c = 0; c < 4; ++c) rinfo[threadIdx.x][c] = info[c];
-        rsign[threadIdx.x] = sg;
+        rsign[threadIdx.x] = (T)sg;
     }
     const int tr = threadIdx.x / 16, tsx = threadIdx.x % 16;  // rows tr*4.., sets tsx*2..
     C2 acc[4][2];
@@ -179,92 +195,85 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
     const double* F = Fk + fk_off[S.ik];
     const double2* Cc = chat + chat_off[kbz];
     const int natom_blk = min(4, nl.natom - a0);
-    for (int g0 = 0; g0 < npw; g0 += PJ_G)
+    const int nlm = (nl.lmax + 1) * (nl.lmax + 1);
+    for (int g0 = 0; g0 < npw; g0 += PG)
     {
-        const int ng = min(PJ_G, npw - g0);
+        const int ng = min(PG, npw - g0);
         __syncthreads();
-        if (threadIdx.x < PJ_G)
         {
-            const int t = threadIdx.x;
-            double y[16];
-            if (t < ng)
+            // K = S (k + G), cartesian (src/nonloc/Vbare_nloc.c:148-168); part 0
+            // tabulates Y_lm and K, parts 0..3 one structure-factor phase each
+            const int t = threadIdx.x % PG, part = threadIdx.x / PG;
+            if (t < ng && (part == 0 || part < natom_blk))
             {
                 const int g = g0 + t;
-                // K = S (k + G), cartesian (src/nonloc/Vbare_nloc.c:148-168)
                 double v0 = S.kcart[0] + G[3 * g], v1 = S.kcart[1] + G[3 * g + 1], v2 = S.kcart[2] + G[3 * g + 2];
                 double K0 = S.R[0] * v0 + S.R[1] * v1 + S.R[2] * v2;
                 double K1 = S.R[3] * v0 + S.R[4] * v1 + S.R[5] * v2;
                 double K2 = S.R[6] * v0 + S.R[7] * v1 + S.R[8] * v2;
-                kx_s[0][t] = K0;
-                kx_s[1][t] = K1;
-                kx_s[2][t] = K2;
-                ylm_all(nl.lmax, K0, K1, K2, y);
-                for (int i = 0; i < (nl.lmax + 1) * (nl.lmax + 1); ++i) ylm_s[i][t] = y[i];
-                for (int aa = 0; aa < natom_blk; ++aa)
+                if (part == 0)
                 {
-                    const double* tau = nl.atom_pos + 3 * (a0 + aa);
+                    double y[16];
+                    kx_s[0 * PG + t] = (T)K0;
+                    kx_s[1 * PG + t] = (T)K1;
+                    kx_s[2 * PG + t] = (T)K2;
+                    ylm_all(nl.lmax, K0, K1, K2, y);
+                    for (int i = 0; i < nlm; ++i) ylm_s[i * PG + t] = (T)y[i];
+                }
+                if (part < natom_blk)
+                {
+                    const double* tau = nl.atom_pos + 3 * (a0 + part);
                     double dot = K0 * tau[0] + K1 * tau[1] + K2 * tau[2];
                     double sn, cs;
                     sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
-                    ph_s[aa][t] = make_double2(cs, -sn);
+                    ph_s[part * PG + t] = mk2<C2>(cs, -sn);
                 }
             }
         }
-        for (int e = threadIdx.x; e < ns * PJ_G; e += blockDim.x)
+        (void)PARTS;
+        for (int e = threadIdx.x; e < ns * PG; e += blockDim.x)
         {
-            const int ss = e / PJ_G, gg = e - ss * PJ_G;
-            ch_s[gg][ss] = gg < ng ? Cc[(size_t)(s0 + ss) * npw + g0 + gg] : make_double2(0.0, 0.0);
+            const int ss = e / PG, gg = e - ss * PG;
+            const double2 c = gg < ng ? Cc[(size_t)(s0 + ss) * npw + g0 + gg] : make_double2(0.0, 0.0);
+            ch_s[gg * (PJ_SETS + 1) + ss] = mk2<C2>(c.x, -c.y);  // conj(c^)
         }
         __syncthreads();
         // beta_x(G) = F e^{-i 2pi K.tau} Y_lm (1 | K_x sign)  (src/nonloc/Vbare_nloc.c:318-363)
-        for (int e = threadIdx.x; e < PJ_ROWS * PJ_G; e += blockDim.x)
+        for (int e = threadIdx.x; e < PJ_ROWS * PG; e += blockDim.x)
         {
-            const int rr = e / PJ_G, gg = e - rr * PJ_G;
-            double2 b = make_double2(0.0, 0.0);
+            const int rr = e / PG, gg = e - rr * PG;
+            C2 b;
+            b.x = 0;
+            b.y = 0;
             if (gg < ng && rinfo[rr][0] >= 0)
             {
-                const double f = F[(size_t)rinfo[rr][2] * npw + g0 + gg];
-                const double2 ph = ph_s[rinfo[rr][0]][gg];
-                const double fy = f * ylm_s[rinfo[rr][1]][gg];
-                b = make_double2(fy * ph.x, fy * ph.y);
+                const T f = (T)F[(size_t)rinfo[rr][2] * npw + g0 + gg];
+                const C2 ph = ph_s[rinfo[rr][0] * PG + gg];
+                T fy = f * ylm_s[rinfo[rr][1] * PG + gg];
                 const int x = rinfo[rr][3];
-                if (x > 0)
-                {
-                    const double w = kx_s[x - 1][gg] * rsign[rr];
-                    b.x *= w;
-                    b.y *= w;
-                }
+                if (x > 0) fy *= kx_s[(x - 1) * PG + gg] * rsign[rr];
+                b.x = fy * ph.x;
+                b.y = fy * ph.y;
             }
-            beta_s[rr][gg] = b;
+            beta_s[rr * (PG + 1) + gg] = b;
         }
         __syncthreads();
         // Pi += beta conj(c^) over the chunk
-#pragma unroll 4
-        for (int gg = 0; gg < PJ_G; ++gg)
+#pragma unroll 8
+        for (int gg = 0; gg < PG; ++gg)
         {
             C2 bv[4], cv[2];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-            {
-                double2 b = beta_s[tr * 4 + i][gg];
-                bv[i].x = b.x;
-                bv[i].y = b.y;
-            }
+            for (int i = 0; i < 4; ++i) bv[i] = beta_s[(tr * 4 + i) * (PG + 1) + gg];
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
-            {
-                double2 c = ch_s[gg][tsx * 2 + j];
-                cv[j].x = c.x;
-                cv[j].y = -c.y;
-            }
+            for (int j = 0; j < 2; ++j) cv[j] = ch_s[gg * (PJ_SETS + 1) + tsx * 2 + j];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
                 for (int j = 0; j < 2; ++j) acc[i][j] = cadd(acc[i][j], cmul(bv[i], cv[j]));
         }
-        if (F32ACC)
+        if (std::is_same<T, float>::value)
         {
-            // chunk sums in FP32, the running sum in FP64
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -285,7 +294,8 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
             const int rr = tr * 4 + i, ss = tsx * 2 + j;
             if (rr < nr && ss < ns)
             {
-                double2 v = F32ACC ? acc64[i][j] : make_double2((double)acc[i][j].x, (double)acc[i][j].y);
+                double2 v = std::is_same<T, float>::value ? acc64[i][j]
+                                                          : make_double2((double)acc[i][j].x, (double)acc[i][j].y);
                 proj[((size_t)kbz * rows_tot + r0 + rr) * nsets + s0 + ss] = v;
             }
         }
@@ -299,12 +309,21 @@ void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const d
     const int nsets = g.nspin * g.nbnds * g.nspinor;
     const int rows = nl.natom * nl.nproj_max * 4;
     dim3 grid(nk, (rows + PJ_ROWS - 1) / PJ_ROWS, (nsets + PJ_SETS - 1) / PJ_SETS);
+    static bool attr = false;
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_projections<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pj_smem_bytes<float>());
+        cudaFuncSetAttribute(k_projections<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pj_smem_bytes<double>());
+        attr = true;
+    }
     if (f32acc)
-        k_projections<1><<<grid, 256, 0, st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off, chat, chat_off, nl, g,
-                                               proj);
+        k_projections<float><<<grid, 256, pj_smem_bytes<float>(), st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off,
+                                                                        chat, chat_off, nl, g, proj);
     else
-        k_projections<0><<<grid, 256, 0, st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off, chat, chat_off, nl, g,
-                                               proj);
+        k_projections<double><<<grid, 256, pj_smem_bytes<double>(), st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk,
+                                                                          fk_off, chat, chat_off, nl, g, proj);
 }
 
 // ------------------------------------------------------------------ finish
@@ -445,7 +464,10 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
 // Finish, one block per (pair, spin): the two projection sets of the pair
 // (this spin) and the pair's eigVec live in shared memory; each thread owns
 // (m, n) elements and keeps the 3*natom displacement sums in registers.
-template <int NJ>
+// T is the arithmetic of the nonlocal combination and the mode transform
+// (double in the plain form, float in the mixed form); the sum of the local
+// sandwich over grid chunks and the final addition are FP64 in both.
+template <int NJ, typename T>
 __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const PairInfo* __restrict__ pairs, int mode_fp64,
                                                      const double2* __restrict__ glocal,
                                                      const float* __restrict__ partials, int nchunks,
@@ -455,6 +477,7 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                                                      const double2* __restrict__ eig, int non_loc, NonlocalDesc nl,
                                                      GeomDev gd, int out_c64, void* __restrict__ gout)
 {
+    typedef typename cplx_of<T>::type C2;
     extern __shared__ __align__(16) unsigned char fsm[];
     const int zp = blockIdx.x;
     const int pair = zp / gd.nspin, spin = zp - pair * gd.nspin;
@@ -464,11 +487,11 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
     const int sets = nb * ns;  // this spin's sets
     const int rows = nl.natom * nl.nproj_max * 4;
     const int nj = 3 * nl.natom;
-    double2* sK = reinterpret_cast<double2*>(fsm);           // [rows][sets]  role k+q
-    double2* sKp = sK + (size_t)rows * sets;                  // [rows][sets]  role k (raw Pi)
-    double2* sE = sKp + (size_t)rows * sets;                  // [nmodes][nj]
+    C2* sK = reinterpret_cast<C2*>(fsm);                     // [rows][sets]  role k+q
+    C2* sKp = sK + (size_t)rows * sets;                      // [rows][sets]  role k (raw Pi)
+    C2* sE = sKp + (size_t)rows * sets;                      // [nmodes][nj]
     int* sch = reinterpret_cast<int*>(sE + (size_t)gd.nmodes * nj);  // channels: [type][8][4] = lidx, l, pbase, foff
-    double* ssoc = reinterpret_cast<double*>(sch + nl.ntype * 8 * 4);
+    T* ssoc = reinterpret_cast<T*>(sch + nl.ntype * 8 * 4);
     if (non_loc)
     {
         const double2* PK = proj + (size_t)P.kbz_kq * rows * nsets + (size_t)spin * sets;
@@ -476,11 +499,16 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
         for (int e = threadIdx.x; e < rows * sets; e += blockDim.x)
         {
             const int r = e / sets, c = e - r * sets;
-            sK[e] = PK[(size_t)r * nsets + c];
-            sKp[e] = PKp[(size_t)r * nsets + c];
+            const double2 k1 = PK[(size_t)r * nsets + c], k2 = PKp[(size_t)r * nsets + c];
+            sK[e] = mk2<C2>(k1.x, k1.y);
+            sKp[e] = mk2<C2>(k2.x, k2.y);
         }
         const double2* E = eig + (size_t)P.qslot * gd.nmodes * gd.nmodes;
-        for (int e = threadIdx.x; e < gd.nmodes * nj; e += blockDim.x) sE[e] = E[(e / nj) * gd.nmodes + (e % nj)];
+        for (int e = threadIdx.x; e < gd.nmodes * nj; e += blockDim.x)
+        {
+            const double2 v = E[(e / nj) * gd.nmodes + (e % nj)];
+            sE[e] = mk2<C2>(v.x, v.y);
+        }
         if (threadIdx.x < nl.ntype)
         {
             const int it = threadIdx.x;
@@ -495,7 +523,7 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 ch[1] = l;
                 ch[2] = pb;
                 ch[3] = nl.fcoef ? nl.fcoef_off[lidx * nl.ntype + it] : -1;
-                ssoc[it * 8 + nc] = (twoj != 0 && !nl.is_soc) ? (twoj + 1.0) / (4.0 * l + 2.0) : 1.0;
+                ssoc[it * 8 + nc] = (T)((twoj != 0 && !nl.is_soc) ? (twoj + 1.0) / (4.0 * l + 2.0) : 1.0);
                 pb += 2 * l + 1;
                 ++nc;
             }
@@ -510,9 +538,9 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
     {
         const int m = e / nb, n = e - m * nb;  // m: band of k, n: band of k+q
-        double2 out[NJ];
+        C2 out[NJ];
 #pragma unroll
-        for (int j = 0; j < NJ; ++j) out[j] = make_double2(0.0, 0.0);
+        for (int j = 0; j < NJ; ++j) out[j] = mk2<C2>(0.0, 0.0);
         if (non_loc)
         {
 #pragma unroll
@@ -522,14 +550,14 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 const int a = j / 3, x = j - 3 * a;
                 const int it = nl.atom_type[a];
                 const int rb = a * nl.nproj_max * 4;
-                double2 acc = make_double2(0.0, 0.0);
+                C2 acc = mk2<C2>(0.0, 0.0);
                 for (int c = 0; c < 8; ++c)
                 {
                     const int* ch = sch + (it * 8 + c) * 4;
                     const int l = ch[1];
                     if (l < 0) break;
                     const int tl = 2 * l + 1, pb = ch[2], foff = ch[3];
-                    const double soc = ssoc[it * 8 + c];
+                    const T soc = ssoc[it * 8 + c];
                     for (int im1 = 0; im1 < tl; ++im1)
                         for (int im2 = 0; im2 < tl; ++im2)
                         {
@@ -538,22 +566,23 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                             for (int s1 = 0; s1 < ns; ++s1)
                                 for (int s2 = 0; s2 < ns; ++s2)
                                 {
-                                    double2 f;
+                                    C2 f;
                                     if (foff >= 0)
                                     {
                                         const double* fc = nl.fcoef + 2 * ((size_t)foff + (im1 * tl + im2) * ns * ns + s1 * ns + s2);
-                                        f = make_double2(fc[0], fc[1]);
+                                        f = mk2<C2>(fc[0], fc[1]);
                                     }
                                     else
                                     {
                                         if (s1 != s2) continue;
-                                        f = make_double2(soc, 0.0);
+                                        f.x = soc;
+                                        f.y = 0;
                                     }
-                                    const double2 K0 = sK[(size_t)(rb + p1 * 4 + 0) * sets + n * ns + s1];
-                                    const double2 Kx = sK[(size_t)(rb + p1 * 4 + 1 + x) * sets + n * ns + s1];
-                                    const double2 Kp0 = cconj(sKp[(size_t)(rb + p2 * 4 + 0) * sets + m * ns + s2]);
-                                    double2 Kpx = sKp[(size_t)(rb + p2 * 4 + 1 + x) * sets + m * ns + s2];
-                                    Kpx = make_double2(-Kpx.x, Kpx.y);  // -conj
+                                    const C2 K0 = sK[(size_t)(rb + p1 * 4 + 0) * sets + n * ns + s1];
+                                    const C2 Kx = sK[(size_t)(rb + p1 * 4 + 1 + x) * sets + n * ns + s1];
+                                    const C2 Kp0 = cconj(sKp[(size_t)(rb + p2 * 4 + 0) * sets + m * ns + s2]);
+                                    C2 Kpx = sKp[(size_t)(rb + p2 * 4 + 1 + x) * sets + m * ns + s2];
+                                    Kpx.x = -Kpx.x;  // -conj
                                     acc = cadd(acc, cmul(f, cadd(cmul(Kx, Kp0), cmul(K0, Kpx))));
                                 }
                         }
@@ -586,11 +615,11 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
             }
             if (non_loc)
             {
-                double2 sacc = make_double2(0.0, 0.0);
+                C2 sacc = mk2<C2>(0.0, 0.0);
 #pragma unroll
                 for (int j = 0; j < NJ; ++j)
                     if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
-                v = cadd(v, cmul(pre, sacc));
+                v = cadd(v, cmul(pre, make_double2((double)sacc.x, (double)sacc.y)));
             }
             const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
             if (out_c64)
@@ -601,12 +630,12 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
     }
 }
 
-static size_t finish_pair_smem(const NonlocalDesc& nl, const GeomDev& g)
+static size_t finish_pair_smem(const NonlocalDesc& nl, const GeomDev& g, size_t csz)
 {
     const size_t rows = (size_t)nl.natom * nl.nproj_max * 4;
     const size_t sets = (size_t)g.nbnds * g.nspinor;
-    return 2 * rows * sets * sizeof(double2) + (size_t)g.nmodes * 3 * nl.natom * sizeof(double2) +
-           (size_t)nl.ntype * 8 * 4 * sizeof(int) + (size_t)nl.ntype * 8 * sizeof(double);
+    return 2 * rows * sets * csz + (size_t)g.nmodes * 3 * nl.natom * csz + (size_t)nl.ntype * 8 * 4 * sizeof(int) +
+           (size_t)nl.ntype * 8 * sizeof(double);
 }
 
 void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const double2* glocal,
@@ -614,22 +643,34 @@ void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const
                          const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,
                          const GeomDev& g, int out_c64, void* gout, cudaStream_t st)
 {
-    const size_t smem = finish_pair_smem(nl, g);
+    const size_t smem = finish_pair_smem(nl, g, mode_fp64 ? sizeof(double2) : sizeof(float2));
     const int nj = 3 * nl.natom;
     if (smem <= 160 * 1024 && nj <= 24)
     {
         static bool attr = false;
         if (!attr)
         {
-            cudaFuncSetAttribute(k_finish_pair<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-            cudaFuncSetAttribute(k_finish_pair<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(k_finish_pair<12, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(k_finish_pair<24, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(k_finish_pair<12, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+            cudaFuncSetAttribute(k_finish_pair<24, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
             attr = true;
         }
         const int nz = npairs * g.nspin;
-#define FINL(NJ) k_finish_pair<NJ><<<nz, NJ <= 12 ? 256 : 128, smem, st>>>(pairs, mode_fp64, glocal, partials, nchunks, mode_scale, \
-                                                          band_scale, proj, eig, non_loc, nl, g, out_c64, gout)
-        if (nj <= 12) FINL(12);
-        else FINL(24);
+#define FINL(NJ, T)                                                                                              \
+    k_finish_pair<NJ, T><<<nz, NJ <= 12 ? 256 : 128, smem, st>>>(pairs, mode_fp64, glocal, partials, nchunks,    \
+                                                                  mode_scale, band_scale, proj, eig, non_loc, nl, g, \
+                                                                  out_c64, gout)
+        if (mode_fp64)
+        {
+            if (nj <= 12) FINL(12, double);
+            else FINL(24, double);
+        }
+        else
+        {
+            if (nj <= 12) FINL(12, float);
+            else FINL(24, float);
+        }
 #undef FINL
         return;
     }

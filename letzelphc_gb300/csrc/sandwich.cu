@@ -15,9 +15,10 @@
 //
 // * k_local_fp64: the plain form, FP64 SIMT.
 // * k_local_tc:   the mixed form on the 5th-generation tensor cores: psi(r)
-//   in FP32, split into 16-bit (hi, lo) pairs, three products
-//   A_hi B_hi + A_hi B_lo + A_lo B_hi accumulated in FP32 in tensor memory per
-//   K chunk; chunks are reduced in FP64 by the finish kernel.
+//   in FP32, A = dV psi_k formed in registers and written to tensor memory
+//   as 16-bit (hi, lo) pairs, B = psi_k+q split likewise in shared memory,
+//   three products A_hi B_hi + A_hi B_lo + A_lo B_hi accumulated in FP32 in
+//   tensor memory per K chunk; chunks are reduced in FP64 by the finish kernel.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -149,10 +150,19 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 // ============================================================= mixed form
 //
 // Warp roles: warp 0 issues TMA, warp 1 owns tensor memory and issues the
-// MMAs, warps 2-9 build the A operand, warps 10.. drain the accumulators
-// (warp w reads TMEM lanes 32*(w%4)..+31, one 64-column half each).
+// MMAs, warps 2-9 build the A operand directly in tensor memory, warps
+// 10.. drain the accumulators.
+//
+// Tensor memory (512 columns): NACC (4, or 2 for wide tiles) accumulators of
+// NT = 2*nbp columns, then NA A-operand slots of 64 columns (A_hi: 32 columns, A_lo: 32 columns; one
+// column holds the (Re, Im) 16-bit pair of one grid point, lane = row).
+// Shared memory holds only TMA tiles, so the TMA ring is up to 8 stages deep:
+// per stage B (k+q split rows, 128-byte swizzle), the FP32 psi_k tile (two
+// 16-point halves, 128-byte swizzle) and the FP32 dV tile of the tile's modes.
 
-#define TC_NST_MAX 4
+#define TC_NST_MAX 8
+#define TC_NA_MAX 6
+#define TC_NACC_MAX 4
 #define TC_SMEM_LIMIT (227 * 1024)
 #define TC_KPTS 32  // complex grid points per pipeline stage (64 16-bit K elements = 128 B rows)
 #define TC_GROUP 2         // pipeline stages chained into one TMEM accumulator before it is drained
@@ -160,10 +170,10 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 
 struct TcSmemLayout
 {
-    uint32_t a_hi, a_lo, b_hi, b_lo, p_hi, p_lo, dv;  // offsets of stage 0
-    uint32_t a_bytes, b_bytes, p_bytes, dv_bytes;     // per stage per half
+    uint32_t b_hi, b_lo, p, dv;               // offsets of stage 0
+    uint32_t b_bytes, p_half, p_bytes, dv_bytes;
     uint32_t stage_bytes;
-    uint32_t nst;
+    uint32_t nst, na, nacc, accw, merged, a_col0;
     uint32_t bar_off, total;
 };
 
@@ -175,32 +185,45 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     TcSmemLayout L;
     const uint32_t NT = 2 * g.nbp;
     const uint32_t nsp = (g.nmag == 4) ? 2 : 1;
-    L.a_bytes = 128 * 128;
     L.b_bytes = NT * 128;
-    L.p_bytes = nsp * g.nbp * 128;
-    L.a_hi = 0;
-    L.a_lo = L.a_hi + L.a_bytes;
-    L.b_hi = L.a_lo + L.a_bytes;
-    L.b_lo = L.b_hi + L.b_bytes;
-    L.p_hi = L.b_lo + L.b_bytes;
-    L.p_lo = L.p_hi + L.p_bytes;
-    L.dv = L.p_lo + L.p_bytes;
+    L.p_half = g.nbp * 128;  // 16 points x 8 B per band row
+    L.p_bytes = nsp * 2 * L.p_half;
     L.dv_bytes = tc_tile_modes(g) * g.nmag * TC_KPTS * 8;
+    L.b_hi = 0;
+    L.b_lo = L.b_hi + L.b_bytes;
+    L.p = L.b_lo + L.b_bytes;
+    L.dv = L.p + L.p_bytes;
     L.stage_bytes = (L.dv + L.dv_bytes + 1023) / 1024 * 1024;
     L.nst = (TC_SMEM_LIMIT - 2048) / L.stage_bytes;
     if (L.nst > TC_NST_MAX) L.nst = TC_NST_MAX;
+    // merged form (NT <= 64): one N = 2*NT MMA A_hi [B_hi; B_lo] and one N = NT
+    // MMA A_lo B_hi per K step; accumulator columns [0, NT) collect hi.hi and
+    // [NT, 2 NT) hi.lo + lo.hi.  Narrow N runs at a fixed per-instruction cost,
+    // so the merge saves a third of the tensor time.  Wider tiles keep three
+    // N = NT products into one accumulator.
+    L.merged = (NT <= 64) ? 1 : 0;
+    L.accw = L.merged ? 2 * NT : NT;
+    L.nacc = (4 * L.accw + 4 * 64 <= 512) ? 4 : 2;
+    L.a_col0 = L.nacc * L.accw;
+    L.na = (512 - L.a_col0) / 64;
+    if (L.na > TC_NA_MAX) L.na = TC_NA_MAX;
     L.bar_off = L.nst * L.stage_bytes;
-    L.total = L.bar_off + 256 + 1024;  // barriers + alignment slack
+    L.total = L.bar_off + 512 + 1024;  // barriers + alignment slack
     return L;
 }
 
 int lelph_local_tc_smem_bytes(const GeomDev& g) { return (int)tc_layout(g).total; }
 int lelph_local_tc_tile_modes(const GeomDev& g) { return tc_tile_modes(g); }
-
-template <int BF16>
-__device__ __forceinline__ void split_store(uint8_t* a_hi, uint8_t* a_lo, uint32_t off, float re, float im)
+int lelph_local_tc_supported(const GeomDev& g)
 {
-    uint32_t h, l;
+    const TcSmemLayout L = tc_layout(g);
+    return (2 * g.nbp <= 128) && L.nst >= 2 && L.na >= 2 && L.a_col0 + L.na * 64 <= 512;
+}
+
+// (hi, lo) 16-bit split of a complex value: hi = rn(v), lo = rn(v - hi)
+template <int BF16>
+__device__ __forceinline__ void split_pair(float re, float im, uint32_t& h, uint32_t& l)
+{
     if (BF16)
     {
         __nv_bfloat162 hv = __floats2bfloat162_rn(re, im);
@@ -217,51 +240,44 @@ __device__ __forceinline__ void split_store(uint8_t* a_hi, uint8_t* a_lo, uint32
         h = *reinterpret_cast<uint32_t*>(&hv);
         l = *reinterpret_cast<uint32_t*>(&lv);
     }
-    *reinterpret_cast<uint32_t*>(a_hi + off) = h;
-    *reinterpret_cast<uint32_t*>(a_lo + off) = l;
 }
 
-template <int BF16>
-__device__ __forceinline__ float2 load_split(const uint8_t* hi, const uint8_t* lo, uint32_t off)
+// A operand for SUB grid points of one row (one lane): a = sum_c dV^{c} psi^{c},
+// split and stored to the lane's TMEM row.  pp[c] points at the lane's psi row
+// (128-byte swizzled half tile), dvp[c] at the row's dV (16 points of the half).
+template <int BF16, int SUB, int NC>
+__device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const float4* const* dvp, uint32_t swz, int j0,
+                                            bool valid, uint32_t tcol_hi, uint32_t tcol_lo)
 {
-    uint32_t h = *reinterpret_cast<const uint32_t*>(hi + off);
-    uint32_t l = *reinterpret_cast<const uint32_t*>(lo + off);
-    float2 a, b;
-    if (BF16)
+    uint32_t hi[SUB], lo[SUB];
+#pragma unroll
+    for (int jj = 0; jj < SUB / 2; ++jj)
     {
-        a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&h));
-        b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&l));
+        const int j = j0 / 2 + jj;  // 16-byte chunk = 2 points
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+        {
+            const float4 ps = *reinterpret_cast<const float4*>(pp[c] + ((((uint32_t)j) ^ swz) << 4));
+            const float4 dv = dvp[c][j];
+            acc.x += dv.x * ps.x - dv.y * ps.y;
+            acc.y += dv.x * ps.y + dv.y * ps.x;
+            acc.z += dv.z * ps.z - dv.w * ps.w;
+            acc.w += dv.z * ps.w + dv.w * ps.z;
+        }
+        if (!valid) acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        split_pair<BF16>(acc.x, acc.y, hi[2 * jj], lo[2 * jj]);
+        split_pair<BF16>(acc.z, acc.w, hi[2 * jj + 1], lo[2 * jj + 1]);
+    }
+    if (SUB == 8)
+    {
+        tmem_st8(tcol_hi, hi);
+        tmem_st8(tcol_lo, lo);
     }
     else
     {
-        a = __half22float2(*reinterpret_cast<__half2*>(&h));
-        b = __half22float2(*reinterpret_cast<__half2*>(&l));
-    }
-    return make_float2(a.x + b.x, a.y + b.y);
-}
-
-// A operand for one pipeline stage, fast path: nb % 8 == 0, one magnetic
-// component per row.  Warp pw owns bands m = pw + 8j (j < BPW = nb/8); row
-// (ml, m) = ml*nb + m keeps the swizzle phase of a band fixed, so each product
-// costs one complex multiply, one (hi, lo) split and two shared stores.
-template <int BF16, int BPW>
-__device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L, const float2* dvs, int MTa, int comp, int nmag, int nbnds, int pw, int lane,
-                                             const uint32_t* off0)
-{
-    float2 psi[BPW];
-#pragma unroll
-    for (int j = 0; j < BPW; ++j)
-        psi[j] = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)(pw + 8 * j) * 128 + 4 * lane);
-    const uint32_t mstride = (uint32_t)(nbnds >> 3) * 1024u;
-    for (int ml = 0; ml < MTa; ++ml)
-    {
-        const float2 dvp = dvs[(ml * nmag + comp) * TC_KPTS + lane];
-#pragma unroll
-        for (int j = 0; j < BPW; ++j)
-        {
-            const float2 a = cmul(dvp, psi[j]);
-            split_store<BF16>(st + L.a_hi, st + L.a_lo, off0[j] + (uint32_t)ml * mstride, a.x, a.y);
-        }
+        tmem_st4(tcol_hi, hi);
+        tmem_st4(tcol_lo, lo);
     }
 }
 
@@ -270,27 +286,26 @@ __device__ __forceinline__ void produce_fast(uint8_t* st, const TcSmemLayout& L,
 // The tensor-core accumulator loses low-order bits on every accumulation
 // (its error grows linearly with the number of MMAs chained into one FP32
 // accumulator), so accumulation chains are kept to TC_GROUP pipeline stages:
-// the MMA warp alternates between two TMEM accumulators, and the drain warps
+// the MMA warp cycles through NACC TMEM accumulators, and the drain warps
 // add each finished accumulator into round-to-nearest FP32 registers, which
 // are written out per K chunk and reduced in FP64 by the finish kernel.
 template <int BF16>
 __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
-    k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapA,
-               const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs,
-               const float* __restrict__ mode_scale, GeomDev gd, int chunk_pts, int nchunks,
-               float* __restrict__ partials, unsigned* __restrict__ status)
+    k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
+               const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
+               int chunk_pts, int nchunks, float* __restrict__ partials, unsigned* __restrict__ status)
 {
     extern __shared__ __align__(1024) uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
     const TcSmemLayout L = tc_layout(gd);
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
-    uint64_t* aready = full + TC_NST_MAX;
-    uint64_t* empty = aready + TC_NST_MAX;
-    uint64_t* accf = empty + TC_NST_MAX;  // [2] accumulator b complete (MMA -> drain)
-    uint64_t* acce = accf + 2;            // [2] accumulator b drained (drain -> MMA)
-    uint64_t* dvbar = acce + 2;           // [NST] scaled dV tile written (producers -> producers)
-    const int NST = (int)L.nst;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(dvbar + TC_NST_MAX);
+    uint64_t* empty = full + TC_NST_MAX;    // TMA slot consumed: MMA commit + 8 producer warps
+    uint64_t* aready = empty + TC_NST_MAX;  // A slot written (producers -> MMA)
+    uint64_t* afree = aready + TC_NA_MAX;   // A slot read (MMA commit -> producers)
+    uint64_t* accf = afree + TC_NA_MAX;     // [nacc] accumulator b complete (MMA -> drain)
+    uint64_t* acce = accf + TC_NACC_MAX;    // [nacc] accumulator b drained (drain -> MMA)
+    const int NST = (int)L.nst, NA = (int)L.na, NACC = (int)L.nacc;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + TC_NACC_MAX);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -303,18 +318,20 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     const int ngroup = (nstage + TC_GROUP - 1) / TC_GROUP;
     const int nsp = (gd.nmag == 4) ? 2 : 1;
     const int ndrain = 4 * ((NT + 63) / 64);
-    const uint32_t ncols = 2 * NT <= 32 ? 32 : (2 * NT <= 64 ? 64 : (2 * NT <= 128 ? 128 : 256));
 
     if (threadIdx.x == 0)
     {
         for (int s = 0; s < NST; ++s)
         {
             mbar_init(&full[s], 1);
-            mbar_init(&aready[s], 8);
-            mbar_init(&empty[s], 1);
-            mbar_init(&dvbar[s], 8);
+            mbar_init(&empty[s], 1 + 8);
         }
-        for (int b = 0; b < 2; ++b)
+        for (int a = 0; a < NA; ++a)
+        {
+            mbar_init(&aready[a], 8);
+            mbar_init(&afree[a], 1);
+        }
+        for (int b = 0; b < NACC; ++b)
         {
             mbar_init(&accf[b], 1);
             mbar_init(&acce[b], ndrain);
@@ -322,14 +339,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         *abort_flag = 0;
         fence_barrier_init();
     }
-    if (warp == 1) tmem_alloc(tmem_slot, ncols);
-    // zero the A operand buffers once (rows past the last (mode, band) stay 0)
-    for (int s = 0; s < NST; ++s)
-    {
-        uint32_t* a = reinterpret_cast<uint32_t*>(sm + s * L.stage_bytes + L.a_hi);
-        for (int i = threadIdx.x; i < (int)(2 * L.a_bytes / 4); i += blockDim.x) a[i] = 0u;
-    }
-    fence_proxy_async_smem();
+    if (warp == 1) tmem_alloc(tmem_slot, 512);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -340,19 +350,26 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         if (lane == 0)
         {
             prefetch_tmap(&tmapB);
-            prefetch_tmap(&tmapA);
+            prefetch_tmap(&tmapP);
             prefetch_tmap(&tmapV);
-            const int rowB_hi = ((P.kbz_kq * gd.nspin + spin) * 2 + 0) * NT;
-            const int rowB_lo = rowB_hi + NT;
-            const int rowP_hi = ((P.kbz_k * gd.nspin + spin) * 2 + 0) * NT;
-            const int rowP_lo = rowP_hi + NT;
-            const uint32_t bytes = 2 * L.b_bytes + 2 * L.p_bytes + L.dv_bytes;
-            const int rowV = (P.dvslot * gd.nmodes + mt * gd.mt_modes) * gd.nmag;
+            // tile-major operands: z = (row group) * blocks + block
+            const int nkb = (int)((long long)gd.nspinor * N / 32);  // 32-point K blocks per row group
+            const int zB_hi = ((P.kbz_kq * gd.nspin + spin) * 2 + 0) * nkb;
+            const int zB_lo = zB_hi + nkb;
+            const int zP = (P.kbz_k * gd.nspin + spin) * 2 * nkb;  // 16-point blocks
+            const int zV = P.dvslot * (int)(N / 32);
+            const int yV = mt * gd.mt_modes * gd.nmag;
+            const uint32_t bytes = 2 * L.b_bytes + L.p_bytes + L.dv_bytes;
             int issued = 0;
-            for (int it = 0; it < nstage; ++it)
+            // a K chunk lies within one spinor component (chunk_pts divides N)
+            const long long kc0 = (long long)chunk * chunk_pts;
+            const int sp = (int)(kc0 / N);
+            const long long r00 = kc0 - (long long)sp * N;
+            // ring positions advance incrementally: no runtime divisions on the issue paths
+            int s = 0;
+            uint32_t ph = 0;
+            for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u)
             {
-                const int s = it % NST;
-                const uint32_t ph = (uint32_t)(it / NST) & 1u;
                 if (!mbar_wait_bounded(&empty[s], ph ^ 1u))
                 {
                     *abort_flag = 1;
@@ -361,21 +378,20 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 }
                 if (*abort_flag) break;
                 uint8_t* st = sm + s * L.stage_bytes;
-                const long long kc = (long long)chunk * chunk_pts + (long long)it * TC_KPTS;
-                const int sp = (int)(kc / N);
-                const long long r0 = kc - (long long)sp * N;
+                const long long kc = kc0 + (long long)it * TC_KPTS;
+                const long long r0 = r00 + (long long)it * TC_KPTS;
                 mbar_arrive_expect_tx(&full[s], bytes);
-                tma_load_2d(st + L.b_hi, &tmapB, &full[s], (int)(2 * kc), rowB_hi);
-                tma_load_2d(st + L.b_lo, &tmapB, &full[s], (int)(2 * kc), rowB_lo);
+                tma_load_3d(st + L.b_hi, &tmapB, &full[s], 0, 0, zB_hi + (int)(kc >> 5));
+                tma_load_3d(st + L.b_lo, &tmapB, &full[s], 0, 0, zB_lo + (int)(kc >> 5));
                 for (int q = 0; q < nsp; ++q)
                 {
                     const int spp = (gd.nmag == 4) ? q : sp;
-                    const int x = (int)(2 * ((long long)spp * N + r0));
-                    tma_load_2d(st + L.p_hi + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_hi);
-                    tma_load_2d(st + L.p_lo + q * gd.nbp * 128, &tmapA, &full[s], x, rowP_lo);
+                    const long long kq = (long long)spp * N + r0;
+                    // both 16-point halves of the stage in one box
+                    tma_load_3d(st + L.p + 2 * q * L.p_half, &tmapP, &full[s], 0, 0, zP + (int)(kq >> 4));
                 }
                 // dV_nu(r) of the tile's modes, all magnetic components: rows (nu, comp) x 32 points
-                tma_load_2d(st + L.dv, &tmapV, &full[s], (int)(2 * r0), rowV);
+                tma_load_3d(st + L.dv, &tmapV, &full[s], 0, yV, zV + (int)(r0 >> 5));
                 issued = it + 1;
             }
             // let every issued copy land before the CTA can retire
@@ -388,68 +404,105 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         if (lane == 0)
         {
             const uint32_t idesc = umma_idesc_f16(BF16 ? 1u : 0u, 128u, (uint32_t)NT);
+            const uint32_t idesc2 = umma_idesc_f16(BF16 ? 1u : 0u, 128u, (uint32_t)(2 * NT));
+            const bool merged = L.merged != 0;
+            int s = 0, a = 0, gi = 0, b = 0;
+            uint32_t pha = 0, phb = 0;
             for (int it = 0; it < nstage; ++it)
             {
-                const int s = it % NST;
-                const uint32_t ph = (uint32_t)(it / NST) & 1u;
-                const int grp = it / TC_GROUP;
-                const int b = grp & 1;
-                const bool first = (it % TC_GROUP) == 0;
-                const bool last = (it % TC_GROUP) == TC_GROUP - 1 || it == nstage - 1;
+                const bool first = gi == 0;
+                const bool last = gi == TC_GROUP - 1 || it == nstage - 1;
+                // MMA issue blocks per instruction, so this thread checks one barrier
+                // per stage: the producers arrive on aready[a] only after they saw the
+                // stage's TMA tiles land (full[s]), which orders B for the MMAs too
                 bool ok = true;
-                if (first) ok = mbar_wait_bounded(&acce[b], (uint32_t)((grp >> 1) & 1) ^ 1u);
-                ok = ok && mbar_wait_bounded(&full[s], ph) && mbar_wait_bounded(&aready[s], ph);
+                if (first) ok = mbar_wait_bounded(&acce[b], phb ^ 1u);
+                ok = ok && mbar_wait_bounded(&aready[a], pha);
                 if (!ok)
                 {
                     *abort_flag = 1;
                     atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
                     break;
                 }
-                if (*abort_flag) break;
                 tc_fence_after();
                 const uint32_t base = smem_u32(sm + s * L.stage_bytes);
-                const uint32_t dacc = tmem + (uint32_t)(b * NT);
+                const uint32_t dacc = tmem + (uint32_t)b * L.accw;
+                const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * 64u;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                 {
-                    const uint64_t ah = umma_desc_sw128(base + L.a_hi + 32 * k);
-                    const uint64_t al = umma_desc_sw128(base + L.a_lo + 32 * k);
                     const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
-                    const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
-                    umma_f16(dacc, ah, bh, idesc, (first && k == 0) ? 0u : 1u);
-                    umma_f16(dacc, ah, bl, idesc, 1u);
-                    umma_f16(dacc, al, bh, idesc, 1u);
+                    const uint32_t en = (first && k == 0) ? 0u : 1u;
+                    if (merged)
+                    {
+                        // rows [0, NT) of the 2*NT-row tile are B_hi, [NT, 2NT) B_lo
+                        umma_f16_ta(dacc, ahi + 8 * k, bh, idesc2, en);
+                        umma_f16_ta(dacc + (uint32_t)NT, ahi + 32 + 8 * k, bh, idesc, 1u);
+                    }
+                    else
+                    {
+                        const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
+                        umma_f16_ta(dacc, ahi + 8 * k, bh, idesc, en);
+                        umma_f16_ta(dacc, ahi + 8 * k, bl, idesc, 1u);
+                        umma_f16_ta(dacc, ahi + 32 + 8 * k, bh, idesc, 1u);
+                    }
                 }
                 umma_commit(&empty[s]);
+                umma_commit(&afree[a]);
                 if (last) umma_commit(&accf[b]);
+                s = (s + 1 == NST) ? 0 : s + 1;
+                if (++a == NA)
+                {
+                    a = 0;
+                    pha ^= 1u;
+                }
+                if (++gi == TC_GROUP)
+                {
+                    gi = 0;
+                    if (++b == NACC)
+                    {
+                        b = 0;
+                        phb ^= 1u;
+                    }
+                }
             }
         }
     }
     else if (warp < 10)
     {
-        // ---------------- A producers: warps 2..9, lane = grid point in stage
-        const int pw = warp - 2;  // 0..7
+        // ---------------- A producers: lane quadrant q = warp % 4 (rows 32q..32q+31),
+        // half h of the stage's 32 points
+        const int q = warp & 3;
+        const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
         const int nu0 = mt * MT;
         const int MTa = min(MT, gd.nmodes - nu0);  // modes present in this tile
-        const bool fast = (gd.nbnds % 8 == 0) && (gd.nmag != 4) && gd.nbnds <= 64;
-        const uint32_t chunk16 = (uint32_t)(lane >> 2), within = (uint32_t)(lane & 3) * 4;
-        const int bpw = gd.nbnds >> 3;
-        uint32_t off0[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-        {
-            const uint32_t m = (uint32_t)(pw + 8 * j);
-            off0[j] = (m >> 3) * 1024 + (m & 7) * 128 + ((chunk16 ^ (m & 7)) << 4) + within;
-        }
+        const int row = 32 * q + lane;
+        const int ml = row / gd.nbnds, m = row - ml * gd.nbnds;
+        const bool valid = ml < MTa;
+        const int mlc = valid ? ml : 0;
+        const uint32_t swz = (uint32_t)(m & 7);
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
         // a K chunk never straddles spinor components (chunk_pts divides N)
         const long long kc0 = (long long)chunk * chunk_pts;
         const int sp = (int)(kc0 / N);
-        for (int it = 0; it < nstage; ++it)
+        int comp0, comp1;
+        if (gd.nmag == 4)
         {
-            const int s = it % NST;
-            const uint32_t ph = (uint32_t)(it / NST) & 1u;
-            bool ok = mbar_wait_bounded(&empty[s], ph ^ 1u) && mbar_wait_bounded(&full[s], ph);
+            comp0 = 2 * sp;
+            comp1 = 2 * sp + 1;
+        }
+        else
+        {
+            comp0 = (gd.nmag == 2) ? spin : 0;
+            comp1 = comp0;
+        }
+        int s = 0, a = 0;
+        uint32_t ph = 0, pha = 0;
+        for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u,
+                 a = (a + 1 == NA) ? 0 : a + 1, pha ^= (a == 0) ? 1u : 0u)
+        {
+            bool ok = mbar_wait_bounded(&afree[a], pha ^ 1u) && mbar_wait_bounded(&full[s], ph);
             ok = __all_sync(0xffffffffu, ok);
             if (!ok && lane == 0)
             {
@@ -457,50 +510,36 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
             }
             if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;
-            uint8_t* st = sm + s * L.stage_bytes;
-            const float2* dvs = reinterpret_cast<const float2*>(st + L.dv);
-            if (fast)
+            tc_fence_after();
+            const uint8_t* st = sm + s * L.stage_bytes;
+            const uint8_t* pp[2];
+            const float4* dvp[2];
+            pp[0] = st + L.p + (0 * 2 + h) * L.p_half + (uint32_t)m * 128;
+            pp[1] = st + L.p + ((nsp - 1) * 2 + h) * L.p_half + (uint32_t)m * 128;
+            const float* dvs = reinterpret_cast<const float*>(st + L.dv);
+            dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * TC_KPTS + 16 * h) * 2);
+            dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * TC_KPTS + 16 * h) * 2);
+            const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * 64u + 16u * (uint32_t)h;
+            if (gd.nmag == 4)
             {
-                const int comp = (gd.nmag == 2) ? spin : 0;
-                switch (bpw)
-                {
-                    case 1: produce_fast<BF16, 1>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 2: produce_fast<BF16, 2>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 3: produce_fast<BF16, 3>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 4: produce_fast<BF16, 4>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 5: produce_fast<BF16, 5>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 6: produce_fast<BF16, 6>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    case 7: produce_fast<BF16, 7>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                    default: produce_fast<BF16, 8>(st, L, dvs, MTa, comp, gd.nmag, gd.nbnds, pw, lane, off0); break;
-                }
+#pragma unroll
+                for (int j0 = 0; j0 < 16; j0 += 4)
+                    produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
             }
             else
             {
-                for (int m = pw; m < gd.nbnds; m += 8)
-                {
-                    float2 psi0 = load_split<BF16>(st + L.p_hi, st + L.p_lo, (uint32_t)m * 128 + 4 * lane);
-                    float2 psi1 = make_float2(0.f, 0.f);
-                    if (gd.nmag == 4)
-                        psi1 = load_split<BF16>(st + L.p_hi + gd.nbp * 128, st + L.p_lo + gd.nbp * 128,
-                                                (uint32_t)m * 128 + 4 * lane);
-                    for (int ml = 0; ml < MTa; ++ml)
-                    {
-                        const int row = ml * gd.nbnds + m;
-                        const float2* dvn = dvs + ml * gd.nmag * TC_KPTS + lane;
-                        float2 a;
-                        if (gd.nmag == 4)
-                            a = cadd(cmul(dvn[(2 * sp) * TC_KPTS], psi0), cmul(dvn[(2 * sp + 1) * TC_KPTS], psi1));
-                        else
-                            a = cmul(dvn[((gd.nmag == 2) ? spin : 0) * TC_KPTS], psi0);
-                        const uint32_t off = (uint32_t)(row >> 3) * 1024 + (uint32_t)(row & 7) * 128 +
-                                             ((chunk16 ^ (uint32_t)(row & 7)) << 4) + within;
-                        split_store<BF16>(st + L.a_hi, st + L.a_lo, off, a.x, a.y);
-                    }
-                }
+#pragma unroll
+                for (int j0 = 0; j0 < 16; j0 += 8)
+                    produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
             }
-            fence_proxy_async_smem();
+            tmem_wait_st();
+            tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&aready[s]);
+            if (lane == 0)
+            {
+                mbar_arrive(&aready[a]);
+                mbar_arrive(&empty[s]);
+            }
         }
     }
     else if (warp < 10 + ndrain)
@@ -514,10 +553,11 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
 #pragma unroll
         for (int i = 0; i < 64; ++i) acc[i] = 0.f;
         bool good = true;
-        for (int grp = 0; grp < ngroup; ++grp)
+        int b = 0;
+        uint32_t phb = 0;
+        for (int grp = 0; grp < ngroup; ++grp, b = (b + 1 == NACC) ? 0 : b + 1, phb ^= (b == 0) ? 1u : 0u)
         {
-            const int b = grp & 1;
-            bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], (uint32_t)(grp >> 1) & 1u);
+            bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], phb);
             ok = __all_sync(0xffffffffu, ok);
             if (!ok)
             {
@@ -530,7 +570,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * NT + c0);
+            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)b * L.accw + (uint32_t)c0;
 #pragma unroll
             for (int c = 0; c < 64; c += 16)
             {
@@ -540,6 +580,12 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     tmem_ld16(ta + (uint32_t)c, v);
 #pragma unroll
                     for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
+                    if (L.merged)
+                    {
+                        tmem_ld16(ta + (uint32_t)(NT + c), v);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
+                    }
                 }
             }
             tc_fence_before();
@@ -561,31 +607,29 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     if (warp == 1)
     {
         tc_fence_after();
-        tmem_dealloc(tmem, ncols);
+        tmem_dealloc(tmem, 512);
     }
 }
 
-void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapA,
-                           const void* tmapV, const float* mode_scale, const GeomDev& g, int ab_bf16, int chunk_pts,
-                           int nchunks, float* partials, unsigned* status, cudaStream_t st)
+void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapP,
+                           const void* tmapV, const GeomDev& g, int ab_bf16, int chunk_pts, int nchunks,
+                           float* partials, unsigned* status, cudaStream_t st)
 {
     const int mtiles = (g.nmodes + g.mt_modes - 1) / g.mt_modes;
     dim3 grid(nchunks, mtiles, npairs * g.nspin);
     const int smem = lelph_local_tc_smem_bytes(g);
     const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
-    const CUtensorMap* tA = static_cast<const CUtensorMap*>(tmapA);
+    const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (ab_bf16)
     {
         cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tA, *tV, pairs, mode_scale, g, chunk_pts, nchunks,
-                                                      partials, status);
+        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, partials, status);
     }
     else
     {
         cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tA, *tV, pairs, mode_scale, g, chunk_pts, nchunks,
-                                                      partials, status);
+        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, partials, status);
     }
 }
