@@ -176,6 +176,19 @@ def tensor_flops_per_pair(s, grid=None):
     return 3 * 2.0 * M * (2 * nbp) * (2 * s.nspinor * N) * s.nspin
 
 
+def traffic_per_launch(pairs_per_launch):
+    """DRAM bytes of one k_local_tc launch: the per-pair figure of the committed
+    ncu capture (dram__bytes_read + dram__bytes_write of an 8-pair launch,
+    divided by 8) times the pairs of the launch."""
+    path = os.path.join(ROOT, "profiles", "k_local_tc_4atom_8pairs.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_pair:"):
+            return float(line.split(":")[1]) * pairs_per_launch
+    return None
+
+
 def err_stats(g, ref):
     a, b = np.abs(g), np.abs(ref)
     e = np.abs(a - b) / np.maximum(b, 1e-6 * b.max())
@@ -357,7 +370,9 @@ def run_ours(args):
                 "flops_per_launch": flops / max(1, local_launches), "launches": local_launches,
                 "product_grid": list(p1["product_grid"]), "reference_box": list(s.fft_dims),
                 "avg_launch_ms": local_ms / max(1, local_launches),
-                "traffic": None, "step_share": local_ms / (local_ms + prep_ms + fin_ms),
+                "traffic": traffic_per_launch(npairs / max(1, local_launches)),
+                "traffic_source": "ncu DRAM bytes per pair of profiles/k_local_tc_4atom_8pairs.md x pairs per launch",
+                "step_share": local_ms / (local_ms + prep_ms + fin_ms),
                 "prepare_ms": prep_ms, "finish_ms": fin_ms}
 
     # ------------------------------------------------ end to end (host buffers)
@@ -437,7 +452,7 @@ def run_ours(args):
                 "data": "synthetic (seeded; no public dataset)",
                 "config": {"workload": WORKLOAD, "pairs_per_step": npairs, "g_elements_per_step": elems,
                            "precision": args.precision, "parallelism": f"q-sharded x{world}",
-                           "l2": "inputs larger than L2 (split operands 29 GB)"},
+                           "l2": f"inputs larger than L2 ({st1['device_bytes'] / 1e9:.1f} GB resident on the device)"},
                 "e2e": {"value": world * elems / (e2e_step_ms * 1e-3), "unit": "g_elements/s",
                         "ms_per_step": e2e_step_ms, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "fp64_form": fp64,
