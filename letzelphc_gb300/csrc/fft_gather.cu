@@ -103,7 +103,10 @@ __device__ __forceinline__ void dft5(T2* v, int sign)
 }
 
 // One Stockham pass of radix R over nlines lines held in shared memory;
-// element e of line l lives at buf[l*ls + e*es].
+// element e of line l lives at buf[l*ls + e*es].  Consecutive threads take
+// consecutive elements of a line when elements are contiguous (es == 1) and
+// consecutive lines otherwise (ls == 1), so that a warp's shared-memory
+// accesses fall into distinct banks either way.
 template <typename T2, typename T, int R>
 __device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int L,
                                               int Ns, int es, int ls, const T2* tw, int sign)
@@ -111,10 +114,20 @@ __device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __
     const int LR = L / R;
     const int nwork = nlines * LR;
     const int tstride = L / (Ns * R);
+    const bool line_fast = es != 1;
     for (int w = threadIdx.x; w < nwork; w += blockDim.x)
     {
-        int line = w / LR;
-        int j = w - line * LR;
+        int line, j;
+        if (line_fast)
+        {
+            j = w / nlines;
+            line = w - j * nlines;
+        }
+        else
+        {
+            line = w / LR;
+            j = w - line * LR;
+        }
         int k = j % Ns;
         const T2* s = src + (size_t)line * ls;
         T2 v[R];
@@ -309,6 +322,9 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
 
 // ------------------------------------------------------------- scatter
 
+// grid: (ceil(npw_max / 256), nk); one thread per plane wave G of a k-point:
+// the box index and the phase e^{-i 2 pi G.tau} depend only on (k, G), so
+// they are formed once and applied to every (spin, band) set.
 template <typename T2>
 __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __restrict__ ks,
                                                  const int* __restrict__ miller, const long long* __restrict__ pw_off,
@@ -318,33 +334,42 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
                                                  const long long* __restrict__ chat_off)
 {
     const int kslot = blockIdx.y;
-    const int set = blockIdx.z;  // spin * nbnds + band
     const int kbz = k0 + kslot;
     const KPointSym s = ks[kbz];
     const int npw = npw_arr[s.ik];
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= npw) return;
     const int* mil = miller + 3 * pw_off[s.ik];
     const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
-    const double2* c = coef + coef_off[s.ik] + (size_t)set * gd.nspinor * npw;
-    double2* ch = chat + chat_off[kbz] + (size_t)set * gd.nspinor * npw;
-    T2* bx = boxes + ((size_t)kslot * gd.nspin * gd.nbnds + set) * gd.nspinor * N;
-    const double2 kph = make_double2(s.kphase[0], s.kphase[1]);
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < npw; g += gridDim.x * blockDim.x)
+    const int nsets = gd.nspin * gd.nbnds;
+    const int n0 = mil[3 * g], n1 = mil[3 * g + 1], n2 = mil[3 * g + 2];
+    const int G0 = s.W[0] * n0 + s.W[1] * n1 + s.W[2] * n2;
+    const int G1 = s.W[3] * n0 + s.W[4] * n1 + s.W[5] * n2;
+    const int G2 = s.W[6] * n0 + s.W[7] * n1 + s.W[8] * n2;
+    // e^{-i 2 pi G.tau} (the reference: cexp(-I*2*ELPH_PI*dot)); then kphase * gphase
+    const double dot = (double)G0 * s.tau_crys[0] + (double)G1 * s.tau_crys[1] + (double)G2 * s.tau_crys[2];
+    double sn, cs;
+    sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
+    const double2 ph = cmul(make_double2(s.kphase[0], s.kphase[1]), make_double2(cs, -sn));
+    int ix = G0 % gd.Nx;
+    if (ix < 0) ix += gd.Nx;
+    int iy = G1 % gd.Ny;
+    if (iy < 0) iy += gd.Ny;
+    int iz = G2 % gd.Nz;
+    if (iz < 0) iz += gd.Nz;
+    const size_t bidx = ((size_t)ix * gd.Ny + iy) * gd.Nz + iz;
+    const double2 u0 = make_double2(s.su2[0], s.su2[1]), u1 = make_double2(s.su2[2], s.su2[3]);
+    const double2 u2 = make_double2(s.su2[4], s.su2[5]), u3 = make_double2(s.su2[6], s.su2[7]);
+    const double2* cbase = coef + coef_off[s.ik];
+    double2* chb = chat + chat_off[kbz];
+    T2* bxb = boxes ? boxes + (size_t)kslot * nsets * gd.nspinor * N : nullptr;
+    for (int set = 0; set < nsets; ++set)
     {
-        int n0 = mil[3 * g], n1 = mil[3 * g + 1], n2 = mil[3 * g + 2];
-        int G0 = s.W[0] * n0 + s.W[1] * n1 + s.W[2] * n2;
-        int G1 = s.W[3] * n0 + s.W[4] * n1 + s.W[5] * n2;
-        int G2 = s.W[6] * n0 + s.W[7] * n1 + s.W[8] * n2;
-        // e^{-i 2 pi G.tau} (the reference: cexp(-I*2*ELPH_PI*dot)); then kphase * gphase
-        double dot = (double)G0 * s.tau_crys[0] + (double)G1 * s.tau_crys[1] + (double)G2 * s.tau_crys[2];
-        double sn, cs;
-        sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
-        double2 ph = cmul(kph, make_double2(cs, -sn));
+        const double2* c = cbase + (size_t)set * gd.nspinor * npw;
         double2 v[2];
         if (gd.nspinor == 2)
         {
-            double2 up = c[g], dw = c[npw + g];
-            double2 u0 = make_double2(s.su2[0], s.su2[1]), u1 = make_double2(s.su2[2], s.su2[3]);
-            double2 u2 = make_double2(s.su2[4], s.su2[5]), u3 = make_double2(s.su2[6], s.su2[7]);
+            const double2 up = c[g], dw = c[npw + g];
             v[0] = cadd(cmul(up, u0), cmul(dw, u1));
             v[1] = cadd(cmul(up, u2), cmul(dw, u3));
         }
@@ -352,19 +377,13 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
         {
             v[0] = c[g];
         }
-        int ix = G0 % gd.Nx;
-        if (ix < 0) ix += gd.Nx;
-        int iy = G1 % gd.Ny;
-        if (iy < 0) iy += gd.Ny;
-        int iz = G2 % gd.Nz;
-        if (iz < 0) iz += gd.Nz;
-        size_t bidx = ((size_t)ix * gd.Ny + iy) * gd.Nz + iz;
+        double2* ch = chb + (size_t)set * gd.nspinor * npw;
         for (int sp = 0; sp < gd.nspinor; ++sp)
         {
             double2 w = cmul(v[sp], ph);
             if (s.trev) w.y = -w.y;
             ch[(size_t)sp * npw + g] = w;
-            if (bx) bx[(size_t)sp * N + bidx] = mk2<T2>(w.x, w.y);
+            if (bxb) bxb[((size_t)set * gd.nspinor + sp) * N + bidx] = mk2<T2>(w.x, w.y);
         }
     }
 }
@@ -480,10 +499,11 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
 }
 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
-                          const int* npw, const double2* coef, const long long* coef_off, const GeomDev& g,
-                          int box_fp64, void* boxes, double2* chat, const long long* chat_off, cudaStream_t st)
+                          const int* npw, int npw_max, const double2* coef, const long long* coef_off,
+                          const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
+                          cudaStream_t st)
 {
-    dim3 grid(4, nk, g.nspin * g.nbnds);
+    dim3 grid((unsigned)((npw_max + 255) / 256), nk);
     if (box_fp64)
         k_scatter<double2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
                                                  (double2*)boxes, chat, chat_off);

@@ -977,6 +977,7 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
     const GeomDev& g = h->g;
     const long long N = (long long)g.Nx * g.Ny * g.Nz;
     const int nbox_per_k = d.nspin * d.nbnds * d.nspinor;
+    const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
     tstart(h);
     int rc;
     if (!h->mixed)
@@ -986,8 +987,8 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
         if (rc) return rc;
         CUDA_TRY(h, cudaMemsetAsync(h->d_psi64.p, 0, bytes, h->st));
         lelph_launch_scatter(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
-                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double2*)h->d_coef.p,
-                             (const long long*)h->d_coefoff.p, g, 1, h->d_psi64.p, (double2*)h->d_chat.p,
+                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
+                             (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 1, h->d_psi64.p, (double2*)h->d_chat.p,
                              (const long long*)h->d_chatoff.p, h->st);
         const long long nbox = (long long)d.nkpts_BZ * nbox_per_k;
         double2* psi = (double2*)h->d_psi64.p;
@@ -1008,8 +1009,8 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
             int nk = std::min(nkc, d.nkpts_BZ - k0);
             CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
             lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
-                                 (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double2*)h->d_coef.p,
-                                 (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p, (double2*)h->d_chat.p,
+                                 (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
+                                 (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p, (double2*)h->d_chat.p,
                                  (const long long*)h->d_chatoff.p, h->st);
             const long long nbox = (long long)nk * nbox_per_k;
             float2* bx = (float2*)h->d_boxes32.p;

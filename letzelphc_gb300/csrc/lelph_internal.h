@@ -63,8 +63,9 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
 
 // sphere -> box scatter with su2, fractional-translation phase and conj
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
-                          const int* npw, const double2* coef, const long long* coef_off, const GeomDev& g,
-                          int box_fp64, void* boxes, double2* chat, const long long* chat_off, cudaStream_t st);
+                          const int* npw, int npw_max, const double2* coef, const long long* coef_off,
+                          const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
+                          cudaStream_t st);
 
 // debugging / parity: box index of each rotated plane wave of one full-BZ k
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,

@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
 
@@ -281,7 +283,11 @@ __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const floa
     }
 }
 
-// grid: (nchunks, mtiles, npairs*nspin); 32*(10 + ndrain) threads.
+// Persistent grid: one CTA per SM; CTA c takes the work units u = c, c + G,
+// c + 2G, ... with u = (pair*nspin + spin, mode tile, K chunk), chunk fastest.
+// The barrier rings, the tensor memory and the TMA pipeline carry over from
+// one unit to the next, so a unit's first tiles are in flight while the
+// previous unit drains.  32*(10 + ndrain) threads.
 //
 // The tensor-core accumulator loses low-order bits on every accumulation
 // (its error grows linearly with the number of MMAs chained into one FP32
@@ -289,11 +295,31 @@ __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const floa
 // the MMA warp cycles through NACC TMEM accumulators, and the drain warps
 // add each finished accumulator into round-to-nearest FP32 registers, which
 // are written out per K chunk and reduced in FP64 by the finish kernel.
+struct TcUnit
+{
+    int chunk, mt, zp, spin;
+    PairInfo P;
+};
+
+__device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int nspin, const PairInfo* pairs)
+{
+    TcUnit w;
+    w.chunk = u % nchunks;
+    const int t = u / nchunks;
+    w.mt = t % mtiles;
+    w.zp = t / mtiles;
+    const int pair = w.zp / nspin;
+    w.spin = w.zp - pair * nspin;
+    w.P = pairs[pair];
+    return w;
+}
+
 template <int BF16>
 __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
-               int chunk_pts, int nchunks, float* __restrict__ partials, unsigned* __restrict__ status)
+               int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
+               unsigned* __restrict__ status)
 {
     extern __shared__ __align__(1024) uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -309,9 +335,6 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunk = blockIdx.x, mt = blockIdx.y, zp = blockIdx.z;
-    const int pair = zp / gd.nspin, spin = zp - pair * gd.nspin;
-    const PairInfo P = pairs[pair];
     const int NT = 2 * gd.nbp;
     const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
     const int nstage = chunk_pts / TC_KPTS;
@@ -352,51 +375,61 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             prefetch_tmap(&tmapB);
             prefetch_tmap(&tmapP);
             prefetch_tmap(&tmapV);
-            // tile-major operands: z = (row group) * blocks + block
             const int nkb = (int)((long long)gd.nspinor * N / 32);  // 32-point K blocks per row group
-            const int zB_hi = ((P.kbz_kq * gd.nspin + spin) * 2 + 0) * nkb;
-            const int zB_lo = zB_hi + nkb;
-            const int zP = (P.kbz_k * gd.nspin + spin) * 2 * nkb;  // 16-point blocks
-            const int zV = P.dvslot * (int)(N / 32);
-            const int yV = mt * gd.mt_modes * gd.nmag;
             const uint32_t bytes = 2 * L.b_bytes + L.p_bytes + L.dv_bytes;
-            int issued = 0;
-            // a K chunk lies within one spinor component (chunk_pts divides N)
-            const long long kc0 = (long long)chunk * chunk_pts;
-            const int sp = (int)(kc0 / N);
-            const long long r00 = kc0 - (long long)sp * N;
             // ring positions advance incrementally: no runtime divisions on the issue paths
             int s = 0;
             uint32_t ph = 0;
-            for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u)
+            long long issued = 0;
+            bool stop = false;
+            for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
             {
-                if (!mbar_wait_bounded(&empty[s], ph ^ 1u))
+                const TcUnit w = tc_unit(u, nchunks, mtiles, gd.nspin, pairs);
+                // tile-major operands: z = (row group) * blocks + block
+                const int zB_hi = ((w.P.kbz_kq * gd.nspin + w.spin) * 2 + 0) * nkb;
+                const int zB_lo = zB_hi + nkb;
+                const int zP = (w.P.kbz_k * gd.nspin + w.spin) * 2 * nkb;  // 16-point blocks
+                const int zV = w.P.dvslot * (int)(N / 32);
+                const int yV = w.mt * gd.mt_modes * gd.nmag;
+                // a K chunk lies within one spinor component (chunk_pts divides N)
+                const long long kc0 = (long long)w.chunk * chunk_pts;
+                const int sp = (int)(kc0 / N);
+                const long long r00 = kc0 - (long long)sp * N;
+                for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u)
                 {
-                    *abort_flag = 1;
-                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
-                    break;
+                    if (!mbar_wait_bounded(&empty[s], ph ^ 1u))
+                    {
+                        *abort_flag = 1;
+                        atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                        stop = true;
+                        break;
+                    }
+                    if (*abort_flag)
+                    {
+                        stop = true;
+                        break;
+                    }
+                    uint8_t* st = sm + s * L.stage_bytes;
+                    const long long kc = kc0 + (long long)it * TC_KPTS;
+                    const long long r0 = r00 + (long long)it * TC_KPTS;
+                    mbar_arrive_expect_tx(&full[s], bytes);
+                    tma_load_3d(st + L.b_hi, &tmapB, &full[s], 0, 0, zB_hi + (int)(kc >> 5));
+                    tma_load_3d(st + L.b_lo, &tmapB, &full[s], 0, 0, zB_lo + (int)(kc >> 5));
+                    for (int q = 0; q < nsp; ++q)
+                    {
+                        const int spp = (gd.nmag == 4) ? q : sp;
+                        const long long kq = (long long)spp * N + r0;
+                        // both 16-point halves of the stage in one box
+                        tma_load_3d(st + L.p + 2 * q * L.p_half, &tmapP, &full[s], 0, 0, zP + (int)(kq >> 4));
+                    }
+                    // dV_nu(r) of the tile's modes, all magnetic components: rows (nu, comp) x 32 points
+                    tma_load_3d(st + L.dv, &tmapV, &full[s], 0, yV, zV + (int)(r0 >> 5));
+                    ++issued;
                 }
-                if (*abort_flag) break;
-                uint8_t* st = sm + s * L.stage_bytes;
-                const long long kc = kc0 + (long long)it * TC_KPTS;
-                const long long r0 = r00 + (long long)it * TC_KPTS;
-                mbar_arrive_expect_tx(&full[s], bytes);
-                tma_load_3d(st + L.b_hi, &tmapB, &full[s], 0, 0, zB_hi + (int)(kc >> 5));
-                tma_load_3d(st + L.b_lo, &tmapB, &full[s], 0, 0, zB_lo + (int)(kc >> 5));
-                for (int q = 0; q < nsp; ++q)
-                {
-                    const int spp = (gd.nmag == 4) ? q : sp;
-                    const long long kq = (long long)spp * N + r0;
-                    // both 16-point halves of the stage in one box
-                    tma_load_3d(st + L.p + 2 * q * L.p_half, &tmapP, &full[s], 0, 0, zP + (int)(kq >> 4));
-                }
-                // dV_nu(r) of the tile's modes, all magnetic components: rows (nu, comp) x 32 points
-                tma_load_3d(st + L.dv, &tmapV, &full[s], 0, yV, zV + (int)(r0 >> 5));
-                issued = it + 1;
             }
             // let every issued copy land before the CTA can retire
-            for (int it = (issued > NST ? issued - NST : 0); it < issued; ++it)
-                mbar_wait_bounded(&full[it % NST], (uint32_t)(it / NST) & 1u);
+            for (long long i = (issued > NST ? issued - NST : 0); i < issued; ++i)
+                mbar_wait_bounded(&full[i % NST], (uint32_t)(i / NST) & 1u);
         }
     }
     else if (warp == 1)
@@ -406,60 +439,61 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             const uint32_t idesc = umma_idesc_f16(BF16 ? 1u : 0u, 128u, (uint32_t)NT);
             const uint32_t idesc2 = umma_idesc_f16(BF16 ? 1u : 0u, 128u, (uint32_t)(2 * NT));
             const bool merged = L.merged != 0;
-            int s = 0, a = 0, gi = 0, b = 0;
+            int s = 0, a = 0, b = 0;
             uint32_t pha = 0, phb = 0;
-            for (int it = 0; it < nstage; ++it)
+            bool stop = false;
+            for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
             {
-                const bool first = gi == 0;
-                const bool last = gi == TC_GROUP - 1 || it == nstage - 1;
-                // MMA issue blocks per instruction, so this thread checks one barrier
-                // per stage: the producers arrive on aready[a] only after they saw the
-                // stage's TMA tiles land (full[s]), which orders B for the MMAs too
-                bool ok = true;
-                if (first) ok = mbar_wait_bounded(&acce[b], phb ^ 1u);
-                ok = ok && mbar_wait_bounded(&aready[a], pha);
-                if (!ok)
+                for (int it = 0; it < nstage; ++it)
                 {
-                    *abort_flag = 1;
-                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t base = smem_u32(sm + s * L.stage_bytes);
-                const uint32_t dacc = tmem + (uint32_t)b * L.accw;
-                const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * 64u;
+                    const bool first = (it % TC_GROUP) == 0;
+                    const bool last = (it % TC_GROUP) == TC_GROUP - 1 || it == nstage - 1;
+                    // MMA issue blocks per instruction, so this thread checks one barrier
+                    // per stage: the producers arrive on aready[a] only after they saw the
+                    // stage's TMA tiles land (full[s]), which orders B for the MMAs too
+                    bool ok = true;
+                    if (first) ok = mbar_wait_bounded(&acce[b], phb ^ 1u);
+                    ok = ok && mbar_wait_bounded(&aready[a], pha);
+                    if (!ok)
+                    {
+                        *abort_flag = 1;
+                        atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = smem_u32(sm + s * L.stage_bytes);
+                    const uint32_t dacc = tmem + (uint32_t)b * L.accw;
+                    const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * 64u;
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                {
-                    const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
-                    const uint32_t en = (first && k == 0) ? 0u : 1u;
-                    if (merged)
+                    for (int k = 0; k < 4; ++k)
                     {
-                        // rows [0, NT) of the 2*NT-row tile are B_hi, [NT, 2NT) B_lo
-                        umma_f16_ta(dacc, ahi + 8 * k, bh, idesc2, en);
-                        umma_f16_ta(dacc + (uint32_t)NT, ahi + 32 + 8 * k, bh, idesc, 1u);
+                        const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
+                        const uint32_t en = (first && k == 0) ? 0u : 1u;
+                        if (merged)
+                        {
+                            // rows [0, NT) of the 2*NT-row tile are B_hi, [NT, 2NT) B_lo
+                            umma_f16_ta(dacc, ahi + 8 * k, bh, idesc2, en);
+                            umma_f16_ta(dacc + (uint32_t)NT, ahi + 32 + 8 * k, bh, idesc, 1u);
+                        }
+                        else
+                        {
+                            const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
+                            umma_f16_ta(dacc, ahi + 8 * k, bh, idesc, en);
+                            umma_f16_ta(dacc, ahi + 8 * k, bl, idesc, 1u);
+                            umma_f16_ta(dacc, ahi + 32 + 8 * k, bh, idesc, 1u);
+                        }
                     }
-                    else
+                    umma_commit(&empty[s]);
+                    umma_commit(&afree[a]);
+                    if (last) umma_commit(&accf[b]);
+                    s = (s + 1 == NST) ? 0 : s + 1;
+                    if (++a == NA)
                     {
-                        const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
-                        umma_f16_ta(dacc, ahi + 8 * k, bh, idesc, en);
-                        umma_f16_ta(dacc, ahi + 8 * k, bl, idesc, 1u);
-                        umma_f16_ta(dacc, ahi + 32 + 8 * k, bh, idesc, 1u);
+                        a = 0;
+                        pha ^= 1u;
                     }
-                }
-                umma_commit(&empty[s]);
-                umma_commit(&afree[a]);
-                if (last) umma_commit(&accf[b]);
-                s = (s + 1 == NST) ? 0 : s + 1;
-                if (++a == NA)
-                {
-                    a = 0;
-                    pha ^= 1u;
-                }
-                if (++gi == TC_GROUP)
-                {
-                    gi = 0;
-                    if (++b == NACC)
+                    if (last && ++b == NACC)
                     {
                         b = 0;
                         phb ^= 1u;
@@ -475,70 +509,77 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
-        const int nu0 = mt * MT;
-        const int MTa = min(MT, gd.nmodes - nu0);  // modes present in this tile
         const int row = 32 * q + lane;
         const int ml = row / gd.nbnds, m = row - ml * gd.nbnds;
-        const bool valid = ml < MTa;
-        const int mlc = valid ? ml : 0;
         const uint32_t swz = (uint32_t)(m & 7);
         const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
-        // a K chunk never straddles spinor components (chunk_pts divides N)
-        const long long kc0 = (long long)chunk * chunk_pts;
-        const int sp = (int)(kc0 / N);
-        int comp0, comp1;
-        if (gd.nmag == 4)
-        {
-            comp0 = 2 * sp;
-            comp1 = 2 * sp + 1;
-        }
-        else
-        {
-            comp0 = (gd.nmag == 2) ? spin : 0;
-            comp1 = comp0;
-        }
         int s = 0, a = 0;
         uint32_t ph = 0, pha = 0;
-        for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u,
-                 a = (a + 1 == NA) ? 0 : a + 1, pha ^= (a == 0) ? 1u : 0u)
+        bool stop = false;
+        for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
         {
-            bool ok = mbar_wait_bounded(&afree[a], pha ^ 1u) && mbar_wait_bounded(&full[s], ph);
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok && lane == 0)
-            {
-                *abort_flag = 1;
-                atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
-            }
-            if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) break;
-            tc_fence_after();
-            const uint8_t* st = sm + s * L.stage_bytes;
-            const uint8_t* pp[2];
-            const float4* dvp[2];
-            pp[0] = st + L.p + (0 * 2 + h) * L.p_half + (uint32_t)m * 128;
-            pp[1] = st + L.p + ((nsp - 1) * 2 + h) * L.p_half + (uint32_t)m * 128;
-            const float* dvs = reinterpret_cast<const float*>(st + L.dv);
-            dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * TC_KPTS + 16 * h) * 2);
-            dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * TC_KPTS + 16 * h) * 2);
-            const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * 64u + 16u * (uint32_t)h;
+            const TcUnit w = tc_unit(u, nchunks, mtiles, gd.nspin, pairs);
+            const int MTa = min(MT, gd.nmodes - w.mt * MT);  // modes present in this tile
+            const bool valid = ml < MTa;
+            const int mlc = valid ? ml : 0;
+            // a K chunk never straddles spinor components (chunk_pts divides N)
+            const int sp = (int)(((long long)w.chunk * chunk_pts) / N);
+            int comp0, comp1;
             if (gd.nmag == 4)
             {
-#pragma unroll
-                for (int j0 = 0; j0 < 16; j0 += 4)
-                    produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
+                comp0 = 2 * sp;
+                comp1 = 2 * sp + 1;
             }
             else
             {
-#pragma unroll
-                for (int j0 = 0; j0 < 16; j0 += 8)
-                    produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
+                comp0 = (gd.nmag == 2) ? w.spin : 0;
+                comp1 = comp0;
             }
-            tmem_wait_st();
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0)
+            for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u,
+                     a = (a + 1 == NA) ? 0 : a + 1, pha ^= (a == 0) ? 1u : 0u)
             {
-                mbar_arrive(&aready[a]);
-                mbar_arrive(&empty[s]);
+                bool ok = mbar_wait_bounded(&afree[a], pha ^ 1u) && mbar_wait_bounded(&full[s], ph);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok && lane == 0)
+                {
+                    *abort_flag = 1;
+                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                }
+                if (__any_sync(0xffffffffu, !ok || *abort_flag != 0))
+                {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint8_t* st = sm + s * L.stage_bytes;
+                const uint8_t* pp[2];
+                const float4* dvp[2];
+                pp[0] = st + L.p + (0 * 2 + h) * L.p_half + (uint32_t)m * 128;
+                pp[1] = st + L.p + ((nsp - 1) * 2 + h) * L.p_half + (uint32_t)m * 128;
+                const float* dvs = reinterpret_cast<const float*>(st + L.dv);
+                dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * TC_KPTS + 16 * h) * 2);
+                dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * TC_KPTS + 16 * h) * 2);
+                const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * 64u + 16u * (uint32_t)h;
+                if (gd.nmag == 4)
+                {
+#pragma unroll
+                    for (int j0 = 0; j0 < 16; j0 += 4)
+                        produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
+                }
+                else
+                {
+#pragma unroll
+                    for (int j0 = 0; j0 < 16; j0 += 8)
+                        produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
+                }
+                tmem_wait_st();
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0)
+                {
+                    mbar_arrive(&aready[a]);
+                    mbar_arrive(&empty[s]);
+                }
             }
         }
     }
@@ -549,54 +590,55 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         const int q = warp & 3;
         const int c0 = (dw >> 2) * 64;
         const int nc = min(64, NT - c0);
-        float acc[64];
-#pragma unroll
-        for (int i = 0; i < 64; ++i) acc[i] = 0.f;
-        bool good = true;
         int b = 0;
         uint32_t phb = 0;
-        for (int grp = 0; grp < ngroup; ++grp, b = (b + 1 == NACC) ? 0 : b + 1, phb ^= (b == 0) ? 1u : 0u)
+        bool stop = false;
+        for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
         {
-            bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], phb);
-            ok = __all_sync(0xffffffffu, ok);
-            if (!ok)
-            {
-                if (lane == 0 && *abort_flag == 0)
-                {
-                    *abort_flag = 1;
-                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
-                }
-                good = false;
-                break;
-            }
-            tc_fence_after();
-            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)b * L.accw + (uint32_t)c0;
+            float acc[64];
 #pragma unroll
-            for (int c = 0; c < 64; c += 16)
+            for (int i = 0; i < 64; ++i) acc[i] = 0.f;
+            for (int grp = 0; grp < ngroup; ++grp, b = (b + 1 == NACC) ? 0 : b + 1, phb ^= (b == 0) ? 1u : 0u)
             {
-                if (c < nc)
+                bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], phb);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok)
                 {
-                    float v[16];
-                    tmem_ld16(ta + (uint32_t)c, v);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
-                    if (L.merged)
+                    if (lane == 0 && *abort_flag == 0)
                     {
-                        tmem_ld16(ta + (uint32_t)(NT + c), v);
+                        *abort_flag = 1;
+                        atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                    }
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)b * L.accw + (uint32_t)c0;
+#pragma unroll
+                for (int c = 0; c < 64; c += 16)
+                {
+                    if (c < nc)
+                    {
+                        float v[16];
+                        tmem_ld16(ta + (uint32_t)c, v);
 #pragma unroll
                         for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
+                        if (L.merged)
+                        {
+                            tmem_ld16(ta + (uint32_t)(NT + c), v);
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) acc[c + i] += v[i];
+                        }
                     }
                 }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acce[b]);
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acce[b]);
-        }
-        if (good)
-        {
+            if (stop) break;
+            const TcUnit w = tc_unit(u, nchunks, mtiles, gd.nspin, pairs);
             const int row = q * 32 + lane;
-            const int mtiles = gridDim.y;
-            float* out = partials + ((((size_t)zp * mtiles + mt) * nchunks + chunk) * 128 + row) * NT + c0;
+            float* out = partials + ((((size_t)w.zp * mtiles + w.mt) * nchunks + w.chunk) * 128 + row) * NT + c0;
 #pragma unroll
             for (int c = 0; c < 64; c += 4)
                 if (c < nc) *reinterpret_cast<float4*>(out + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
@@ -616,20 +658,27 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
                            float* partials, unsigned* status, cudaStream_t st)
 {
     const int mtiles = (g.nmodes + g.mt_modes - 1) / g.mt_modes;
-    dim3 grid(nchunks, mtiles, npairs * g.nspin);
+    const long long units = (long long)npairs * g.nspin * mtiles * nchunks;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = (int)std::min<long long>(units, std::max(1, nsm));
     const int smem = lelph_local_tc_smem_bytes(g);
     const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
+    if (units <= 0) return;
     if (ab_bf16)
     {
         cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, partials, status);
+        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, (int)units,
+                                                   partials, status);
     }
     else
     {
         cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, partials, status);
+        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, (int)units,
+                                                   partials, status);
     }
 }
