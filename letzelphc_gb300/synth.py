@@ -307,6 +307,12 @@ class System:
     eigVec: np.ndarray             # (nq, nmodes, nmodes)
     dVscf: np.ndarray              # (nq, nmodes, nmag, Nx, Ny, Nz)
     extra: dict = field(default_factory=dict)
+    # local pseudopotential per species (struct local_pseudo): radial mesh,
+    # its derivative, V_loc(r) in Ry, valence charge
+    loc_r: Optional[list] = None
+    loc_rab: Optional[list] = None
+    loc_v: Optional[list] = None
+    loc_zval: Optional[np.ndarray] = None
 
     @property
     def natom(self):
@@ -476,8 +482,33 @@ def make_system(name: str = "c0", overrides: Optional[dict] = None) -> System:
                   nspin=nspin, nspinor=nspinor, nmag=nmag, nbnds=nb, gvec=gvec, miller=miller, wfc=wfc,
                   Fk=Fk, PP_table=PP_table, Fsign=Fsign, fCoeff=fCoeff, lmax=max(ls),
                   is_soc_present=soc, qpts=qpts, eigVec=eig, dVscf=dV)
+    local_pseudo(sysm, cfg.get("seed", 1000))
     check_box(sysm)
     return sysm
+
+
+def local_pseudo(s: System, seed: int):
+    """Seeded local pseudopotential of every species (own generator, so the
+    rest of the system does not depend on it): a QE-style logarithmic mesh
+    r_i = exp(xmin + i dx) / Z, rab_i = r_i dx, out to ~10 bohr, and
+    V_loc(r) = -Z e2 erf(r / rc) / r + a exp(-(r / w)^2) (Ry, e2 = 2)."""
+    rng = np.random.default_rng(seed + 7919)
+    e2 = 2.0
+    s.loc_zval = rng.choice([1.0, 3.0, 4.0, 5.0, 6.0], size=s.ntype)
+    s.loc_r, s.loc_rab, s.loc_v = [], [], []
+    for t in range(s.ntype):
+        z = s.loc_zval[t]
+        xmin, dx = -7.0, 0.0125
+        n = int((np.log(10.0 * z) - xmin) / dx) + 1
+        r = np.exp(xmin + dx * np.arange(n)) / z
+        rc = rng.uniform(0.6, 1.0)
+        a = rng.uniform(-1.5, -0.3)
+        w = rng.uniform(0.6, 1.2)
+        from math import erf
+        v = np.array([-z * e2 * erf(ri / rc) / ri for ri in r]) + a * np.exp(-(r / w) ** 2)
+        s.loc_r.append(r)
+        s.loc_rab.append(r * dx)
+        s.loc_v.append(v)
 
 
 def check_box(s: System):
@@ -547,6 +578,12 @@ def write_system(s: System, path: str, kminusq: bool = False, non_loc: bool = Tr
             for i, fc in enumerate(s.fCoeff):
                 if fc is not None:
                     _rec(f, f"fCoeff{i}", fc)
+        if s.loc_zval is not None:
+            _rec(f, "loc_zval", np.asarray(s.loc_zval, np.float64))
+            for t in range(s.ntype):
+                _rec(f, f"loc_r{t}", s.loc_r[t])
+                _rec(f, f"loc_rab{t}", s.loc_rab[t])
+                _rec(f, f"loc_v{t}", s.loc_v[t])
         f.write(b"END\0" + b"\0" * 28)
 
 

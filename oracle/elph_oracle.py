@@ -10,6 +10,11 @@ It restates, in numpy FP64, the reference's G-space algorithm for one q-point
 * ``elph_local``        src/dvloc/compute_Vbare_loc.c:17-353
 * ``add_elph_nonlocal`` src/nonloc/Vbare_nloc.c:35-577 (+ sum_VNL_KKp.c:8-58)
 * ``elph_q_rotate``     src/symmetries/elphq_expand.c:16-73
+* ``vloc_table``, ``dvlocq``, ``add_dvscf_qe`` (the per-q local bare
+  potential that elph_driver adds before the stage,
+  src/elph/elph_driver.c:234-252): src/dvloc/vlocg_table.c:16-154,
+  src/dvloc/VlocG_atom.c:10-57, src/common/spline.c:13-139,
+  src/dvloc/dVbare_loc.c:16-231, src/dvloc/add_dvscf.c:12-92
 
 FFTW is replaced by numpy's pocketfft: the reference's FFT is a pruned,
 slab-distributed 3-D complex DFT (src/fft/*.c); pruning changes nothing but
@@ -427,4 +432,163 @@ def elph_q_rotate(Dl, g, Dr, tim_rev):
             A = np.conj(gq).T if tim_rev else gq.T
             tmp = A @ np.conj(Dr[isp]).T
             out[iv, isp] = tmp.T @ Dl[isp].T
+    return out
+
+
+# ------------------------------------------------------- local bare potential
+
+def simpson_weights(n):
+    """Weights w with  sum_i w_i f_i dx_i / 3  = the reference's Simpson rule
+    (src/common/numerical_func.c:155-192), including its even-n end correction."""
+    w = np.zeros(n)
+    if n < 3:
+        return w
+    w[0] = 1.0
+    w[1:n - 1:2] += 4.0
+    w[2:n - 1:2] += 2.0
+    if n % 2:
+        w[n - 1] += 1.0
+    else:
+        w[n - 3] -= 0.25
+        w[n - 2] += 1.0
+        w[n - 1] += 1.25
+    return w
+
+
+def vloc_gspace(G, r, rab, vloc, zval, volume, cutoff="3", eta=1.0):
+    """4 pi / V int dr (sin(G r)/G) (r V_loc(r) + e2 Z erf(sqrt(eta) r)) for an
+    array of |G| (src/dvloc/VlocG_atom.c:10-57); at G = 0 the sin(Gr)/G factor
+    is r, and in 3-D the erf is dropped there."""
+    from scipy.special import erf
+    G = np.atleast_1d(np.asarray(G, float))
+    w = simpson_weights(len(r)) * rab
+    out = np.empty(len(G))
+    base = r * vloc + ELPH_E2 * zval * erf(r * math.sqrt(eta))
+    base0 = r * vloc + ELPH_E2 * zval
+    for c0 in range(0, len(G), 512):
+        g = G[c0:c0 + 512, None]
+        small = g < ELPH_EPS
+        fac = np.where(small, r[None, :], np.sin(r[None, :] * g) / np.where(small, 1.0, g))
+        body = np.where(small & (cutoff == "3"), base0[None, :], base[None, :])
+        out[c0:c0 + 512] = (fac * body) @ w / 3.0
+    return 4 * ELPH_PI * out / volume
+
+
+def prepare_spline(x, y):
+    """Slopes of the not-a-knot cubic spline through (x, y)
+    (src/common/spline.c:30-139: tridiagonal system, Thomas algorithm)."""
+    n = len(x)
+    a = np.zeros(n); b = np.zeros(n); c = np.zeros(n); d = np.zeros(n)
+    dx1 = x[1] - x[0]; s1 = (y[1] - y[0]) / dx1
+    dx2 = x[2] - x[1]; s2 = (y[2] - y[1]) / dx2
+    a[0] = dx2 * dx2; b[0] = dx2 * dx2 - dx1 * dx1; c[0] = -dx1 * dx1
+    d[0] = 2 * (s1 * dx2 * dx2 - s2 * dx1 * dx1)
+    dx1 = x[n - 2] - x[n - 3]; s1 = (y[n - 2] - y[n - 3]) / dx1
+    dx2 = x[n - 1] - x[n - 2]; s2 = (y[n - 1] - y[n - 2]) / dx2
+    a[n - 1] = dx2 * dx2; b[n - 1] = dx2 * dx2 - dx1 * dx1; c[n - 1] = -dx1 * dx1
+    d[n - 1] = 2 * (s1 * dx2 * dx2 - s2 * dx1 * dx1)
+    dxi = x[2:] - x[1:-1]; dxn = x[1:-1] - x[:-2]
+    si = (y[2:] - y[1:-1]) / dxi; sn = (y[1:-1] - y[:-2]) / dxn
+    a[1:-1] = dxi; b[1:-1] = 2.0 * (dxi + dxn); c[1:-1] = dxn; d[1:-1] = 3 * (sn * dxi + si * dxn)
+    al = -c[0] / c[1]
+    a[0] += al * a[1]; b[0] += al * b[1]; c[0] += al * c[1]; d[0] += al * d[1]
+    c[0] = b[0]; b[0] = a[0]; a[0] = 0.0
+    al = -a[n - 1] / a[n - 2]
+    a[n - 1] += al * a[n - 2]; b[n - 1] += al * b[n - 2]; c[n - 1] += al * c[n - 2]; d[n - 1] += al * d[n - 2]
+    a[n - 1] = b[n - 1]; b[n - 1] = c[n - 1]; c[n - 1] = 0.0
+    for i in range(1, n):
+        ww = a[i] / b[i - 1]
+        b[i] -= ww * c[i - 1]
+        d[i] -= ww * d[i - 1]
+    dy = np.zeros(n)
+    dy[n - 1] = d[n - 1] / b[n - 1]
+    for i in range(n - 2, -1, -1):
+        dy[i] = (d[i] - c[i] * dy[i + 1]) / b[i]
+    return dy
+
+
+def spline_interpolate(xq, idx, x, y, dy):
+    """Cubic Hermite form of the spline on [x_idx, x_idx+1] (src/common/spline.c:13-28)."""
+    h = x[idx + 1] - x[idx]
+    t = (xq - x[idx]) / h
+    ax = dy[idx] * h - (y[idx + 1] - y[idx])
+    bx = -dy[idx + 1] * h + (y[idx + 1] - y[idx])
+    return (1 - t) * y[idx] + t * y[idx + 1] + t * (1 - t) * ((1 - t) * ax + t * bx)
+
+
+def vloc_table(s, qmax_abs):
+    """|G| grid and V_loc(|G|) table with spline slopes per species
+    (create_vlocg_table, src/dvloc/vlocg_table.c:16-154)."""
+    volume = abs(det3x3(s.alat))
+    blat = np.asarray(s.blat)
+    bi = np.sqrt((blat ** 2).sum(axis=0))
+    bmin, bmax = bi.min(), bi.max()
+    nmax = max(s.fft_dims)
+    if bmin > 0.01:
+        bmin = 0.01
+    gmax = (1.7 * (nmax + 4.0) + 3 * abs(qmax_abs)) * bmax
+    npts = int(math.ceil(gmax / bmin))
+    dg = gmax / (npts - 1.0)
+    g = np.arange(npts) * dg
+    vals, slopes = [], []
+    for t in range(s.ntype):
+        v = vloc_gspace(g, s.loc_r[t], s.loc_rab[t], s.loc_v[t], s.loc_zval[t], volume, s.dimension)
+        vals.append(v)
+        slopes.append(prepare_spline(g, v))
+    return {"g": g, "dg": dg, "v": np.array(vals), "dv": np.array(slopes), "volume": volume}
+
+
+def miller_of_index(N):
+    """FFT index -> Miller index (get_miller_idx, src/common/numerical_func.c:436-448)."""
+    i = np.arange(N)
+    mid = (N - 1) // 2 + 1
+    return np.where(i < mid, i, (i - mid) - N // 2)
+
+
+def dvlocq(s, qpt, eigVec, table):
+    """Local bare potential change per mode in real space, (nmodes, Nx, Ny, Nz)
+    (dVlocq, src/dvloc/dVbare_loc.c:16-231)."""
+    Nx, Ny, Nz = s.fft_dims
+    mx, my, mz = miller_of_index(Nx), miller_of_index(Ny), miller_of_index(Nz)
+    M = np.stack(np.meshgrid(mx + qpt[0], my + qpt[1], mz + qpt[2], indexing="ij"), -1).reshape(-1, 3)
+    qG = M @ np.asarray(s.blat).T                      # blat . (G + q), 2 pi included
+    nrm = np.sqrt((qG ** 2).sum(1))
+    g = table["g"]
+    if nrm.max() > g[-1]:
+        raise ValueError("Vlocg interpolation out of bounds")
+    idx = np.floor(nrm / table["dg"]).astype(int)
+    cut = np.ones_like(nrm)
+    if s.dimension == "2":
+        c = s.alat[2, 2]
+        gp = np.sqrt(qG[:, 0] ** 2 + qG[:, 1] ** 2)
+        cs = np.cos(qG[:, 2] * c * 0.5)
+        big = gp > ELPH_EPS
+        cs = np.where(big, cs - np.sin(qG[:, 2] * c * 0.5) * qG[:, 2] / np.where(big, gp, 1.0), cs)
+        cut = 1 - np.exp(-c * gp * 0.5) * cs
+    V = np.empty((s.ntype, len(nrm)))
+    for t in range(s.ntype):
+        v = spline_interpolate(nrm, idx, g, table["v"][t], table["dv"][t])
+        lr = (4 * ELPH_PI * ELPH_E2) * s.loc_zval[t] * np.exp(-nrm * nrm * 0.25) * cut / \
+            (np.where(nrm >= ELPH_EPS, nrm * nrm, 1.0) * table["volume"])
+        V[t] = np.where(nrm >= ELPH_EPS, v - lr, v)
+    cart = np.empty((len(nrm), 3 * s.natom), complex)
+    for a in range(s.natom):
+        fac = -1j * np.exp(-1j * (qG @ s.atom_pos[a])) * V[s.atom_type[a]]
+        cart[:, 3 * a:3 * a + 3] = fac[:, None] * qG
+    VG = (np.asarray(eigVec) @ cart.T).reshape(-1, Nx, Ny, Nz)
+    return np.fft.ifftn(VG, axes=(1, 2, 3)) * (Nx * Ny * Nz)
+
+
+def add_dvscf_qe(dv, vloc, nmag):
+    """dV_scf (nmodes, nmag, ...) plus the local bare part, with the nmag = 4
+    composite [V + Bz, Bx - iBy, Bx + iBy, V - Bz] (src/dvloc/add_dvscf.c:12-92)."""
+    out = np.array(dv, complex, copy=True)
+    for m in range(2 if nmag == 2 else 1):
+        out[:, m] += vloc
+    if nmag == 4:
+        V, Bx, By, Bz = out[:, 0].copy(), out[:, 1].copy(), out[:, 2].copy(), out[:, 3].copy()
+        out[:, 0] = V + Bz
+        out[:, 1] = Bx - 1j * By
+        out[:, 2] = Bx + 1j * By
+        out[:, 3] = V - Bz
     return out

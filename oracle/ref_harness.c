@@ -9,9 +9,19 @@
  * as complex128 (nq, nk_BZ, nmodes, nspin, nb, nb).
  *
  * usage: lelph_ref <system.bin> <g_out.bin> [rotate <D_in.bin> <g_rot_out.bin>]
+ *        lelph_ref <system.bin> <g_out.bin> dvloc <v_out.bin>
+ *
+ * dvloc: the system's dVscf records are the induced part (QE's dvscf); the
+ * harness builds the V_loc table (create_vlocg_table, src/dvloc/vlocg_table.c)
+ * from the loc_* records, and per q runs dVlocq and add_dvscf_qe
+ * (src/dvloc/dVbare_loc.c:16, src/dvloc/add_dvscf.c:12) the way elph_driver
+ * does (src/elph/elph_driver.c:234-252) before compute_and_write_elphq.
+ * v_out.bin receives, per q, Vlocr (nmodes, nfft) then the summed dV
+ * (nmodes, nmag, nfft), complex128.
  *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
+#include <math.h>
 #include <stdbool.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -20,6 +30,7 @@
 
 #include "common/ELPH_timers.h"
 #include "common/dtypes.h"
+#include "dvloc/dvloc.h"
 #include "elph/elph.h"
 #include "netcdf.h"
 #include "symmetries/symmetries.h"
@@ -242,6 +253,54 @@ int main(int argc, char** argv)
     double _Complex* eig = get("eigVec", 1)->data;
     double _Complex* dv = get("dVscf", 1)->data;
     size_t nfft = (size_t)Nx * Ny * Nz;
+    if (argc >= 5 && !strcmp(argv[3], "dvloc"))
+    {
+        const double* A = lat.alat_vec;
+        double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                     A[2] * (A[3] * A[7] - A[4] * A[6]);
+        lat.volume = det < 0 ? -det : det;
+        const double* zv = get("loc_zval", 1)->data;
+        ps.loc_pseudo = calloc((size_t)ntype, sizeof(struct local_pseudo));
+        ps.ngrid_max = 0;
+        for (int t = 0; t < ntype; ++t)
+        {
+            char nm[32];
+            snprintf(nm, 32, "loc_r%d", t);
+            struct rec* rr = get(nm, 1);
+            snprintf(nm, 32, "loc_rab%d", t);
+            struct rec* ra = get(nm, 1);
+            snprintf(nm, 32, "loc_v%d", t);
+            struct rec* rv = get(nm, 1);
+            ps.loc_pseudo[t].r_grid = rr->data;
+            ps.loc_pseudo[t].rab_grid = ra->data;
+            ps.loc_pseudo[t].Vloc_atomic = rv->data;
+            ps.loc_pseudo[t].ngrid = rr->dims[0];
+            ps.loc_pseudo[t].Zval = zv[t];
+            if (rr->dims[0] > ps.ngrid_max) ps.ngrid_max = rr->dims[0];
+        }
+        /* qmax_abs as src/io/get_save_data.c:622-631 sets it */
+        double qmax = 0;
+        for (int i = 0; i < 3 * nq; ++i)
+        {
+            double a = ph.qpts_iBZ[i] < 0 ? -ph.qpts_iBZ[i] : ph.qpts_iBZ[i];
+            if (a > qmax) qmax = a;
+        }
+        ps.vloc_table->qmax_abs = ceil(qmax) + 1;
+        create_vlocg_table(&lat, &ps, &comm);
+        FILE* fv = fopen(argv[4], "wb");
+        if (!fv) die("cannot write dvloc output");
+        double _Complex* vloc = malloc(sizeof(double _Complex) * (size_t)nmodes * nfft);
+        for (int iq = 0; iq < nq; ++iq)
+        {
+            double _Complex* dvq = dv + (size_t)iq * nmodes * nmag * nfft;
+            dVlocq(ph.qpts_iBZ + 3 * iq, &lat, &ps, eig + (size_t)iq * nmodes * nmodes, vloc, comm.commK);
+            add_dvscf_qe(dvq, vloc, &lat);
+            fwrite(vloc, sizeof(double _Complex), (size_t)nmodes * nfft, fv);
+            fwrite(dvq, sizeof(double _Complex), (size_t)nmodes * nmag * nfft, fv);
+        }
+        fclose(fv);
+        free(vloc);
+    }
     for (int iq = 0; iq < nq; ++iq)
     {
         compute_and_write_elphq(wfcs, &lat, &ps, &ph, iq, eig + (size_t)iq * nmodes * nmodes,

@@ -5,7 +5,10 @@ letzelphc_gb300.synth.make_system from the spec stored in the fixture) and
 the elph matrix elements that the reference's own per-q stage
 (compute_and_write_elphq, src/elph/compute_elph_matq.c:20, FP64 build)
 produced for it, run through oracle/_ref/lelph_ref (oracle/Makefile).
-A second fixture pins elph_q_rotate (src/symmetries/elphq_expand.c:16).
+A second fixture pins elph_q_rotate (src/symmetries/elphq_expand.c:16), and
+the dvloc_* fixtures pin the local bare potential added per q before the
+stage (create_vlocg_table / dVlocq / add_dvscf_qe, src/dvloc/), with the
+matrix elements computed from the summed dV.
 
 Run from the repo root after ``make -C oracle``:
     python tests/golden/make_golden.py
@@ -54,6 +57,41 @@ def run(name, base, ov, kmq, nl, tmp):
     print(name, g.shape, float(np.abs(g).max()))
 
 
+# systems whose dVscf is the induced part: the reference adds the local bare
+# potential (create_vlocg_table, dVlocq, add_dvscf_qe) before the stage
+# name -> (base config, overrides, kminusq, non_loc)
+GOLDEN_DVLOC = {
+    "dvloc_c0": ("c0", {"kgrid": (2, 2, 2), "nbnds": 4, "qpts": [(0, 0, 0), (0.5, 0, 0)]}, False, True),
+    "dvloc_2d": ("c2", {"kgrid": (3, 3, 1), "fft": (15, 15, 60), "nbnds": 4, "npw": 100,
+                        "qpts": [(1 / 3, 0, 0)]}, False, True),
+    "dvloc_lsda": ("c0", {"nspin": 2, "nbnds": 4, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}, False, True),
+    "dvloc_soc": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True,
+                         "ls": (0, 1, 2), "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (2, 2, 2),
+                         "qpts": [(0.5, 0.5, 0)]}, False, True),
+}
+SAMPLE = 4099  # every SAMPLE-th element of V_loc(r) and of the summed dV is stored
+
+
+def run_dvloc(name, base, ov, kmq, nl, tmp):
+    s = synth.make_system(base, dict(ov))
+    sysf = os.path.join(tmp, name + ".bin")
+    gf = os.path.join(tmp, name + "_g.bin")
+    vf = os.path.join(tmp, name + "_v.bin")
+    synth.write_system(s, sysf, kminusq=kmq, non_loc=nl)
+    subprocess.run([REF, sysf, gf, "dvloc", vf], check=True)
+    g = synth.read_g(gf, s, len(s.qpts))
+    N = int(np.prod(s.fft_dims))
+    raw = np.fromfile(vf, np.complex128).reshape(len(s.qpts), -1)
+    vloc = raw[:, :s.nmodes * N]
+    dv = raw[:, s.nmodes * N:]
+    spec = json.dumps({"base": base, "overrides": ov, "kminusq": kmq, "non_loc": nl})
+    np.savez(os.path.join(ROOT, "tests", "golden", name + ".npz"), g=g, spec=np.array(spec),
+             vloc_sample=vloc[:, ::SAMPLE], dv_sample=dv[:, ::SAMPLE], sample=np.array(SAMPLE),
+             vloc_norm=np.linalg.norm(vloc, axis=1), dv_norm=np.linalg.norm(dv, axis=1),
+             wfc_sum=np.array([np.abs(w).sum() for w in s.wfc]), dv_sum=np.abs(s.dVscf).sum())
+    print(name, g.shape, float(np.abs(g).max()), float(np.abs(vloc).max()))
+
+
 def rotate_fixture(tmp):
     s = synth.make_system("c0", {"nbnds": 5})
     rng = np.random.default_rng(7)
@@ -85,4 +123,6 @@ if __name__ == "__main__":
     with tempfile.TemporaryDirectory() as tmp:
         for name, (base, ov, kmq, nl) in GOLDEN.items():
             run(name, base, ov, kmq, nl, tmp)
+        for name, (base, ov, kmq, nl) in GOLDEN_DVLOC.items():
+            run_dvloc(name, base, ov, kmq, nl, tmp)
         rotate_fixture(tmp)

@@ -9,6 +9,8 @@ from letzelphc_gb300 import synth
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = ["c0", "c0_local", "zb_tr", "zb_tr_kmq", "lsda", "soc_tr", "spinor_nosoc", "l12_small"]
+# fixtures whose dVscf is the induced part; the reference added the local bare potential
+DVLOC_NAMES = ["dvloc_c0", "dvloc_2d", "dvloc_lsda", "dvloc_soc"]
 
 
 def load(name):
@@ -21,3 +23,11 @@ def load(name):
     assert np.allclose([np.abs(w).sum() for w in s.wfc], z["wfc_sum"], rtol=1e-12)
     assert np.isclose(np.abs(s.dVscf).sum(), float(z["dv_sum"]), rtol=1e-12)
     return s, z["g"], bool(spec["kminusq"]), bool(spec["non_loc"])
+
+
+def load_dvloc(name):
+    """(system, fixture) of a dvloc_* fixture: g from the summed dV, every
+    `sample`-th element of V_loc(r) and of the summed dV per q, their norms."""
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    s, _, _, _ = load(name)
+    return s, z

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import elph_oracle as O
-from golden_util import NAMES, load
+from golden_util import DVLOC_NAMES, NAMES, load, load_dvloc
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -13,6 +13,26 @@ def test_oracle_matches_reference(name):
     g = np.array([O.compute_elphq(s, iq, non_loc=nl, kminusq=kmq) for iq in range(len(s.qpts))])
     err = np.abs(g - g_ref).max() / np.abs(g_ref).max()
     assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("name", DVLOC_NAMES)
+def test_local_bare_potential_matches_reference(name):
+    """V_loc table + dVlocq + add_dvscf_qe, then the stage on the summed dV."""
+    s, z = load_dvloc(name)
+    step = int(z["sample"])
+    tab = O.vloc_table(s, np.ceil(np.abs(s.qpts).max()) + 1)
+    g = []
+    for iq in range(len(s.qpts)):
+        v = O.dvlocq(s, s.qpts[iq], s.eigVec[iq], tab).reshape(-1)
+        dv = O.add_dvscf_qe(s.dVscf[iq], v.reshape(s.nmodes, *s.fft_dims), s.nmag)
+        assert np.abs(v[::step] - z["vloc_sample"][iq]).max() < 1e-12 * np.abs(z["vloc_sample"][iq]).max()
+        assert abs(np.linalg.norm(v) - z["vloc_norm"][iq]) < 1e-12 * z["vloc_norm"][iq]
+        flat = dv.reshape(-1)
+        assert np.abs(flat[::step] - z["dv_sample"][iq]).max() < 1e-12 * np.abs(z["dv_sample"][iq]).max()
+        assert abs(np.linalg.norm(flat) - z["dv_norm"][iq]) < 1e-12 * z["dv_norm"][iq]
+        g.append(O.compute_elphq(s, iq, dVscfq=dv, non_loc=True))
+    g = np.array(g)
+    assert np.abs(g - z["g"]).max() < 1e-12 * np.abs(z["g"]).max()
 
 
 def test_q_rotate_matches_reference():
