@@ -149,6 +149,30 @@ int lelph_gpu_run_device(lelph_gpu* h, int n, const int* qslot, const int* kbz, 
 int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslot, const int* kbz, int non_loc, int kminusq,
                                  int out_type, void* g_out_dev);
 
+/* Local pseudopotential of every species on its radial mesh -- the fields of
+ * struct local_pseudo (src/common/dtypes.h:204-217): ngrid[t] points r_grid[t],
+ * mesh derivative rab_grid[t], V_loc in Ry, valence charge zval[t] -- and the
+ * cell's periodicity ('3', or '2' for a slab with the Coulomb cutoff along z).
+ * Builds the V_loc(|G|) interpolation table of create_vlocg_table
+ * (src/dvloc/vlocg_table.c:16-154) on the device; qmax_abs bounds |q| in
+ * crystal units as Vloc_table.qmax_abs does (ceil(max |q_i|) + 1). */
+int lelph_gpu_set_local_pseudo(lelph_gpu* h, const int* ngrid, const double* const* r_grid,
+                               const double* const* rab_grid, const double* const* vloc_atomic, const double* zval,
+                               int dimension, double qmax_abs);
+
+/* dVlocq (src/dvloc/dVbare_loc.c:16-231): the local bare potential change of
+ * every mode of q in real space, Vlocr (nmodes, Nx, Ny, Nz) complex, on the
+ * reference's FFT box.  Needs lelph_gpu_set_local_pseudo. */
+int lelph_gpu_dvlocq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, double* Vlocr);
+
+/* lelph_gpu_set_q from the induced potential alone: dVscf_induced
+ * (nmodes, nmag, Nx, Ny, Nz) is QE's dvscf (dV_Ha + dV_xc), or NULL for the
+ * bare kernels; the library adds dVlocq on the device with add_dvscf_qe's
+ * rule (src/dvloc/add_dvscf.c:12-92), as elph_driver does before
+ * compute_and_write_elphq (src/elph/elph_driver.c:234-252). */
+int lelph_gpu_set_q_induced(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                            const double* dVscf_induced);
+
 /* compute_and_write_elphq for one iBZ q without the netCDF writes: every
  * full-BZ k, output (nkpts_BZ, nmodes, nspin, nbnds, nbnds) complex double. */
 int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, const double* dVscfq,

@@ -87,6 +87,12 @@ struct lelph_gpu
     int tmapV_rows = 0;
     int nslots_alloc = 0;
     int chunk_pts = 0, nchunks = 0;
+    // local bare potential: V_loc(|G|) table and its spline slopes per species
+    DevBuf d_vl_v, d_vl_dv, d_vl_in, d_vloc;
+    bool vl_ready = false;
+    int vl_npts = 0, vl_dim2 = 0;
+    double vl_dg = 0, vl_volume = 0;
+    std::vector<double> vl_zval;
 };
 
 namespace
@@ -842,7 +848,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_fcoefoff, &h->d_tw64[0], &h->d_tw64[1], &h->d_tw64[2], &h->d_tw32[0], &h->d_tw32[1],
                       &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
-                      &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp};
+                      &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
+                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1070,10 +1077,11 @@ __global__ void k_dv_window(const double2* __restrict__ dvhat, int ncomp, int Nx
     }
 }
 
-extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
-                               const double* dVscf)
+// Load q slot `slot`: eigVec and dV (host); dVscf == nullptr loads zeros.
+static int set_q_common(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                        const double* dVscf)
 {
-    if (!h || slot < 0 || !qpt_crys || !eigVec || !dVscf) return LELPH_GPU_ERR_INVALID;
+    if (!h || slot < 0 || !qpt_crys || !eigVec) return LELPH_GPU_ERR_INVALID;
     if (slot > 4096) return fail(h, LELPH_GPU_ERR_INVALID, "slot index too large");
     CUDA_TRY(h, cudaSetDevice(h->device));
     const lelph_gpu_desc& d = h->d;
@@ -1124,10 +1132,251 @@ extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3],
         }
     CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_eig.p + (size_t)slot * d.nmodes * d.nmodes, eigVec,
                                 sizeof(double2) * d.nmodes * d.nmodes, cudaMemcpyHostToDevice, h->st));
-    CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_dvr.p + (size_t)slot * dvn, dVscf, sizeof(double2) * dvn,
-                                cudaMemcpyHostToDevice, h->st));
+    if (dVscf)
+        CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_dvr.p + (size_t)slot * dvn, dVscf, sizeof(double2) * dvn,
+                                    cudaMemcpyHostToDevice, h->st));
+    else
+        CUDA_TRY(h, cudaMemsetAsync((double2*)h->d_dvr.p + (size_t)slot * dvn, 0, sizeof(double2) * dvn, h->st));
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     q.set = true;
+    h->windows_ok = false;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                               const double* dVscf)
+{
+    if (!h || !dVscf) return LELPH_GPU_ERR_INVALID;
+    return set_q_common(h, slot, qpt_crys, eigVec, dVscf);
+}
+
+// ------------------------------------------------------ local bare potential
+
+// Slopes of the not-a-knot cubic spline through (i*dg, y_i): the usual
+// tridiagonal system for the slopes with third-derivative continuity at the
+// second and next-to-last knots, the two extra entries removed by one row
+// operation each, solved by the Thomas algorithm.
+static std::vector<double> spline_slopes(const std::vector<double>& y, double dg)
+{
+    const int n = (int)y.size();
+    std::vector<double> lo(n), di(n), up(n), rh(n), d(n);
+    auto sl = [&](int i) { return (y[i + 1] - y[i]) / dg; };
+    for (int i = 1; i < n - 1; ++i)
+    {
+        lo[i] = dg;
+        di[i] = 4.0 * dg;
+        up[i] = dg;
+        rh[i] = 3.0 * (sl(i - 1) * dg + sl(i) * dg);
+    }
+    // first row (not-a-knot at x_1): dx^2 d0 + 0 d1 - dx^2 d2 = 2 (s0 - s1) dx^2, its
+    // d2 entry removed against row 1
+    {
+        const double h2 = dg * dg;
+        double a0 = h2, b0 = 0.0, c0 = -h2, r0 = 2.0 * (sl(0) - sl(1)) * h2;
+        const double al = -c0 / up[1];
+        a0 += al * lo[1];
+        b0 += al * di[1];
+        r0 += al * rh[1];
+        di[0] = a0;
+        up[0] = b0;
+        rh[0] = r0;
+    }
+    {
+        // last row: dx^2 d_{n-3} + 0 d_{n-2} - dx^2 d_{n-1} = 2 (s_{n-3} - s_{n-2}) dx^2,
+        // its d_{n-3} entry removed against row n-2
+        const double h2 = dg * dg;
+        const double cm3 = h2, cm2 = 0.0, cm1 = -h2;
+        const double al = -cm3 / lo[n - 2];
+        lo[n - 1] = cm2 + al * di[n - 2];
+        di[n - 1] = cm1 + al * up[n - 2];
+        rh[n - 1] = 2.0 * (sl(n - 3) - sl(n - 2)) * h2 + al * rh[n - 2];
+    }
+    for (int i = 1; i < n; ++i)
+    {
+        const double w = lo[i] / di[i - 1];
+        di[i] -= w * up[i - 1];
+        rh[i] -= w * rh[i - 1];
+    }
+    d[n - 1] = rh[n - 1] / di[n - 1];
+    for (int i = n - 2; i >= 0; --i) d[i] = (rh[i] - up[i] * d[i + 1]) / di[i];
+    return d;
+}
+
+extern "C" int lelph_gpu_set_local_pseudo(lelph_gpu* h, const int* ngrid, const double* const* r_grid,
+                                          const double* const* rab_grid, const double* const* vloc_atomic,
+                                          const double* zval, int dimension, double qmax_abs)
+{
+    if (!h || !ngrid || !r_grid || !rab_grid || !vloc_atomic || !zval) return LELPH_GPU_ERR_INVALID;
+    if (dimension != '3' && dimension != '2') return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "dimension must be '3' or '2'");
+    if (h->ntype > LELPH_VLOC_MAXTYPE) return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "too many species");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const double* A = h->alat.data();
+    const double* B = h->blat.data();
+    const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                       A[2] * (A[3] * A[7] - A[4] * A[6]);
+    h->vl_volume = std::fabs(det);
+    // |G| range of the table: |q + G| <= b_max (1.7 (N_max + 4) + 3 |q|_max), spacing
+    // b_min capped at 0.01 (src/dvloc/vlocg_table.c:29-95)
+    double bmin = 1e300, bmax = 0;
+    int nmax = 0;
+    for (int i = 0; i < 3; ++i)
+    {
+        const double b = std::sqrt(B[i] * B[i] + B[3 + i] * B[3 + i] + B[6 + i] * B[6 + i]);
+        bmin = std::min(bmin, b);
+        bmax = std::max(bmax, b);
+        nmax = std::max(nmax, h->Nbox[i]);
+    }
+    if (bmin > 0.01) bmin = 0.01;
+    const double gmax = (1.7 * (nmax + 4.0) + 3 * std::fabs(qmax_abs)) * bmax;
+    const int npts = (int)std::ceil(gmax / bmin);
+    if (npts < 3) return fail(h, LELPH_GPU_ERR_INVALID, "V_loc table too short");
+    h->vl_npts = npts;
+    h->vl_dg = gmax / (npts - 1.0);
+    h->vl_dim2 = dimension == '2';
+    h->vl_zval.assign(zval, zval + h->ntype);
+    int rc = ensure(h, h->d_vl_v, sizeof(double) * (size_t)h->ntype * npts);
+    if (rc) return rc;
+    rc = ensure(h, h->d_vl_dv, sizeof(double) * (size_t)h->ntype * npts);
+    if (rc) return rc;
+    int ngmax = 0;
+    for (int t = 0; t < h->ntype; ++t)
+    {
+        if (ngrid[t] < 3 || !r_grid[t] || !rab_grid[t] || !vloc_atomic[t])
+            return fail(h, LELPH_GPU_ERR_INVALID, "radial mesh of a species");
+        ngmax = std::max(ngmax, ngrid[t]);
+    }
+    rc = ensure(h, h->d_vl_in, sizeof(double) * 3 * (size_t)ngmax);
+    if (rc) return rc;
+    std::vector<double> in(3 * (size_t)ngmax), table((size_t)h->ntype * npts), slopes((size_t)h->ntype * npts);
+    for (int t = 0; t < h->ntype; ++t)
+    {
+        const int n = ngrid[t];
+        // Simpson weights of the reference's rule (src/common/numerical_func.c:155-192)
+        // times the mesh derivative; the kernel divides the sum by 3
+        std::vector<double> w(n, 0.0);
+        w[0] = 1.0;
+        for (int i = 1; i < n - 1; i += 2) w[i] += 4.0;
+        for (int i = 2; i < n - 1; i += 2) w[i] += 2.0;
+        if (n % 2)
+            w[n - 1] += 1.0;
+        else
+        {
+            w[n - 3] -= 0.25;
+            w[n - 2] += 1.0;
+            w[n - 1] += 1.25;
+        }
+        for (int i = 0; i < n; ++i)
+        {
+            in[i] = r_grid[t][i];
+            in[ngmax + i] = w[i] * rab_grid[t][i];
+            in[2 * (size_t)ngmax + i] = vloc_atomic[t][i];
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_vl_in.p, in.data(), sizeof(double) * 3 * ngmax, cudaMemcpyHostToDevice,
+                                    h->st));
+        const double* din = (const double*)h->d_vl_in.p;
+        lelph_launch_vloc_table(din, din + ngmax, din + 2 * ngmax, n, zval[t], h->vl_volume, dimension == '3',
+                                h->vl_dg, npts, (double*)h->d_vl_v.p + (size_t)t * npts, h->st);
+        h->stats.kernel_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+        CUDA_TRY(h, cudaMemcpyAsync(table.data() + (size_t)t * npts, (double*)h->d_vl_v.p + (size_t)t * npts,
+                                    sizeof(double) * npts, cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    }
+    for (int t = 0; t < h->ntype; ++t)
+    {
+        std::vector<double> y(table.begin() + (size_t)t * npts, table.begin() + (size_t)(t + 1) * npts);
+        std::vector<double> d = spline_slopes(y, h->vl_dg);
+        std::copy(d.begin(), d.end(), slopes.begin() + (size_t)t * npts);
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_vl_dv.p, slopes.data(), sizeof(double) * slopes.size(), cudaMemcpyHostToDevice,
+                                h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    h->vl_ready = true;
+    return LELPH_GPU_OK;
+}
+
+// dV_loc (nmodes, N) of q into h->d_vloc (device, reference box)
+static int dvloc_device(lelph_gpu* h, const double qpt_crys[3], const double2* eig_dev)
+{
+    if (!h->vl_ready) return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_set_local_pseudo was not called");
+    const lelph_gpu_desc& d = h->d;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    int rc = ensure(h, h->d_vloc, sizeof(double2) * (size_t)d.nmodes * NN);
+    if (rc) return rc;
+    VlocDesc vd;
+    vd.Nx = h->Nbox[0];
+    vd.Ny = h->Nbox[1];
+    vd.Nz = h->Nbox[2];
+    vd.natom = d.natom;
+    vd.ntype = h->ntype;
+    vd.nmodes = d.nmodes;
+    vd.npts = h->vl_npts;
+    vd.dim2 = h->vl_dim2;
+    for (int x = 0; x < 3; ++x) vd.q[x] = qpt_crys[x];
+    for (int i = 0; i < 9; ++i) vd.blat[i] = h->blat[i];
+    vd.alat_zz = h->alat[8];
+    vd.dg = h->vl_dg;
+    vd.volume = h->vl_volume;
+    for (int t = 0; t < LELPH_VLOC_MAXTYPE; ++t) vd.zval[t] = t < h->ntype ? h->vl_zval[t] : 0.0;
+    vd.v = (const double*)h->d_vl_v.p;
+    vd.dv = (const double*)h->d_vl_dv.p;
+    vd.atom_pos = (const double*)h->d_apos.p;
+    vd.atom_type = (const int*)h->d_atype.p;
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+    if (lelph_launch_dvloc_g(vd, eig_dev, (double2*)h->d_vloc.p, (unsigned*)h->d_status.p, h->st))
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "too many species or modes for the local potential");
+    double2* v = (double2*)h->d_vloc.p;
+    // unnormalised inverse transform on the reference box (FFTW_BACKWARD)
+    lelph_launch_fft_contig_d(v, (long long)d.nmodes * h->Nbox[0] * h->Nbox[1], h->planN[2],
+                              (const double2*)h->d_twN[2].p, +1, h->st);
+    lelph_launch_fft_strided_d(v, (long long)d.nmodes * h->Nbox[0], h->Nbox[2], h->planN[1],
+                               (const double2*)h->d_twN[1].p, +1, h->st);
+    lelph_launch_fft_strided_d(v, (long long)d.nmodes, h->Nbox[1] * h->Nbox[2], h->planN[0],
+                               (const double2*)h->d_twN[0].p, +1, h->st);
+    h->stats.kernel_launches += 4;
+    CUDA_TRY(h, cudaGetLastError());
+    unsigned st = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    if (st) return fail(h, LELPH_GPU_ERR_GEOMETRY, "|q+G| beyond the V_loc table");
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_dvlocq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, double* Vlocr)
+{
+    if (!h || !qpt_crys || !eigVec || !Vlocr) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const lelph_gpu_desc& d = h->d;
+    int rc = ensure(h, h->d_tmp, std::max(h->d_tmp.n, sizeof(double2) * (size_t)d.nmodes * d.nmodes));
+    if (rc) return rc;
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, eigVec, sizeof(double2) * d.nmodes * d.nmodes, cudaMemcpyHostToDevice,
+                                h->st));
+    rc = dvloc_device(h, qpt_crys, (const double2*)h->d_tmp.p);
+    if (rc) return rc;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    CUDA_TRY(h, cudaMemcpyAsync(Vlocr, h->d_vloc.p, sizeof(double2) * (size_t)d.nmodes * NN, cudaMemcpyDeviceToHost,
+                                h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_set_q_induced(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                                       const double* dVscf_induced)
+{
+    if (!h) return LELPH_GPU_ERR_INVALID;
+    if (!h->vl_ready) return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_set_local_pseudo was not called");
+    int rc = set_q_common(h, slot, qpt_crys, eigVec, dVscf_induced);
+    if (rc) return rc;
+    const lelph_gpu_desc& d = h->d;
+    rc = dvloc_device(h, qpt_crys, (const double2*)h->d_eig.p + (size_t)slot * d.nmodes * d.nmodes);
+    if (rc) return rc;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    const size_t dvn = (size_t)d.nmodes * d.nmag * NN;
+    lelph_launch_add_dvscf((double2*)h->d_dvr.p + (size_t)slot * dvn, (const double2*)h->d_vloc.p, d.nmodes, d.nmag,
+                           NN, h->st);
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->windows_ok = false;
     return LELPH_GPU_OK;
 }

@@ -100,3 +100,27 @@ void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const
                          const float* partials, int nchunks, const float* mode_scale, const float* band_scale,
                          const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,
                          const GeomDev& g, int out_c64, void* gout, cudaStream_t st);
+
+// ---------------------------------------------------------- local bare potential
+#define LELPH_VLOC_MAXTYPE 16
+#define LELPH_VLOC_MAXMODES 48
+struct VlocDesc
+{
+    int Nx, Ny, Nz;             // the reference's FFT box
+    int natom, ntype, nmodes;
+    int npts;                   // |G| table points, spacing dg
+    int dim2;                   // 2-D Coulomb cutoff (slab along z)
+    double q[3];                // crystal coordinates
+    double blat[9];             // b_i = blat[:, i], 2 pi included
+    double alat_zz;             // alat_vec[2][2], the slab period used by the cutoff
+    double dg, volume;
+    double zval[LELPH_VLOC_MAXTYPE];
+    const double* v;            // (ntype, npts) V_loc(|G|)
+    const double* dv;           // (ntype, npts) spline slopes
+    const double* atom_pos;     // (natom, 3) cartesian
+    const int* atom_type;       // (natom)
+};
+void lelph_launch_vloc_table(const double* r, const double* wrab, const double* vloc, int ngrid, double zval,
+                             double volume, int cut3, double dg, int npts, double* out, cudaStream_t st);
+int lelph_launch_dvloc_g(const VlocDesc& vd, const double2* eig, double2* out, unsigned* status, cudaStream_t st);
+void lelph_launch_add_dvscf(double2* dv, const double2* vloc, int nmodes, int nmag, long long N, cudaStream_t st);

@@ -56,6 +56,7 @@ EXPORTS = [
     "lelph_gpu_run_device", "lelph_gpu_compute_elphq", "lelph_gpu_elph_q_rotate", "lelph_gpu_debug_gvec_map",
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
+    "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced",
 ]
 
 _lib = None
@@ -74,6 +75,10 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_set_wavefunctions.argtypes = [vp, C.POINTER(_dp)]
     L.lelph_gpu_prepare.argtypes = [vp]
     L.lelph_gpu_set_q.argtypes = [vp, C.c_int, _dp, _dp, _dp]
+    L.lelph_gpu_set_local_pseudo.argtypes = [vp, _ip, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _dp,
+                                             C.c_int, C.c_double]
+    L.lelph_gpu_dvlocq.argtypes = [vp, _dp, _dp, _dp]
+    L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device_noalloc.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
@@ -201,6 +206,43 @@ class LelphGPU:
         e = np.ascontiguousarray(eigVec, dtype=np.complex128)
         v = np.ascontiguousarray(dVscf, dtype=np.complex128)
         self._check(self._L.lelph_gpu_set_q(self.h, slot, _ptr(q), _ptr(e), _ptr(v)))
+
+    def set_local_pseudo(self, qmax_abs=None):
+        """Local pseudopotentials of the system's species (loc_r, loc_rab,
+        loc_v, loc_zval) -> the device V_loc(|G|) table.  qmax_abs defaults to
+        ceil(max |q_i|) + 1 over the system's q-points."""
+        s = self.sys
+        if qmax_abs is None:
+            qmax_abs = float(np.ceil(np.abs(np.asarray(s.qpts)).max()) + 1)
+        keep = [[np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+                for arrs in (s.loc_r, s.loc_rab, s.loc_v)]
+        self._keep_vloc = keep
+        ngrid = np.array([len(r) for r in keep[0]], dtype=np.int32)
+        tabs = [(_dp * s.ntype)(*[_ptr(a) for a in arrs]) for arrs in keep]
+        z = np.ascontiguousarray(s.loc_zval, dtype=np.float64)
+        self._check(self._L.lelph_gpu_set_local_pseudo(self.h, _ptr(ngrid, _ip), tabs[0], tabs[1], tabs[2], _ptr(z),
+                                                       ord(s.dimension), qmax_abs))
+
+    def dvlocq(self, qpt, eigVec):
+        """dVlocq: (nmodes, Nx, Ny, Nz) complex on the reference box."""
+        s = self.sys
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        out = np.empty((s.nmodes, *s.fft_dims), dtype=np.complex128)
+        self._check(self._L.lelph_gpu_dvlocq(self.h, _ptr(q), _ptr(e), _ptr(out)))
+        return out
+
+    def set_q_induced(self, slot, qpt, eigVec, dVscf_induced=None):
+        """Load a q slot from the induced dV (None: the bare kernels); the
+        local bare potential is added on the device."""
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        if dVscf_induced is None:
+            vp = None
+        else:
+            v = np.ascontiguousarray(dVscf_induced, dtype=np.complex128)
+            vp = _ptr(v)
+        self._check(self._L.lelph_gpu_set_q_induced(self.h, slot, _ptr(q), _ptr(e), vp))
 
     def run(self, qslots, kbz, non_loc=True, kminusq=False, out=OUT_C128, g_out=None):
         qs = np.ascontiguousarray(qslots, dtype=np.int32)
