@@ -173,6 +173,16 @@ int lelph_gpu_dvlocq(lelph_gpu* h, const double qpt_crys[3], const double* eigVe
 int lelph_gpu_set_q_induced(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
                             const double* dVscf_induced);
 
+/* rotate_dvscf (src/symmetries/rotate_dvscf.c:22-368): dV_scf of S q from
+ * dV_scf of q for the symmetry (Rmat cartesian row-major, tau cartesian,
+ * time_rev) -- the box permutation S^-1 (r - tau), the phase e^{-i (Sq).tau},
+ * the SU(2) rotation of the spin part for nmag = 4 (composite_form: inputs
+ * already [V+Bz, Bx-iBy, Bx+iBy, V-Bz]) and the conjugate for time reversal.
+ * dvscf_in, dvscf_out: (nmodes, nmag, Nx, Ny, Nz) complex on the reference box.
+ * LELPH_GPU_ERR_GEOMETRY if the operation does not map the FFT grid onto itself. */
+int lelph_gpu_rotate_dvscf(lelph_gpu* h, const double qpt_crys[3], const double Rmat[9], const double tau[3],
+                           int time_rev, int composite_form, const double* dvscf_in, double* dvscf_out);
+
 /* compute_and_write_elphq for one iBZ q without the netCDF writes: every
  * full-BZ k, output (nkpts_BZ, nmodes, nspin, nbnds, nbnds) complex double. */
 int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, const double* dVscfq,

@@ -1150,6 +1150,78 @@ extern "C" int lelph_gpu_set_q(lelph_gpu* h, int slot, const double qpt_crys[3],
     return set_q_common(h, slot, qpt_crys, eigVec, dVscf);
 }
 
+// ------------------------------------------------------------ dV rotation
+
+extern "C" int lelph_gpu_rotate_dvscf(lelph_gpu* h, const double qpt_crys[3], const double Rmat[9],
+                                      const double tau[3], int time_rev, int composite_form, const double* dvscf_in,
+                                      double* dvscf_out)
+{
+    if (!h || !qpt_crys || !Rmat || !tau || !dvscf_in || !dvscf_out) return LELPH_GPU_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const lelph_gpu_desc& d = h->d;
+    RotDvDesc rd;
+    rd.Nx = h->Nbox[0];
+    rd.Ny = h->Nbox[1];
+    rd.Nz = h->Nbox[2];
+    rd.nmodes = d.nmodes;
+    rd.nmag = d.nmag;
+    rd.trev = time_rev != 0;
+    rd.composite = composite_form != 0;
+    // box coordinates of S^-1 (r - tau): tau_red = blat^T tau / 2pi and
+    // sym_red = blat^T (R^T alat) / 2pi, both negated for time reversal
+    // (src/symmetries/rotate_dvscf.c:118-143)
+    const double* A = h->alat.data();
+    const double* B = h->blat.data();
+    mat_vec3(B, tau, true, rd.tau_red);
+    double tmp[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+        {
+            double v = 0;
+            for (int k = 0; k < 3; ++k) v += Rmat[3 * k + i] * A[3 * k + j];
+            tmp[3 * i + j] = v / (2 * PI_T);
+        }
+    for (int i = 0; i < 3; ++i)
+    {
+        rd.tau_red[i] /= (2 * PI_T);
+        if (rd.trev) rd.tau_red[i] = -rd.tau_red[i];
+    }
+    if (rd.trev)
+        for (double& v : tmp) v = -v;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+        {
+            double v = 0;
+            for (int k = 0; k < 3; ++k) v += B[3 * k + i] * tmp[3 * k + j];
+            rd.sym_red[3 * i + j] = v;
+        }
+    double qc[3], Rq[3];
+    mat_vec3(B, qpt_crys, false, qc);
+    mat_vec3(Rmat, qc, false, Rq);
+    const double ang = Rq[0] * tau[0] + Rq[1] * tau[1] + Rq[2] * tau[2];
+    rd.ph = make_double2(std::cos(ang), -std::sin(ang));
+    std::complex<double> u[4];
+    if (!su2mat(Rmat, d.nspinor, rd.trev, u)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "improper symmetry matrix");
+    for (int i = 0; i < 4; ++i) rd.su2[i] = make_double2(u[i].real(), u[i].imag());
+    const long long NN = (long long)rd.Nx * rd.Ny * rd.Nz;
+    const size_t n = (size_t)d.nmodes * d.nmag * NN;
+    int rc = ensure(h, h->d_wtmpN, std::max(h->d_wtmpN.n, sizeof(double2) * 2 * n));
+    if (rc) return rc;
+    double2* din = (double2*)h->d_wtmpN.p;
+    double2* dout = din + n;
+    CUDA_TRY(h, cudaMemcpyAsync(din, dvscf_in, sizeof(double2) * n, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+    lelph_launch_rotate_dvscf(rd, din, dout, (unsigned*)h->d_status.p, h->st);
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    unsigned st = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&st, h->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dvscf_out, dout, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    if (st) return fail(h, LELPH_GPU_ERR_GEOMETRY, "symmetry operation is incompatible with the FFT grid");
+    return LELPH_GPU_OK;
+}
+
 // ------------------------------------------------------ local bare potential
 
 // Slopes of the not-a-knot cubic spline through (i*dg, y_i): the usual

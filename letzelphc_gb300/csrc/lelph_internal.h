@@ -124,3 +124,16 @@ void lelph_launch_vloc_table(const double* r, const double* wrab, const double* 
                              double volume, int cut3, double dg, int npts, double* out, cudaStream_t st);
 int lelph_launch_dvloc_g(const VlocDesc& vd, const double2* eig, double2* out, unsigned* status, cudaStream_t st);
 void lelph_launch_add_dvscf(double2* dv, const double2* vloc, int nmodes, int nmag, long long N, cudaStream_t st);
+
+// ------------------------------------------------------------ dV rotation
+struct RotDvDesc
+{
+    int Nx, Ny, Nz, nmodes, nmag;
+    int trev, composite;
+    double sym_red[9];   // crystal action on box coordinates (rows), sign of time reversal included
+    double tau_red[3];   // fractional translation in box (crystal) units
+    double2 ph;          // e^{-i (S q).tau}
+    double2 su2[4];      // SU(2) matrix of the operation (nmag = 4)
+};
+void lelph_launch_rotate_dvscf(const RotDvDesc& rd, const double2* in, double2* out, unsigned* status,
+                               cudaStream_t st);

@@ -56,7 +56,7 @@ EXPORTS = [
     "lelph_gpu_run_device", "lelph_gpu_compute_elphq", "lelph_gpu_elph_q_rotate", "lelph_gpu_debug_gvec_map",
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
-    "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced",
+    "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
 ]
 
 _lib = None
@@ -79,6 +79,7 @@ def load_library(path: str = LIB_PATH):
                                              C.c_int, C.c_double]
     L.lelph_gpu_dvlocq.argtypes = [vp, _dp, _dp, _dp]
     L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
+    L.lelph_gpu_rotate_dvscf.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device_noalloc.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
@@ -243,6 +244,18 @@ class LelphGPU:
             v = np.ascontiguousarray(dVscf_induced, dtype=np.complex128)
             vp = _ptr(v)
         self._check(self._L.lelph_gpu_set_q_induced(self.h, slot, _ptr(q), _ptr(e), vp))
+
+    def rotate_dvscf(self, qpt, R, tau, time_rev, composite, dv_in):
+        """rotate_dvscf on the device: dV of S q, same shape as dv_in
+        (nmodes, nmag, Nx, Ny, Nz)."""
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        Rm = np.ascontiguousarray(R, dtype=np.float64)
+        t = np.ascontiguousarray(tau, dtype=np.float64)
+        v = np.ascontiguousarray(dv_in, dtype=np.complex128)
+        out = np.empty_like(v)
+        self._check(self._L.lelph_gpu_rotate_dvscf(self.h, _ptr(q), _ptr(Rm), _ptr(t), int(time_rev), int(composite),
+                                                   _ptr(v), _ptr(out)))
+        return out
 
     def run(self, qslots, kbz, non_loc=True, kminusq=False, out=OUT_C128, g_out=None):
         qs = np.ascontiguousarray(qslots, dtype=np.int32)

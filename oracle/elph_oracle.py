@@ -592,3 +592,64 @@ def add_dvscf_qe(dv, vloc, nmag):
         out[:, 2] = Bx + 1j * By
         out[:, 3] = V - Bz
     return out
+
+
+# ------------------------------------------------------ dV rotation (star of q)
+
+def rotate_dvscf_index(s, R, tau, trev):
+    """FFT-box permutation of rotate_dvscf (src/symmetries/rotate_dvscf.c:118-205):
+    point i of the output takes point rot_idx[i] of the input.  Raises if the
+    operation does not map the FFT grid onto itself."""
+    blat = np.asarray(s.blat, float)
+    alat = np.asarray(s.alat, float)
+    tau_red = blat.T @ np.asarray(tau, float) / (2 * ELPH_PI)
+    tmp = np.asarray(R, float).T @ alat / (2 * ELPH_PI)
+    if trev:
+        tau_red = -tau_red
+        tmp = -tmp
+    sym_red = blat.T @ tmp
+    N = np.array(s.fft_dims)
+    ii = np.stack(np.meshgrid(*[np.arange(n) for n in N], indexing="ij"), -1).reshape(-1, 3).astype(float)
+    t = ii / N - tau_red
+    x = t @ sym_red.T
+    x = x - np.floor(x)
+    x = x - np.floor(x + ELPH_EPS)
+    x = x - ELPH_EPS
+    x = x * N
+    diff = x - np.rint(x)
+    if np.any(np.abs(diff) > 1e-3 + 5e-5 * np.abs(x)):
+        raise ValueError("Symmetry operation is incompatible with FFT grid.")
+    r = np.rint(x).astype(np.int64)
+    return (r[:, 0] * N[1] + r[:, 1]) * N[2] + r[:, 2]
+
+
+def rotate_dvscf(s, qpt, dv_in, R, tau, trev, composite):
+    """dV_scf of S q from dV_scf of q, (nmodes, nmag, Nx, Ny, Nz)
+    (rotate_dvscf, src/symmetries/rotate_dvscf.c:22-368): permutation of the
+    box, phase e^{-i (S q).tau}, for nmag = 4 the spin rotation
+    U (V + B.sigma) U^dagger (inputs in the [V, Bx, By, Bz] form unless
+    `composite`), complex conjugate for time-reversed operations."""
+    idx = rotate_dvscf_index(s, R, tau, trev)
+    qc = np.asarray(s.blat, float) @ np.asarray(qpt, float)
+    Rq = np.asarray(R, float) @ qc
+    ph = np.exp(-1j * float(Rq @ np.asarray(tau, float)))
+    nm, nmag = dv_in.shape[:2]
+    flat = dv_in.reshape(nm, nmag, -1)
+    out = ph * flat[:, :, idx]
+    if nmag == 4:
+        u = su2mat(R, s.nspinor, False, trev)
+        d0, d1, d2, d3 = (out[:, i].copy() for i in range(4))
+        if not composite:
+            d0, d1, d2, d3 = d0 + d3, d1 - 1j * d2, d1 + 1j * d2, d0 - d3
+        cu = np.conj(u)
+        m0 = u[0] * (d0 * cu[0] + d1 * cu[1]) + u[1] * (d2 * cu[0] + d3 * cu[1])
+        m1 = u[0] * (d0 * cu[2] + d1 * cu[3]) + u[1] * (d2 * cu[2] + d3 * cu[3])
+        m2 = u[2] * (d0 * cu[0] + d1 * cu[1]) + u[3] * (d2 * cu[0] + d3 * cu[1])
+        m3 = u[2] * (d0 * cu[2] + d1 * cu[3]) + u[3] * (d2 * cu[2] + d3 * cu[3])
+        if composite:
+            out = np.stack([m0, m1, m2, m3], 1)
+        else:
+            out = np.stack([(m0 + m3) / 2, (m1 + m2) / 2, -1j * (m2 - m1) / 2, (m0 - m3) / 2], 1)
+    if trev:
+        out = np.conj(out)
+    return out.reshape(dv_in.shape)

@@ -10,6 +10,7 @@
  *
  * usage: lelph_ref <system.bin> <g_out.bin> [rotate <D_in.bin> <g_rot_out.bin>]
  *        lelph_ref <system.bin> <g_out.bin> dvloc <v_out.bin>
+ *        lelph_ref <system.bin> <unused> rotdv <spec.bin> <dv_out.bin>
  *
  * dvloc: the system's dVscf records are the induced part (QE's dvscf); the
  * harness builds the V_loc table (create_vlocg_table, src/dvloc/vlocg_table.c)
@@ -18,6 +19,10 @@
  * does (src/elph/elph_driver.c:234-252) before compute_and_write_elphq.
  * v_out.bin receives, per q, Vlocr (nmodes, nfft) then the summed dV
  * (nmodes, nmag, nfft), complex128.
+ *
+ * rotdv: rotate_dvscf (src/symmetries/rotate_dvscf.c:22) of the spec's dV
+ * (records rq, rR, rtau, rtrev, rcomp, rdv) on the system's lattice; the
+ * matrix elements are not computed.
  *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
@@ -247,6 +252,25 @@ int main(int argc, char** argv)
     comm.nqpools = comm.nkpools = 1;
     comm.commW_size = comm.commQ_size = comm.commK_size = comm.commR_size = comm.commRq_size = 1;
 
+    if (argc >= 6 && !strcmp(argv[3], "rotdv"))
+    {
+        nrec = 0;
+        load(argv[4]);
+        struct symmetry sy;
+        memset(&sy, 0, sizeof(sy));
+        memcpy(sy.Rmat, get("rR", 1)->data, 9 * sizeof(double));
+        memcpy(sy.tau, get("rtau", 1)->data, 3 * sizeof(double));
+        sy.time_rev = ((const int*)get("rtrev", 1)->data)[0] != 0;
+        const int comp = ((const int*)get("rcomp", 1)->data)[0];
+        struct rec* din = get("rdv", 1);
+        double _Complex* out = malloc(din->nbytes);
+        rotate_dvscf(get("rq", 1)->data, din->data, &sy, &lat, comp != 0, out, comm.commK);
+        FILE* fr = fopen(argv[5], "wb");
+        if (!fr) die("cannot write rotdv output");
+        fwrite(out, 1, din->nbytes, fr);
+        fclose(fr);
+        return 0;
+    }
     g_slice = (size_t)nmodes * nspin * nbnds * nbnds;
     g_nk = (size_t)nkbz;
     g_all = calloc((size_t)nq * g_nk * g_slice, sizeof(double _Complex));

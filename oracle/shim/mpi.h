@@ -34,6 +34,13 @@ typedef int MPI_Op;
 #define MPI_LOR ((MPI_Op)4)
 #define MPI_LAND ((MPI_Op)5)
 
+typedef long MPI_Aint;
+/* derived datatypes (vector, resized) get negative handles */
+int MPI_Type_vector(int count, int blocklength, int stride, MPI_Datatype oldtype, MPI_Datatype* newtype);
+int MPI_Type_create_resized(MPI_Datatype oldtype, MPI_Aint lb, MPI_Aint extent, MPI_Datatype* newtype);
+int MPI_Type_commit(MPI_Datatype* datatype);
+int MPI_Type_free(MPI_Datatype* datatype);
+
 int MPI_Init(int* argc, char*** argv);
 int MPI_Finalize(void);
 int MPI_Comm_size(MPI_Comm comm, int* size);

@@ -92,6 +92,63 @@ def run_dvloc(name, base, ov, kmq, nl, tmp):
     print(name, g.shape, float(np.abs(g).max()), float(np.abs(vloc).max()))
 
 
+# rotate_dvscf (src/symmetries/rotate_dvscf.c:22) cases:
+# name -> (base config, overrides, symmetry index, time-reversal override, composite form)
+ROTDV_SYS = {
+    "c0": ("c0", {"kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}),
+    "soc": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True, "ls": (0, 1, 2),
+                   "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (2, 2, 2), "qpts": [(0.5, 0.5, 0)]}),
+}
+ROTDV_CASES = [("c0", 5, None, 0), ("c0", 24, None, 0), ("c0", 47, None, 0), ("c0", 7, 1, 0),
+               ("soc", 3, None, 0), ("soc", 11, None, 1), ("soc", 47, None, 0), ("soc", 47, None, 1)]
+
+
+def rotdv_fixture(tmp):
+    """Outputs of the reference's rotate_dvscf and the box permutation it used,
+    recovered exactly from its output (the inputs are distinct random values)."""
+    rec = {}
+    for sysname, isym, trev_ov, comp in ROTDV_CASES:
+        base, ov = ROTDV_SYS[sysname]
+        s = synth.make_system(base, dict(ov))
+        sysf = os.path.join(tmp, "rot_" + sysname + ".bin")
+        synth.write_system(s, sysf)
+        R, tau = s.sym_R[isym], s.sym_tau[isym]
+        trev = int(s.sym_trev[isym]) if trev_ov is None else trev_ov
+        dv = s.dVscf[0]
+        spec = os.path.join(tmp, "rotspec.bin")
+        with open(spec, "wb") as f:
+            f.write(b"LELPHSYS")
+            synth._rec(f, "rq", np.asarray(s.qpts[0], float))
+            synth._rec(f, "rR", np.asarray(R, float))
+            synth._rec(f, "rtau", np.asarray(tau, float))
+            synth._rec(f, "rtrev", np.array([trev], np.int32))
+            synth._rec(f, "rcomp", np.array([comp], np.int32))
+            synth._rec(f, "rdv", dv)
+            f.write(b"END\0" + b"\0" * 28)
+        out_f = os.path.join(tmp, "rotout.bin")
+        subprocess.run([REF, sysf, os.path.join(tmp, "unused.bin"), "rotdv", spec, out_f], check=True)
+        out = np.fromfile(out_f, np.complex128).reshape(dv.shape)
+        key = f"{sysname}_{isym}_{trev}_{comp}"
+        if s.nmag == 1:
+            # output point i holds ph * in[idx[i]] (conjugated when time-reversed)
+            a = out[0, 0].reshape(-1)
+            a = np.conj(a) if trev else a
+            b = dv[0, 0].reshape(-1)
+            # the phase has modulus 1: match by modulus, then check one common phase
+            lookup = {round(float(abs(v)), 11): j for j, v in enumerate(b)}
+            assert len(lookup) == len(b)
+            idx = np.array([lookup[round(float(abs(v)), 11)] for v in a], np.int32)
+            ratio = a / b[idx]
+            assert np.abs(ratio - ratio[0]).max() < 1e-12 and abs(abs(ratio[0]) - 1) < 1e-12
+            rec[key + "_idx"] = idx
+        rec[key + "_sample"] = out.reshape(-1)[::97]
+        rec[key + "_norm"] = np.array(np.linalg.norm(out))
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "rotate_dvscf.npz"),
+                        cases=np.array(json.dumps([list(c) for c in ROTDV_CASES])),
+                        systems=np.array(json.dumps(ROTDV_SYS)), **rec)
+    print("rotate_dvscf", len(ROTDV_CASES))
+
+
 def rotate_fixture(tmp):
     s = synth.make_system("c0", {"nbnds": 5})
     rng = np.random.default_rng(7)
@@ -126,3 +183,4 @@ if __name__ == "__main__":
         for name, (base, ov, kmq, nl) in GOLDEN_DVLOC.items():
             run_dvloc(name, base, ov, kmq, nl, tmp)
         rotate_fixture(tmp)
+        rotdv_fixture(tmp)

@@ -53,3 +53,35 @@ def test_synthetic_generator_shapes():
     for i, (ik, isym) in enumerate(s.kmap):
         k = s.alat.T @ (s.sym_R[isym] @ s.kibz[ik])
         assert np.allclose(k, s.kbz_crys[i])
+
+
+def _rotdv_cases():
+    import json
+    import os
+    from golden_util import GOLDEN_DIR
+    z = np.load(os.path.join(GOLDEN_DIR, "rotate_dvscf.npz"))
+    return z, json.loads(str(z["cases"])), json.loads(str(z["systems"]))
+
+
+def rotdv_system(systems, name):
+    from letzelphc_gb300 import synth
+    base, ov = systems[name]
+    ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls") else v) for k, v in ov.items()}
+    return synth.make_system(base, ov)
+
+
+def test_rotate_dvscf_matches_reference():
+    """Box permutation bit-exact, rotated dV to 1e-12 (src/symmetries/rotate_dvscf.c)."""
+    z, cases, systems = _rotdv_cases()
+    cache = {}
+    for sysname, isym, trev_ov, comp in cases:
+        s = cache.setdefault(sysname, rotdv_system(systems, sysname))
+        trev = int(s.sym_trev[isym]) if trev_ov is None else trev_ov
+        key = f"{sysname}_{isym}_{trev}_{comp}"
+        if key + "_idx" in z.files:
+            idx = O.rotate_dvscf_index(s, s.sym_R[isym], s.sym_tau[isym], trev)
+            assert np.array_equal(idx, z[key + "_idx"]), key
+        out = O.rotate_dvscf(s, s.qpts[0], s.dVscf[0], s.sym_R[isym], s.sym_tau[isym], trev, comp)
+        smp = z[key + "_sample"]
+        assert np.abs(out.reshape(-1)[::97] - smp).max() < 1e-12 * np.abs(smp).max(), key
+        assert abs(np.linalg.norm(out) - float(z[key + "_norm"])) < 1e-12 * float(z[key + "_norm"])
