@@ -632,6 +632,18 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->g.nmag = d.nmag;
     h->g.nmodes = d.nmodes;
     h->g.mt_modes = std::min(d.nmodes, std::max(1, 128 / d.nbnds));
+    // 64-point pipeline stages when three stages and two A slots fit, else 32
+    h->g.kpts = 64;
+    if (!lelph_local_tc_supported(h->g)) h->g.kpts = 32;
+    {
+        GeomDev g3 = h->g;
+        if (h->g.kpts == 64 && lelph_local_tc_smem_bytes(g3) > 0)
+        {
+            // a 64-point ring shallower than three stages loses to 32-point stages
+            g3.kpts = 64;
+            if (lelph_local_tc_stages(g3) < 3) h->g.kpts = 32;
+        }
+    }
     if (h->mixed && (2 * h->g.nbp > 128 || !lelph_local_tc_supported(h->g)))
         return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
     h->ntype = d.ntype;
@@ -805,7 +817,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                 for (int c : cand[2])
                 {
                     long long p = (long long)a * b * c;
-                    if (h->mixed && p % TC_KPTS_HOST != 0) continue;
+                    if (h->mixed && p % 32 != 0) continue;
                     if (best < 0 || p < best)
                     {
                         best = p;
@@ -825,7 +837,11 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     const long long N = (long long)h->g.Nx * h->g.Ny * h->g.Nz;
     if (h->mixed)
     {
-        if (N % TC_KPTS_HOST != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
+        if (N % 32 != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
+        if (N % h->g.kpts != 0) h->g.kpts = 32;
+        // override for tests and tuning: LELPH_TC_STAGE = 32 forces 32-point stages
+        if (const char* e = getenv("LELPH_TC_STAGE"))
+            if (atoi(e) == 32) h->g.kpts = 32;
         if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
     }
     // chat offsets per full-BZ k
@@ -936,26 +952,29 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                         2 * h->g.nbp, 1, true);
         if (rc) return bad(rc, h->err);
         // FP32 psi(r) of the k role, tile-major: blocks (k, spin, 16-point block) of nbp rows x 32 floats,
-        // two blocks (one 32-point stage) per box, 128-byte swizzled
+        // four blocks (one 64-point stage) per box, 128-byte swizzled
         const size_t prow = (size_t)d.nkpts_BZ * d.nspin * h->g.nbp;
         rc = ensure(h, h->d_psi32, sizeof(float) * Kr * prow);
         if (rc) return bad(rc, h->err);
         if (cudaMemsetAsync(h->d_psi32.p, 0, h->d_psi32.n, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
         rc = make_tmap3(h, &h->tmapP, h->d_psi32.p, true, 32, h->g.nbp, (size_t)d.nkpts_BZ * d.nspin * (Kr / 32),
-                        h->g.nbp, 2, true);
+                        h->g.nbp, (unsigned)(h->g.kpts / 16), true);
         if (rc) return bad(rc, h->err);
-        // K chunk per CTA: a multiple of 32 grid points dividing nspinor*N, near 4096
+        // K chunk per work unit: a multiple of the stage dividing N (so a chunk stays
+        // within one spinor component), as large as possible up to 8192 points: each
+        // chunk's FP32 sum is one FP64 term of the finish kernel
+        const int kp = h->g.kpts;
         long long Ktot = (long long)d.nspinor * N;
-        long long units = N / TC_KPTS_HOST;  // chunks divide N so a chunk stays within one spinor component
+        long long units = N / kp;
         long long best = 1;
         for (long long c = 1; c <= units; ++c)
-            if (units % c == 0 && c * TC_KPTS_HOST <= 4096) best = c;
-        h->chunk_pts = (int)(best * TC_KPTS_HOST);
-        // tuning override: LELPH_TC_CHUNK = grid points per K chunk (multiple of 32 dividing nspinor*N)
+            if (units % c == 0 && c * kp <= 8192) best = c;
+        h->chunk_pts = (int)(best * kp);
+        // tuning override: LELPH_TC_CHUNK = grid points per K chunk (multiple of the stage dividing N)
         if (const char* e = getenv("LELPH_TC_CHUNK"))
         {
             long long c = atoll(e);
-            if (c > 0 && c % TC_KPTS_HOST == 0 && N % c == 0) h->chunk_pts = (int)c;
+            if (c > 0 && c % kp == 0 && N % c == 0) h->chunk_pts = (int)c;
         }
         h->nchunks = (int)(Ktot / h->chunk_pts);
     }
@@ -1608,7 +1627,8 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         // dV windows, tile-major: blocks (window, 32-point block) of (mode, component) rows x 64 floats
         const long long M = (long long)g.Nx * g.Ny * g.Nz;
         rc = make_tmap3(h, &h->tmapV, h->d_win32.p, true, 64, (unsigned long long)d.nmodes * d.nmag,
-                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag), 1, false);
+                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag),
+                        (unsigned)(g.kpts / 32), false);
         if (rc) return rc;
         h->tmapV_base = h->d_win32.p;
         h->tmapV_rows = h->nwin;
@@ -1811,7 +1831,8 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
     {
         const long long M = (long long)g.Nx * g.Ny * g.Nz;
         rc = make_tmap3(h, &h->tmapV, h->d_win32.p, true, 64, (unsigned long long)d.nmodes * d.nmag,
-                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag), 1, false);
+                        (unsigned long long)h->nwin * (M / 32), (unsigned)(g.mt_modes * d.nmag),
+                        (unsigned)(g.kpts / 32), false);
         if (rc) return rc;
         h->tmapV_base = h->d_win32.p;
         h->tmapV_rows = h->nwin;

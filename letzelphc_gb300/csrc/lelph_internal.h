@@ -5,7 +5,7 @@
 #include <stdint.h>
 
 #define LELPH_MAX_RADIX_STAGES 12
-#define TC_KPTS_HOST 32  // grid points per pipeline stage of the tensor-core sandwich
+#define TC_KPTS_MAX 64  // largest pipeline stage of the tensor-core sandwich (grid points)
 
 // One 1-D transform length L = prod(radix[0..nstage)), radices in {2,3,4,5}.
 struct FftPlan1D
@@ -45,6 +45,7 @@ struct GeomDev
     int Nx, Ny, Nz;
     int nspin, nspinor, nbnds, nbp, nmag, nmodes;
     int mt_modes;  // whole modes per 128-row tile of the tensor-core sandwich: min(nmodes, max(1, 128/nbnds))
+    int kpts;      // grid points per pipeline stage of the tensor-core sandwich (64, or 32 for wide tiles)
 };
 
 // FFT (fft_gather.cu)
@@ -75,6 +76,7 @@ void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const lo
 void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* psi, const double2* dV,
                              const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st);
 int lelph_local_tc_smem_bytes(const GeomDev& g);
+int lelph_local_tc_stages(const GeomDev& g);
 int lelph_local_tc_tile_modes(const GeomDev& g);
 int lelph_local_tc_supported(const GeomDev& g);
 void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapP,

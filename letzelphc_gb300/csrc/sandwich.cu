@@ -155,9 +155,9 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 // MMAs, warps 2-9 build the A operand directly in tensor memory, warps
 // 10.. drain the accumulators.
 //
-// Tensor memory (512 columns): NACC (4, or 2 for wide tiles) accumulators of
-// NT = 2*nbp columns, then NA A-operand slots of 64 columns (A_hi: 32 columns, A_lo: 32 columns; one
-// column holds the (Re, Im) 16-bit pair of one grid point, lane = row).
+// Tensor memory (512 columns): NACC (4, or 2 for wide tiles) accumulators,
+// then NA A-operand slots of 128 columns (A_hi: 64 columns, A_lo: 64 columns;
+// one column holds the (Re, Im) 16-bit pair of one grid point, lane = row).
 // Shared memory holds only TMA tiles, so the TMA ring is up to 8 stages deep:
 // per stage B (k+q split rows, 128-byte swizzle), the FP32 psi_k tile (two
 // 16-point halves, 128-byte swizzle) and the FP32 dV tile of the tile's modes.
@@ -166,14 +166,15 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 #define TC_NA_MAX 6
 #define TC_NACC_MAX 4
 #define TC_SMEM_LIMIT (227 * 1024)
-#define TC_KPTS 32  // complex grid points per pipeline stage (64 16-bit K elements = 128 B rows)
-#define TC_GROUP 2         // pipeline stages chained into one TMEM accumulator before it is drained
+// A pipeline stage is KP grid points (KP/32 K atoms of 128 bytes); one TMEM
+// accumulator chains 64 points (two 32-point stages or one 64-point stage)
+// before it is drained.
 #define TC_MAX_THREADS 576 // 10 role warps + up to 8 drain warps
 
 struct TcSmemLayout
 {
-    uint32_t b_hi, b_lo, p, dv;               // offsets of stage 0
-    uint32_t b_bytes, p_half, p_bytes, dv_bytes;
+    uint32_t b_hi, b_lo, p, dv;               // offsets of stage 0 (B: K atom 0; atom j at + j * b_atom)
+    uint32_t b_bytes, b_atom, p_half, p_bytes, dv_bytes, dv_block;
     uint32_t stage_bytes;
     uint32_t nst, na, nacc, accw, merged, a_col0;
     uint32_t bar_off, total;
@@ -187,13 +188,18 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     TcSmemLayout L;
     const uint32_t NT = 2 * g.nbp;
     const uint32_t nsp = (g.nmag == 4) ? 2 : 1;
+    // B per K atom (32 points): NT hi rows then NT lo rows, 128 B each, so the
+    // merged N = 2 NT operand of an atom is one contiguous K-major tile
     L.b_bytes = NT * 128;
+    L.b_atom = 2 * L.b_bytes;
     L.p_half = g.nbp * 128;  // 16 points x 8 B per band row
-    L.p_bytes = nsp * 2 * L.p_half;
-    L.dv_bytes = tc_tile_modes(g) * g.nmag * TC_KPTS * 8;
+    const uint32_t natom = (uint32_t)g.kpts / 32;
+    L.p_bytes = nsp * (2 * natom) * L.p_half;
+    L.dv_block = tc_tile_modes(g) * g.nmag * 32 * 8;  // rows (mode, component) x 32 points
+    L.dv_bytes = natom * L.dv_block;
     L.b_hi = 0;
     L.b_lo = L.b_hi + L.b_bytes;
-    L.p = L.b_lo + L.b_bytes;
+    L.p = natom * L.b_atom;
     L.dv = L.p + L.p_bytes;
     L.stage_bytes = (L.dv + L.dv_bytes + 1023) / 1024 * 1024;
     L.nst = (TC_SMEM_LIMIT - 2048) / L.stage_bytes;
@@ -207,7 +213,7 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     L.accw = L.merged ? 2 * NT : NT;
     L.nacc = (4 * L.accw + 4 * 64 <= 512) ? 4 : 2;
     L.a_col0 = L.nacc * L.accw;
-    L.na = (512 - L.a_col0) / 64;
+    L.na = (512 - L.a_col0) / (2 * (uint32_t)g.kpts);
     if (L.na > TC_NA_MAX) L.na = TC_NA_MAX;
     L.bar_off = L.nst * L.stage_bytes;
     L.total = L.bar_off + 512 + 1024;  // barriers + alignment slack
@@ -215,11 +221,12 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
 }
 
 int lelph_local_tc_smem_bytes(const GeomDev& g) { return (int)tc_layout(g).total; }
+int lelph_local_tc_stages(const GeomDev& g) { return (int)tc_layout(g).nst; }
 int lelph_local_tc_tile_modes(const GeomDev& g) { return tc_tile_modes(g); }
 int lelph_local_tc_supported(const GeomDev& g)
 {
     const TcSmemLayout L = tc_layout(g);
-    return (2 * g.nbp <= 128) && L.nst >= 2 && L.na >= 2 && L.a_col0 + L.na * 64 <= 512;
+    return (2 * g.nbp <= 128) && L.nst >= 2 && L.na >= 2 && L.a_col0 + L.na * 2 * (uint32_t)g.kpts <= 512;
 }
 
 // (hi, lo) 16-bit split of a complex value: hi = rn(v), lo = rn(v - hi)
@@ -314,7 +321,7 @@ __device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int ns
     return w;
 }
 
-template <int BF16>
+template <int BF16, int KP>
 __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
@@ -337,7 +344,9 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int NT = 2 * gd.nbp;
     const long long N = (long long)gd.Nx * gd.Ny * gd.Nz;
-    const int nstage = chunk_pts / TC_KPTS;
+    constexpr int TC_GROUP = 64 / KP;
+    constexpr int NATOM = KP / 32;
+    const int nstage = chunk_pts / KP;
     const int ngroup = (nstage + TC_GROUP - 1) / TC_GROUP;
     const int nsp = (gd.nmag == 4) ? 2 : 1;
     const int ndrain = 4 * ((NT + 63) / 64);
@@ -376,7 +385,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             prefetch_tmap(&tmapP);
             prefetch_tmap(&tmapV);
             const int nkb = (int)((long long)gd.nspinor * N / 32);  // 32-point K blocks per row group
-            const uint32_t bytes = 2 * L.b_bytes + L.p_bytes + L.dv_bytes;
+            const uint32_t bytes = NATOM * L.b_atom + L.p_bytes + L.dv_bytes;
             // ring positions advance incrementally: no runtime divisions on the issue paths
             int s = 0;
             uint32_t ph = 0;
@@ -410,19 +419,23 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                         break;
                     }
                     uint8_t* st = sm + s * L.stage_bytes;
-                    const long long kc = kc0 + (long long)it * TC_KPTS;
-                    const long long r0 = r00 + (long long)it * TC_KPTS;
+                    const long long kc = kc0 + (long long)it * KP;
+                    const long long r0 = r00 + (long long)it * KP;
                     mbar_arrive_expect_tx(&full[s], bytes);
-                    tma_load_3d(st + L.b_hi, &tmapB, &full[s], 0, 0, zB_hi + (int)(kc >> 5));
-                    tma_load_3d(st + L.b_lo, &tmapB, &full[s], 0, 0, zB_lo + (int)(kc >> 5));
+                    for (int j = 0; j < NATOM; ++j)
+                    {
+                        tma_load_3d(st + j * L.b_atom + L.b_hi, &tmapB, &full[s], 0, 0, zB_hi + (int)(kc >> 5) + j);
+                        tma_load_3d(st + j * L.b_atom + L.b_lo, &tmapB, &full[s], 0, 0, zB_lo + (int)(kc >> 5) + j);
+                    }
                     for (int q = 0; q < nsp; ++q)
                     {
                         const int spp = (gd.nmag == 4) ? q : sp;
                         const long long kq = (long long)spp * N + r0;
-                        // both 16-point halves of the stage in one box
-                        tma_load_3d(st + L.p + 2 * q * L.p_half, &tmapP, &full[s], 0, 0, zP + (int)(kq >> 4));
+                        // the stage's 16-point blocks in one box
+                        tma_load_3d(st + L.p + 2 * NATOM * q * L.p_half, &tmapP, &full[s], 0, 0, zP + (int)(kq >> 4));
                     }
-                    // dV_nu(r) of the tile's modes, all magnetic components: rows (nu, comp) x 32 points
+                    // dV_nu(r) of the tile's modes, all magnetic components: two blocks of
+                    // rows (nu, comp) x 32 points
                     tma_load_3d(st + L.dv, &tmapV, &full[s], 0, yV, zV + (int)(r0 >> 5));
                     ++issued;
                 }
@@ -464,24 +477,25 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     tc_fence_after();
                     const uint32_t base = smem_u32(sm + s * L.stage_bytes);
                     const uint32_t dacc = tmem + (uint32_t)b * L.accw;
-                    const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * 64u;
+                    const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * (2u * KP);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
+                    for (int k = 0; k < KP / 8; ++k)
                     {
-                        const uint64_t bh = umma_desc_sw128(base + L.b_hi + 32 * k);
+                        const uint32_t atom = base + (uint32_t)(k >> 2) * L.b_atom + 32u * (uint32_t)(k & 3);
+                        const uint64_t bh = umma_desc_sw128(atom + L.b_hi);
                         const uint32_t en = (first && k == 0) ? 0u : 1u;
                         if (merged)
                         {
-                            // rows [0, NT) of the 2*NT-row tile are B_hi, [NT, 2NT) B_lo
+                            // rows [0, NT) of the atom's 2*NT-row tile are B_hi, [NT, 2NT) B_lo
                             umma_f16_ta(dacc, ahi + 8 * k, bh, idesc2, en);
-                            umma_f16_ta(dacc + (uint32_t)NT, ahi + 32 + 8 * k, bh, idesc, 1u);
+                            umma_f16_ta(dacc + (uint32_t)NT, ahi + KP + 8 * k, bh, idesc, 1u);
                         }
                         else
                         {
-                            const uint64_t bl = umma_desc_sw128(base + L.b_lo + 32 * k);
+                            const uint64_t bl = umma_desc_sw128(atom + L.b_lo);
                             umma_f16_ta(dacc, ahi + 8 * k, bh, idesc, en);
                             umma_f16_ta(dacc, ahi + 8 * k, bl, idesc, 1u);
-                            umma_f16_ta(dacc, ahi + 32 + 8 * k, bh, idesc, 1u);
+                            umma_f16_ta(dacc, ahi + KP + 8 * k, bh, idesc, 1u);
                         }
                     }
                     umma_commit(&empty[s]);
@@ -505,7 +519,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     else if (warp < 10)
     {
         // ---------------- A producers: lane quadrant q = warp % 4 (rows 32q..32q+31),
-        // half h of the stage's 32 points
+        // half h of the stage's 64 points
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
@@ -552,25 +566,32 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 }
                 tc_fence_after();
                 const uint8_t* st = sm + s * L.stage_bytes;
-                const uint8_t* pp[2];
-                const float4* dvp[2];
-                pp[0] = st + L.p + (0 * 2 + h) * L.p_half + (uint32_t)m * 128;
-                pp[1] = st + L.p + ((nsp - 1) * 2 + h) * L.p_half + (uint32_t)m * 128;
-                const float* dvs = reinterpret_cast<const float*>(st + L.dv);
-                dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * TC_KPTS + 16 * h) * 2);
-                dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * TC_KPTS + 16 * h) * 2);
-                const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * 64u + 16u * (uint32_t)h;
-                if (gd.nmag == 4)
+                // points h*KP/2 .. (h+1)*KP/2 - 1 of the stage, in 16-point blocks
+#pragma unroll 1
+                for (int b = 0; b < KP / 32; ++b)
                 {
+                    const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
+                    const int pb = p0 >> 4;                // 16-point psi block
+                    const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
+                    const uint8_t* pp[2];
+                    const float4* dvp[2];
+                    pp[0] = st + L.p + (0 * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
+                    pp[1] = st + L.p + ((nsp - 1) * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
+                    dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * 32 + (p0 & 31)) * 2);
+                    dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * 32 + (p0 & 31)) * 2);
+                    const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * (2u * KP) + (uint32_t)p0;
+                    if (gd.nmag == 4)
+                    {
 #pragma unroll
-                    for (int j0 = 0; j0 < 16; j0 += 4)
-                        produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
-                }
-                else
-                {
+                        for (int j0 = 0; j0 < 16; j0 += 4)
+                            produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + KP + j0);
+                    }
+                    else
+                    {
 #pragma unroll
-                    for (int j0 = 0; j0 < 16; j0 += 8)
-                        produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + 32 + j0);
+                        for (int j0 = 0; j0 < 16; j0 += 8)
+                            produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + KP + j0);
+                    }
                 }
                 tmem_wait_st();
                 tc_fence_before();
@@ -669,16 +690,22 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (units <= 0) return;
+#define TC_LAUNCH(BF, KPV)                                                                                       \
+    do                                                                                                           \
+    {                                                                                                            \
+        cudaFuncSetAttribute(k_local_tc<BF, KPV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
+        k_local_tc<BF, KPV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles,     \
+                                                         (int)units, partials, status);                          \
+    } while (0)
     if (ab_bf16)
     {
-        cudaFuncSetAttribute(k_local_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<1><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, (int)units,
-                                                   partials, status);
+        if (g.kpts == 64) TC_LAUNCH(1, 64);
+        else TC_LAUNCH(1, 32);
     }
     else
     {
-        cudaFuncSetAttribute(k_local_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        k_local_tc<0><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, (int)units,
-                                                   partials, status);
+        if (g.kpts == 64) TC_LAUNCH(0, 64);
+        else TC_LAUNCH(0, 32);
     }
+#undef TC_LAUNCH
 }

@@ -85,6 +85,20 @@ def test_mixed_against_fp64(name, prec):
     assert erms < (2e-5 if prec == "mixed_f16" else 2e-4), erms
 
 
+@pytest.mark.parametrize("stage", ["64", "32"])
+@pytest.mark.parametrize("name", ["c0", "soc_tr", "l12_small"])
+def test_mixed_both_stage_sizes(name, stage, monkeypatch):
+    """The tensor-core sandwich with 64- and 32-point pipeline stages (the
+    latter is what wide tiles use) against the FP64 form."""
+    monkeypatch.setenv("LELPH_TC_STAGE", stage)
+    s, _, kmq, nl = load(name)
+    g64 = run_all(s, "fp64", non_loc=nl, kminusq=kmq)
+    g = run_all(s, "mixed_f16", non_loc=nl, kminusq=kmq)
+    emax, erms, enorm = errors(g, g64)
+    assert enorm < 2e-6, enorm
+    assert erms < 2e-5, erms
+
+
 def test_c64_output_matches_c128():
     s, g_ref, kmq, nl = load("c0")
     g = run_all(s, "mixed", out=OUT_C64)
