@@ -177,18 +177,52 @@ __device__ T2* fft_smem(T2* a, T2* b, int nlines, int es, int ls, const FftPlan1
 
 // ---------------------------------------------------- contiguous-line pass
 
+// With a box mask, only the lines of occupied (x, y) columns are read,
+// transformed and written back; the others are all zero and stay so.
 template <typename T2, typename T>
 __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long long nlines, FftPlan1D p,
-                                                    const T2* __restrict__ tw, int sign, int lpc)
+                                                    const T2* __restrict__ tw, int sign, int lpc, BoxMask mk)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     T2* a = reinterpret_cast<T2*>(smraw);
     T2* b = a + (size_t)lpc * p.L;
     T2* tws = b + (size_t)lpc * p.L;
+    int* act = reinterpret_cast<int*>(tws + p.L);  // [lpc] active lines of the block
+    __shared__ int nact;
     for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
     long long l0 = (long long)blockIdx.x * lpc;
     int nl = (int)min((long long)lpc, nlines - l0);
     T2* g = data + l0 * p.L;
+    if (mk.col)
+    {
+        if (threadIdx.x == 0) nact = 0;
+        __syncthreads();
+        const long long ncol = (long long)mk.Nx * mk.Ny;
+        for (int j = threadIdx.x; j < nl; j += blockDim.x)
+        {
+            const long long line = l0 + j;
+            const long long box = line / ncol;
+            const long long col = line - box * ncol;
+            const long long kslot = box / mk.nbox_per_k;
+            if (mk.col[kslot * ncol + col]) act[atomicAdd(&nact, 1)] = j;
+        }
+        __syncthreads();
+        const int na = nact;
+        if (na == 0) return;
+        for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+        {
+            const int j = i / p.L, e = i - j * p.L;
+            a[i] = g[(size_t)act[j] * p.L + e];
+        }
+        __syncthreads();
+        T2* r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
+        for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+        {
+            const int j = i / p.L, e = i - j * p.L;
+            g[(size_t)act[j] * p.L + e] = r[i];
+        }
+        return;
+    }
     int n = nl * p.L;
     for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = g[i];
     __syncthreads();
@@ -200,16 +234,24 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
 // data viewed as [nouter][L][inner]; one CTA = one outer index and a chunk
 // of `ich` inner positions, loaded as an [L][ich] tile (coalesced in inner).
 
+// With a box mask (y pass: outer = (box, x)), empty x planes are skipped.
 template <typename T2, typename T>
 __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long long nouter, int inner, int ich,
-                                                     int nchunk, FftPlan1D p, const T2* __restrict__ tw, int sign)
+                                                     int nchunk, FftPlan1D p, const T2* __restrict__ tw, int sign,
+                                                     BoxMask mk)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     T2* a = reinterpret_cast<T2*>(smraw);
     T2* b = a + (size_t)ich * p.L;
     T2* tws = b + (size_t)ich * p.L;
-    for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
     long long o = blockIdx.x / nchunk;
+    if (mk.xpl)
+    {
+        const long long box = o / mk.Nx;
+        const long long x = o - box * mk.Nx;
+        if (!mk.xpl[(box / mk.nbox_per_k) * mk.Nx + x]) return;
+    }
+    for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
     int c = blockIdx.x - (int)(o * nchunk);
     int i0 = c * ich;
     int ic = min(ich, inner - i0);
@@ -259,7 +301,8 @@ template <int BF16>
 __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ boxes, int nbox, int k0, int ich,
                                                      int nchunk, FftPlan1D p, const float2* __restrict__ tw,
                                                      int sign, GeomDev gd, const float* __restrict__ band_scale,
-                                                     uint16_t* __restrict__ Bsplit, float2* __restrict__ psi32)
+                                                     uint16_t* __restrict__ Bsplit, float2* __restrict__ psi32,
+                                                     BoxMask mk)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* a = reinterpret_cast<float2*>(smraw);
@@ -274,10 +317,12 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     int ic = min(ich, inner - i0);
     const float2* g = boxes + (size_t)o * N + i0;
     int n = p.L * ic;
+    // x planes that the sphere of this k-point does not reach are zero: not read
+    const uint8_t* xpl = mk.xpl ? mk.xpl + (size_t)(o / mk.nbox_per_k) * gd.Nx : nullptr;
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
         int l = idx / ic, i = idx - l * ic;
-        a[l * ic + i] = g[(size_t)l * inner + i];
+        a[l * ic + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : g[(size_t)l * inner + i];
     }
     __syncthreads();
     float2* r = fft_smem<float2, float>(a, b, ic, ic, 1, p, tws, sign);
@@ -331,7 +376,7 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
                                                  const int* __restrict__ npw_arr, const double2* __restrict__ coef,
                                                  const long long* __restrict__ coef_off, GeomDev gd,
                                                  T2* __restrict__ boxes, double2* __restrict__ chat,
-                                                 const long long* __restrict__ chat_off)
+                                                 const long long* __restrict__ chat_off, BoxMask mk)
 {
     const int kslot = blockIdx.y;
     const int kbz = k0 + kslot;
@@ -358,6 +403,11 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
     int iz = G2 % gd.Nz;
     if (iz < 0) iz += gd.Nz;
     const size_t bidx = ((size_t)ix * gd.Ny + iy) * gd.Nz + iz;
+    if (mk.col)
+    {
+        mk.col[((size_t)kslot * gd.Nx + ix) * gd.Ny + iy] = 1;
+        mk.xpl[(size_t)kslot * gd.Nx + ix] = 1;
+    }
     const double2 u0 = make_double2(s.su2[0], s.su2[1]), u1 = make_double2(s.su2[2], s.su2[3]);
     const double2 u2 = make_double2(s.su2[4], s.su2[5]), u3 = make_double2(s.su2[6], s.su2[7]);
     const double2* cbase = coef + coef_off[s.ik];
@@ -418,12 +468,13 @@ static int ich_for(int L, int inner, int elems)
 }
 
 template <typename T2, typename T>
-static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st)
+static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st,
+                          const BoxMask& mk)
 {
     const int elems = sizeof(T) == 8 ? 2048 : 4096;
     int lpc = elems / p.L;
     if (lpc < 1) lpc = 1;
-    size_t smem = (size_t)(2 * lpc * p.L + p.L) * sizeof(T2);
+    size_t smem = (size_t)(2 * lpc * p.L + p.L) * sizeof(T2) + sizeof(int) * lpc;
     static bool attr_set = false;
     if (!attr_set)
     {
@@ -431,12 +482,12 @@ static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const 
         attr_set = true;
     }
     long long nb = (nlines + lpc - 1) / lpc;
-    k_fft_contig<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nlines, p, tw, sign, lpc);
+    k_fft_contig<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nlines, p, tw, sign, lpc, mk);
 }
 
 template <typename T2, typename T>
 static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1D& p, const T2* tw, int sign,
-                           cudaStream_t st)
+                           cudaStream_t st, const BoxMask& mk)
 {
     const int elems = sizeof(T) == 8 ? 2048 : 4096;
     int ich = ich_for(p.L, inner, elems);
@@ -449,33 +500,33 @@ static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1
         attr_set = true;
     }
     long long nb = nouter * nchunk;
-    k_fft_strided<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign);
+    k_fft_strided<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign, mk);
 }
 
 void lelph_launch_fft_contig_d(double2* data, long long nlines, const FftPlan1D& p, const double2* tw, int sign,
                                cudaStream_t st)
 {
-    launch_contig<double2, double>(data, nlines, p, tw, sign, st);
+    launch_contig<double2, double>(data, nlines, p, tw, sign, st, BoxMask());
 }
 void lelph_launch_fft_contig_f(float2* data, long long nlines, const FftPlan1D& p, const float2* tw, int sign,
-                               cudaStream_t st)
+                               cudaStream_t st, const BoxMask& mk)
 {
-    launch_contig<float2, float>(data, nlines, p, tw, sign, st);
+    launch_contig<float2, float>(data, nlines, p, tw, sign, st, mk);
 }
 void lelph_launch_fft_strided_d(double2* data, long long nouter, int inner, const FftPlan1D& p, const double2* tw,
                                 int sign, cudaStream_t st)
 {
-    launch_strided<double2, double>(data, nouter, inner, p, tw, sign, st);
+    launch_strided<double2, double>(data, nouter, inner, p, tw, sign, st, BoxMask());
 }
 void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const FftPlan1D& p, const float2* tw,
-                                int sign, cudaStream_t st)
+                                int sign, cudaStream_t st, const BoxMask& mk)
 {
-    launch_strided<float2, float>(data, nouter, inner, p, tw, sign, st);
+    launch_strided<float2, float>(data, nouter, inner, p, tw, sign, st, mk);
 }
 
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
-                                 float2* psi32, cudaStream_t st)
+                                 float2* psi32, cudaStream_t st, const BoxMask& mk)
 {
     const int inner = g.Ny * g.Nz;
     int ich = ich_for(p.L, inner, 4096);
@@ -492,24 +543,24 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
     unsigned nb = (unsigned)(nbox * nchunk);
     if (ab_bf16)
         k_fft_x_split<1><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
-                                                psi32);
+                                                psi32, mk);
     else
         k_fft_x_split<0><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
-                                                psi32);
+                                                psi32, mk);
 }
 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
                           const int* npw, int npw_max, const double2* coef, const long long* coef_off,
                           const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
-                          cudaStream_t st)
+                          cudaStream_t st, const BoxMask& mk)
 {
     dim3 grid((unsigned)((npw_max + 255) / 256), nk);
     if (box_fp64)
         k_scatter<double2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
-                                                 (double2*)boxes, chat, chat_off);
+                                                 (double2*)boxes, chat, chat_off, mk);
     else
         k_scatter<float2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
-                                                (float2*)boxes, chat, chat_off);
+                                                (float2*)boxes, chat, chat_off, mk);
 }
 
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,

@@ -89,6 +89,7 @@ struct lelph_gpu
     int chunk_pts = 0, nchunks = 0;
     // local bare potential: V_loc(|G|) table and its spline slopes per species
     DevBuf d_vl_v, d_vl_dv, d_vl_in, d_vloc;
+    DevBuf d_colmask;  // box occupancy of a chunk of k-points (z-columns, then x planes)
     bool vl_ready = false;
     int vl_npts = 0, vl_dim2 = 0;
     double vl_dg = 0, vl_volume = 0;
@@ -865,7 +866,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
-                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc};
+                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1030,21 +1031,35 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
         int nkc = (int)std::max<size_t>(1, std::min<size_t>((size_t)d.nkpts_BZ, (4ull << 30) / per_k));
         rc = ensure(h, h->d_boxes32, per_k * nkc);
         if (rc) return rc;
+        const size_t mask_k = (size_t)g.Nx * g.Ny + g.Nx;
+        rc = ensure(h, h->d_colmask, mask_k * nkc);
+        if (rc) return rc;
+        BoxMask mk;
+        mk.col = (uint8_t*)h->d_colmask.p;
+        mk.xpl = mk.col + (size_t)nkc * g.Nx * g.Ny;
+        mk.Nx = g.Nx;
+        mk.Ny = g.Ny;
+        mk.nbox_per_k = nbox_per_k;
         for (int k0 = 0; k0 < d.nkpts_BZ; k0 += nkc)
         {
             int nk = std::min(nkc, d.nkpts_BZ - k0);
             CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
+            CUDA_TRY(h, cudaMemsetAsync(h->d_colmask.p, 0, mask_k * nkc, h->st));
             lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
                                  (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
-                                 (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p, (double2*)h->d_chat.p,
-                                 (const long long*)h->d_chatoff.p, h->st);
+                                 (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p,
+                                 (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st, mk);
             const long long nbox = (long long)nk * nbox_per_k;
             float2* bx = (float2*)h->d_boxes32.p;
-            lelph_launch_fft_contig_f(bx, nbox * g.Nx * g.Ny, h->plan[2], (const float2*)h->d_tw32[2].p, +1, h->st);
-            lelph_launch_fft_strided_f(bx, nbox * g.Nx, g.Nz, h->plan[1], (const float2*)h->d_tw32[1].p, +1, h->st);
+            // z pass on the occupied columns, y pass on the occupied x planes, x pass
+            // reading only those planes (the rest of every box is zero)
+            lelph_launch_fft_contig_f(bx, nbox * g.Nx * g.Ny, h->plan[2], (const float2*)h->d_tw32[2].p, +1, h->st,
+                                      mk);
+            lelph_launch_fft_strided_f(bx, nbox * g.Nx, g.Nz, h->plan[1], (const float2*)h->d_tw32[1].p, +1, h->st,
+                                       mk);
             lelph_launch_fft_x_to_split(bx, nk, k0, h->plan[0], (const float2*)h->d_tw32[0].p, +1, g,
                                         (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p,
-                                        (float2*)h->d_psi32.p, h->st);
+                                        (float2*)h->d_psi32.p, h->st, mk);
             h->stats.kernel_launches += 4;
         }
     }

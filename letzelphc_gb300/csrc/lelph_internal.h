@@ -48,25 +48,36 @@ struct GeomDev
     int kpts;      // grid points per pipeline stage of the tensor-core sandwich (64, or 32 for wide tiles)
 };
 
+// Occupancy of the boxes of a chunk of k-points after the sphere -> box
+// scatter: col[(kslot*Nx + x)*Ny + y] != 0 when the z-column (x, y) holds a
+// plane wave of k, xpl[kslot*Nx + x] != 0 when the plane x does.  Every band
+// of a k-point shares its sphere.  col == nullptr: no masking.
+struct BoxMask
+{
+    uint8_t* col = nullptr;
+    uint8_t* xpl = nullptr;
+    int Nx = 0, Ny = 0, nbox_per_k = 1;
+};
+
 // FFT (fft_gather.cu)
 void lelph_launch_fft_contig_d(double2* data, long long nlines, const FftPlan1D& p, const double2* tw, int sign,
                                cudaStream_t st);
 void lelph_launch_fft_contig_f(float2* data, long long nlines, const FftPlan1D& p, const float2* tw, int sign,
-                               cudaStream_t st);
+                               cudaStream_t st, const BoxMask& mk = BoxMask());
 void lelph_launch_fft_strided_d(double2* data, long long nouter, int inner, const FftPlan1D& p, const double2* tw,
                                 int sign, cudaStream_t st);
 void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const FftPlan1D& p, const float2* tw,
-                                int sign, cudaStream_t st);
+                                int sign, cudaStream_t st, const BoxMask& mk = BoxMask());
 // x-pass of the mixed form writing the split tensor-core operand directly
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
-                                 float2* psi32, cudaStream_t st);
+                                 float2* psi32, cudaStream_t st, const BoxMask& mk = BoxMask());
 
 // sphere -> box scatter with su2, fractional-translation phase and conj
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
                           const int* npw, int npw_max, const double2* coef, const long long* coef_off,
                           const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
-                          cudaStream_t st);
+                          cudaStream_t st, const BoxMask& mk = BoxMask());
 
 // debugging / parity: box index of each rotated plane wave of one full-BZ k
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,
