@@ -216,7 +216,7 @@ __host__ __device__ inline TcSmemLayout tc_layout(const GeomDev& g)
     L.na = (512 - L.a_col0) / (2 * (uint32_t)g.kpts);
     if (L.na > TC_NA_MAX) L.na = TC_NA_MAX;
     L.bar_off = L.nst * L.stage_bytes;
-    L.total = L.bar_off + 512 + 1024;  // barriers + alignment slack
+    L.total = L.bar_off + 512 + 256 + 1024;  // barriers, a zero dV row, alignment slack
     return L;
 }
 
@@ -256,7 +256,7 @@ __device__ __forceinline__ void split_pair(float re, float im, uint32_t& h, uint
 // (128-byte swizzled half tile), dvp[c] at the row's dV (16 points of the half).
 template <int BF16, int SUB, int NC>
 __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const float4* const* dvp, uint32_t swz, int j0,
-                                            bool valid, uint32_t tcol_hi, uint32_t tcol_lo)
+                                            uint32_t tcol_hi, uint32_t tcol_lo)
 {
     uint32_t hi[SUB], lo[SUB];
 #pragma unroll
@@ -274,7 +274,6 @@ __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const floa
             acc.z += dv.z * ps.z - dv.w * ps.w;
             acc.w += dv.z * ps.w + dv.w * ps.z;
         }
-        if (!valid) acc = make_float4(0.f, 0.f, 0.f, 0.f);
         split_pair<BF16>(acc.x, acc.y, hi[2 * jj], lo[2 * jj]);
         split_pair<BF16>(acc.z, acc.w, hi[2 * jj + 1], lo[2 * jj + 1]);
     }
@@ -340,6 +339,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     const int NST = (int)L.nst, NA = (int)L.na, NACC = (int)L.nacc;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + TC_NACC_MAX);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const float4* zero_dv = reinterpret_cast<const float4*>(sm + L.bar_off + 512);  // 256 zero bytes
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int NT = 2 * gd.nbp;
@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         *abort_flag = 0;
         fence_barrier_init();
     }
+    if (threadIdx.x < 64) reinterpret_cast<float*>(sm + L.bar_off + 512)[threadIdx.x] = 0.f;
     if (warp == 1) tmem_alloc(tmem_slot, 512);
     tc_fence_before();
     __syncthreads();
@@ -533,9 +534,9 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
         {
             const TcUnit w = tc_unit(u, nchunks, mtiles, gd.nspin, pairs);
-            const int MTa = min(MT, gd.nmodes - w.mt * MT);  // modes present in this tile
-            const bool valid = ml < MTa;
-            const int mlc = valid ? ml : 0;
+            // rows of modes past nmodes read the TMA zero fill of the dV tile; rows
+            // past the tile's MT*nb read the zero block
+            const bool in_tile = ml < MT;
             // a K chunk never straddles spinor components (chunk_pts divides N)
             const int sp = (int)(((long long)w.chunk * chunk_pts) / N);
             int comp0, comp1;
@@ -577,20 +578,22 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     const float4* dvp[2];
                     pp[0] = st + L.p + (0 * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
                     pp[1] = st + L.p + ((nsp - 1) * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
-                    dvp[0] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp0) * 32 + (p0 & 31)) * 2);
-                    dvp[1] = reinterpret_cast<const float4*>(dvs + ((size_t)(mlc * gd.nmag + comp1) * 32 + (p0 & 31)) * 2);
+                    dvp[0] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * gd.nmag + comp0) * 32 + (p0 & 31)) * 2)
+                                     : zero_dv;
+                    dvp[1] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * gd.nmag + comp1) * 32 + (p0 & 31)) * 2)
+                                     : zero_dv;
                     const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * (2u * KP) + (uint32_t)p0;
                     if (gd.nmag == 4)
                     {
 #pragma unroll
                         for (int j0 = 0; j0 < 16; j0 += 4)
-                            produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + KP + j0);
+                            produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, col_hi + j0, col_hi + KP + j0);
                     }
                     else
                     {
 #pragma unroll
                         for (int j0 = 0; j0 < 16; j0 += 8)
-                            produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, valid, col_hi + j0, col_hi + KP + j0);
+                            produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, col_hi + j0, col_hi + KP + j0);
                     }
                 }
                 tmem_wait_st();
