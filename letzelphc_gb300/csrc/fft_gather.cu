@@ -343,25 +343,55 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     const size_t npb = (size_t)gd.nspinor * N / 16;
     const size_t rg_hi = (size_t)(kbz * gd.nspin + spin) * 2;
     const size_t pg = (size_t)(kbz * gd.nspin + spin);
-    uint32_t* Bw = reinterpret_cast<uint32_t*>(Bsplit);
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    // 64-bit bases of this box's rows; per element only 32-bit offsets: row
+    // `band` (and nbp + band) of K block kb sits at kb*NT*32 + row*32 words
+    uint32_t* const Bhi = reinterpret_cast<uint32_t*>(Bsplit) + rg_hi * nkb * NT * 32 + (size_t)band * 32;
+    uint32_t* const Blo = Bhi + nkb * NT * 32;
+    const uint32_t rot = (uint32_t)gd.nbp * 32;  // (-Im, Re) rows
+    float2* const P = psi32 + pg * npb * gd.nbp * 16 + (size_t)band * 16;
+    const uint32_t kbase = (uint32_t)((long long)sp * N) + (uint32_t)i0;  // K index of (x = 0, column 0)
+    // one column per thread, rows (x) stepping by the columns a block covers
+    const int rows_per = blockDim.x / ic;
+    const int i = threadIdx.x % ic;
+    if (rows_per > 0 && threadIdx.x < rows_per * ic)
     {
-        int l = idx / ic, i = idx - l * ic;
-        float2 v = r[l * ic + i];
-        v.x *= sc;
-        v.y *= sc;
-        long long kc = (long long)sp * N + (long long)l * inner + i0 + i;
-        uint32_t h0, l0, h1, l1;
-        split2<BF16>(v.x, v.y, h0, l0);
-        split2<BF16>(-v.y, v.x, h1, l1);
-        const size_t kb = (size_t)(kc >> 5), kw = (size_t)(kc & 31);
-        const size_t t_hi = (rg_hi * nkb + kb) * NT, t_lo = ((rg_hi + 1) * nkb + kb) * NT;
-        Bw[(t_hi + band) * 32 + kw] = h0;
-        Bw[(t_lo + band) * 32 + kw] = l0;
-        Bw[(t_hi + gd.nbp + band) * 32 + kw] = h1;
-        Bw[(t_lo + gd.nbp + band) * 32 + kw] = l1;
-        // FP32 copy of the scaled psi(r) (rows (kbz, spin, band))
-        psi32[((pg * npb + (size_t)(kc >> 4)) * gd.nbp + band) * 16 + (kc & 15)] = v;
+        for (int l = threadIdx.x / ic; l < p.L; l += rows_per)
+        {
+            float2 v = r[l * ic + i];
+            v.x *= sc;
+            v.y *= sc;
+            const uint32_t kc = kbase + (uint32_t)(l * inner + i);
+            uint32_t h0, l0, h1, l1;
+            split2<BF16>(v.x, v.y, h0, l0);
+            split2<BF16>(-v.y, v.x, h1, l1);
+            const uint32_t off = (kc >> 5) * (uint32_t)NT * 32u + (kc & 31u);
+            Bhi[off] = h0;
+            Blo[off] = l0;
+            Bhi[off + rot] = h1;
+            Blo[off + rot] = l1;
+            // FP32 copy of the scaled psi(r) (rows (kbz, spin, band))
+            P[(kc >> 4) * (uint32_t)gd.nbp * 16u + (kc & 15u)] = v;
+        }
+    }
+    else
+    {
+        for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+        {
+            const int l = idx / ic, ii = idx - l * ic;
+            float2 v = r[l * ic + ii];
+            v.x *= sc;
+            v.y *= sc;
+            const uint32_t kc = kbase + (uint32_t)(l * inner + ii);
+            uint32_t h0, l0, h1, l1;
+            split2<BF16>(v.x, v.y, h0, l0);
+            split2<BF16>(-v.y, v.x, h1, l1);
+            const uint32_t off = (kc >> 5) * (uint32_t)NT * 32u + (kc & 31u);
+            Bhi[off] = h0;
+            Blo[off] = l0;
+            Bhi[off + rot] = h1;
+            Blo[off + rot] = l1;
+            P[(kc >> 4) * (uint32_t)gd.nbp * 16u + (kc & 15u)] = v;
+        }
     }
 }
 

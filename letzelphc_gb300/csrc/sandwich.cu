@@ -245,7 +245,9 @@ __device__ __forceinline__ void split_pair(float re, float im, uint32_t& h, uint
     {
         __half2 hv = __floats2half2_rn(re, im);
         float2 hf = __half22float2(hv);
-        __half2 lv = __floats2half2_rn(re - hf.x, im - hf.y);
+        // both residuals in one packed FP32x2 FMA: (re, im) - hi, exactly rounded
+        const float2 d = __ffma2_rn(hf, make_float2(-1.f, -1.f), make_float2(re, im));
+        __half2 lv = __floats2half2_rn(d.x, d.y);
         h = *reinterpret_cast<uint32_t*>(&hv);
         l = *reinterpret_cast<uint32_t*>(&lv);
     }
