@@ -193,6 +193,20 @@ int lelph_gpu_compute_elphq(lelph_gpu* h, const double qpt_crys[3], const double
 int lelph_gpu_elph_q_rotate(lelph_gpu* h, const double* Dmats_l, const double* elph_q, const double* Dmats_r,
                             int time_rev, double* elph_Sq);
 
+/* Dmats: the electronic representation matrices of compute_and_write_dmats
+ * (src/elph/compute_dmats.c:20-131), one electronic_reps
+ * (src/symmetries/elec_reps.c:16-413) per (symmetry, full-BZ k) pair
+ * idmat = isym * nkpts_BZ + ikBZ, for idmat = first .. first + count - 1 (the
+ * block distribute_to_grps gives a pool, compute_dmats.c:95-97).  Rmat
+ * (nsym, 3, 3) cartesian row-major, tau (nsym, 3) cartesian, time_rev (nsym):
+ * the phonon symmetries (struct symmetry).  Dmats (may be NULL): complex double
+ * (count, nspin, nbnds, nbnds), D[., s, b, a] = <psi_{Rk,b}| U(R) |psi_{k,a}>,
+ * the reference's ndb.Dmats slice layout.  The block also stays on the device.
+ * LELPH_GPU_ERR_GEOMETRY if R k is not on the k grid ("Rotated k point not
+ * found") or an operation is not integral on the lattice. */
+int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
+                    long long first, long long count, double* Dmats);
+
 /* Rotated (and umklapp-shifted) Miller indices of full-BZ k-point kbz, as the
  * device computes them: out[npw*3].  Parity check of the integer maps of
  * rotateGvecs + Sort_pw (src/wfc/rotate_Gvecs.c:15-81, src/wfc/sortpw.c:95-315). */

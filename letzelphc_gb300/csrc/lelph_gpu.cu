@@ -90,6 +90,12 @@ struct lelph_gpu
     // local bare potential: V_loc(|G|) table and its spline slopes per species
     DevBuf d_vl_v, d_vl_dv, d_vl_in, d_vloc;
     DevBuf d_colmask;  // box occupancy of a chunk of k-points (z-columns, then x planes)
+    // Dmats: Miller -> position tables of the iBZ lists, the job table and the
+    // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
+    DevBuf d_dmgtab, d_dmjobs, d_dmats;
+    bool dm_gtab_ready = false;
+    long long dm_first = 0, dm_count = 0;
+    int dm_nsym = 0;
     bool vl_ready = false;
     int vl_npts = 0, vl_dim2 = 0;
     double vl_dg = 0, vl_volume = 0;
@@ -866,7 +872,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
-                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask};
+                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
+                      &h->d_dmjobs, &h->d_dmats};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1732,6 +1739,222 @@ extern "C" int lelph_gpu_elph_q_rotate(lelph_gpu* h, const double* Dl, const dou
     h->stats.kernel_launches += 2;
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpyAsync(out, dout, sizeof(double2) * gs, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}
+
+// ============================================ Dmats (electronic representations)
+
+namespace
+{
+typedef std::complex<double> cd;
+
+// integer action alat^T R A^-T of a cartesian rotation on Miller indices
+int miller_action(const lelph_gpu* h, const double* R, int* W)
+{
+    double B[9];
+    for (int i = 0; i < 9; ++i) B[i] = h->blat[i] / (2 * PI_T);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+        {
+            double acc = 0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) acc += h->alat[3 * k + r] * R[3 * k + l] * B[3 * l + c];
+            double w = std::rint(acc);
+            if (std::fabs(acc - w) > 1e-6) return -1;
+            W[3 * r + c] = (int)w;
+        }
+    return 0;
+}
+
+// inverse of a unimodular integer matrix (adjugate / determinant)
+int int_inverse3(const int* m, int* inv)
+{
+    const long long det = (long long)m[0] * (m[4] * m[8] - m[5] * m[7]) - (long long)m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                          (long long)m[2] * (m[3] * m[7] - m[4] * m[6]);
+    if (det != 1 && det != -1) return -1;
+    const int d = (int)det;
+    inv[0] = d * (m[4] * m[8] - m[5] * m[7]);
+    inv[1] = d * (m[2] * m[7] - m[1] * m[8]);
+    inv[2] = d * (m[1] * m[5] - m[2] * m[4]);
+    inv[3] = d * (m[5] * m[6] - m[3] * m[8]);
+    inv[4] = d * (m[0] * m[8] - m[2] * m[6]);
+    inv[5] = d * (m[2] * m[3] - m[0] * m[5]);
+    inv[6] = d * (m[3] * m[7] - m[4] * m[6]);
+    inv[7] = d * (m[1] * m[6] - m[0] * m[7]);
+    inv[8] = d * (m[0] * m[4] - m[1] * m[3]);
+    return 0;
+}
+
+inline cd conj_if(cd z, bool c) { return c ? std::conj(z) : z; }
+
+// Job of the pair (symmetry isym, full-BZ k ikBZ): the reference's sequence
+// (src/symmetries/elec_reps.c:33-372) folded into one spinor matrix, one
+// conjugation, one constant phase and one phase vector per side.  With
+// x^(c) the conjugate of x when c holds:
+//   right: w = phR^(trR) ph1^(tr1^trR) e^{-i 2 pi m.tw} UR^(trR) U1^(tr1^trR) psi_k1^(tr1^trR),
+//          tw = s1 W1^T tau1 + sR W_RS1^T tauR  (s = -1 where conjugated)
+//   left:  v = ph2^(!tr2) e^{-i 2 pi m.tv} U2^(!tr2) psi_k2^(!tr2),  tv = s2 W_RS1^T tau2
+// ph1 = e^{-i 2 pi (S1 k1).tau1}, phR = e^{-i 2 pi (R S1 k1).tauR}, ph2 = e^{-i 2 pi (R S1 k1).tau2}.
+int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_crys, const cd* UR, bool trR,
+             int ikBZ, DmatJob& J)
+{
+    const lelph_gpu_desc& d = h->d;
+    double kc[3], Rk[3], Rkc[3];
+    for (int x = 0; x < 3; ++x)
+        kc[x] = (h->blat[3 * x] * h->kbz_crys[3 * ikBZ] + h->blat[3 * x + 1] * h->kbz_crys[3 * ikBZ + 1] +
+                 h->blat[3 * x + 2] * h->kbz_crys[3 * ikBZ + 2]) /
+                (2 * PI_T);
+    mat_vec3(R, kc, false, Rk);
+    mat_vec3(d.alat_vec, Rk, true, Rkc);
+    const int iRk = find_k(h, Rkc);
+    if (iRk < 0)
+        return fail(h, LELPH_GPU_ERR_GEOMETRY,
+                    "Rotated k point not found. Either Wrong Phonon symmetry or using non-uniform kgrid");
+    const KPointSym& s1 = h->ksym[ikBZ];
+    const KPointSym& s2 = h->ksym[iRk];
+    memset(&J, 0, sizeof(J));
+    J.ik1 = s1.ik;
+    J.ik2 = s2.ik;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            J.WRS1[3 * r + c] = WR[3 * r] * s1.W[c] + WR[3 * r + 1] * s1.W[3 + c] + WR[3 * r + 2] * s1.W[6 + c];
+    if (int_inverse3(s2.W, J.W2inv)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "symmetry not unimodular on the lattice");
+    const double* S1 = &h->symR[9 * s1.isym];
+    const double* S2 = &h->symR[9 * s2.isym];
+    double RS1[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) RS1[3 * r + c] = R[3 * r] * S1[c] + R[3 * r + 1] * S1[3 + c] + R[3 * r + 2] * S1[6 + c];
+    double RS1k1[3], S2k2[3], u[3], uc[3], Rkcrys[3];
+    mat_vec3(RS1, &h->kibz[3 * s1.ik], false, RS1k1);
+    mat_vec3(S2, &h->kibz[3 * s2.ik], false, S2k2);
+    for (int x = 0; x < 3; ++x) u[x] = S2k2[x] - RS1k1[x];
+    mat_vec3(d.alat_vec, u, true, uc);
+    for (int x = 0; x < 3; ++x)
+    {
+        J.ulm[x] = (int)std::rint(uc[x]);
+        if (std::fabs(uc[x] - J.ulm[x]) > 1e-4) return fail(h, LELPH_GPU_ERR_GEOMETRY, "S2 k2 - R S1 k1 not a G vector");
+    }
+    mat_vec3(d.alat_vec, RS1k1, true, Rkcrys);
+    const bool tr1 = s1.trev != 0, tr2 = s2.trev != 0, x1 = tr1 != trR, nt2 = !tr2;
+    auto kph = [](const double* k, const double* t) {
+        return std::exp(cd(0, -2 * PI_T * (k[0] * t[0] + k[1] * t[1] + k[2] * t[2])));
+    };
+    const cd ph1(s1.kphase[0], s1.kphase[1]);
+    const cd phR = kph(Rkcrys, tauR_crys), ph2 = kph(Rkcrys, s2.tau_crys);
+    cd U1[4], U2[4], Mw[4];
+    for (int e = 0; e < 4; ++e)
+    {
+        U1[e] = conj_if(cd(s1.su2[2 * e], s1.su2[2 * e + 1]), x1);
+        U2[e] = conj_if(cd(s2.su2[2 * e], s2.su2[2 * e + 1]), nt2);
+    }
+    cd URc[4];
+    for (int e = 0; e < 4; ++e) URc[e] = conj_if(UR[e], trR);
+    Mw[0] = URc[0] * U1[0] + URc[1] * U1[2];
+    Mw[1] = URc[0] * U1[1] + URc[1] * U1[3];
+    Mw[2] = URc[2] * U1[0] + URc[3] * U1[2];
+    Mw[3] = URc[2] * U1[1] + URc[3] * U1[3];
+    const cd Cw = conj_if(phR, trR) * conj_if(ph1, x1), Cv = conj_if(ph2, nt2);
+    const double sg1 = x1 ? -1.0 : 1.0, sgR = trR ? -1.0 : 1.0, sg2 = nt2 ? -1.0 : 1.0;
+    for (int c = 0; c < 3; ++c)
+    {
+        double a = 0, b = 0, e = 0;
+        for (int r = 0; r < 3; ++r)
+        {
+            a += s1.W[3 * r + c] * s1.tau_crys[r];
+            b += J.WRS1[3 * r + c] * tauR_crys[r];
+            e += J.WRS1[3 * r + c] * s2.tau_crys[r];
+        }
+        J.tw[c] = sg1 * a + sgR * b;
+        J.tv[c] = sg2 * e;
+    }
+    J.conj_w = x1;
+    J.conj_v = nt2;
+    J.Cw = make_double2(Cw.real(), Cw.imag());
+    J.Cv = make_double2(Cv.real(), Cv.imag());
+    for (int e = 0; e < 4; ++e)
+    {
+        J.Mw[e] = make_double2(Mw[e].real(), Mw[e].imag());
+        J.Mv[e] = make_double2(U2[e].real(), U2[e].imag());
+    }
+    return LELPH_GPU_OK;
+}
+}  // namespace
+
+extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
+                               long long first, long long count, double* Dmats)
+{
+    if (!h || nsym <= 0 || !Rmat || !tau || !time_rev || first < 0 || count < 0) return LELPH_GPU_ERR_INVALID;
+    const lelph_gpu_desc& d = h->d;
+    const long long nkbz = d.nkpts_BZ;
+    if (first + count > (long long)nsym * nkbz) return fail(h, LELPH_GPU_ERR_INVALID, "Dmat range beyond nsym * nk_BZ");
+    if (count == 0) return LELPH_GPU_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    // per-symmetry integer action, crystal translation and SU(2) matrix
+    std::vector<int> WR(9 * (size_t)nsym);
+    std::vector<double> tauc(3 * (size_t)nsym);
+    std::vector<cd> UR(4 * (size_t)nsym);
+    for (int is = 0; is < nsym; ++is)
+    {
+        if (miller_action(h, Rmat + 9 * is, &WR[9 * is]))
+            return fail(h, LELPH_GPU_ERR_GEOMETRY, "symmetry not integral on the reciprocal lattice");
+        double tc[3];
+        mat_vec3(d.blat_vec, tau + 3 * is, true, tc);
+        for (int x = 0; x < 3; ++x) tauc[3 * is + x] = tc[x] / (2 * PI_T);
+        if (!su2mat(Rmat + 9 * is, d.nspinor, time_rev[is] != 0, &UR[4 * is]))
+            return fail(h, LELPH_GPU_ERR_GEOMETRY, "Wrong symmetric matrices");
+    }
+    std::vector<DmatJob> jobs((size_t)count);
+    for (long long i = 0; i < count; ++i)
+    {
+        const long long id = first + i;
+        const int is = (int)(id / nkbz), ik = (int)(id % nkbz);
+        int rc = dmat_job(h, Rmat + 9 * is, &WR[9 * is], &tauc[3 * is], &UR[4 * is], time_rev[is] != 0, ik,
+                          jobs[(size_t)i]);
+        if (rc) return rc;
+    }
+    // Miller -> position tables of the iBZ lists on the reference's box, built once
+    DmatGeom dg;
+    dg.nb = d.nbnds;
+    dg.nspin = d.nspin;
+    dg.nspinor = d.nspinor;
+    dg.Nx = h->Nbox[0];
+    dg.Ny = h->Nbox[1];
+    dg.Nz = h->Nbox[2];
+    dg.ntab = dg.Nx + dg.Ny + dg.Nz + 3;
+    if (!h->dm_gtab_ready)
+    {
+        for (long long i = 0; i < 3 * h->total_pw; ++i)
+            if (2 * std::abs(h->miller[i]) > h->Nbox[i % 3])
+                return fail(h, LELPH_GPU_ERR_GEOMETRY, "plane wave outside the FFT box");
+        const size_t nbox = (size_t)dg.Nx * dg.Ny * dg.Nz;
+        int rc = ensure(h, h->d_dmgtab, sizeof(int) * nbox * d.nkpts_iBZ);
+        if (rc) return rc;
+        CUDA_TRY(h, cudaMemsetAsync(h->d_dmgtab.p, 0xff, sizeof(int) * nbox * d.nkpts_iBZ, h->st));
+        int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
+        lelph_launch_dm_gtab((const int*)h->d_miller.p, (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p,
+                             d.nkpts_iBZ, npw_max, dg.Nx, dg.Ny, dg.Nz, (int*)h->d_dmgtab.p, h->st);
+        h->stats.kernel_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+        h->dm_gtab_ready = true;
+    }
+    const int fp64 = h->mixed ? 0 : 1;
+    if (lelph_dmats_smem_bytes(dg, fp64) > 200 * 1024) return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "FFT box too large for the Dmat phase tables");
+    int rc = upload(h, h->d_dmjobs, jobs.data(), sizeof(DmatJob) * jobs.size());
+    if (rc) return rc;
+    const size_t dbytes = sizeof(double2) * (size_t)count * d.nspin * d.nbnds * d.nbnds;
+    rc = ensure(h, h->d_dmats, dbytes);
+    if (rc) return rc;
+    if (lelph_launch_dmats((const DmatJob*)h->d_dmjobs.p, count, dg, fp64, (const double2*)h->d_coef.p,
+                           (const long long*)h->d_coefoff.p, (const int*)h->d_miller.p, (const long long*)h->d_pwoff.p,
+                           (const int*)h->d_npw.p, (const int*)h->d_dmgtab.p, (double2*)h->d_dmats.p, h->st))
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "Dmat launch configuration");
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    h->dm_first = first;
+    h->dm_count = count;
+    h->dm_nsym = nsym;
+    if (Dmats) CUDA_TRY(h, cudaMemcpyAsync(Dmats, h->d_dmats.p, dbytes, cudaMemcpyDeviceToHost, h->st));
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     return LELPH_GPU_OK;
 }

@@ -150,3 +150,29 @@ struct RotDvDesc
 };
 void lelph_launch_rotate_dvscf(const RotDvDesc& rd, const double2* in, double2* out, unsigned* status,
                                cudaStream_t st);
+
+// ------------------------------------------------------------ Dmats
+struct DmatGeom
+{
+    int nb, nspin, nspinor;
+    int Nx, Ny, Nz;  // the reference's FFT box (Miller range of the plane-wave lists)
+    int ntab;        // Nx + Ny + Nz + 3 per-axis phase factors
+};
+// One (symmetry R, full-BZ k) job: k = S1 k1, Rk = S2 k2 (irreducible k1, k2).
+struct DmatJob
+{
+    int ik1, ik2;
+    int WRS1[9];     // R S1 on Miller indices (row-major)
+    int W2inv[9];    // S2^-1 on Miller indices
+    int ulm[3];      // G0 = S2 k2 - R S1 k1 (crystal)
+    int conj_w, conj_v;
+    double tw[3], tv[3];  // plane-wave phase e^{-i 2 pi m.t} of each side (m: Miller index in the k1 list)
+    double2 Cw, Cv;       // constant phase of each side
+    double2 Mw[4], Mv[4]; // 2x2 spinor matrix of each side (row-major)
+};
+size_t lelph_dmats_smem_bytes(const DmatGeom& dg, int fp64);
+void lelph_launch_dm_gtab(const int* miller, const long long* pw_off, const int* npw, int nk, int npw_max, int Nx,
+                          int Ny, int Nz, int* gtab, cudaStream_t st);
+int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg, int fp64, const double2* coef,
+                       const long long* coef_off, const int* miller, const long long* pw_off, const int* npw,
+                       const int* gtab, double2* out, cudaStream_t st);

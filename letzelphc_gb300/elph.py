@@ -57,6 +57,7 @@ EXPORTS = [
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
     "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
+    "lelph_gpu_dmats",
 ]
 
 _lib = None
@@ -80,6 +81,7 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_dvlocq.argtypes = [vp, _dp, _dp, _dp]
     L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_rotate_dvscf.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
+    L.lelph_gpu_dmats.argtypes = [vp, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_longlong, _dp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device_noalloc.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
@@ -255,6 +257,23 @@ class LelphGPU:
         out = np.empty_like(v)
         self._check(self._L.lelph_gpu_rotate_dvscf(self.h, _ptr(q), _ptr(Rm), _ptr(t), int(time_rev), int(composite),
                                                    _ptr(v), _ptr(out)))
+        return out
+
+    def dmats(self, sym_R, sym_tau, sym_trev, first=0, count=None, host=True):
+        """Dmats of compute_and_write_dmats for the (symmetry, full-BZ k) pairs
+        first .. first + count - 1 (pair = isym * nk_BZ + ik): complex
+        (count, nspin, nb, nb), or None with ``host=False`` (the block then
+        only stays on the device)."""
+        R = np.ascontiguousarray(sym_R, dtype=np.float64).reshape(-1, 3, 3)
+        t = np.ascontiguousarray(sym_tau, dtype=np.float64).reshape(-1, 3)
+        tr = np.ascontiguousarray(np.asarray(sym_trev).astype(np.int32))
+        nsym = R.shape[0]
+        nk = self.sys.nk_bz
+        if count is None:
+            count = nsym * nk - first
+        out = np.empty((count, self.sys.nspin, self.sys.nbnds, self.sys.nbnds), np.complex128) if host else None
+        self._check(self._L.lelph_gpu_dmats(self.h, nsym, _ptr(R), _ptr(t), tr.ctypes.data_as(_ip), int(first),
+                                            int(count), _ptr(out) if host else None))
         return out
 
     def run(self, qslots, kbz, non_loc=True, kminusq=False, out=OUT_C128, g_out=None):

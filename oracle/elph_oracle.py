@@ -10,6 +10,8 @@ It restates, in numpy FP64, the reference's G-space algorithm for one q-point
 * ``elph_local``        src/dvloc/compute_Vbare_loc.c:17-353
 * ``add_elph_nonlocal`` src/nonloc/Vbare_nloc.c:35-577 (+ sum_VNL_KKp.c:8-58)
 * ``elph_q_rotate``     src/symmetries/elphq_expand.c:16-73
+* ``electronic_reps``, ``dmats`` (the Dmats that elph_driver computes before
+  the q loop): src/symmetries/elec_reps.c:16-413, src/elph/compute_dmats.c:20-131
 * ``vloc_table``, ``dvlocq``, ``add_dvscf_qe`` (the per-q local bare
   potential that elph_driver adds before the stage,
   src/elph/elph_driver.c:234-252): src/dvloc/vlocg_table.c:16-154,
@@ -433,6 +435,76 @@ def elph_q_rotate(Dl, g, Dr, tim_rev):
             tmp = A @ np.conj(Dr[isp]).T
             out[iv, isp] = tmp.T @ Dl[isp].T
     return out
+
+
+# ---------------------------------------------- electronic representations
+
+def kbz_cart(s):
+    """Cartesian full-BZ k-points as the lattice struct holds them:
+    blat k_crys / (2 pi) with the reference's pi."""
+    return s.kbz_crys @ s.blat.T / (2 * ELPH_PI)
+
+
+def electronic_reps(s, R, tauR, trevR, ikBZ):
+    """electronic_reps, src/symmetries/elec_reps.c:16-413:
+    D[spin, b, a] = <psi_{Rk, b} | U(R) | psi_{k, a}>, with Rk = S2 k2 and
+    k = S1 k1 unfolded from the irreducible wedge (kmap), the S2 k2
+    coefficients reordered onto the R S1 k1 plane-wave list (find_gvecs_idxs,
+    src/wfc/gsort.c:49-93; unmatched entries zero) and
+    D = (conj-prepared S2 k2 rows) @ (R S1 k1 rows)^T (elec_reps.c:375-392)."""
+    alat, blat = s.alat, s.blat
+    R = np.asarray(R, float)
+    kcart = kbz_cart(s)
+    Rk = mat_vec3(alat, mat_vec3(R, kcart[ikBZ]), True)                      # :35-38
+    iRk = find_kidx_in_list(s.kbz_crys, Rk)                                   # :41-49
+    if iRk < 0:
+        raise ValueError("Rotated k point not found")
+    ik1, isym1 = (int(v) for v in s.kmap[ikBZ])                               # :66-70
+    ik2, isym2 = (int(v) for v in s.kmap[iRk])
+    S1, tau1, tr1 = s.sym_R[isym1], s.sym_tau[isym1], bool(s.sym_trev[isym1])
+    S2, tau2, tr2 = s.sym_R[isym2], s.sym_tau[isym2], bool(s.sym_trev[isym2])
+    k1, k2 = s.kibz[ik1], s.kibz[ik2]
+    kcrys = mat_vec3(alat, mat_vec3(S1, k1), True)                            # :94-97
+    tcr = [mat_vec3(blat, t, True) / (2 * ELPH_PI) for t in (tau1, tauR, tau2)]  # :100-109
+    su1 = su2mat(S1, s.nspinor, False, tr1)                                   # :128-134
+    suR = su2mat(R, s.nspinor, False, trevR)
+    su2_ = su2mat(S2, s.nspinor, False, tr2)
+    RS1 = R @ S1                                                              # :146
+    RS1k1 = mat_vec3(RS1, k1)
+    ulm = mat_vec3(S2, k2) - RS1k1                                            # :149-161
+    Rkcrys = mat_vec3(alat, RS1k1, True)
+    G_S1k1 = rotate_gvecs(s.gvec[ik1], S1, alat)                              # :165-171
+    G_RS1k1 = rotate_gvecs(s.gvec[ik1], RS1, alat)
+    G_S2k2 = rotate_gvecs(s.gvec[ik2], S2, alat, ulm)
+    pos = {tuple(v): i for i, v in enumerate(np.rint(G_RS1k1).astype(np.int64))}
+    idx = np.array([pos.get(tuple(v), -1) for v in np.rint(G_S2k2).astype(np.int64)])
+    nsp, nb, ns = s.nspin, s.nbnds, s.nspinor
+    w1 = s.wfc[ik1].reshape(nsp * nb, ns, -1)
+    w2 = s.wfc[ik2].reshape(nsp * nb, ns, -1)
+    a = su2rotate(su1, w1)                                                    # :311-316
+    a = apply_trans_wfc(tcr[0], kcrys, G_S1k1, a, tr1)
+    a = su2rotate(suR, a)                                                     # :321-325
+    a = apply_trans_wfc(tcr[1], Rkcrys, G_RS1k1, a, trevR)
+    b = np.zeros_like(w1)                                                     # :331-361
+    hit = idx >= 0
+    b[:, :, idx[hit]] = w2[:, :, hit]
+    b = su2rotate(su2_, b)                                                    # :364-372
+    b = apply_trans_wfc(tcr[2], Rkcrys, G_RS1k1, b, not tr2)
+    a = a.reshape(nsp, nb, -1)
+    b = b.reshape(nsp, nb, -1)
+    return np.einsum("sbk,sak->sba", b, a)                                    # :375-392
+
+
+def dmats(s, sym_R=None, sym_tau=None, sym_trev=None, pairs=None):
+    """compute_and_write_dmats, src/elph/compute_dmats.c:20-131: D for every
+    (symmetry, full-BZ k) in (isym, ik) order, (nsym, nk, nspin, nb, nb); with
+    ``pairs`` only those (isym, ik)."""
+    sym_R = s.sym_R if sym_R is None else sym_R
+    sym_tau = s.sym_tau if sym_tau is None else sym_tau
+    sym_trev = s.sym_trev if sym_trev is None else sym_trev
+    if pairs is None:
+        pairs = [(i, k) for i in range(len(sym_R)) for k in range(len(s.kbz_crys))]
+    return np.array([electronic_reps(s, sym_R[i], sym_tau[i], bool(sym_trev[i]), k) for i, k in pairs])
 
 
 # ------------------------------------------------------- local bare potential

@@ -11,6 +11,7 @@
  * usage: lelph_ref <system.bin> <g_out.bin> [rotate <D_in.bin> <g_rot_out.bin>]
  *        lelph_ref <system.bin> <g_out.bin> dvloc <v_out.bin>
  *        lelph_ref <system.bin> <unused> rotdv <spec.bin> <dv_out.bin>
+ *        lelph_ref <system.bin> <unused> dmats <D_out.bin>
  *
  * dvloc: the system's dVscf records are the induced part (QE's dvscf); the
  * harness builds the V_loc table (create_vlocg_table, src/dvloc/vlocg_table.c)
@@ -23,6 +24,11 @@
  * rotdv: rotate_dvscf (src/symmetries/rotate_dvscf.c:22) of the spec's dV
  * (records rq, rR, rtau, rtrev, rcomp, rdv) on the system's lattice; the
  * matrix elements are not computed.
+ *
+ * dmats: electronic_reps (src/symmetries/elec_reps.c:16) for every symmetry of
+ * the system and every full-BZ k, in the order of compute_and_write_dmats
+ * (src/elph/compute_dmats.c:99-118); D_out.bin is complex128
+ * (nsym, nk_BZ, nspin, nb, nb).  The matrix elements are not computed.
  *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
@@ -269,6 +275,23 @@ int main(int argc, char** argv)
         if (!fr) die("cannot write rotdv output");
         fwrite(out, 1, din->nbytes, fr);
         fclose(fr);
+        return 0;
+    }
+    if (argc >= 5 && !strcmp(argv[3], "dmats"))
+    {
+        /* every (symmetry, full-BZ k) Dmat, in compute_and_write_dmats' order */
+        size_t ds = (size_t)nspin * nbnds * nbnds;
+        double _Complex* D = malloc(sizeof(double _Complex) * ds);
+        FILE* fd = fopen(argv[4], "wb");
+        if (!D || !fd) die("cannot write dmats output");
+        for (int is = 0; is < nsym; ++is)
+            for (int ik = 0; ik < nkbz; ++ik)
+            {
+                electronic_reps(wfcs, &lat, lat.syms[is].Rmat, lat.syms[is].tau, lat.syms[is].time_rev, ik, D,
+                                &comm);
+                fwrite(D, sizeof(double _Complex), ds, fd);
+            }
+        fclose(fd);
         return 0;
     }
     g_slice = (size_t)nmodes * nspin * nbnds * nbnds;

@@ -8,10 +8,13 @@ produced for it, run through oracle/_ref/lelph_ref (oracle/Makefile).
 A second fixture pins elph_q_rotate (src/symmetries/elphq_expand.c:16), and
 the dvloc_* fixtures pin the local bare potential added per q before the
 stage (create_vlocg_table / dVlocq / add_dvscf_qe, src/dvloc/), with the
-matrix elements computed from the summed dV.
+matrix elements computed from the summed dV; rotate_dvscf.npz pins
+rotate_dvscf and dmats.npz the electronic representation matrices
+(electronic_reps, src/symmetries/elec_reps.c:16).
 
 Run from the repo root after ``make -C oracle``:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            (every fixture)
+    python tests/golden/make_golden.py dmats      (only dmats.npz)
 """
 import json
 import os
@@ -176,11 +179,47 @@ def rotate_fixture(tmp):
     print("q_rotate", g.shape)
 
 
+# Dmats (electronic_reps, src/symmetries/elec_reps.c:16, for every symmetry
+# of the system and every full-BZ k): name -> (base config, overrides)
+DMATS_SYS = {
+    "c0": ("c0", {"kgrid": (2, 2, 2), "nbnds": 4}),
+    "zb_tr": ("c0", {"kind": "zincblende", "timerev": True, "nbnds": 3, "kgrid": (2, 2, 2)}),
+    "l12": ("c1", {"nbnds": 4, "kgrid": (2, 2, 2), "npw": 300, "fft": (24, 24, 24), "qpts": [(0.5, 0, 0)]}),
+    "soc_tr": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True,
+                      "ls": (0, 1, 2), "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (2, 2, 2),
+                      "qpts": [(0.5, 0.5, 0)]}),
+    "lsda": ("c0", {"nspin": 2, "nbnds": 3, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}),
+    "hex_ragged": ("c2", {"kgrid": (3, 3, 1), "fft": (15, 15, 60), "nbnds": 3, "npw": (80, 120),
+                          "qpts": [(1 / 3, 0, 0)]}),
+}
+DMATS_STRIDE = 3  # every third (symmetry, k) pair is stored whole; the norms of all of them
+
+
+def dmats_fixture(tmp):
+    rec = {}
+    for name, (base, ov) in DMATS_SYS.items():
+        s = synth.make_system(base, dict(ov))
+        sysf = os.path.join(tmp, "dm_" + name + ".bin")
+        synth.write_system(s, sysf)
+        out_f = os.path.join(tmp, "dm_out.bin")
+        subprocess.run([REF, sysf, os.path.join(tmp, "unused.bin"), "dmats", out_f], check=True)
+        D = np.fromfile(out_f, np.complex128).reshape(len(s.sym_R) * s.nk_bz, s.nspin, s.nbnds, s.nbnds)
+        rec[name + "_sub"] = D[::DMATS_STRIDE]
+        rec[name + "_norm"] = np.linalg.norm(D.reshape(len(D), -1), axis=1)
+        print("dmats", name, D.shape, float(np.abs(D).max()))
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "dmats.npz"), systems=np.array(json.dumps(DMATS_SYS)),
+                        stride=np.array(DMATS_STRIDE), **rec)
+
+
 if __name__ == "__main__":
+    only = sys.argv[1:]
     with tempfile.TemporaryDirectory() as tmp:
-        for name, (base, ov, kmq, nl) in GOLDEN.items():
-            run(name, base, ov, kmq, nl, tmp)
-        for name, (base, ov, kmq, nl) in GOLDEN_DVLOC.items():
-            run_dvloc(name, base, ov, kmq, nl, tmp)
-        rotate_fixture(tmp)
-        rotdv_fixture(tmp)
+        if not only:
+            for name, (base, ov, kmq, nl) in GOLDEN.items():
+                run(name, base, ov, kmq, nl, tmp)
+            for name, (base, ov, kmq, nl) in GOLDEN_DVLOC.items():
+                run_dvloc(name, base, ov, kmq, nl, tmp)
+            rotate_fixture(tmp)
+            rotdv_fixture(tmp)
+        if not only or "dmats" in only:
+            dmats_fixture(tmp)

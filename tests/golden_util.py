@@ -31,3 +31,18 @@ def load_dvloc(name):
     z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
     s, _, _, _ = load(name)
     return s, z
+
+
+def load_dmats():
+    """(npz, {name: System}) of tests/golden/dmats.npz: D of the reference's
+    electronic_reps for every (symmetry, full-BZ k) pair of each system,
+    every ``stride``-th pair stored whole and the norms of all of them."""
+    import json
+    from letzelphc_gb300 import synth
+    z = np.load(os.path.join(GOLDEN_DIR, "dmats.npz"))
+    systems = {}
+    for name, (base, ov) in json.loads(str(z["systems"])).items():
+        ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls", "npw") else v)
+              for k, v in ov.items()}
+        systems[name] = synth.make_system(base, ov)
+    return z, systems

@@ -85,3 +85,19 @@ def test_rotate_dvscf_matches_reference():
         smp = z[key + "_sample"]
         assert np.abs(out.reshape(-1)[::97] - smp).max() < 1e-12 * np.abs(smp).max(), key
         assert abs(np.linalg.norm(out) - float(z[key + "_norm"])) < 1e-12 * float(z[key + "_norm"])
+
+
+def test_dmats_match_reference():
+    """electronic_reps (src/symmetries/elec_reps.c:16-413) for every
+    (symmetry, full-BZ k) pair: stored pairs to 1e-12, norms of all pairs to
+    1e-12; the systems cover time reversal, fractional translations, spinors,
+    two spins and k-points with different plane-wave spheres."""
+    from golden_util import load_dmats
+    z, systems = load_dmats()
+    st = int(z["stride"])
+    for name, s in systems.items():
+        D = O.dmats(s).reshape(-1, s.nspin, s.nbnds, s.nbnds)
+        ref = z[name + "_sub"]
+        assert np.abs(D[::st] - ref).max() < 1e-12, name
+        nrm = np.linalg.norm(D.reshape(len(D), -1), axis=1)
+        assert np.abs(nrm - z[name + "_norm"]).max() < 1e-12, name
