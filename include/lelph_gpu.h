@@ -94,6 +94,9 @@ typedef struct lelph_gpu_stats
     size_t device_bytes;         /* device memory held by the context */
     int product_grid[3];         /* grid of the real-space sandwich and wavefunction FFTs */
     int chunk_points;            /* grid points per K chunk of the tensor-core sandwich (mixed form) */
+    double dmats_ms;             /* device time of the Dmat kernels (index maps + contraction, profiling on) */
+    double dmats_host_ms;        /* host time spent building Dmat jobs (always measured) */
+    long long dmats_done;        /* Dmats computed */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

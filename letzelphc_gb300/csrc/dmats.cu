@@ -10,17 +10,21 @@
 // coefficient whose Miller index is W2^-1 (W_RS1 m - G0), G0 = S2 k2 - R S1 k1,
 // looked up in a per-k Miller -> position table of the FFT box and checked
 // (absent: zero), which is the reference's find_gvecs_idxs match
-// (src/wfc/gsort.c:49-93) read from the other side.  The SU(2) factors,
-// fractional-translation phases and conjugations of the reference's sequence
-// (elec_reps.c:301-372) fold per job into one 2x2 spinor matrix, one conjugation
-// flag, one constant phase and one phase vector t; the plane-wave phase
-// e^{-i 2 pi m.t} is the product of three per-axis factors tabulated per job.
-// D is then one complex contraction over (spinor, plane wave), tiled 32 x 32
-// and four-by-four per thread, with the operands staged in shared memory.
+// (src/wfc/gsort.c:49-93) read from the other side; a first kernel writes
+// these maps for every job.  The SU(2) factors, fractional-translation phases
+// and conjugations of the reference's sequence (elec_reps.c:301-372) fold per
+// job onto the k2 side: D = sum_p v(p) . psi_k1(p)^(c) with
+// v = C e^{-i 2 pi m.t} M psi_k2^(c'), so the k1 rows are staged into shared
+// memory unchanged by asynchronous copies (double-buffered, one chunk ahead)
+// and only the gathered k2 rows are transformed; the plane-wave phase is the
+// product of three per-axis factors tabulated per job.  D is one complex
+// contraction over (spinor, plane wave), tiled 32 x 32 and four-by-four per
+// thread.
 //
 // Plain form: FP64 throughout.  Mixed form: the per-axis phase angles are
-// reduced in FP64, the operands and the contraction are FP32, and the FP32
-// partial sums are flushed into FP64 accumulators every DM_GROUP chunks.
+// reduced in FP64, operands and contraction are FP32 (an FP32 copy of the
+// coefficients), with partial sums over DM_GROUP chunks added into a second
+// FP32 accumulator (pairwise summation).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -30,17 +34,9 @@
 #define DM_TB 32       // D tile (bands) per CTA, both sides
 #define DM_KC 32       // plane waves per staged chunk
 #define DM_THREADS 64  // 8 x 8 threads, 4 x 4 complex entries of the tile each
-#define DM_GROUP 16    // chunks summed in FP32 before the FP64 flush (mixed form)
+#define DM_GROUP 16    // chunks per partial sum (mixed form)
 
-// element (kk, col) of a staged operand: 16-byte pairs of columns XOR-swizzled by kk
-__device__ __forceinline__ int dm_idx(int kk, int col)
-{
-    return kk * DM_TB + ((((col >> 1) ^ (kk & 15)) << 1) | (col & 1));
-}
-
-template <typename T2> struct DmReal;
-template <> struct DmReal<float2> { typedef float type; };
-template <> struct DmReal<double2> { typedef double type; };
+#define DM_TBP 34      // staged row stride (complex): 16-byte aligned rows, 2-way conflicts on the column writes
 
 // e^{-i 2 pi_T x} for a per-axis angle x (in turns): the reduction to
 // [-1/2, 1/2] is FP64, the evaluation in the operand type.
@@ -79,217 +75,278 @@ template <> __device__ __forceinline__ void dm_ld_pair<double2>(const double2* p
     b = p[1];
 }
 
-template <typename T2> __device__ __forceinline__ void dm_cfma(T2& acc, T2 v, T2 w)
+template <int B> __device__ __forceinline__ void dm_cp(uint32_t dst, const void* src, int src_bytes);
+template <> __device__ __forceinline__ void dm_cp<8>(uint32_t dst, const void* src, int src_bytes)
 {
-    acc.x = fma(v.x, w.x, acc.x);
-    acc.x = fma(-v.y, w.y, acc.x);
-    acc.y = fma(v.x, w.y, acc.y);
-    acc.y = fma(v.y, w.x, acc.y);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+template <> __device__ __forceinline__ void dm_cp<16>(uint32_t dst, const void* src, int src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void dm_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void dm_cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// acc += v w (CJ: acc += v conj(w))
+template <bool CJ, typename T2> __device__ __forceinline__ void dm_cfma(T2& acc, T2 v, T2 w)
+{
+    if (CJ)
+    {
+        acc.x = fma(v.x, w.x, acc.x);
+        acc.x = fma(v.y, w.y, acc.x);
+        acc.y = fma(v.y, w.x, acc.y);
+        acc.y = fma(-v.x, w.y, acc.y);
+    }
+    else
+    {
+        acc.x = fma(v.x, w.x, acc.x);
+        acc.x = fma(-v.y, w.y, acc.x);
+        acc.y = fma(v.x, w.y, acc.y);
+        acc.y = fma(v.y, w.x, acc.y);
+    }
 }
 
-// Stage one operand row segment: coefficient(s) x of band row `row` at
-// position j, conjugated if asked, spinor-mixed by M, times the position's
-// phase c, into the shared tile.
-template <typename T2>
-__device__ __forceinline__ void dm_stage(T2* tile, int j, int r, int ns, const double2* x, bool cj, const T2* M, T2 c)
+// k2 position of every plane wave of the k1 list, per job (-1: not in the k2
+// list): the reference's find_gvecs_idxs match read from the k1 side.
+__global__ void __launch_bounds__(256) k_dm_map(const DmatJob* __restrict__ jobs, DmatGeom dg,
+                                                const int* __restrict__ miller, const long long* __restrict__ pw_off,
+                                                const int* __restrict__ npw_arr, const int* __restrict__ gtab,
+                                                int stride, int* __restrict__ map)
 {
-    T2 y0 = dm_cvt<T2>(x[0]), y1 = dm_cvt<T2>(x[1]);
-    if (cj)
-    {
-        y0 = cconj(y0);
-        y1 = cconj(y1);
-    }
-    if (ns == 2)
-    {
-        const T2 z0 = cadd(cmul(M[0], y0), cmul(M[1], y1));
-        const T2 z1 = cadd(cmul(M[2], y0), cmul(M[3], y1));
-        tile[dm_idx(DM_KC + j, r)] = cmul(z1, c);
-        y0 = z0;
-    }
-    tile[dm_idx(j, r)] = cmul(y0, c);
-}
-
-template <typename T2>
-__global__ void __launch_bounds__(DM_THREADS) k_dmats(const DmatJob* __restrict__ jobs, DmatGeom dg,
-                                                      const double2* __restrict__ coef,
-                                                      const long long* __restrict__ coef_off,
-                                                      const int* __restrict__ miller,
-                                                      const long long* __restrict__ pw_off,
-                                                      const int* __restrict__ npw_arr, const int* __restrict__ gtab,
-                                                      double2* __restrict__ out)
-{
-    extern __shared__ __align__(16) unsigned char dm_smem[];
-    const int ns = dg.nspinor, nb = dg.nb;
-    const int KCS = ns * DM_KC;
-    T2* sv = reinterpret_cast<T2*>(dm_smem);
-    T2* sw = sv + KCS * DM_TB;
-    T2* tabw = sw + KCS * DM_TB;               // per-axis phase factors, (Nx+1) + (Ny+1) + (Nz+1)
-    T2* tabv = tabw + dg.ntab;
-    T2* scw = tabv + dg.ntab;                  // per-position phases of the chunk
-    T2* scv = scw + DM_KC;
-    int* sii = reinterpret_cast<int*>(scv + DM_KC);  // k2 position of each k1 plane wave (-1: absent)
     __shared__ DmatJob J;
-
-    const int t = threadIdx.x;
     const long long ijob = blockIdx.x;
-    const int ntile = (nb + DM_TB - 1) / DM_TB;
-    const int b0 = (blockIdx.y / ntile) * DM_TB, a0 = (blockIdx.y % ntile) * DM_TB;
-    const int spin = blockIdx.z;
-    if (t == 0) J = jobs[ijob];
+    if (threadIdx.x == 0) J = jobs[ijob];
     __syncthreads();
-
-    // per-axis phase tables over the box's Miller range [-N/2, N/2]
-    const int Nax[3] = {dg.Nx, dg.Ny, dg.Nz};
-    {
-        int base = 0;
-        for (int ax = 0; ax < 3; ++ax)
-        {
-            for (int i = t; i <= Nax[ax]; i += DM_THREADS)
-            {
-                const double m = (double)(i - Nax[ax] / 2);
-                tabw[base + i] = dm_phase<T2>(m * J.tw[ax]);
-                tabv[base + i] = dm_phase<T2>(m * J.tv[ax]);
-            }
-            base += Nax[ax] + 1;
-        }
-    }
-    T2 Mw[4], Mv[4];
+    const int p = blockIdx.y * blockDim.x + threadIdx.x;
+    const int npw1 = npw_arr[J.ik1];
+    if (p >= npw1) return;
+    const int npw2 = npw_arr[J.ik2];
+    const int* m = miller + 3 * (pw_off[J.ik1] + p);
+    const int* mil2 = miller + 3 * pw_off[J.ik2];
+    int g[3], n[3];
 #pragma unroll
-    for (int e = 0; e < 4; ++e)
+    for (int r = 0; r < 3; ++r) g[r] = J.WRS1[3 * r] * m[0] + J.WRS1[3 * r + 1] * m[1] + J.WRS1[3 * r + 2] * m[2] - J.ulm[r];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) n[r] = J.W2inv[3 * r] * g[0] + J.W2inv[3 * r + 1] * g[1] + J.W2inv[3 * r + 2] * g[2];
+    const int bx = ((n[0] % dg.Nx) + dg.Nx) % dg.Nx, by = ((n[1] % dg.Ny) + dg.Ny) % dg.Ny,
+              bz = ((n[2] % dg.Nz) + dg.Nz) % dg.Nz;
+    const int cand = gtab[(long long)J.ik2 * dg.Nx * dg.Ny * dg.Nz + ((long long)bx * dg.Ny + by) * dg.Nz + bz];
+    int ii = -1;
+    if (cand >= 0 && cand < npw2)
     {
-        Mw[e] = dm_cvt<T2>(J.Mw[e]);
-        Mv[e] = dm_cvt<T2>(J.Mv[e]);
+        const int* mc = mil2 + 3 * cand;
+        if (mc[0] == n[0] && mc[1] == n[1] && mc[2] == n[2]) ii = cand;
     }
-    const T2 Cw = dm_cvt<T2>(J.Cw), Cv = dm_cvt<T2>(J.Cv);
+    map[ijob * stride + p] = ii;
+}
+
+// The contraction of one job (CJ: the k1 operand enters conjugated).
+template <typename T2, int NS, bool CJ>
+__device__ __forceinline__ void dm_body(const DmatJob& J, const DmatGeom& dg, const T2* __restrict__ coef,
+                                        const long long* __restrict__ coef_off, const int* __restrict__ miller,
+                                        const long long* __restrict__ pw_off, const int* __restrict__ npw_arr,
+                                        const int* __restrict__ jmap, int spin, int b0, int a0, T2* sv, T2* sw,
+                                        const T2* tab, T2* sc, int* sii, double2* __restrict__ D)
+{
+    constexpr bool F32 = sizeof(T2) == sizeof(float2);
+    constexpr int KCS = NS * DM_KC;
+    constexpr int RB = 8 / NS;  // rows loaded per batch by each thread
+    const int t = threadIdx.x;
+    const int nb = dg.nb;
+    T2 M[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) M[e] = dm_cvt<T2>(J.M[e]);
+    const bool cjv = J.conj_v != 0;
+    const T2 C = dm_cvt<T2>(J.C);
     const int npw1 = npw_arr[J.ik1], npw2 = npw_arr[J.ik2];
     const int* mil1 = miller + 3 * pw_off[J.ik1];
-    const int* mil2 = miller + 3 * pw_off[J.ik2];
-    const double2* c1 = coef + coef_off[J.ik1] + (long long)spin * nb * ns * npw1;
-    const double2* c2 = coef + coef_off[J.ik2] + (long long)spin * nb * ns * npw2;
-    const long long Nbox = (long long)dg.Nx * dg.Ny * dg.Nz;
-    const int* tab2 = gtab + (long long)J.ik2 * Nbox;
+    const T2* c1 = coef + coef_off[J.ik1] + (long long)spin * nb * NS * npw1;
+    const T2* c2 = coef + coef_off[J.ik2] + (long long)spin * nb * NS * npw2;
     const int oy = dg.Nx + 1, oz = dg.Nx + dg.Ny + 2;
-
     const int rb = t >> 3, ca = t & 7;
-    T2 acc[4][4];
-    double2 accd[4][4];
+    const int j = t & (DM_KC - 1), r0 = t >> 5;
+    const uint32_t sw0 = smem_u32(sw);
+
+    // the k1 rows of chunk c, copied as they are into w buffer c & 1
+    auto issue_w = [&](int c) {
+        const int p = c * DM_KC + j;
+        const uint32_t base = sw0 + (uint32_t)((c & 1) * KCS * DM_TBP * sizeof(T2));
+#pragma unroll
+        for (int i = 0; i < DM_TB / 2; ++i)
+        {
+            const int r = r0 + 2 * i, a = a0 + r;
+            const bool ok = a < nb && p < npw1;
+#pragma unroll
+            for (int s = 0; s < NS; ++s)
+                dm_cp<sizeof(T2)>(base + (uint32_t)(((s * DM_KC + j) * DM_TBP + r) * sizeof(T2)),
+                                  ok ? (const void*)(c1 + ((long long)a * NS + s) * npw1 + p) : (const void*)c1,
+                                  ok ? (int)sizeof(T2) : 0);
+        }
+    };
+
+    T2 acc[4][4], acc2[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-        {
-            acc[i][j] = mk2<T2>(0.0, 0.0);
-            accd[i][j] = make_double2(0.0, 0.0);
-        }
+        for (int k = 0; k < 4; ++k) acc[i][k] = acc2[i][k] = mk2<T2>(0.0, 0.0);
+
+    // per-position data of the next chunk, prefetched one chunk ahead
+    int pm[3] = {0, 0, 0}, pii = -1;
+    if (t < DM_KC && t < npw1)
+    {
+        pm[0] = mil1[3 * t];
+        pm[1] = mil1[3 * t + 1];
+        pm[2] = mil1[3 * t + 2];
+        pii = jmap[t];
+    }
+    issue_w(0);
+    dm_cp_commit();
 
     const int nchunk = (npw1 + DM_KC - 1) / DM_KC;
     for (int ch = 0; ch < nchunk; ++ch)
     {
         const int p0 = ch * DM_KC;
-        __syncthreads();  // previous chunk's contraction is done with the tiles
         if (t < DM_KC)
         {
-            // right operand phase of plane wave p (k1 list, Miller m)
-            const int p = p0 + t;
             T2 c = mk2<T2>(0.0, 0.0);
-            if (p < npw1)
+            const bool in = p0 + t < npw1;
+            if (in && pii >= 0)
             {
-                const int* m = mil1 + 3 * p;
-                c = cmul(cmul(tabw[m[0] + dg.Nx / 2], tabw[oy + m[1] + dg.Ny / 2]), tabw[oz + m[2] + dg.Nz / 2]);
-                c = cmul(c, Cw);
+                c = cmul(cmul(tab[pm[0] + dg.Nx / 2], tab[oy + pm[1] + dg.Ny / 2]), tab[oz + pm[2] + dg.Nz / 2]);
+                c = cmul(c, C);
             }
-            scw[t] = c;
-        }
-        else
-        {
-            // left operand: the k2 plane wave landing on p, and its phase
-            const int j = t - DM_KC, p = p0 + j;
-            T2 c = mk2<T2>(0.0, 0.0);
-            int ii = -1;
-            if (p < npw1)
+            sc[t] = c;
+            sii[t] = in ? pii : -1;
+            const int pn = p0 + DM_KC + t;
+            if (pn < npw1)
             {
-                const int* m = mil1 + 3 * p;
-                int g[3], n[3];
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    g[r] = J.WRS1[3 * r] * m[0] + J.WRS1[3 * r + 1] * m[1] + J.WRS1[3 * r + 2] * m[2] - J.ulm[r];
-#pragma unroll
-                for (int r = 0; r < 3; ++r) n[r] = J.W2inv[3 * r] * g[0] + J.W2inv[3 * r + 1] * g[1] + J.W2inv[3 * r + 2] * g[2];
-                const int bx = ((n[0] % dg.Nx) + dg.Nx) % dg.Nx, by = ((n[1] % dg.Ny) + dg.Ny) % dg.Ny,
-                          bz = ((n[2] % dg.Nz) + dg.Nz) % dg.Nz;
-                const int cand = tab2[((long long)bx * dg.Ny + by) * dg.Nz + bz];
-                if (cand >= 0 && cand < npw2)
-                {
-                    const int* mc = mil2 + 3 * cand;
-                    if (mc[0] == n[0] && mc[1] == n[1] && mc[2] == n[2]) ii = cand;
-                }
-                if (ii >= 0)
-                {
-                    c = cmul(cmul(tabv[m[0] + dg.Nx / 2], tabv[oy + m[1] + dg.Ny / 2]), tabv[oz + m[2] + dg.Nz / 2]);
-                    c = cmul(c, Cv);
-                }
+                pm[0] = mil1[3 * pn];
+                pm[1] = mil1[3 * pn + 1];
+                pm[2] = mil1[3 * pn + 2];
+                pii = jmap[pn];
             }
-            sii[j] = ii;
-            scv[j] = c;
         }
-        __syncthreads();
+        __syncthreads();  // positions of this chunk visible; the previous contraction is done
+        if (ch + 1 < nchunk) issue_w(ch + 1);
+        dm_cp_commit();
         {
-            const int j = t & (DM_KC - 1);
-            const int p = p0 + j;
+            // k2 rows: gathered, conjugated if asked, spinor-mixed, times the phase
             const int ii = sii[j];
-            const T2 cw = scw[j], cv = scv[j];
-            for (int r = t >> 5; r < DM_TB; r += DM_THREADS / DM_KC)
+            const T2 c = sc[j];
+#pragma unroll
+            for (int bt = 0; bt < (DM_TB / 2) / RB; ++bt)
             {
-                double2 x[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
-                const int a = a0 + r;
-                if (a < nb && p < npw1)
-                    for (int s = 0; s < ns; ++s) x[s] = c1[((long long)a * ns + s) * npw1 + p];
-                dm_stage<T2>(sw, j, r, ns, x, J.conj_w != 0, Mw, cw);
-                x[0] = x[1] = make_double2(0.0, 0.0);
-                const int b = b0 + r;
-                if (b < nb && ii >= 0)
-                    for (int s = 0; s < ns; ++s) x[s] = c2[((long long)b * ns + s) * npw2 + ii];
-                dm_stage<T2>(sv, j, r, ns, x, J.conj_v != 0, Mv, cv);
+                T2 x[RB][NS];
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                {
+                    const int b = b0 + r0 + 2 * (bt * RB + i);
+#pragma unroll
+                    for (int s = 0; s < NS; ++s)
+                        x[i][s] = (b < nb && ii >= 0) ? c2[((long long)b * NS + s) * npw2 + ii] : mk2<T2>(0.0, 0.0);
+                }
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                {
+                    const int r = r0 + 2 * (bt * RB + i);
+                    T2 y0 = x[i][0];
+                    if (cjv) y0 = cconj(y0);
+                    if (NS == 2)
+                    {
+                        T2 y1 = x[i][NS - 1];
+                        if (cjv) y1 = cconj(y1);
+                        const T2 z0 = cadd(cmul(M[0], y0), cmul(M[1], y1));
+                        const T2 z1 = cadd(cmul(M[2], y0), cmul(M[3], y1));
+                        sv[(DM_KC + j) * DM_TBP + r] = cmul(z1, c);
+                        y0 = z0;
+                    }
+                    sv[j * DM_TBP + r] = cmul(y0, c);
+                }
             }
         }
+        dm_cp_wait1();    // this chunk's k1 rows have landed (the next chunk's may be in flight)
         __syncthreads();
+        const T2* wb = sw + (ch & 1) * KCS * DM_TBP;
+#pragma unroll 8
         for (int kk = 0; kk < KCS; ++kk)
         {
             T2 v[4], w[4];
-            dm_ld_pair<T2>(sv + dm_idx(kk, 4 * rb), v[0], v[1]);
-            dm_ld_pair<T2>(sv + dm_idx(kk, 4 * rb + 2), v[2], v[3]);
-            dm_ld_pair<T2>(sw + dm_idx(kk, 4 * ca), w[0], w[1]);
-            dm_ld_pair<T2>(sw + dm_idx(kk, 4 * ca + 2), w[2], w[3]);
+            dm_ld_pair<T2>(sv + kk * DM_TBP + 4 * rb, v[0], v[1]);
+            dm_ld_pair<T2>(sv + kk * DM_TBP + 4 * rb + 2, v[2], v[3]);
+            dm_ld_pair<T2>(wb + kk * DM_TBP + 4 * ca, w[0], w[1]);
+            dm_ld_pair<T2>(wb + kk * DM_TBP + 4 * ca + 2, w[2], w[3]);
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) dm_cfma(acc[i][j], v[i], w[j]);
+                for (int k = 0; k < 4; ++k) dm_cfma<CJ>(acc[i][k], v[i], w[k]);
         }
-        if (sizeof(T2) == sizeof(float2) && ((ch + 1) % DM_GROUP == 0 || ch + 1 == nchunk))
+        if (F32 && ((ch + 1) % DM_GROUP == 0 || ch + 1 == nchunk))
         {
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
+                for (int k = 0; k < 4; ++k)
                 {
-                    accd[i][j].x += (double)acc[i][j].x;
-                    accd[i][j].y += (double)acc[i][j].y;
-                    acc[i][j] = mk2<T2>(0.0, 0.0);
+                    acc2[i][k] = cadd(acc2[i][k], acc[i][k]);
+                    acc[i][k] = mk2<T2>(0.0, 0.0);
                 }
         }
     }
-    double2* D = out + (ijob * dg.nspin + spin) * (long long)nb * nb;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 4; ++k)
         {
-            const int b = b0 + 4 * rb + i, a = a0 + 4 * ca + j;
-            if (b < nb && a < nb)
-                D[(long long)b * nb + a] = sizeof(T2) == sizeof(float2)
-                                               ? accd[i][j]
-                                               : make_double2((double)acc[i][j].x, (double)acc[i][j].y);
+            const int b = b0 + 4 * rb + i, a = a0 + 4 * ca + k;
+            const T2 r = F32 ? acc2[i][k] : acc[i][k];
+            if (b < nb && a < nb) D[(long long)b * nb + a] = make_double2((double)r.x, (double)r.y);
         }
+}
+
+template <typename T2, int NS>
+__global__ void __launch_bounds__(DM_THREADS, 8) k_dmats(const DmatJob* __restrict__ jobs, DmatGeom dg,
+                                                         const T2* __restrict__ coef,
+                                                         const long long* __restrict__ coef_off,
+                                                         const int* __restrict__ miller,
+                                                         const long long* __restrict__ pw_off,
+                                                         const int* __restrict__ npw_arr, const int* __restrict__ map,
+                                                         int stride, double2* __restrict__ out)
+{
+    constexpr int KCS = NS * DM_KC;
+    extern __shared__ __align__(16) unsigned char dm_smem[];
+    T2* sv = reinterpret_cast<T2*>(dm_smem);
+    T2* sw = sv + KCS * DM_TBP;        // two buffers
+    T2* tab = sw + 2 * KCS * DM_TBP;   // per-axis phase factors, (Nx+1) + (Ny+1) + (Nz+1)
+    T2* sc = tab + dg.ntab;            // per-position phases of the chunk
+    int* sii = reinterpret_cast<int*>(sc + DM_KC);
+    __shared__ DmatJob J;
+
+    const int t = threadIdx.x;
+    const long long ijob = blockIdx.x;
+    const int ntile = (dg.nb + DM_TB - 1) / DM_TB;
+    const int b0 = (blockIdx.y / ntile) * DM_TB, a0 = (blockIdx.y % ntile) * DM_TB;
+    const int spin = blockIdx.z;
+    if (t == 0) J = jobs[ijob];
+    __syncthreads();
+    {
+        const int Nax[3] = {dg.Nx, dg.Ny, dg.Nz};
+        int base = 0;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+        {
+            for (int i = t; i <= Nax[ax]; i += DM_THREADS) tab[base + i] = dm_phase<T2>((double)(i - Nax[ax] / 2) * J.t[ax]);
+            base += Nax[ax] + 1;
+        }
+    }
+    // (the tables are published by the first __syncthreads of the chunk loop)
+    double2* D = out + (ijob * dg.nspin + spin) * (long long)dg.nb * dg.nb;
+    const int* jmap = map + ijob * stride;
+    if (J.conj_w)
+        dm_body<T2, NS, true>(J, dg, coef, coef_off, miller, pw_off, npw_arr, jmap, spin, b0, a0, sv, sw, tab, sc,
+                              sii, D);
+    else
+        dm_body<T2, NS, false>(J, dg, coef, coef_off, miller, pw_off, npw_arr, jmap, spin, b0, a0, sv, sw, tab, sc,
+                               sii, D);
 }
 
 // Miller -> position table of every iBZ plane-wave list on the FFT box
@@ -313,7 +370,7 @@ __global__ void k_dm_gtab(const int* __restrict__ miller, const long long* __res
 size_t lelph_dmats_smem_bytes(const DmatGeom& dg, int fp64)
 {
     const size_t e = fp64 ? sizeof(double2) : sizeof(float2);
-    return e * (2 * (size_t)dg.nspinor * DM_KC * DM_TB + 2 * (size_t)dg.ntab + 2 * DM_KC) + sizeof(int) * DM_KC;
+    return e * (3 * (size_t)dg.nspinor * DM_KC * DM_TBP + (size_t)dg.ntab + DM_KC) + sizeof(int) * DM_KC;
 }
 
 void lelph_launch_dm_gtab(const int* miller, const long long* pw_off, const int* npw, int nk, int npw_max, int Nx,
@@ -323,26 +380,52 @@ void lelph_launch_dm_gtab(const int* miller, const long long* pw_off, const int*
     k_dm_gtab<<<grid, 256, 0, st>>>(miller, pw_off, npw, nk, Nx, Ny, Nz, gtab);
 }
 
-int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg, int fp64, const double2* coef,
+// FP32 copy of the iBZ coefficients (the mixed form's operands)
+__global__ void k_dm_c64(const double2* __restrict__ in, long long n, float2* __restrict__ out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+void lelph_launch_dm_c64(const double2* in, long long n, float2* out, cudaStream_t st)
+{
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (blocks < 1) blocks = 1;
+    k_dm_c64<<<(unsigned)blocks, 256, 0, st>>>(in, n, out);
+}
+
+template <typename T2, int NS>
+static int launch_dm(dim3 grid, size_t smem, cudaStream_t st, const DmatJob* jobs, const DmatGeom& dg,
+                     const T2* coef, const long long* coef_off, const int* miller, const long long* pw_off,
+                     const int* npw, const int* map, int stride, double2* out)
+{
+    if (cudaFuncSetAttribute(k_dmats<T2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    k_dmats<T2, NS><<<grid, DM_THREADS, smem, st>>>(jobs, dg, coef, coef_off, miller, pw_off, npw, map, stride, out);
+    return 0;
+}
+
+int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg, const double2* coef64,
+                       const float2* coef32,
                        const long long* coef_off, const int* miller, const long long* pw_off, const int* npw,
-                       const int* gtab, double2* out, cudaStream_t st)
+                       const int* gtab, int npw_max, int* map, double2* out, cudaStream_t st)
 {
     if (njobs <= 0) return 0;
-    if (njobs > 0x7fffffffLL) return -1;
+    if (njobs > 0x7fffffffLL || npw_max <= 0) return -1;
+    // index maps first (one thread per (job, plane wave)), then the contraction
+    dim3 mgrid((unsigned)njobs, (unsigned)((npw_max + 255) / 256));
+    k_dm_map<<<mgrid, 256, 0, st>>>(jobs, dg, miller, pw_off, npw, gtab, npw_max, map);
     const int ntile = (dg.nb + DM_TB - 1) / DM_TB;
-    const size_t smem = lelph_dmats_smem_bytes(dg, fp64);
+    const size_t smem = lelph_dmats_smem_bytes(dg, coef32 ? 0 : 1);
     dim3 grid((unsigned)njobs, (unsigned)(ntile * ntile), (unsigned)dg.nspin);
-    if (fp64)
-    {
-        if (cudaFuncSetAttribute(k_dmats<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return -1;
-        k_dmats<double2><<<grid, DM_THREADS, smem, st>>>(jobs, dg, coef, coef_off, miller, pw_off, npw, gtab, out);
-    }
-    else
-    {
-        if (cudaFuncSetAttribute(k_dmats<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return -1;
-        k_dmats<float2><<<grid, DM_THREADS, smem, st>>>(jobs, dg, coef, coef_off, miller, pw_off, npw, gtab, out);
-    }
-    return 0;
+    if (!coef32)
+        return dg.nspinor == 2 ? launch_dm<double2, 2>(grid, smem, st, jobs, dg, coef64, coef_off, miller, pw_off,
+                                                       npw, map, npw_max, out)
+                               : launch_dm<double2, 1>(grid, smem, st, jobs, dg, coef64, coef_off, miller, pw_off,
+                                                       npw, map, npw_max, out);
+    return dg.nspinor == 2 ? launch_dm<float2, 2>(grid, smem, st, jobs, dg, coef32, coef_off, miller, pw_off, npw,
+                                                  map, npw_max, out)
+                           : launch_dm<float2, 1>(grid, smem, st, jobs, dg, coef32, coef_off, miller, pw_off, npw,
+                                                  map, npw_max, out);
 }

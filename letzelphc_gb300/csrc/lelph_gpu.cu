@@ -9,6 +9,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -16,6 +17,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/lelph_gpu.h"
@@ -92,7 +95,10 @@ struct lelph_gpu
     DevBuf d_colmask;  // box occupancy of a chunk of k-points (z-columns, then x planes)
     // Dmats: Miller -> position tables of the iBZ lists, the job table and the
     // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
-    DevBuf d_dmgtab, d_dmjobs, d_dmats;
+    DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32;
+    bool dm_coef32_ready = false;
+    long long coef_total = 0;  // complex coefficients of every iBZ k
+    std::unordered_map<long long, int> khash;  // full-BZ k-points by wrapped, quantised coordinates
     bool dm_gtab_ready = false;
     long long dm_first = 0, dm_count = 0;
     int dm_nsym = 0;
@@ -413,6 +419,45 @@ int make_tmap3(lelph_gpu* h, CUtensorMap* m, void* base, bool f32, unsigned long
     return LELPH_GPU_OK;
 }
 
+// key of a k-point on a 2^-20 lattice of its coordinates wrapped into [0, 1)
+long long k_hash_key(const double* k)
+{
+    long long key = 0;
+    for (int x = 0; x < 3; ++x)
+    {
+        const double f = k[x] - std::floor(k[x]);
+        long long q = std::llround(f * 1048576.0) & 1048575;
+        key = (key << 20) | q;
+    }
+    return key;
+}
+
+int find_k(const lelph_gpu* h, const double* kpt);
+
+// find_k through a hash of the full-BZ list; a miss, or a hit that fails the
+// reference's tolerance test, falls back to the linear search
+int find_k_fast(lelph_gpu* h, const double* kpt)
+{
+    if (h->khash.empty())
+        for (int i = 0; i < h->d.nkpts_BZ; ++i) h->khash.emplace(k_hash_key(&h->kbz_crys[3 * i]), i);
+    auto it = h->khash.find(k_hash_key(kpt));
+    if (it != h->khash.end())
+    {
+        const int i = it->second;
+        double s = 0;
+        for (int x = 0; x < 3; ++x)
+        {
+            double dd = h->kbz_crys[3 * i + x] - kpt[x];
+            dd -= std::rint(dd);
+            s += dd * dd;
+        }
+        // grid points lie far more than 2 EPS_K apart, so a point within
+        // EPS_K is the one the linear search would return
+        if (std::sqrt(s) < EPS_K) return i;
+    }
+    return find_k(h, kpt);
+}
+
 int find_k(const lelph_gpu* h, const double* kpt)
 {
     const int nk = h->d.nkpts_BZ;
@@ -591,6 +636,7 @@ static int upload_wfc(lelph_gpu* h, const double* const* wfc)
     if (rc) return rc;
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->prepared = false;
+    h->dm_coef32_ready = false;
     return LELPH_GPU_OK;
 }
 
@@ -873,7 +919,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
-                      &h->d_dmjobs, &h->d_dmats};
+                      &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -941,6 +987,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     }
     rc = ensure(h, h->d_coef, sizeof(double2) * (size_t)ctot);
     if (rc) return bad(rc, h->err);
+    h->coef_total = ctot;
     rc = ensure(h, h->d_chat, sizeof(double2) * (size_t)chtot);
     if (rc) return bad(rc, h->err);
     rc = ensure(h, h->d_proj, sizeof(double2) * (size_t)d.nkpts_BZ * d.natom * h->nproj_max * 4 * nsets);
@@ -1789,15 +1836,17 @@ int int_inverse3(const int* m, int* inv)
 inline cd conj_if(cd z, bool c) { return c ? std::conj(z) : z; }
 
 // Job of the pair (symmetry isym, full-BZ k ikBZ): the reference's sequence
-// (src/symmetries/elec_reps.c:33-372) folded into one spinor matrix, one
-// conjugation, one constant phase and one phase vector per side.  With
-// x^(c) the conjugate of x when c holds:
-//   right: w = phR^(trR) ph1^(tr1^trR) e^{-i 2 pi m.tw} UR^(trR) U1^(tr1^trR) psi_k1^(tr1^trR),
+// (src/symmetries/elec_reps.c:33-372) folded onto the k2 side.  With x^(c)
+// the conjugate of x when c holds, the two sides of the reference are
+//   right: w = phR^(trR) ph1^(x1) e^{-i 2 pi m.tw} UR^(trR) U1^(x1) psi_k1^(x1),  x1 = tr1 xor trR,
 //          tw = s1 W1^T tau1 + sR W_RS1^T tauR  (s = -1 where conjugated)
 //   left:  v = ph2^(!tr2) e^{-i 2 pi m.tv} U2^(!tr2) psi_k2^(!tr2),  tv = s2 W_RS1^T tau2
-// ph1 = e^{-i 2 pi (S1 k1).tau1}, phR = e^{-i 2 pi (R S1 k1).tauR}, ph2 = e^{-i 2 pi (R S1 k1).tau2}.
+// with ph1 = e^{-i 2 pi (S1 k1).tau1}, phR = e^{-i 2 pi (R S1 k1).tauR},
+// ph2 = e^{-i 2 pi (R S1 k1).tau2}; D = sum_p v . w moves every factor of w
+// but psi_k1^(x1) onto v: t = tw + tv, C = phR^(trR) ph1^(x1) ph2^(!tr2),
+// M = (UR^(trR) U1^(x1))^T U2^(!tr2).
 int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_crys, const cd* UR, bool trR,
-             int ikBZ, DmatJob& J)
+             int ikBZ, DmatJob& J, const char** why)
 {
     const lelph_gpu_desc& d = h->d;
     double kc[3], Rk[3], Rkc[3];
@@ -1807,10 +1856,12 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
                 (2 * PI_T);
     mat_vec3(R, kc, false, Rk);
     mat_vec3(d.alat_vec, Rk, true, Rkc);
-    const int iRk = find_k(h, Rkc);
+    const int iRk = find_k_fast(h, Rkc);
     if (iRk < 0)
-        return fail(h, LELPH_GPU_ERR_GEOMETRY,
-                    "Rotated k point not found. Either Wrong Phonon symmetry or using non-uniform kgrid");
+    {
+        *why = "Rotated k point not found. Either Wrong Phonon symmetry or using non-uniform kgrid";
+        return LELPH_GPU_ERR_GEOMETRY;
+    }
     const KPointSym& s1 = h->ksym[ikBZ];
     const KPointSym& s2 = h->ksym[iRk];
     memset(&J, 0, sizeof(J));
@@ -1819,7 +1870,11 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
     for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c)
             J.WRS1[3 * r + c] = WR[3 * r] * s1.W[c] + WR[3 * r + 1] * s1.W[3 + c] + WR[3 * r + 2] * s1.W[6 + c];
-    if (int_inverse3(s2.W, J.W2inv)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "symmetry not unimodular on the lattice");
+    if (int_inverse3(s2.W, J.W2inv))
+    {
+        *why = "symmetry not unimodular on the lattice";
+        return LELPH_GPU_ERR_GEOMETRY;
+    }
     const double* S1 = &h->symR[9 * s1.isym];
     const double* S2 = &h->symR[9 * s2.isym];
     double RS1[9];
@@ -1833,7 +1888,11 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
     for (int x = 0; x < 3; ++x)
     {
         J.ulm[x] = (int)std::rint(uc[x]);
-        if (std::fabs(uc[x] - J.ulm[x]) > 1e-4) return fail(h, LELPH_GPU_ERR_GEOMETRY, "S2 k2 - R S1 k1 not a G vector");
+        if (std::fabs(uc[x] - J.ulm[x]) > 1e-4)
+        {
+            *why = "S2 k2 - R S1 k1 not a G vector";
+            return LELPH_GPU_ERR_GEOMETRY;
+        }
     }
     mat_vec3(d.alat_vec, RS1k1, true, Rkcrys);
     const bool tr1 = s1.trev != 0, tr2 = s2.trev != 0, x1 = tr1 != trR, nt2 = !tr2;
@@ -1854,7 +1913,10 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
     Mw[1] = URc[0] * U1[1] + URc[1] * U1[3];
     Mw[2] = URc[2] * U1[0] + URc[3] * U1[2];
     Mw[3] = URc[2] * U1[1] + URc[3] * U1[3];
-    const cd Cw = conj_if(phR, trR) * conj_if(ph1, x1), Cv = conj_if(ph2, nt2);
+    // M = Mw^T U2
+    const cd M[4] = {Mw[0] * U2[0] + Mw[2] * U2[2], Mw[0] * U2[1] + Mw[2] * U2[3], Mw[1] * U2[0] + Mw[3] * U2[2],
+                     Mw[1] * U2[1] + Mw[3] * U2[3]};
+    const cd C = conj_if(phR, trR) * conj_if(ph1, x1) * conj_if(ph2, nt2);
     const double sg1 = x1 ? -1.0 : 1.0, sgR = trR ? -1.0 : 1.0, sg2 = nt2 ? -1.0 : 1.0;
     for (int c = 0; c < 3; ++c)
     {
@@ -1865,18 +1927,12 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
             b += J.WRS1[3 * r + c] * tauR_crys[r];
             e += J.WRS1[3 * r + c] * s2.tau_crys[r];
         }
-        J.tw[c] = sg1 * a + sgR * b;
-        J.tv[c] = sg2 * e;
+        J.t[c] = sg1 * a + sgR * b + sg2 * e;
     }
     J.conj_w = x1;
     J.conj_v = nt2;
-    J.Cw = make_double2(Cw.real(), Cw.imag());
-    J.Cv = make_double2(Cv.real(), Cv.imag());
-    for (int e = 0; e < 4; ++e)
-    {
-        J.Mw[e] = make_double2(Mw[e].real(), Mw[e].imag());
-        J.Mv[e] = make_double2(U2[e].real(), U2[e].imag());
-    }
+    J.C = make_double2(C.real(), C.imag());
+    for (int e = 0; e < 4; ++e) J.M[e] = make_double2(M[e].real(), M[e].imag());
     return LELPH_GPU_OK;
 }
 }  // namespace
@@ -1904,15 +1960,51 @@ extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const
         if (!su2mat(Rmat + 9 * is, d.nspinor, time_rev[is] != 0, &UR[4 * is]))
             return fail(h, LELPH_GPU_ERR_GEOMETRY, "Wrong symmetric matrices");
     }
+    const auto th0 = std::chrono::steady_clock::now();
     std::vector<DmatJob> jobs((size_t)count);
-    for (long long i = 0; i < count; ++i)
-    {
+    if (h->khash.empty())
+        for (int i = 0; i < d.nkpts_BZ; ++i) h->khash.emplace(k_hash_key(&h->kbz_crys[3 * i]), i);
+    auto build = [&](long long i) {
         const long long id = first + i;
         const int is = (int)(id / nkbz), ik = (int)(id % nkbz);
+        const char* why = "";
         int rc = dmat_job(h, Rmat + 9 * is, &WR[9 * is], &tauc[3 * is], &UR[4 * is], time_rev[is] != 0, ik,
-                          jobs[(size_t)i]);
-        if (rc) return rc;
+                          jobs[(size_t)i], &why);
+        return std::make_pair(rc, why);
+    };
+    // job construction on the host cores: every worker records its first
+    // failing job; the lowest one is rebuilt alone to report its error
+    const int nthr = (int)std::min<long long>(std::max(1u, std::thread::hardware_concurrency()), (count + 1023) / 1024);
+    std::vector<long long> bad_job((size_t)std::max(1, nthr), -1);
+    if (nthr <= 1)
+    {
+        for (long long i = 0; i < count; ++i)
+        {
+            auto r = build(i);
+            if (r.first) return fail(h, r.first, r.second);
+        }
     }
+    else
+    {
+        std::vector<std::thread> pool;
+        for (int w = 0; w < nthr; ++w)
+            pool.emplace_back([&, w]() {
+                for (long long i = count * w / nthr; i < count * (w + 1) / nthr; ++i)
+                    if (build(i).first != 0)
+                    {
+                        bad_job[(size_t)w] = i;
+                        return;
+                    }
+            });
+        for (auto& t : pool) t.join();
+        for (long long b : bad_job)
+            if (b >= 0)
+            {
+                auto r = build(b);
+                return fail(h, r.first, r.second);
+            }
+    }
+    h->stats.dmats_host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
     // Miller -> position tables of the iBZ lists on the reference's box, built once
     DmatGeom dg;
     dg.nb = d.nbnds;
@@ -1945,12 +2037,30 @@ extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const
     const size_t dbytes = sizeof(double2) * (size_t)count * d.nspin * d.nbnds * d.nbnds;
     rc = ensure(h, h->d_dmats, dbytes);
     if (rc) return rc;
-    if (lelph_launch_dmats((const DmatJob*)h->d_dmjobs.p, count, dg, fp64, (const double2*)h->d_coef.p,
+    const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
+    rc = ensure(h, h->d_dmmap, sizeof(int) * (size_t)count * npw_max);
+    if (rc) return rc;
+    if (!fp64 && !h->dm_coef32_ready)
+    {
+        const long long n = h->coef_total;
+        rc = ensure(h, h->d_dmcoef32, sizeof(float2) * (size_t)n);
+        if (rc) return rc;
+        lelph_launch_dm_c64((const double2*)h->d_coef.p, n, (float2*)h->d_dmcoef32.p, h->st);
+        h->stats.kernel_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+        h->dm_coef32_ready = true;
+    }
+    tstart(h);
+    if (lelph_launch_dmats((const DmatJob*)h->d_dmjobs.p, count, dg, (const double2*)h->d_coef.p,
+                           fp64 ? nullptr : (const float2*)h->d_dmcoef32.p,
                            (const long long*)h->d_coefoff.p, (const int*)h->d_miller.p, (const long long*)h->d_pwoff.p,
-                           (const int*)h->d_npw.p, (const int*)h->d_dmgtab.p, (double2*)h->d_dmats.p, h->st))
+                           (const int*)h->d_npw.p, (const int*)h->d_dmgtab.p, npw_max, (int*)h->d_dmmap.p,
+                           (double2*)h->d_dmats.p, h->st))
         return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "Dmat launch configuration");
-    h->stats.kernel_launches += 1;
+    h->stats.kernel_launches += 2;
     CUDA_TRY(h, cudaGetLastError());
+    h->stats.dmats_ms += tstop(h);
+    h->stats.dmats_done += count;
     h->dm_first = first;
     h->dm_count = count;
     h->dm_nsym = nsym;

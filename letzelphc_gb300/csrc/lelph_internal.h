@@ -159,6 +159,9 @@ struct DmatGeom
     int ntab;        // Nx + Ny + Nz + 3 per-axis phase factors
 };
 // One (symmetry R, full-BZ k) job: k = S1 k1, Rk = S2 k2 (irreducible k1, k2).
+// D[b][a] = sum_{p,t} v_{b,t}(p) y~_{a,t}(p): y~ = psi_k1 (conjugated when
+// conj_w), v = C e^{-i 2 pi m.t} M x~ with x~ = psi_k2 at the matched plane
+// wave (conjugated when conj_v), m the Miller index of plane wave p of k1.
 struct DmatJob
 {
     int ik1, ik2;
@@ -166,13 +169,18 @@ struct DmatJob
     int W2inv[9];    // S2^-1 on Miller indices
     int ulm[3];      // G0 = S2 k2 - R S1 k1 (crystal)
     int conj_w, conj_v;
-    double tw[3], tv[3];  // plane-wave phase e^{-i 2 pi m.t} of each side (m: Miller index in the k1 list)
-    double2 Cw, Cv;       // constant phase of each side
-    double2 Mw[4], Mv[4]; // 2x2 spinor matrix of each side (row-major)
+    double t[3];     // phase vector
+    double2 C;       // constant phase
+    double2 M[4];    // 2x2 spinor matrix (row-major)
 };
+static_assert(sizeof(DmatJob) == 208, "DmatJob layout");
 size_t lelph_dmats_smem_bytes(const DmatGeom& dg, int fp64);
 void lelph_launch_dm_gtab(const int* miller, const long long* pw_off, const int* npw, int nk, int npw_max, int Nx,
                           int Ny, int Nz, int* gtab, cudaStream_t st);
-int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg, int fp64, const double2* coef,
+void lelph_launch_dm_c64(const double2* in, long long n, float2* out, cudaStream_t st);
+// index maps (njobs x npw_max ints in `map`) then the contraction: FP32
+// operands from coef32 when it is given (mixed form), else FP64 from coef64
+int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg, const double2* coef64,
+                       const float2* coef32,
                        const long long* coef_off, const int* miller, const long long* pw_off, const int* npw,
-                       const int* gtab, double2* out, cudaStream_t st);
+                       const int* gtab, int npw_max, int* map, double2* out, cudaStream_t st);

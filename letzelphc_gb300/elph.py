@@ -48,6 +48,7 @@ class Stats(C.Structure):
         ("kernel_launches", C.c_longlong), ("local_launches", C.c_longlong), ("local_ms", C.c_double),
         ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
         ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
+        ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
     ]
 
 
