@@ -97,6 +97,7 @@ typedef struct lelph_gpu_stats
     double dmats_ms;             /* device time of the Dmat kernels (index maps + contraction, profiling on) */
     double dmats_host_ms;        /* host time spent building Dmat jobs (always measured) */
     long long dmats_done;        /* Dmats computed */
+    double qstar_ms;             /* device time of the q-star rotations (profiling on) */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,
@@ -209,6 +210,26 @@ int lelph_gpu_elph_q_rotate(lelph_gpu* h, const double* Dmats_l, const double* e
  * found") or an operation is not integral on the lattice. */
 int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
                     long long first, long long count, double* Dmats);
+
+/* compute_and_write_elphq with its q-star expansion
+ * (src/elph/compute_elph_matq.c:20-234) without the netCDF I/O: g of the
+ * irreducible q (qpt_crys, eigVec, dVscfq, non_loc, kminusq as in
+ * lelph_gpu_compute_elphq) at every full-BZ k, then for each star member
+ * istar = 1 .. nstar-1 with phonon symmetry S = star_sym[istar] (the
+ * reference's phonon->qmap[2*(qpos+istar)+1]):
+ *   g(Sq, Sk) = elph_q_rotate(D[S][k+q], g(q, k), D[S][k], time_rev(S)),
+ * stored at S k.  ph_Rmat (nph_sym, 3, 3), ph_tau (nph_sym, 3), ph_time_rev
+ * (nph_sym): the phonon symmetries (phonon->ph_syms).  The Dmats come from the
+ * block lelph_gpu_dmats left on the device when it was made for the same
+ * symmetries and holds the star's rows; otherwise the needed rows are computed
+ * here.  out: (nstar, nkpts_BZ, nmodes, nspin, nbnds, nbnds) of out_type, the
+ * ndb.elph rows qpos .. qpos+nstar-1.  star_sym[0] must be 0 (the reference's
+ * check "Qpoint in iBZ cannot be traced in phonon qmap"); LELPH_GPU_ERR_GEOMETRY
+ * if S k is off the grid.  Rotations need 4 nbnds^2 complex in shared memory:
+ * up to 83 bands (mixed form) or 58 (plain form) when nstar > 1. */
+int lelph_gpu_compute_elphq_star(lelph_gpu* h, const double qpt_crys[3], const double* eigVec, const double* dVscfq,
+                                 int non_loc, int kminusq, int nph_sym, const double* ph_Rmat, const double* ph_tau,
+                                 const int* ph_time_rev, int nstar, const int* star_sym, int out_type, void* out);
 
 /* Rotated (and umklapp-shifted) Miller indices of full-BZ k-point kbz, as the
  * device computes them: out[npw*3].  Parity check of the integer maps of

@@ -95,13 +95,15 @@ struct lelph_gpu
     DevBuf d_colmask;  // box occupancy of a chunk of k-points (z-columns, then x planes)
     // Dmats: Miller -> position tables of the iBZ lists, the job table and the
     // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
-    DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32;
+    DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32, d_dmstar, d_gstar, d_qsitems;
     bool dm_coef32_ready = false;
     long long coef_total = 0;  // complex coefficients of every iBZ k
     std::unordered_map<long long, int> khash;  // full-BZ k-points by wrapped, quantised coordinates
     bool dm_gtab_ready = false;
     long long dm_first = 0, dm_count = 0;
     int dm_nsym = 0;
+    std::vector<double> dm_R, dm_tau;  // the symmetries of the resident block
+    std::vector<int> dm_trev;
     bool vl_ready = false;
     int vl_npts = 0, vl_dim2 = 0;
     double vl_dg = 0, vl_volume = 0;
@@ -919,7 +921,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
-                      &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32};
+                      &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
+                      &h->d_qsitems};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1937,15 +1940,14 @@ int dmat_job(lelph_gpu* h, const double* R, const int* WR, const double* tauR_cr
 }
 }  // namespace
 
-extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
-                               long long first, long long count, double* Dmats)
+// Dmats of the (symmetry, full-BZ k) pairs id = isym * nk_BZ + ik, for
+// id = first + i (ids == NULL) or id = ids[i], i < count, into the device
+// array out (count, nspin, nb, nb).
+static int dmats_run(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
+                     long long first, long long count, const long long* ids, double2* out)
 {
-    if (!h || nsym <= 0 || !Rmat || !tau || !time_rev || first < 0 || count < 0) return LELPH_GPU_ERR_INVALID;
     const lelph_gpu_desc& d = h->d;
     const long long nkbz = d.nkpts_BZ;
-    if (first + count > (long long)nsym * nkbz) return fail(h, LELPH_GPU_ERR_INVALID, "Dmat range beyond nsym * nk_BZ");
-    if (count == 0) return LELPH_GPU_OK;
-    CUDA_TRY(h, cudaSetDevice(h->device));
     // per-symmetry integer action, crystal translation and SU(2) matrix
     std::vector<int> WR(9 * (size_t)nsym);
     std::vector<double> tauc(3 * (size_t)nsym);
@@ -1965,7 +1967,7 @@ extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const
     if (h->khash.empty())
         for (int i = 0; i < d.nkpts_BZ; ++i) h->khash.emplace(k_hash_key(&h->kbz_crys[3 * i]), i);
     auto build = [&](long long i) {
-        const long long id = first + i;
+        const long long id = ids ? ids[i] : first + i;
         const int is = (int)(id / nkbz), ik = (int)(id % nkbz);
         const char* why = "";
         int rc = dmat_job(h, Rmat + 9 * is, &WR[9 * is], &tauc[3 * is], &UR[4 * is], time_rev[is] != 0, ik,
@@ -2034,9 +2036,6 @@ extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const
     if (lelph_dmats_smem_bytes(dg, fp64) > 200 * 1024) return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "FFT box too large for the Dmat phase tables");
     int rc = upload(h, h->d_dmjobs, jobs.data(), sizeof(DmatJob) * jobs.size());
     if (rc) return rc;
-    const size_t dbytes = sizeof(double2) * (size_t)count * d.nspin * d.nbnds * d.nbnds;
-    rc = ensure(h, h->d_dmats, dbytes);
-    if (rc) return rc;
     const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
     rc = ensure(h, h->d_dmmap, sizeof(int) * (size_t)count * npw_max);
     if (rc) return rc;
@@ -2055,16 +2054,166 @@ extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const
                            fp64 ? nullptr : (const float2*)h->d_dmcoef32.p,
                            (const long long*)h->d_coefoff.p, (const int*)h->d_miller.p, (const long long*)h->d_pwoff.p,
                            (const int*)h->d_npw.p, (const int*)h->d_dmgtab.p, npw_max, (int*)h->d_dmmap.p,
-                           (double2*)h->d_dmats.p, h->st))
+                           out, h->st))
         return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "Dmat launch configuration");
     h->stats.kernel_launches += 2;
     CUDA_TRY(h, cudaGetLastError());
     h->stats.dmats_ms += tstop(h);
     h->stats.dmats_done += count;
+    return LELPH_GPU_OK;
+}
+
+extern "C" int lelph_gpu_dmats(lelph_gpu* h, int nsym, const double* Rmat, const double* tau, const int* time_rev,
+                               long long first, long long count, double* Dmats)
+{
+    if (!h || nsym <= 0 || !Rmat || !tau || !time_rev || first < 0 || count < 0) return LELPH_GPU_ERR_INVALID;
+    const lelph_gpu_desc& d = h->d;
+    if (first + count > (long long)nsym * d.nkpts_BZ)
+        return fail(h, LELPH_GPU_ERR_INVALID, "Dmat range beyond nsym * nk_BZ");
+    if (count == 0) return LELPH_GPU_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t dbytes = sizeof(double2) * (size_t)count * d.nspin * d.nbnds * d.nbnds;
+    int rc = ensure(h, h->d_dmats, dbytes);
+    if (rc) return rc;
+    h->dm_count = 0;
+    rc = dmats_run(h, nsym, Rmat, tau, time_rev, first, count, nullptr, (double2*)h->d_dmats.p);
+    if (rc) return rc;
+    // the resident block and the symmetries it belongs to
     h->dm_first = first;
     h->dm_count = count;
     h->dm_nsym = nsym;
+    h->dm_R.assign(Rmat, Rmat + 9 * (size_t)nsym);
+    h->dm_tau.assign(tau, tau + 3 * (size_t)nsym);
+    h->dm_trev.assign(time_rev, time_rev + nsym);
     if (Dmats) CUDA_TRY(h, cudaMemcpyAsync(Dmats, h->d_dmats.p, dbytes, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    return LELPH_GPU_OK;
+}
+
+// ============================================ q-star expansion of one irreducible q
+
+extern "C" int lelph_gpu_compute_elphq_star(lelph_gpu* h, const double qpt_crys[3], const double* eigVec,
+                                            const double* dVscfq, int non_loc, int kminusq, int nph_sym,
+                                            const double* ph_Rmat, const double* ph_tau, const int* ph_time_rev,
+                                            int nstar, const int* star_sym, int out_type, void* out)
+{
+    if (!h || !qpt_crys || !eigVec || !out || nstar < 1 || !star_sym || nph_sym < 1 || !ph_Rmat || !ph_tau ||
+        !ph_time_rev)
+        return LELPH_GPU_ERR_INVALID;
+    if (out_type != LELPH_GPU_OUT_C128 && out_type != LELPH_GPU_OUT_C64) return fail(h, LELPH_GPU_ERR_INVALID, "out_type");
+    for (int i = 0; i < nstar; ++i)
+        if (star_sym[i] < 0 || star_sym[i] >= nph_sym) return fail(h, LELPH_GPU_ERR_INVALID, "star symmetry index");
+    // the first member is the irreducible q itself (compute_elph_matq.c:45-49)
+    if (star_sym[0] != 0) return fail(h, LELPH_GPU_ERR_INVALID, "Qpoint in iBZ cannot be traced in phonon qmap");
+    const lelph_gpu_desc& d = h->d;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const int nk = d.nkpts_BZ, nb = d.nbnds;
+    const int fp64 = h->mixed ? 0 : 1;
+    if (nstar > 1 && lelph_qstar_smem_bytes(nb, fp64) > 220 * 1024)
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "too many bands for the q-star rotation");
+    int rc = lelph_gpu_set_q(h, 0, qpt_crys, eigVec, dVscfq);
+    if (rc) return rc;
+    const size_t gsz = (size_t)d.nmodes * d.nspin * nb * nb;
+    const size_t esz = out_type == LELPH_GPU_OUT_C64 ? sizeof(float2) : sizeof(double2);
+    const size_t total = esz * gsz * (size_t)nk * nstar;
+    rc = ensure(h, h->d_gstar, total);
+    if (rc) return rc;
+    // row 0: the irreducible q at every k
+    {
+        std::vector<int> qs(nk, 0), ks(nk);
+        for (int i = 0; i < nk; ++i) ks[i] = i;
+        rc = run_impl(h, nk, qs.data(), ks.data(), non_loc, kminusq, out_type, h->d_gstar.p, true);
+        if (rc) return rc;
+    }
+    if (nstar > 1)
+    {
+        // Dmats of the star's symmetries: the resident block when it was made
+        // for these symmetries and holds their rows, else computed here
+        std::vector<int> uniq(star_sym + 1, star_sym + nstar);
+        std::sort(uniq.begin(), uniq.end());
+        uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+        bool resident = h->dm_count > 0 && h->dm_nsym == nph_sym &&
+                        std::equal(h->dm_R.begin(), h->dm_R.end(), ph_Rmat) &&
+                        std::equal(h->dm_tau.begin(), h->dm_tau.end(), ph_tau) &&
+                        std::equal(h->dm_trev.begin(), h->dm_trev.end(), ph_time_rev);
+        for (int S : uniq)
+            resident = resident && (long long)S * nk >= h->dm_first &&
+                       (long long)(S + 1) * nk <= h->dm_first + h->dm_count;
+        std::vector<long long> rowbase(nph_sym, -1);
+        const double2* Dbase = nullptr;
+        if (resident)
+        {
+            for (int S : uniq) rowbase[S] = (long long)S * nk - h->dm_first;
+            Dbase = (const double2*)h->d_dmats.p;
+        }
+        else
+        {
+            std::vector<long long> ids;
+            ids.reserve(uniq.size() * nk);
+            for (size_t j = 0; j < uniq.size(); ++j)
+            {
+                rowbase[uniq[j]] = (long long)j * nk;
+                for (int k = 0; k < nk; ++k) ids.push_back((long long)uniq[j] * nk + k);
+            }
+            rc = ensure(h, h->d_dmstar, sizeof(double2) * ids.size() * d.nspin * nb * nb);
+            if (rc) return rc;
+            rc = dmats_run(h, nph_sym, ph_Rmat, ph_tau, ph_time_rev, 0, (long long)ids.size(), ids.data(),
+                           (double2*)h->d_dmstar.p);
+            if (rc) return rc;
+            Dbase = (const double2*)h->d_dmstar.p;
+        }
+        // (member, k) items: k+q as the stage finds it (compute_elph_matq.c:65-128),
+        // S k in the full-BZ list (:186-205)
+        if (h->khash.empty())
+            for (int i = 0; i < nk; ++i) h->khash.emplace(k_hash_key(&h->kbz_crys[3 * i]), i);
+        std::vector<int> kq_of(nk);
+        for (int i = 0; i < nk; ++i)
+        {
+            double kq[3];
+            for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * i + x] + (kminusq ? -qpt_crys[x] : qpt_crys[x]);
+            kq_of[i] = find_k_fast(h, kq);
+            if (kq_of[i] < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
+        }
+        std::vector<QStarItem> items((size_t)(nstar - 1) * nk);
+        for (int m = 1; m < nstar; ++m)
+        {
+            const int S = star_sym[m];
+            const double* R = ph_Rmat + 9 * S;
+            for (int i = 0; i < nk; ++i)
+            {
+                int idx_k = i, idx_kq = kq_of[i];
+                if (kminusq) std::swap(idx_k, idx_kq);
+                double kc[3], Sk[3], Skc[3];
+                for (int x = 0; x < 3; ++x)
+                    kc[x] = (h->blat[3 * x] * h->kbz_crys[3 * i] + h->blat[3 * x + 1] * h->kbz_crys[3 * i + 1] +
+                             h->blat[3 * x + 2] * h->kbz_crys[3 * i + 2]) /
+                            (2 * PI_T);
+                mat_vec3(R, kc, false, Sk);
+                mat_vec3(d.alat_vec, Sk, true, Skc);
+                const int isk = find_k_fast(h, Skc);
+                if (isk < 0)
+                    return fail(h, LELPH_GPU_ERR_GEOMETRY,
+                                "Unable to to find S*k index This is due to incommenserate k and q grids.");
+                QStarItem& it = items[(size_t)(m - 1) * nk + i];
+                it.src = i;
+                it.dst = m * nk + isk;
+                it.dl = rowbase[S] + idx_kq;
+                it.dr = rowbase[S] + idx_k;
+                it.trev = ph_time_rev[S] != 0;
+                it.pad = 0;
+            }
+        }
+        rc = upload(h, h->d_qsitems, items.data(), sizeof(QStarItem) * items.size());
+        if (rc) return rc;
+        tstart(h);
+        if (lelph_launch_qstar((const QStarItem*)h->d_qsitems.p, (long long)items.size(), nb, d.nspin, d.nmodes, Dbase,
+                               fp64, out_type == LELPH_GPU_OUT_C64, h->d_gstar.p, h->d_gstar.p, h->st))
+            return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "q-star launch configuration");
+        h->stats.kernel_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+        h->stats.qstar_ms += tstop(h);
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_gstar.p, total, cudaMemcpyDeviceToHost, h->st));
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     return LELPH_GPU_OK;
 }

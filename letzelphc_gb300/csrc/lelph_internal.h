@@ -184,3 +184,17 @@ int lelph_launch_dmats(const DmatJob* jobs, long long njobs, const DmatGeom& dg,
                        const float2* coef32,
                        const long long* coef_off, const int* miller, const long long* pw_off, const int* npw,
                        const int* gtab, int npw_max, int* map, double2* out, cudaStream_t st);
+
+// ------------------------------------------------------------ q-star expansion
+// One (star member, k) item: g of row src (the irreducible q at k) rotated
+// with Dl = D[dl] (k+q) and Dr = D[dr] (k) into row dst (the member at S k).
+struct QStarItem
+{
+    int src, dst;
+    long long dl, dr;  // matrix indices in the Dmats array (each nspin x nb x nb)
+    int trev;
+    int pad;
+};
+size_t lelph_qstar_smem_bytes(int nb, int fp64);
+int lelph_launch_qstar(const QStarItem* items, long long nitems, int nb, int nspin, int nmodes, const double2* D,
+                       int fp64, int out_c64, const void* g, void* out, cudaStream_t st);

@@ -49,6 +49,7 @@ class Stats(C.Structure):
         ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
         ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
         ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
+        ("qstar_ms", C.c_double),
     ]
 
 
@@ -58,7 +59,7 @@ EXPORTS = [
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
     "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
-    "lelph_gpu_dmats",
+    "lelph_gpu_dmats", "lelph_gpu_compute_elphq_star",
 ]
 
 _lib = None
@@ -83,6 +84,8 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_rotate_dvscf.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
     L.lelph_gpu_dmats.argtypes = [vp, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_longlong, _dp]
+    L.lelph_gpu_compute_elphq_star.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int,
+                                               _ip, C.c_int, vp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
     L.lelph_gpu_run_device_noalloc.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
@@ -276,6 +279,27 @@ class LelphGPU:
         self._check(self._L.lelph_gpu_dmats(self.h, nsym, _ptr(R), _ptr(t), tr.ctypes.data_as(_ip), int(first),
                                             int(count), _ptr(out) if host else None))
         return out
+
+    def compute_elphq_star(self, qpt, eigVec, dVscfq, star_syms, sym_R=None, sym_tau=None, sym_trev=None,
+                           non_loc=True, kminusq=False, out=OUT_C128):
+        """compute_and_write_elphq with its q-star expansion: (nstar, nk_BZ,
+        nmodes, nspin, nb, nb); row istar belongs to the star member of
+        symmetry star_syms[istar] (star_syms[0] = 0, the irreducible q).  The
+        phonon symmetries default to the system's."""
+        s = self.sys
+        R = np.ascontiguousarray(s.sym_R if sym_R is None else sym_R, dtype=np.float64).reshape(-1, 3, 3)
+        t = np.ascontiguousarray(s.sym_tau if sym_tau is None else sym_tau, dtype=np.float64).reshape(-1, 3)
+        tr = np.ascontiguousarray(np.asarray(s.sym_trev if sym_trev is None else sym_trev).astype(np.int32))
+        st = np.ascontiguousarray(star_syms, dtype=np.int32)
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        v = np.ascontiguousarray(dVscfq, dtype=np.complex128)
+        dt = np.complex64 if out == OUT_C64 else np.complex128
+        g = np.empty((len(st), s.nk_bz, s.nmodes, s.nspin, s.nbnds, s.nbnds), dt)
+        self._check(self._L.lelph_gpu_compute_elphq_star(
+            self.h, _ptr(q), _ptr(e), _ptr(v), int(non_loc), int(kminusq), R.shape[0], _ptr(R), _ptr(t),
+            tr.ctypes.data_as(_ip), len(st), st.ctypes.data_as(_ip), int(out), g.ctypes.data_as(C.c_void_p)))
+        return g
 
     def run(self, qslots, kbz, non_loc=True, kminusq=False, out=OUT_C128, g_out=None):
         qs = np.ascontiguousarray(qslots, dtype=np.int32)

@@ -12,6 +12,8 @@ It restates, in numpy FP64, the reference's G-space algorithm for one q-point
 * ``elph_q_rotate``     src/symmetries/elphq_expand.c:16-73
 * ``electronic_reps``, ``dmats`` (the Dmats that elph_driver computes before
   the q loop): src/symmetries/elec_reps.c:16-413, src/elph/compute_dmats.c:20-131
+* ``compute_elphq_star`` (the q-star loop of the stage):
+  src/elph/compute_elph_matq.c:116-217
 * ``vloc_table``, ``dvlocq``, ``add_dvscf_qe`` (the per-q local bare
   potential that elph_driver adds before the stage,
   src/elph/elph_driver.c:234-252): src/dvloc/vlocg_table.c:16-154,
@@ -505,6 +507,48 @@ def dmats(s, sym_R=None, sym_tau=None, sym_trev=None, pairs=None):
     if pairs is None:
         pairs = [(i, k) for i in range(len(sym_R)) for k in range(len(s.kbz_crys))]
     return np.array([electronic_reps(s, sym_R[i], sym_tau[i], bool(sym_trev[i]), k) for i, k in pairs])
+
+
+def q_star(s, qpt, sym_R=None):
+    """Members of the star of q (crystal) under the phonon symmetries, each
+    with the first symmetry that produces it, identity first: the (qmap,
+    nqstar) a phonon code hands to the stage for this q."""
+    sym_R = s.sym_R if sym_R is None else sym_R
+    qc = np.linalg.solve(s.alat.T, np.asarray(qpt, float))  # crystal -> cartesian (no 2 pi)
+    members, syms = [], []
+    for i, R in enumerate(sym_R):
+        sq = mat_vec3(s.alat, mat_vec3(R, qc), True)
+        if find_kidx_in_list(np.array(members).reshape(-1, 3), sq) < 0:
+            members.append(sq)
+            syms.append(i)
+    return np.array(members), np.array(syms, np.int32)
+
+
+def compute_elphq_star(s, iq, star_syms, D, eigVec=None, dVscfq=None, non_loc=True, kminusq=False):
+    """compute_and_write_elphq with its q-star loop, src/elph/compute_elph_matq.c:116-217:
+    row 0 is g(q, k) at k; row istar holds
+    elph_q_rotate(D[S][k+q], g(q, k), D[S][k], time_rev(S)) at S k, S = star_syms[istar].
+    D: Dmats (nsym, nk, nspin, nb, nb).  Returns (nstar, nk, nmodes, nspin, nb, nb)."""
+    qpt = np.asarray(s.qpts[iq], float)
+    g = compute_elphq(s, iq, eigVec, dVscfq, non_loc, kminusq)
+    qt = -qpt if kminusq else qpt
+    kpq = get_kplusq_idxs(s.kbz_crys, qt)
+    kcart = kbz_cart(s)
+    out = np.zeros((len(star_syms),) + g.shape, complex)
+    out[0] = g
+    for i in range(s.nk_bz):
+        idx_k, idx_kq = i, int(kpq[i])
+        if kminusq:
+            idx_k, idx_kq = idx_kq, idx_k
+        for istar in range(1, len(star_syms)):
+            S = int(star_syms[istar])
+            gs = elph_q_rotate(D[S, idx_kq], g[i], D[S, idx_k], bool(s.sym_trev[S]))
+            sk = mat_vec3(s.alat, mat_vec3(s.sym_R[S], kcart[i]), True)
+            isk = find_kidx_in_list(s.kbz_crys, sk)
+            if isk < 0:
+                raise ValueError("Unable to to find S*k index")
+            out[istar, isk] = gs
+    return out
 
 
 # ------------------------------------------------------- local bare potential

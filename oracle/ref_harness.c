@@ -12,6 +12,7 @@
  *        lelph_ref <system.bin> <g_out.bin> dvloc <v_out.bin>
  *        lelph_ref <system.bin> <unused> rotdv <spec.bin> <dv_out.bin>
  *        lelph_ref <system.bin> <unused> dmats <D_out.bin>
+ *        lelph_ref <system.bin> <g_out.bin> star <star.bin>
  *
  * dvloc: the system's dVscf records are the induced part (QE's dvscf); the
  * harness builds the V_loc table (create_vlocg_table, src/dvloc/vlocg_table.c)
@@ -29,6 +30,12 @@
  * the system and every full-BZ k, in the order of compute_and_write_dmats
  * (src/elph/compute_dmats.c:99-118); D_out.bin is complex128
  * (nsym, nk_BZ, nspin, nb, nb).  The matrix elements are not computed.
+ *
+ * star: q stars from star.bin (records nqstar: members per iBZ q, qsym: the
+ * phonon symmetry of every member, identity first); the Dmats of every
+ * (symmetry, k) are computed with electronic_reps and served to the stage's
+ * reads, so compute_and_write_elphq expands each q over its star
+ * (src/elph/compute_elph_matq.c:159-217); g_out.bin is (nq_BZ, nk_BZ, ...).
  *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
@@ -296,7 +303,40 @@ int main(int argc, char** argv)
     }
     g_slice = (size_t)nmodes * nspin * nbnds * nbnds;
     g_nk = (size_t)nkbz;
-    g_all = calloc((size_t)nq * g_nk * g_slice, sizeof(double _Complex));
+    size_t nq_bz = (size_t)nq;
+    if (argc >= 5 && !strcmp(argv[3], "star"))
+    {
+        /* q stars: nqstar per iBZ q and the phonon symmetry of every member
+         * (qmap), with the Dmats of every (symmetry, k) served to the stage's
+         * nc_get_vara reads (compute_elph_matq.c:159-217) */
+        load(argv[4]);
+        const int* ns = get("nqstar", 1)->data;
+        const int* qs = get("qsym", 1)->data;
+        nq_bz = 0;
+        for (int i = 0; i < nq; ++i) nq_bz += (size_t)ns[i];
+        free(ph.qmap);
+        ph.qmap = malloc(sizeof(int) * 2 * nq_bz);
+        size_t pos = 0;
+        for (int i = 0; i < nq; ++i)
+        {
+            ph.nqstar[i] = ns[i];
+            for (int j = 0; j < ns[i]; ++j, ++pos)
+            {
+                ph.qmap[2 * pos] = i;
+                ph.qmap[2 * pos + 1] = qs[pos];
+            }
+        }
+        ph.nq_BZ = (ND_int)nq_bz;
+        dmat_slice = (size_t)nspin * nbnds * nbnds;
+        dmat_nk = (size_t)nkbz;
+        dmats = malloc(sizeof(double _Complex) * (size_t)nsym * dmat_nk * dmat_slice);
+        if (!dmats) die("out of memory for Dmats");
+        for (int is = 0; is < nsym; ++is)
+            for (int ik = 0; ik < nkbz; ++ik)
+                electronic_reps(wfcs, &lat, lat.syms[is].Rmat, lat.syms[is].tau, lat.syms[is].time_rev, ik,
+                                dmats + ((size_t)is * dmat_nk + ik) * dmat_slice, &comm);
+    }
+    g_all = calloc(nq_bz * g_nk * g_slice, sizeof(double _Complex));
     double _Complex* eig = get("eigVec", 1)->data;
     double _Complex* dv = get("dVscf", 1)->data;
     size_t nfft = (size_t)Nx * Ny * Nz;
@@ -356,7 +396,7 @@ int main(int argc, char** argv)
     }
     FILE* fo = fopen(argv[2], "wb");
     if (!fo) die("cannot write output");
-    fwrite(g_all, sizeof(double _Complex), (size_t)nq * g_nk * g_slice, fo);
+    fwrite(g_all, sizeof(double _Complex), nq_bz * g_nk * g_slice, fo);
     fclose(fo);
 
     if (argc >= 6 && !strcmp(argv[3], "rotate"))

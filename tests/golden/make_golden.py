@@ -9,12 +9,14 @@ A second fixture pins elph_q_rotate (src/symmetries/elphq_expand.c:16), and
 the dvloc_* fixtures pin the local bare potential added per q before the
 stage (create_vlocg_table / dVlocq / add_dvscf_qe, src/dvloc/), with the
 matrix elements computed from the summed dV; rotate_dvscf.npz pins
-rotate_dvscf and dmats.npz the electronic representation matrices
-(electronic_reps, src/symmetries/elec_reps.c:16).
+rotate_dvscf, dmats.npz the electronic representation matrices
+(electronic_reps, src/symmetries/elec_reps.c:16) and star_*.npz the stage's
+q-star expansion (src/elph/compute_elph_matq.c:159-217).
 
 Run from the repo root after ``make -C oracle``:
     python tests/golden/make_golden.py            (every fixture)
     python tests/golden/make_golden.py dmats      (only dmats.npz)
+    python tests/golden/make_golden.py star       (only star_*.npz)
 """
 import json
 import os
@@ -211,6 +213,48 @@ def dmats_fixture(tmp):
                         stride=np.array(DMATS_STRIDE), **rec)
 
 
+# q stars (the stage's star loop, src/elph/compute_elph_matq.c:159-217, with
+# Dmats from electronic_reps): name -> (base config, overrides, kminusq)
+STAR_SYS = {
+    "star_c0": ("c0", {"kgrid": (2, 2, 2), "nbnds": 3, "qpts": [(0.5, 0, 0), (0.5, 0.5, 0)]}, False),
+    "star_zb_tr_kmq": ("c0", {"kind": "zincblende", "timerev": True, "nbnds": 3, "kgrid": (2, 2, 2),
+                              "qpts": [(0.5, 0, 0)]}, True),
+    "star_l12": ("c1", {"nbnds": 3, "kgrid": (2, 2, 2), "npw": 300, "fft": (24, 24, 24),
+                        "qpts": [(0.5, 0.5, 0)]}, False),
+    "star_soc": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True,
+                        "ls": (0, 1, 2), "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (2, 2, 2),
+                        "qpts": [(0.5, 0.5, 0)]}, False),
+}
+
+
+def star_fixture(tmp):
+    """g of every member of each q's star from the reference's own stage; the
+    stars (members and the first symmetry producing each) are built here the
+    way a phonon code lists them and stored with the output."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import elph_oracle as O
+    for name, (base, ov, kmq) in STAR_SYS.items():
+        s = synth.make_system(base, dict(ov))
+        stars = [O.q_star(s, q) for q in s.qpts]
+        ns = np.array([len(m) for m, _ in stars], np.int32)
+        qs = np.concatenate([sy for _, sy in stars]).astype(np.int32)
+        sysf = os.path.join(tmp, name + ".bin")
+        synth.write_system(s, sysf, kminusq=kmq)
+        spec_f = os.path.join(tmp, name + "_star.bin")
+        with open(spec_f, "wb") as f:
+            f.write(b"LELPHSYS")
+            synth._rec(f, "nqstar", ns)
+            synth._rec(f, "qsym", qs)
+            f.write(b"END\0" + b"\0" * 28)
+        gf = os.path.join(tmp, name + "_g.bin")
+        subprocess.run([REF, sysf, gf, "star", spec_f], check=True, stdout=subprocess.DEVNULL)
+        g = np.fromfile(gf, np.complex128).reshape(int(ns.sum()), s.nk_bz, s.nmodes, s.nspin, s.nbnds, s.nbnds)
+        spec = json.dumps({"base": base, "overrides": ov, "kminusq": kmq, "non_loc": True})
+        np.savez_compressed(os.path.join(ROOT, "tests", "golden", name + ".npz"), g=g, spec=np.array(spec),
+                            nqstar=ns, qsym=qs)
+        print(name, g.shape, ns.tolist(), float(np.abs(g).max()))
+
+
 if __name__ == "__main__":
     only = sys.argv[1:]
     with tempfile.TemporaryDirectory() as tmp:
@@ -223,3 +267,5 @@ if __name__ == "__main__":
             rotdv_fixture(tmp)
         if not only or "dmats" in only:
             dmats_fixture(tmp)
+        if not only or "star" in only:
+            star_fixture(tmp)

@@ -46,3 +46,16 @@ def load_dmats():
               for k, v in ov.items()}
         systems[name] = synth.make_system(base, ov)
     return z, systems
+
+
+STAR_NAMES = ["star_c0", "star_zb_tr_kmq", "star_l12", "star_soc"]
+
+
+def load_star(name):
+    """(npz, System, kminusq) of a q-star fixture: g of every star member
+    from the reference's stage, with the stars (nqstar, qsym) it used."""
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    spec = json.loads(str(z["spec"]))
+    ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls", "npw") else v)
+          for k, v in spec["overrides"].items()}
+    return z, synth.make_system(spec["base"], ov), bool(spec["kminusq"])

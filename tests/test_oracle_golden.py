@@ -101,3 +101,24 @@ def test_dmats_match_reference():
         assert np.abs(D[::st] - ref).max() < 1e-12, name
         nrm = np.linalg.norm(D.reshape(len(D), -1), axis=1)
         assert np.abs(nrm - z[name + "_norm"]).max() < 1e-12, name
+
+
+def test_qstar_expansion_matches_reference():
+    """The stage's q-star loop (src/elph/compute_elph_matq.c:159-217, Dmats from
+    electronic_reps): every star member at every S k to 1e-12 of max|g|, with
+    time reversal, the k-q convention and spinors among the systems."""
+    from golden_util import STAR_NAMES, load_star
+    for name in STAR_NAMES:
+        z, s, kmq = load_star(name)
+        D = O.dmats(s).reshape(len(s.sym_R), s.nk_bz, s.nspin, s.nbnds, s.nbnds)
+        ns, qs = z["nqstar"], z["qsym"]
+        stars = [O.q_star(s, q) for q in s.qpts]
+        assert [len(m) for m, _ in stars] == list(ns), name
+        assert np.array_equal(np.concatenate([sy for _, sy in stars]), qs), name
+        ref = z["g"]
+        pos = 0
+        for iq in range(len(s.qpts)):
+            g = O.compute_elphq_star(s, iq, qs[pos:pos + ns[iq]], D, kminusq=kmq)
+            r = ref[pos:pos + ns[iq]]
+            assert np.abs(g - r).max() < 1e-12 * np.abs(r).max(), (name, iq)
+            pos += ns[iq]
