@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
-    p.add_argument("--workload", default="elph", choices=["elph", "dmats"],
+    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
-                        "of the same system (every symmetry x full-BZ k)")
+                        "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
+                        "q-star expansion of each of the 8 q")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
     return p.parse_args()
 
@@ -585,10 +586,93 @@ def run_dmats(args):
     return 0
 
 
+def run_star(args):
+    """The stage with its q-star expansion: for each of the bench's 8 q, g at
+    every full-BZ k and its rotation onto every member of the q's star
+    (compute_elphq_star), with the Dmats of the 48 operations resident."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64
+    build_library()
+    s = synth.make_system("c1")
+    # the stars as a phonon code lists them: members S q, the first S producing each
+    A, qst = s.alat, []
+    for q in s.qpts:
+        qc = np.linalg.solve(A.T, np.asarray(q, float))
+        mem, sy = [], []
+        for i, R in enumerate(s.sym_R):
+            sq = A.T @ (R @ qc)
+            if not any(np.linalg.norm((sq - m) - np.rint(sq - m)) < 1e-5 for m in mem):
+                mem.append(sq)
+                sy.append(i)
+        qst.append(np.array(sy, np.int32))
+    nq_bz = sum(len(x) for x in qst)
+    gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+    elems = nq_bz * s.nk_bz * gsz
+    prec = args.precision
+    ctx = LelphGPU(s, prec, device=local)
+    ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev, host=False)
+
+    def step():
+        for iq in range(len(s.qpts)):
+            ctx.compute_elphq_star(s.qpts[iq], s.eigVec[iq], s.dVscf[iq], qst[iq], out=OUT_C64)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    st0 = ctx.stats()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    st1 = ctx.stats()
+    launches = (st1["kernel_launches"] - st0["kernel_launches"]) // args.steps
+    ctx.set_profiling(True)
+    p0 = ctx.stats()
+    step()
+    p1 = ctx.stats()
+    ctx.set_profiling(False)
+    ctx.close()
+    qs_ms = p1["qstar_ms"] - p0["qstar_ms"]
+    items = (nq_bz - len(s.qpts)) * s.nk_bz
+    flops = items * s.nmodes * s.nspin * 2 * 8.0 * s.nbnds ** 3
+    sm_mhz = clk.get("sm_mhz") or 1920.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    line = {"metric": "g elements/s per GB300 with the q-star expansion (every star member at every S k)",
+            "value": elems / wall, "unit": "g_elements/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": prec, "data": "synthetic (seeded, c1 shapes)",
+            "config": {"workload": f"{WORKLOAD}; stars of the 8 q: {[len(x) for x in qst]} members, "
+                                   f"{nq_bz} q in all", "g_elements_per_step": elems,
+                       "timing": "host wall clock around the 8 C-ABI calls (each ends with its D2H copy)"},
+            "e2e": {"value": elems / wall, "unit": "g_elements/s", "h2d_bytes_per_step": int(s.dVscf.nbytes),
+                    "d2h_bytes_per_step": int(elems * 8)},
+            "gpu_launches": int(launches), "clocks": clk,
+            "roofline": {"kernel": "k_qstar", "bound": "fp32 (SIMT FMA)" if prec != "fp64" else "fp64",
+                         "achieved": flops / (qs_ms * 1e-3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": flops / (qs_ms * 1e-3) / 1e12 / fp32_peak, "kernel_ms": qs_ms,
+                         "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x median SM clock under load",
+                         "flops_per_step": flops, "traffic": None}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "dmats":
         return run_dmats(args)
+    if args.workload == "star":
+        return run_star(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
