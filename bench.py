@@ -56,10 +56,11 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
-    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star"],
+    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
                         "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
-                        "q-star expansion of each of the 8 q")
+                        "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
+                        "file layout")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
     return p.parse_args()
 
@@ -667,8 +668,81 @@ def run_star(args):
     return 0
 
 
+def run_dvscf(args):
+    """dV_scf ingest of the bench's 8 q: QE-layout (pattern, nmag, Nz, Ny, Nx)
+    arrays in pinned host memory -> q slots in the mode basis (transpose and
+    eig pats^H on the device)."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU
+    build_library()
+    s = synth.make_system("c1")
+    rng = np.random.default_rng(5)
+    nm, nq = s.nmodes, len(s.qpts)
+    Nx, Ny, Nz = s.fft_dims
+    raws = [torch.empty((nm, s.nmag, Nz, Ny, Nx), dtype=torch.complex128, pin_memory=True) for _ in range(nq)]
+    for r in raws:
+        r.numpy()[...] = s.dVscf[0].transpose(0, 1, 4, 3, 2)
+    pats = np.linalg.qr(rng.standard_normal((nm, nm)) + 1j * rng.standard_normal((nm, nm)))[0]
+    ctx = LelphGPU(s, args.precision, device=local)
+
+    def step():
+        for iq in range(nq):
+            ctx.set_q_dvscf_qe(iq, s.qpts[iq], s.eigVec[iq], pats, raws[iq].numpy())
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    ctx.set_profiling(True)
+    p0 = ctx.stats()
+    step()
+    p1 = ctx.stats()
+    ctx.set_profiling(False)
+    ctx.close()
+    kern = (p1["dvscf_ms"] - p0["dvscf_ms"]) / nq
+    N = Nx * Ny * Nz
+    byts = 2 * nm * s.nmag * N * 16  # one read of the QE layout, one write of the mode basis
+    flops = 8.0 * nm * nm * s.nmag * N  # eig pats^H applied at every point (complex multiply-add = 8 flops)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs") or 6800.0
+    line = {"metric": "dV_scf ingests/s per GB300 (QE layout -> mode-basis q slot)", "value": nq / wall,
+            "unit": "q/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded, c1 shapes)",
+            "config": {"workload": f"8 q of the 4-atom cell: {nm} patterns x {s.nmag} x 48^3 complex128 each "
+                                   f"({nm * s.nmag * N * 16 / 1e6:.1f} MB)",
+                       "timing": "host wall clock around the 8 C-ABI calls (pinned host arrays, H2D included)"},
+            "e2e": {"value": nq / wall, "unit": "q/s", "h2d_bytes_per_step": int(nq * nm * s.nmag * N * 16),
+                    "d2h_bytes_per_step": 0},
+            "gpu_launches": nq, "clocks": clk,
+            "roofline": {"kernel": "k_dvscf_ingest", "bound": "fp64",
+                         "achieved": flops / (kern * 1e-3) / 1e12, "peak": 1.25, "unit": "TFLOP/s",
+                         "frac": flops / (kern * 1e-3) / 1e12 / 1.25, "kernel_ms": kern,
+                         "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak)",
+                         "flops_per_launch": flops, "hbm_gbs": byts / (kern * 1e-3) / 1e9,
+                         "hbm_frac": byts / (kern * 1e-3) / 1e9 / peak, "bytes_per_launch": byts, "traffic": None}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "dvscf":
+        return run_dvscf(args)
     if args.workload == "dmats":
         return run_dmats(args)
     if args.workload == "star":

@@ -98,6 +98,7 @@ typedef struct lelph_gpu_stats
     double dmats_host_ms;        /* host time spent building Dmat jobs (always measured) */
     long long dmats_done;        /* Dmats computed */
     double qstar_ms;             /* device time of the q-star rotations (profiling on) */
+    double dvscf_ms;             /* device time of the dV_scf ingest kernel (profiling on) */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,
@@ -176,6 +177,18 @@ int lelph_gpu_dvlocq(lelph_gpu* h, const double qpt_crys[3], const double* eigVe
  * compute_and_write_elphq (src/elph/elph_driver.c:234-252). */
 int lelph_gpu_set_q_induced(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
                             const double* dVscf_induced);
+
+/* read_dvscf_qe (src/io/qe/read_dvscf.c:15-172) after the file read, on the
+ * device: dvscf_qe is the content of QE's dvscf file for this q, (nmodes
+ * patterns, nmag, Nz, Ny, Nx) complex double in the pattern basis; it is
+ * transposed to (Nx, Ny, Nz), taken to the mode basis (eigVec pats^H dV,
+ * pats = the patterns (nmodes, natom, 3) of read_pattern_qe) and loaded into
+ * q slot `slot`: as the induced part with dVlocq added when induced != 0
+ * (like lelph_gpu_set_q_induced), else as the whole dV (like
+ * lelph_gpu_set_q).  dvscf_out (may be NULL) receives the mode-basis dV
+ * before any dVlocq, (nmodes, nmag, Nx, Ny, Nz) -- read_dvscf_qe's output. */
+int lelph_gpu_set_q_dvscf_qe(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                             const double* pats, const double* dvscf_qe, int induced, double* dvscf_out);
 
 /* rotate_dvscf (src/symmetries/rotate_dvscf.c:22-368): dV_scf of S q from
  * dV_scf of q for the symmetry (Rmat cartesian row-major, tau cartesian,

@@ -96,6 +96,7 @@ struct lelph_gpu
     // Dmats: Miller -> position tables of the iBZ lists, the job table and the
     // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
     DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32, d_dmstar, d_gstar, d_qsitems;
+    DevBuf d_dvraw;  // QE-layout dV_scf of the last ingest and eig pats^H
     bool dm_coef32_ready = false;
     long long coef_total = 0;  // complex coefficients of every iBZ k
     std::unordered_map<long long, int> khash;  // full-BZ k-points by wrapped, quantised coordinates
@@ -922,7 +923,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
-                      &h->d_qsitems};
+                      &h->d_qsitems, &h->d_dvraw};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1211,7 +1212,7 @@ static int set_q_common(lelph_gpu* h, int slot, const double qpt_crys[3], const 
         {
             double kq[3];
             for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * k + x] + (conv ? -qpt_crys[x] : qpt_crys[x]);
-            int o = find_k(h, kq);
+            int o = find_k_fast(h, kq);
             if (o < 0) continue;  // the run reports non-commensurate grids
             int ik = conv ? o : k, ikq = conv ? k : o;
             int u[3];
@@ -1544,6 +1545,56 @@ extern "C" int lelph_gpu_set_q_induced(lelph_gpu* h, int slot, const double qpt_
     return LELPH_GPU_OK;
 }
 
+extern "C" int lelph_gpu_set_q_dvscf_qe(lelph_gpu* h, int slot, const double qpt_crys[3], const double* eigVec,
+                                        const double* pats, const double* dvscf_qe, int induced, double* dvscf_out)
+{
+    if (!h || !pats || !dvscf_qe) return LELPH_GPU_ERR_INVALID;
+    if (induced && !h->vl_ready) return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_set_local_pseudo was not called");
+    int rc = set_q_common(h, slot, qpt_crys, eigVec, nullptr);
+    if (rc) return rc;
+    const lelph_gpu_desc& d = h->d;
+    const int nm = d.nmodes;
+    const long long NN = (long long)h->Nbox[0] * h->Nbox[1] * h->Nbox[2];
+    const size_t dvn = (size_t)nm * d.nmag * NN;
+    // eig pats^H (read_dvscf.c:113-128), host
+    std::vector<double2> M((size_t)nm * nm);
+    for (int v = 0; v < nm; ++v)
+        for (int p = 0; p < nm; ++p)
+        {
+            std::complex<double> acc = 0;
+            for (int a = 0; a < nm; ++a)
+                acc += std::complex<double>(eigVec[2 * (v * nm + a)], eigVec[2 * (v * nm + a) + 1]) *
+                       std::conj(std::complex<double>(pats[2 * (p * nm + a)], pats[2 * (p * nm + a) + 1]));
+            M[(size_t)v * nm + p] = make_double2(acc.real(), acc.imag());
+        }
+    rc = ensure(h, h->d_dvraw, sizeof(double2) * (dvn + (size_t)nm * nm));
+    if (rc) return rc;
+    double2* raw = (double2*)h->d_dvraw.p;
+    double2* dM = raw + dvn;
+    CUDA_TRY(h, cudaMemcpyAsync(raw, dvscf_qe, sizeof(double2) * dvn, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dM, M.data(), sizeof(double2) * M.size(), cudaMemcpyHostToDevice, h->st));
+    double2* slot_dv = (double2*)h->d_dvr.p + (size_t)slot * dvn;
+    tstart(h);
+    if (lelph_launch_dvscf_ingest(raw, dM, nm, d.nmag, h->Nbox[0], h->Nbox[1], h->Nbox[2], slot_dv, h->st))
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "dvscf ingest launch configuration");
+    h->stats.kernel_launches += 1;
+    CUDA_TRY(h, cudaGetLastError());
+    h->stats.dvscf_ms += tstop(h);
+    if (dvscf_out)
+        CUDA_TRY(h, cudaMemcpyAsync(dvscf_out, slot_dv, sizeof(double2) * dvn, cudaMemcpyDeviceToHost, h->st));
+    if (induced)
+    {
+        rc = dvloc_device(h, qpt_crys, (const double2*)h->d_eig.p + (size_t)slot * nm * nm);
+        if (rc) return rc;
+        lelph_launch_add_dvscf(slot_dv, (const double2*)h->d_vloc.p, nm, d.nmag, NN, h->st);
+        h->stats.kernel_launches += 1;
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    h->windows_ok = false;
+    return LELPH_GPU_OK;
+}
+
 // dV windows of every loaded q slot on the product grid (FP64 plain form;
 // FP32 scaled by a per-mode power of two in the mixed form)
 static int build_windows(lelph_gpu* h)
@@ -1670,7 +1721,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         double qt[3], kq[3];
         for (int x = 0; x < 3; ++x) qt[x] = kminusq ? -q[x] : q[x];
         for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * kbz[i] + x] + qt[x];
-        int ikq = find_k(h, kq);
+        int ikq = find_k_fast(h, kq);
         if (ikq < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
         int idx_k = kbz[i], idx_kq = ikq;
         if (kminusq) std::swap(idx_k, idx_kq);

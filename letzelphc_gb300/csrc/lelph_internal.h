@@ -198,3 +198,8 @@ struct QStarItem
 size_t lelph_qstar_smem_bytes(int nb, int fp64);
 int lelph_launch_qstar(const QStarItem* items, long long nitems, int nb, int nspin, int nmodes, const double2* D,
                        int fp64, int out_c64, const void* g, void* out, cudaStream_t st);
+
+// ------------------------------------------------------------ dV_scf ingest
+// raw (pattern, nmag, Nz, Ny, Nx) -> out (mode, nmag, Nx, Ny, Nz) = M raw, M = eig pats^H
+int lelph_launch_dvscf_ingest(const double2* raw, const double2* M, int nmodes, int nmag, int Nx, int Ny, int Nz,
+                              double2* out, cudaStream_t st);

@@ -49,7 +49,7 @@ class Stats(C.Structure):
         ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
         ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
         ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
-        ("qstar_ms", C.c_double),
+        ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double),
     ]
 
 
@@ -59,7 +59,7 @@ EXPORTS = [
     "lelph_gpu_set_profiling", "lelph_gpu_stats_get", "lelph_gpu_stream", "lelph_gpu_strerror",
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
     "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
-    "lelph_gpu_dmats", "lelph_gpu_compute_elphq_star",
+    "lelph_gpu_dmats", "lelph_gpu_compute_elphq_star", "lelph_gpu_set_q_dvscf_qe",
 ]
 
 _lib = None
@@ -84,6 +84,7 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_rotate_dvscf.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
     L.lelph_gpu_dmats.argtypes = [vp, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_longlong, _dp]
+    L.lelph_gpu_set_q_dvscf_qe.argtypes = [vp, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp]
     L.lelph_gpu_compute_elphq_star.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int,
                                                _ip, C.c_int, vp]
     L.lelph_gpu_run.argtypes = [vp, C.c_int, _ip, _ip, C.c_int, C.c_int, C.c_int, vp]
@@ -250,6 +251,20 @@ class LelphGPU:
             v = np.ascontiguousarray(dVscf_induced, dtype=np.complex128)
             vp = _ptr(v)
         self._check(self._L.lelph_gpu_set_q_induced(self.h, slot, _ptr(q), _ptr(e), vp))
+
+    def set_q_dvscf_qe(self, slot, qpt, eigVec, pats, dvscf_qe, induced=False, want_dv=False):
+        """Load a q slot from QE's dvscf layout (patterns, nmag, Nz, Ny, Nx)
+        through the device ingest; with want_dv, return the mode-basis dV
+        (nmodes, nmag, Nx, Ny, Nz)."""
+        q = np.ascontiguousarray(qpt, dtype=np.float64)
+        e = np.ascontiguousarray(eigVec, dtype=np.complex128)
+        p = np.ascontiguousarray(pats, dtype=np.complex128)
+        raw = np.ascontiguousarray(dvscf_qe, dtype=np.complex128)
+        s = self.sys
+        out = np.empty((s.nmodes, s.nmag) + tuple(s.fft_dims), np.complex128) if want_dv else None
+        self._check(self._L.lelph_gpu_set_q_dvscf_qe(self.h, slot, _ptr(q), _ptr(e), _ptr(p), _ptr(raw),
+                                                     int(induced), _ptr(out) if want_dv else None))
+        return out
 
     def rotate_dvscf(self, qpt, R, tau, time_rev, composite, dv_in):
         """rotate_dvscf on the device: dV of S q, same shape as dv_in

@@ -14,6 +14,8 @@ It restates, in numpy FP64, the reference's G-space algorithm for one q-point
   the q loop): src/symmetries/elec_reps.c:16-413, src/elph/compute_dmats.c:20-131
 * ``compute_elphq_star`` (the q-star loop of the stage):
   src/elph/compute_elph_matq.c:116-217
+* ``read_dvscf_qe`` (the dV_scf ingest after the file read):
+  src/io/qe/read_dvscf.c:15-172
 * ``vloc_table``, ``dvlocq``, ``add_dvscf_qe`` (the per-q local bare
   potential that elph_driver adds before the stage,
   src/elph/elph_driver.c:234-252): src/dvloc/vlocg_table.c:16-154,
@@ -549,6 +551,17 @@ def compute_elphq_star(s, iq, star_syms, D, eigVec=None, dVscfq=None, non_loc=Tr
                 raise ValueError("Unable to to find S*k index")
             out[istar, isk] = gs
     return out
+
+
+def read_dvscf_qe(raw, eig, pats, nmag, fft_dims):
+    """read_dvscf_qe after the file read, src/io/qe/read_dvscf.c:15-172: raw
+    (patterns, nmag, Nz, Ny, Nx) -> (x, y, z), then the mode basis
+    dV_nu = sum_p (eig pats^H)[nu][p] dV_p.  Returns (nmodes, nmag, Nx, Ny, Nz)."""
+    Nx, Ny, Nz = fft_dims
+    nm = eig.shape[0]
+    d = np.asarray(raw).reshape(nm, nmag, Nz, Ny, Nx).transpose(0, 1, 4, 3, 2)
+    M = eig.reshape(nm, -1) @ np.conj(np.asarray(pats).reshape(nm, -1)).T
+    return np.einsum("vp,pmxyz->vmxyz", M, d)
 
 
 # ------------------------------------------------------- local bare potential

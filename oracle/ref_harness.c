@@ -13,6 +13,7 @@
  *        lelph_ref <system.bin> <unused> rotdv <spec.bin> <dv_out.bin>
  *        lelph_ref <system.bin> <unused> dmats <D_out.bin>
  *        lelph_ref <system.bin> <g_out.bin> star <star.bin>
+ *        lelph_ref <system.bin> <unused> dvscf <spec.bin> <dvscf_file> <dv_out.bin>
  *
  * dvloc: the system's dVscf records are the induced part (QE's dvscf); the
  * harness builds the V_loc table (create_vlocg_table, src/dvloc/vlocg_table.c)
@@ -37,6 +38,10 @@
  * reads, so compute_and_write_elphq expands each q over its star
  * (src/elph/compute_elph_matq.c:159-217); g_out.bin is (nq_BZ, nk_BZ, ...).
  *
+ * dvscf: read_dvscf_qe (src/io/qe/read_dvscf.c:15-172) of dvscf_file (QE's
+ * layout: (patterns, nmag, Nz, Ny, Nx) complex128) with the spec's eig and
+ * pats records; dv_out.bin is the dV in the mode basis (nmodes, nmag, Nx, Ny, Nz).
+ *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
 #include <math.h>
@@ -50,6 +55,7 @@
 #include "common/dtypes.h"
 #include "dvloc/dvloc.h"
 #include "elph/elph.h"
+#include "io/qe/qe_io.h"
 #include "netcdf.h"
 #include "symmetries/symmetries.h"
 
@@ -282,6 +288,21 @@ int main(int argc, char** argv)
         if (!fr) die("cannot write rotdv output");
         fwrite(out, 1, din->nbytes, fr);
         fclose(fr);
+        return 0;
+    }
+    if (argc >= 7 && !strcmp(argv[3], "dvscf"))
+    {
+        /* read_dvscf_qe of a dvscf file in QE's layout, with the eig and pats
+         * records of the spec (pattern -> mode basis) */
+        load(argv[4]);
+        const size_t n = (size_t)nmodes * nmag * Nx * Ny * Nz;
+        double _Complex* dvo = malloc(sizeof(double _Complex) * n);
+        if (!dvo) die("out of memory");
+        read_dvscf_qe(argv[5], &lat, get("eig", 1)->data, get("pats", 1)->data, dvo, comm.commK);
+        FILE* fo = fopen(argv[6], "wb");
+        if (!fo) die("cannot write dvscf output");
+        fwrite(dvo, sizeof(double _Complex), n, fo);
+        fclose(fo);
         return 0;
     }
     if (argc >= 5 && !strcmp(argv[3], "dmats"))

@@ -65,3 +65,18 @@ int MPI_Alltoallv(const void* s, const int* scs, const int* sdispls, MPI_Datatyp
 double MPI_Wtime(void);
 int MPI_Abort(MPI_Comm comm, int code);
 int MPI_Error_string(int code, char* str, int* len);
+
+/* MPI-IO: a rank's file view is the whole file (one process) */
+typedef struct
+{
+    int source, tag, error;
+} MPI_Status;
+typedef int MPI_Info;
+typedef void* MPI_File;
+typedef long long MPI_Offset;
+#define MPI_STATUS_IGNORE ((MPI_Status*)0)
+#define MPI_INFO_NULL ((MPI_Info)0)
+#define MPI_MODE_RDONLY 2
+int MPI_File_open(MPI_Comm comm, const char* filename, int amode, MPI_Info info, MPI_File* fh);
+int MPI_File_read_at_all(MPI_File fh, MPI_Offset offset, void* buf, int count, MPI_Datatype t, MPI_Status* status);
+int MPI_File_close(MPI_File* fh);

@@ -192,3 +192,26 @@ int MPI_Error_string(int code, char* str, int* len)
     *len = snprintf(str, MPI_MAX_ERROR_STRING, "single-rank MPI stand-in error %d", code);
     return 0;
 }
+
+int MPI_File_open(MPI_Comm comm, const char* filename, int amode, MPI_Info info, MPI_File* fh)
+{
+    (void)comm; (void)info;
+    if (amode != MPI_MODE_RDONLY) return 1;
+    FILE* f = fopen(filename, "rb");
+    *fh = f;
+    return f ? MPI_SUCCESS : 1;
+}
+int MPI_File_read_at_all(MPI_File fh, MPI_Offset offset, void* buf, int count, MPI_Datatype t, MPI_Status* status)
+{
+    (void)status;
+    FILE* f = (FILE*)fh;
+    if (fseek(f, (long)offset, SEEK_SET)) return 1;
+    const size_t n = (size_t)count * tsize(t);
+    return fread(buf, 1, n, f) == n ? MPI_SUCCESS : 1;
+}
+int MPI_File_close(MPI_File* fh)
+{
+    int e = fclose((FILE*)*fh);
+    *fh = NULL;
+    return e ? 1 : MPI_SUCCESS;
+}

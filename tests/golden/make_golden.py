@@ -11,12 +11,14 @@ stage (create_vlocg_table / dVlocq / add_dvscf_qe, src/dvloc/), with the
 matrix elements computed from the summed dV; rotate_dvscf.npz pins
 rotate_dvscf, dmats.npz the electronic representation matrices
 (electronic_reps, src/symmetries/elec_reps.c:16) and star_*.npz the stage's
-q-star expansion (src/elph/compute_elph_matq.c:159-217).
+q-star expansion (src/elph/compute_elph_matq.c:159-217); dvscf_qe.npz pins
+the dV_scf ingest (read_dvscf_qe, src/io/qe/read_dvscf.c:15).
 
 Run from the repo root after ``make -C oracle``:
     python tests/golden/make_golden.py            (every fixture)
     python tests/golden/make_golden.py dmats      (only dmats.npz)
     python tests/golden/make_golden.py star       (only star_*.npz)
+    python tests/golden/make_golden.py dvscf      (only dvscf_qe.npz)
 """
 import json
 import os
@@ -255,6 +257,54 @@ def star_fixture(tmp):
         print(name, g.shape, ns.tolist(), float(np.abs(g).max()))
 
 
+# read_dvscf_qe (src/io/qe/read_dvscf.c:15): seeded QE-layout dvscf files and
+# patterns; name -> (base config, overrides, seed)
+DVSCF_SYS = {
+    "c0": ("c0", {"kgrid": (2, 2, 2), "nbnds": 2, "qpts": [(0.5, 0, 0)]}, 11),
+    "lsda": ("c0", {"nspin": 2, "nbnds": 2, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}, 12),
+    "soc": ("c0", {"kind": "zincblende", "timerev": True, "nspinor": 2, "nmag": 4, "soc": True, "ls": (0, 1, 2),
+                   "nbnds": 2, "npw": 150, "fft": (20, 20, 20), "kgrid": (2, 2, 2), "qpts": [(0.5, 0.5, 0)]}, 13),
+    "hex_odd": ("c2", {"kgrid": (3, 3, 1), "fft": (15, 15, 60), "nbnds": 2, "npw": 100,
+                       "qpts": [(1 / 3, 0, 0)]}, 14),
+}
+DVSCF_SAMPLE = 997
+
+
+def dvscf_inputs(s, seed):
+    """QE-layout dvscf (patterns, nmag, Nz, Ny, Nx) and unitary patterns, seeded."""
+    rng = np.random.default_rng(seed)
+    Nx, Ny, Nz = s.fft_dims
+    nm = s.nmodes
+    raw = rng.standard_normal((nm, s.nmag, Nz, Ny, Nx)) + 1j * rng.standard_normal((nm, s.nmag, Nz, Ny, Nx))
+    pats = np.linalg.qr(rng.standard_normal((nm, nm)) + 1j * rng.standard_normal((nm, nm)))[0]
+    return raw, pats
+
+
+def dvscf_fixture(tmp):
+    rec = {}
+    for name, (base, ov, seed) in DVSCF_SYS.items():
+        s = synth.make_system(base, dict(ov))
+        raw, pats = dvscf_inputs(s, seed)
+        sysf = os.path.join(tmp, "dvs_" + name + ".bin")
+        synth.write_system(s, sysf)
+        spec = os.path.join(tmp, "dvs_spec.bin")
+        with open(spec, "wb") as f:
+            f.write(b"LELPHSYS")
+            synth._rec(f, "eig", s.eigVec[0])
+            synth._rec(f, "pats", pats)
+            f.write(b"END\0" + b"\0" * 28)
+        rawf = os.path.join(tmp, "dvscf_raw.bin")
+        raw.astype(np.complex128).tofile(rawf)
+        outf = os.path.join(tmp, "dvscf_out.bin")
+        subprocess.run([REF, sysf, os.path.join(tmp, "unused.bin"), "dvscf", spec, rawf, outf], check=True)
+        out = np.fromfile(outf, np.complex128)
+        rec[name + "_sample"] = out[::DVSCF_SAMPLE]
+        rec[name + "_norm"] = np.linalg.norm(out.reshape(s.nmodes, -1), axis=1)
+        print("dvscf", name, out.shape, float(np.abs(out).max()))
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "dvscf_qe.npz"), systems=np.array(json.dumps(DVSCF_SYS)),
+                        sample=np.array(DVSCF_SAMPLE), **rec)
+
+
 if __name__ == "__main__":
     only = sys.argv[1:]
     with tempfile.TemporaryDirectory() as tmp:
@@ -269,3 +319,5 @@ if __name__ == "__main__":
             dmats_fixture(tmp)
         if not only or "star" in only:
             star_fixture(tmp)
+        if not only or "dvscf" in only:
+            dvscf_fixture(tmp)

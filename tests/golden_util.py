@@ -59,3 +59,22 @@ def load_star(name):
     ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls", "npw") else v)
           for k, v in spec["overrides"].items()}
     return z, synth.make_system(spec["base"], ov), bool(spec["kminusq"])
+
+
+def load_dvscf_qe():
+    """(npz, {name: (System, raw, pats)}) of tests/golden/dvscf_qe.npz: the
+    QE-layout dvscf inputs are regenerated from their seeds (the arithmetic of
+    tests/golden/make_golden.py:dvscf_inputs)."""
+    z = np.load(os.path.join(GOLDEN_DIR, "dvscf_qe.npz"))
+    out = {}
+    for name, (base, ov, seed) in json.loads(str(z["systems"])).items():
+        ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls", "npw") else v)
+              for k, v in ov.items()}
+        s = synth.make_system(base, ov)
+        rng = np.random.default_rng(seed)
+        Nx, Ny, Nz = s.fft_dims
+        nm = s.nmodes
+        raw = rng.standard_normal((nm, s.nmag, Nz, Ny, Nx)) + 1j * rng.standard_normal((nm, s.nmag, Nz, Ny, Nx))
+        pats = np.linalg.qr(rng.standard_normal((nm, nm)) + 1j * rng.standard_normal((nm, nm)))[0]
+        out[name] = (s, raw, pats)
+    return z, out

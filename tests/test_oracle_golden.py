@@ -122,3 +122,18 @@ def test_qstar_expansion_matches_reference():
             r = ref[pos:pos + ns[iq]]
             assert np.abs(g - r).max() < 1e-12 * np.abs(r).max(), (name, iq)
             pos += ns[iq]
+
+
+def test_dvscf_ingest_matches_reference():
+    """read_dvscf_qe (src/io/qe/read_dvscf.c:15-172): transpose of QE's layout and
+    pattern -> mode basis, samples and per-mode norms to 1e-12 (nmag 1, 2, 4 and
+    a box whose sides are not multiples of the device tile)."""
+    from golden_util import load_dvscf_qe
+    z, cases = load_dvscf_qe()
+    st = int(z["sample"])
+    for name, (s, raw, pats) in cases.items():
+        out = O.read_dvscf_qe(raw, s.eigVec[0], pats, s.nmag, s.fft_dims).reshape(-1)
+        smp = z[name + "_sample"]
+        assert np.abs(out[::st] - smp).max() < 1e-12 * np.abs(smp).max(), name
+        nrm = np.linalg.norm(out.reshape(s.nmodes, -1), axis=1)
+        assert np.abs(nrm - z[name + "_norm"]).max() < 1e-12 * nrm.max(), name
