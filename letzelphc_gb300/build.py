@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liblelph_gpu.so")
 SOURCES = ["fft_gather.cu", "sandwich.cu", "nonlocal.cu", "dvloc.cu", "rotate_dv.cu", "dmats.cu", "qstar.cu",
-           "dvscf.cu", "lelph_gpu.cu"]
+           "dvscf.cu", "lelph_gpu.cu", "ndb_elph.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -30,7 +30,8 @@ def _stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "lelph_gpu.h")]
+    inc = os.path.join(HERE, "..", "include")
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(inc, f) for f in os.listdir(inc)]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
@@ -42,7 +43,7 @@ def build_library(force=False, verbose=False):
     nvcc = _nvcc()
 
     def one(src):
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

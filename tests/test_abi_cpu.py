@@ -29,6 +29,15 @@ def test_library_exports_header_symbols():
     assert set(names) == set(elph.EXPORTS)
 
 
+def test_ndb_writer_exports_header_symbols():
+    from letzelphc_gb300 import ndb
+    lib = ctypes.CDLL(build_library())
+    names = sorted(set(re.findall(r"\b(lelph_ndb_[a-z_]+)\s*\(", open(os.path.join(ROOT, "include", "lelph_ndb.h")).read())))
+    assert set(names) == set(ndb.EXPORTS)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
 def test_descriptor_layout_matches_c():
     src = r'''
 #include <stdio.h>

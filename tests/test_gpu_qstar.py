@@ -66,3 +66,25 @@ def test_qstar_rejects_non_identity_first_member():
         with pytest.raises(LelphError) as e:
             ctx.compute_elphq_star(s.qpts[0], s.eigVec[0], s.dVscf[0], [3, 0])
         assert e.value.status == -1
+
+
+def test_qstar_rows_through_the_ndb_writer(tmp_path):
+    """The drop-in output path: star rows from the device written with the
+    ndb.elph writer and read back by an independent netCDF reader equal the
+    reference's elph_mat."""
+    netcdf = pytest.importorskip("scipy.io").netcdf_file
+    from letzelphc_gb300.ndb import NdbElph
+    z, s, kmq = load_star("star_c0")
+    ns, qs = z["nqstar"], z["qsym"]
+    qmap = [(iq, int(qs[int(ns[:iq].sum()) + j])) for iq in range(len(s.qpts)) for j in range(ns[iq])]
+    path = str(tmp_path / "ndb.elph")
+    with LelphGPU(s, "fp64") as ctx, NdbElph(path, s, np.zeros((len(qmap), 3)), s.qpts, qmap) as f:
+        for iq in range(len(s.qpts)):
+            pos, n = _rows(z, iq)
+            g = ctx.compute_elphq_star(s.qpts[iq], s.eigVec[iq], s.dVscf[iq], qs[pos:pos + n], kminusq=kmq)
+            for j in range(n):
+                f.put_elph(pos + j, 0, g[j])
+    with netcdf(path, "r", mmap=False) as f:
+        g = f.variables["elph_mat"].data
+        got = g[..., 0] + 1j * g[..., 1]
+    assert np.abs(got - z["g"]).max() < 1e-10 * np.abs(z["g"]).max()
