@@ -74,7 +74,7 @@ struct lelph_gpu
     DevBuf d_miller, d_pwoff, d_npw, d_coef, d_coefoff, d_gvec, d_fk, d_fkoff, d_ksym, d_chat, d_chatoff;
     DevBuf d_psi64, d_boxes32, d_bsplit, d_psi32, d_band_scale, d_proj;
     DevBuf d_atype, d_apos, d_pp, d_fsign, d_fcoef, d_fcoefoff;
-    DevBuf d_tw64[3], d_tw32[3], d_twN[3];
+    DevBuf d_tw64[3], d_tw32[3], d_twN[3], d_twN32[3];
     DevBuf d_dvr, d_eig, d_maxabs;                 // per q slot: dV_scf on the reference box (FP64), eigVec
     DevBuf d_win64, d_win32, d_winscale, d_wtmpN, d_wtmpM;  // dV windows on the product grid, per (slot, umklapp)
     DevBuf d_pairs, d_glocal, d_partials, d_gout, d_status, d_tmp;
@@ -274,7 +274,8 @@ float pow2_scale(double bound, double target)
 
 // scaled FP32 copy of nwin windows (rows (mode, component) of M points) into the
 // tile-major window array: 32-point blocks of all ncomp rows of a window contiguous
-__global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict__ out, int nwin, int ncomp,
+template <typename T2>
+__global__ void k_dv_convert(const T2* __restrict__ in, float2* __restrict__ out, int nwin, int ncomp,
                              long long M, int wbase, int nmag, const float* __restrict__ scale)
 {
     const long long nkb = M / 32;
@@ -287,32 +288,34 @@ __global__ void k_dv_convert(const double2* __restrict__ in, float2* __restrict_
         t /= ncomp;
         const long long kb = t % nkb;
         const int w = (int)(t / nkb);
-        const double2 v = in[((size_t)w * ncomp + row) * M + kb * 32 + p];
-        const double sc = (double)scale[(size_t)w * (ncomp / nmag) + row / nmag];
+        const T2 v = in[((size_t)w * ncomp + row) * M + kb * 32 + p];
+        const float sc = scale[(size_t)w * (ncomp / nmag) + row / nmag];  // a power of two: exact in either type
         out[(((size_t)(wbase + w) * nkb + kb) * ncomp + row) * 32 + p] = make_float2((float)(v.x * sc), (float)(v.y * sc));
     }
 }
 
 // max over r (and spin rows s) of sum_{s'} |dV^{s s'}(r)| per mode -> atomicMax on float bits
-__global__ void k_dv_maxabs(const double2* __restrict__ dv, int nmodes, int nmag, long long N,
+template <typename T2>
+__global__ void k_dv_maxabs(const T2* __restrict__ dv, int nmodes, int nmag, long long N,
                             unsigned* __restrict__ maxbits)
 {
     const int nu = blockIdx.y;
-    const double2* d = dv + (size_t)nu * nmag * N;
+    const T2* d = dv + (size_t)nu * nmag * N;
     float m = 0.f;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x)
     {
         double v;
         if (nmag == 4)
         {
-            double a0 = hypot(d[r].x, d[r].y) + hypot(d[N + r].x, d[N + r].y);
-            double a1 = hypot(d[2 * N + r].x, d[2 * N + r].y) + hypot(d[3 * N + r].x, d[3 * N + r].y);
+            double a0 = hypot((double)d[r].x, (double)d[r].y) + hypot((double)d[N + r].x, (double)d[N + r].y);
+            double a1 = hypot((double)d[2 * N + r].x, (double)d[2 * N + r].y) +
+                        hypot((double)d[3 * N + r].x, (double)d[3 * N + r].y);
             v = fmax(a0, a1);
         }
         else
         {
             v = 0;
-            for (int c = 0; c < nmag; ++c) v = fmax(v, hypot(d[c * N + r].x, d[c * N + r].y));
+            for (int c = 0; c < nmag; ++c) v = fmax(v, hypot((double)d[c * N + r].x, (double)d[c * N + r].y));
         }
         m = fmaxf(m, (float)v);
     }
@@ -918,7 +921,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_fkoff, &h->d_ksym, &h->d_chat, &h->d_chatoff, &h->d_psi64, &h->d_boxes32, &h->d_bsplit,
                       &h->d_psi32, &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
                       &h->d_fcoefoff, &h->d_tw64[0], &h->d_tw64[1], &h->d_tw64[2], &h->d_tw32[0], &h->d_tw32[1],
-                      &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_dvr, &h->d_eig,
+                      &h->d_tw32[2], &h->d_twN[0], &h->d_twN[1], &h->d_twN[2], &h->d_twN32[0], &h->d_twN32[1],
+                      &h->d_twN32[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
@@ -967,7 +971,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         if (pack.size() == 2) h->d_fcoef.n = 16;  // marks "no coefficients"
         UP(h->d_fcoefoff, off.data(), sizeof(int) * off.size());
     }
-    // twiddles e^{+2 pi i t / L}: product grid (FP64, FP32) and reference box (FP64)
+    // twiddles e^{+2 pi i t / L}: product grid and reference box, FP64 and FP32
     for (int x = 0; x < 6; ++x)
     {
         int L = x < 3 ? (x == 0 ? h->g.Nx : (x == 1 ? h->g.Ny : h->g.Nz)) : d.fft_dims[x - 3];
@@ -987,6 +991,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         else
         {
             UP(h->d_twN[x - 3], t64.data(), sizeof(double2) * L);
+            UP(h->d_twN32[x - 3], t32.data(), sizeof(float2) * L);
         }
     }
     rc = ensure(h, h->d_coef, sizeof(double2) * (size_t)ctot);
@@ -1141,16 +1146,17 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
 //   dV_G0(r') = sum_d dVhat(d + G0) e^{i d.r'},  d over one period of the product grid
 // (signed representatives), so that (1/M) sum_r' dV_G0 psi_k conj(psi_kq) equals
 // the reference's sum_{G1,G'} c_k(G1) conj(c_kq(G')) dVhat(G' - G1) exactly.
-__global__ void k_dv_window(const double2* __restrict__ dvhat, int ncomp, int Nx, int Ny, int Nz,
+template <typename T2>
+__global__ void k_dv_window(const T2* __restrict__ dvhat, int ncomp, int Nx, int Ny, int Nz,
                             const int* __restrict__ ulms, int nu, int3 dmin, GeomDev g, double invN,
-                            double2* __restrict__ out)
+                            T2* __restrict__ out)
 {
     const long long M = (long long)g.Nx * g.Ny * g.Nz;
     const int c = blockIdx.y;   // (mode, component)
     const int u = blockIdx.z;   // umklapp index
     const int ux = ulms[3 * u], uy = ulms[3 * u + 1], uz = ulms[3 * u + 2];
-    const double2* src = dvhat + (size_t)c * ((size_t)Nx * Ny * Nz);
-    double2* dst = out + ((size_t)u * ncomp + c) * M;
+    const T2* src = dvhat + (size_t)c * ((size_t)Nx * Ny * Nz);
+    T2* dst = out + ((size_t)u * ncomp + c) * M;
     // grid residue x stands for the difference D' = G'' - G1 in [dmin - G0, dmin - G0 + M); value dVhat(D' + G0)
     const int lx = dmin.x - ux, ly = dmin.y - uy, lz = dmin.z - uz;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < M; r += (long long)gridDim.x * blockDim.x)
@@ -1164,8 +1170,8 @@ __global__ void k_dv_window(const double2* __restrict__ dvhat, int ncomp, int Nx
         int ix = ((dx + ux) % Nx + Nx) % Nx;
         int iy = ((dy + uy) % Ny + Ny) % Ny;
         int iz = ((dz + uz) % Nz + Nz) % Nz;
-        double2 v = src[((size_t)ix * Ny + iy) * Nz + iz];
-        dst[r] = make_double2(v.x * invN, v.y * invN);
+        const T2 v = src[((size_t)ix * Ny + iy) * Nz + iz];
+        dst[r] = mk2<T2>((double)v.x * invN, (double)v.y * invN);
     }
 }
 
@@ -1645,6 +1651,43 @@ static int build_windows(lelph_gpu* h)
         if (!h->qslots[s].set) continue;
         const int nu = (int)h->qslots[s].ulms.size() / 3;
         if (nu == 0) continue;
+        if (h->mixed)
+        {
+            // mixed form: FP32 transforms (the windows end up as FP32 tiles);
+            // the scratch arrays of the FP64 path hold the FP32 data
+            float2* tN = (float2*)h->d_wtmpN.p;
+            float2* tM = (float2*)h->d_wtmpM.p;
+            lelph_launch_dm_c64((const double2*)h->d_dvr.p + (size_t)s * ncomp * NN, (long long)ncomp * NN, tN, h->st);
+            lelph_launch_fft_contig_f(tN, (long long)ncomp * h->Nbox[0] * h->Nbox[1], h->planN[2],
+                                      (const float2*)h->d_twN32[2].p, -1, h->st);
+            lelph_launch_fft_strided_f(tN, (long long)ncomp * h->Nbox[0], h->Nbox[2], h->planN[1],
+                                       (const float2*)h->d_twN32[1].p, -1, h->st);
+            lelph_launch_fft_strided_f(tN, (long long)ncomp, h->Nbox[1] * h->Nbox[2], h->planN[0],
+                                       (const float2*)h->d_twN32[0].p, -1, h->st);
+            CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->qslots[s].ulms.data(), sizeof(int) * 3 * nu,
+                                        cudaMemcpyHostToDevice, h->st));
+            const int3 dm = make_int3(h->qslots[s].dmin[0], h->qslots[s].dmin[1], h->qslots[s].dmin[2]);
+            k_dv_window<float2><<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
+                                                                        (const int*)h->d_tmp.p, nu, dm, g,
+                                                                        1.0 / (double)NN, tM);
+            lelph_launch_fft_contig_f(tM, (long long)nu * ncomp * g.Nx * g.Ny, h->plan[2],
+                                      (const float2*)h->d_tw32[2].p, +1, h->st);
+            lelph_launch_fft_strided_f(tM, (long long)nu * ncomp * g.Nx, g.Nz, h->plan[1],
+                                       (const float2*)h->d_tw32[1].p, +1, h->st);
+            lelph_launch_fft_strided_f(tM, (long long)nu * ncomp, g.Ny * g.Nz, h->plan[0],
+                                       (const float2*)h->d_tw32[0].p, +1, h->st);
+            unsigned* mx = (unsigned*)h->d_maxabs.p;
+            float* sc = (float*)h->d_winscale.p + (size_t)h->win_base[s] * d.nmodes;
+            CUDA_TRY(h, cudaMemsetAsync(mx, 0, sizeof(unsigned) * nu * d.nmodes, h->st));
+            k_dv_maxabs<float2><<<dim3(64, nu * d.nmodes), 256, 0, h->st>>>(tM, nu * d.nmodes, d.nmag, M, mx);
+            k_mode_scale<<<(nu * d.nmodes + 63) / 64, 64, 0, h->st>>>(mx, nu * d.nmodes, sc);
+            k_dv_convert<float2><<<1024, 256, 0, h->st>>>(tM, (float2*)h->d_win32.p, nu, (int)ncomp, M,
+                                                          h->win_base[s], d.nmag, sc);
+            h->stats.kernel_launches += 11;
+            CUDA_TRY(h, cudaGetLastError());
+            continue;
+        }
+        // plain form: FP64 transforms
         double2* tN = (double2*)h->d_wtmpN.p;
         double2* tM = (double2*)h->d_wtmpM.p;
         CUDA_TRY(h, cudaMemcpyAsync(tN, (const double2*)h->d_dvr.p + (size_t)s * ncomp * NN,
@@ -1659,7 +1702,7 @@ static int build_windows(lelph_gpu* h)
         CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->qslots[s].ulms.data(), sizeof(int) * 3 * nu,
                                     cudaMemcpyHostToDevice, h->st));
         const int3 dm = make_int3(h->qslots[s].dmin[0], h->qslots[s].dmin[1], h->qslots[s].dmin[2]);
-        k_dv_window<<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
+        k_dv_window<double2><<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
                                                              (const int*)h->d_tmp.p, nu, dm, g, 1.0 / (double)NN, tM);
         // inverse transform on the product grid
         lelph_launch_fft_contig_d(tM, (long long)nu * ncomp * g.Nx * g.Ny, h->plan[2], (const double2*)h->d_tw64[2].p,
@@ -1669,22 +1712,9 @@ static int build_windows(lelph_gpu* h)
         lelph_launch_fft_strided_d(tM, (long long)nu * ncomp, g.Ny * g.Nz, h->plan[0], (const double2*)h->d_tw64[0].p,
                                    +1, h->st);
         const size_t base = (size_t)h->win_base[s] * ncomp * M;
-        if (!h->mixed)
-        {
-            CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_win64.p + base, tM, sizeof(double2) * (size_t)nu * ncomp * M,
-                                        cudaMemcpyDeviceToDevice, h->st));
-        }
-        else
-        {
-            unsigned* mx = (unsigned*)h->d_maxabs.p;
-            float* sc = (float*)h->d_winscale.p + (size_t)h->win_base[s] * d.nmodes;
-            CUDA_TRY(h, cudaMemsetAsync(mx, 0, sizeof(unsigned) * nu * d.nmodes, h->st));
-            k_dv_maxabs<<<dim3(64, nu * d.nmodes), 256, 0, h->st>>>(tM, nu * d.nmodes, d.nmag, M, mx);
-            k_mode_scale<<<(nu * d.nmodes + 63) / 64, 64, 0, h->st>>>(mx, nu * d.nmodes, sc);
-            k_dv_convert<<<1024, 256, 0, h->st>>>(tM, (float2*)h->d_win32.p, nu, (int)ncomp, M, h->win_base[s],
-                                                  d.nmag, sc);
-        }
-        h->stats.kernel_launches += h->mixed ? 10 : 7;
+        CUDA_TRY(h, cudaMemcpyAsync((double2*)h->d_win64.p + base, tM, sizeof(double2) * (size_t)nu * ncomp * M,
+                                    cudaMemcpyDeviceToDevice, h->st));
+        h->stats.kernel_launches += 7;
         CUDA_TRY(h, cudaGetLastError());
     }
     h->windows_ok = true;
