@@ -107,6 +107,32 @@ __device__ __forceinline__ void dft5(T2* v, int sign)
 // consecutive elements of a line when elements are contiguous (es == 1) and
 // consecutive lines otherwise (ls == 1), so that a warp's shared-memory
 // accesses fall into distinct banks either way.
+// Division by a run-time divisor d through its FP32 reciprocal: q = trunc(x/d)
+// is at most one off for 0 <= x < 2^24 and is corrected from the remainder
+// (the index arithmetic of the passes stays far below that bound).
+struct RecipDiv
+{
+    float inv;
+    int d;
+};
+__device__ __forceinline__ RecipDiv recip_div(int d) { return RecipDiv{__frcp_rn((float)d), d}; }
+__device__ __forceinline__ int div_rem(int x, const RecipDiv& f, int& r)
+{
+    int q = __float2int_rz((float)x * f.inv);
+    r = x - q * f.d;
+    if (r < 0)
+    {
+        --q;
+        r += f.d;
+    }
+    else if (r >= f.d)
+    {
+        ++q;
+        r -= f.d;
+    }
+    return q;
+}
+
 template <typename T2, typename T, int R>
 __device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int L,
                                               int Ns, int es, int ls, const T2* tw, int sign)
@@ -115,20 +141,16 @@ __device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __
     const int nwork = nlines * LR;
     const int tstride = L / (Ns * R);
     const bool line_fast = es != 1;
+    const RecipDiv dl = recip_div(line_fast ? nlines : LR), dn = recip_div(Ns);
     for (int w = threadIdx.x; w < nwork; w += blockDim.x)
     {
         int line, j;
         if (line_fast)
-        {
-            j = w / nlines;
-            line = w - j * nlines;
-        }
+            j = div_rem(w, dl, line);
         else
-        {
-            line = w / LR;
-            j = w - line * LR;
-        }
-        int k = j % Ns;
+            line = div_rem(w, dl, j);
+        int k;
+        const int jq = div_rem(j, dn, k);
         const T2* s = src + (size_t)line * ls;
         T2 v[R];
 #pragma unroll
@@ -148,7 +170,7 @@ __device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __
         if (R == 4) dft4<T2, T>(v, sign);
         if (R == 5) dft5<T2, T>(v, sign);
         T2* d = dst + (size_t)line * ls;
-        int base = (j / Ns) * Ns * R + k;
+        int base = jq * Ns * R + k;
 #pragma unroll
         for (int r = 0; r < R; ++r) d[(size_t)(base + r * Ns) * es] = v[r];
     }
@@ -209,16 +231,19 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
         __syncthreads();
         const int na = nact;
         if (na == 0) return;
+        const RecipDiv dL = recip_div(p.L);
         for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
         {
-            const int j = i / p.L, e = i - j * p.L;
+            int e;
+            const int j = div_rem(i, dL, e);
             a[i] = g[(size_t)act[j] * p.L + e];
         }
         __syncthreads();
         T2* r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
         for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
         {
-            const int j = i / p.L, e = i - j * p.L;
+            int e;
+            const int j = div_rem(i, dL, e);
             g[(size_t)act[j] * p.L + e] = r[i];
         }
         return;
@@ -257,16 +282,19 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
     int ic = min(ich, inner - i0);
     T2* g = data + (size_t)o * p.L * inner + i0;
     int n = p.L * ic;
+    const RecipDiv dc = recip_div(ic);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
-        int l = idx / ic, i = idx - l * ic;
+        int i;
+        const int l = div_rem(idx, dc, i);
         a[l * ic + i] = g[(size_t)l * inner + i];
     }
     __syncthreads();
     T2* r = fft_smem<T2, T>(a, b, ic, ic, 1, p, tws, sign);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
-        int l = idx / ic, i = idx - l * ic;
+        int i;
+        const int l = div_rem(idx, dc, i);
         g[(size_t)l * inner + i] = r[l * ic + i];
     }
 }
@@ -319,9 +347,11 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     int n = p.L * ic;
     // x planes that the sphere of this k-point does not reach are zero: not read
     const uint8_t* xpl = mk.xpl ? mk.xpl + (size_t)(o / mk.nbox_per_k) * gd.Nx : nullptr;
+    const RecipDiv dc = recip_div(ic);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
-        int l = idx / ic, i = idx - l * ic;
+        int i;
+        const int l = div_rem(idx, dc, i);
         a[l * ic + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : g[(size_t)l * inner + i];
     }
     __syncthreads();
