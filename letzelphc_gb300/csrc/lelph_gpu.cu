@@ -623,16 +623,29 @@ static int upload_wfc(lelph_gpu* h, const double* const* wfc)
     }
     // power-of-two operand scales: |psi_b(r)| <= sum_G sum_s |c_b,s(G)| (L1 bound)
     const int nb = d.nbnds;
+    // (the 1.0001 margin covers the rounding of the sum; the host cores share the k-points)
     std::vector<float> sc_ibz((size_t)d.nkpts_iBZ * d.nspin * nb);
-    for (int ik = 0; ik < d.nkpts_iBZ; ++ik)
+    auto scales_of = [&](int ik) {
         for (int s = 0; s < d.nspin; ++s)
             for (int b = 0; b < nb; ++b)
             {
                 const double* c = wfc[ik] + 2 * ((size_t)(s * nb + b) * d.nspinor * h->npw[ik]);
                 double l1 = 0;
-                for (long long i = 0; i < (long long)d.nspinor * h->npw[ik]; ++i) l1 += std::hypot(c[2 * i], c[2 * i + 1]);
+                for (long long i = 0; i < (long long)d.nspinor * h->npw[ik]; ++i)
+                    l1 += std::sqrt(c[2 * i] * c[2 * i] + c[2 * i + 1] * c[2 * i + 1]);
                 sc_ibz[((size_t)ik * d.nspin + s) * nb + b] = pow2_scale(l1 * 1.0001, 16384.0);
             }
+    };
+    {
+        const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), d.nkpts_iBZ));
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nthr; ++w)
+            pool.emplace_back([&, w]() {
+                for (int ik = w; ik < d.nkpts_iBZ; ik += nthr) scales_of(ik);
+            });
+        for (int ik = 0; ik < d.nkpts_iBZ; ik += nthr) scales_of(ik);
+        for (auto& t : pool) t.join();
+    }
     h->band_scale.resize((size_t)d.nkpts_BZ * d.nspin * nb);
     for (int i = 0; i < d.nkpts_BZ; ++i)
         for (int s = 0; s < d.nspin; ++s)
