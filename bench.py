@@ -62,6 +62,8 @@ def parse():
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
                         "file layout")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
+    p.add_argument("--small", action="store_true",
+                   help="star / dvscf workloads on the same cell with a 2x2x2 k grid (profiling cases)")
     return p.parse_args()
 
 
@@ -601,7 +603,7 @@ def run_star(args):
     from letzelphc_gb300.build import build_library
     from letzelphc_gb300.elph import LelphGPU, OUT_C64
     build_library()
-    s = synth.make_system("c1")
+    s = synth.make_system("c1", {"kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0), (0.5, 0.5, 0)]} if args.small else None)
     # the stars as a phonon code lists them: members S q, the first S producing each
     A, qst = s.alat, []
     for q in s.qpts:
@@ -681,7 +683,7 @@ def run_dvscf(args):
     from letzelphc_gb300.build import build_library
     from letzelphc_gb300.elph import LelphGPU
     build_library()
-    s = synth.make_system("c1")
+    s = synth.make_system("c1", {"kgrid": (2, 2, 2)} if args.small else None)
     rng = np.random.default_rng(5)
     nm, nq = s.nmodes, len(s.qpts)
     Nx, Ny, Nz = s.fft_dims

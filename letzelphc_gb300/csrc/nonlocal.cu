@@ -535,6 +535,7 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
     const int mtiles = (gd.nmodes + gd.mt_modes - 1) / gd.mt_modes;
     const int NT = 2 * gd.nbp;
     const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
+    const C2 preT = mk2<C2>(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
     {
         const int m = e / nb, n = e - m * nb;  // m: band of k, n: band of k+q
@@ -592,40 +593,61 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
         }
         for (int nu = 0; nu < gd.nmodes; ++nu)
         {
-            double2 v;
+            const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
             if (mode_fp64)
             {
-                v = glocal[((size_t)zp * gd.nmodes * nb + nu * nb + m) * nb + n];
+                double2 v = glocal[((size_t)zp * gd.nmodes * nb + nu * nb + m) * nb + n];
+                if (non_loc)
+                {
+                    C2 sacc = mk2<C2>(0.0, 0.0);
+#pragma unroll
+                    for (int j = 0; j < NJ; ++j)
+                        if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
+                    v = cadd(v, cmul(pre, make_double2((double)sacc.x, (double)sacc.y)));
+                }
+                if (out_c64)
+                    reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
+                else
+                    reinterpret_cast<double2*>(gout)[oidx] = v;
             }
             else
             {
+                // mixed form: the K-chunk partials summed in the operand type with
+                // TwoSum compensation (as accurate as an FP64 sum of these terms
+                // for an output of this precision), times the exact inverse of the
+                // power-of-two operand scales and 1/M; no FP64 arithmetic
                 const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
                 const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
-                double re = 0.0, im = 0.0;
+                T sre = 0, ere = 0, sim = 0, eim = 0;
                 for (int c = 0; c < nchunks; ++c)
                 {
-                    re += (double)pp[(size_t)c * 128 * NT + n];
-                    im += (double)pp[(size_t)c * 128 * NT + gd.nbp + n];
+                    const T xr = (T)pp[(size_t)c * 128 * NT + n], xi = (T)pp[(size_t)c * 128 * NT + gd.nbp + n];
+                    T t = sre + xr, z = t - sre;
+                    ere += (sre - (t - z)) + (xr - z);
+                    sre = t;
+                    t = sim + xi;
+                    z = t - sim;
+                    eim += (sim - (t - z)) + (xi - z);
+                    sim = t;
                 }
-                const double sc = (double)mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
-                                  (double)band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
-                                  (double)band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
-                const double f = invN / sc;
-                v = make_double2(re * f, im * f);
-            }
-            if (non_loc)
-            {
-                C2 sacc = mk2<C2>(0.0, 0.0);
+                const float sc = mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
+                                 band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
+                                 band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
+                const T f = (T)invN * (T)(1.0f / sc);  // 1/sc: a power of two, exact
+                C2 v = mk2<C2>((double)((sre + ere) * f), (double)((sim + eim) * f));
+                if (non_loc)
+                {
+                    C2 sacc = mk2<C2>(0.0, 0.0);
 #pragma unroll
-                for (int j = 0; j < NJ; ++j)
-                    if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
-                v = cadd(v, cmul(pre, make_double2((double)sacc.x, (double)sacc.y)));
+                    for (int j = 0; j < NJ; ++j)
+                        if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
+                    v = cadd(v, cmul(preT, sacc));
+                }
+                if (out_c64)
+                    reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
+                else
+                    reinterpret_cast<double2*>(gout)[oidx] = make_double2((double)v.x, (double)v.y);
             }
-            const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
-            if (out_c64)
-                reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
-            else
-                reinterpret_cast<double2*>(gout)[oidx] = v;
         }
     }
 }
