@@ -612,10 +612,12 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
             }
             else
             {
-                // mixed form: the K-chunk partials summed in the operand type with
-                // TwoSum compensation (as accurate as an FP64 sum of these terms
-                // for an output of this precision), times the exact inverse of the
-                // power-of-two operand scales and 1/M; no FP64 arithmetic
+                // mixed form: the K-chunk partials are summed in the operand type
+                // with TwoSum compensation (the pair (s, e) holds the sum to about
+                // twice the operand precision) and combined, unscaled (exact inverse
+                // of the power-of-two operand scales, 1/M) and added to the nonlocal
+                // term in FP64: a few FP64 operations per element instead of one
+                // FP64 addition per chunk
                 const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
                 const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
                 T sre = 0, ere = 0, sim = 0, eim = 0;
@@ -633,20 +635,22 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 const float sc = mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
                                  band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
                                  band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
-                const T f = (T)invN * (T)(1.0f / sc);  // 1/sc: a power of two, exact
-                C2 v = mk2<C2>((double)((sre + ere) * f), (double)((sim + eim) * f));
+                const double f = invN * (double)(1.0f / sc);  // 1/sc: a power of two, exact
+                double vr = ((double)sre + (double)ere) * f, vi = ((double)sim + (double)eim) * f;
                 if (non_loc)
                 {
                     C2 sacc = mk2<C2>(0.0, 0.0);
 #pragma unroll
                     for (int j = 0; j < NJ; ++j)
                         if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
-                    v = cadd(v, cmul(preT, sacc));
+                    const C2 t = cmul(preT, sacc);
+                    vr += (double)t.x;
+                    vi += (double)t.y;
                 }
                 if (out_c64)
-                    reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
+                    reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)vr, (float)vi);
                 else
-                    reinterpret_cast<double2*>(gout)[oidx] = make_double2((double)v.x, (double)v.y);
+                    reinterpret_cast<double2*>(gout)[oidx] = make_double2(vr, vi);
             }
         }
     }
