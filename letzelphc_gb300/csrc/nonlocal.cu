@@ -14,6 +14,8 @@
 // with Pi[k][a][p][x][set] = sum_G beta_x(G) conj(c^(G)), c^ the unfolded
 // coefficients (SU(2), fractional-translation phase, time-reversal conj).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include <type_traits>
@@ -112,7 +114,9 @@ template <typename T> static constexpr size_t pj_smem_bytes()
     return sizeof(C2) * (PJ_ROWS * (G + 1) + G * (PJ_SETS + 1) + 4 * G) + sizeof(T) * (16 * G + 3 * G);
 }
 
-// grid: (nk, row blocks, set blocks); 256 threads, 4 rows x 2 sets per thread.
+// grid: (nk, row blocks, set blocks x gsplit); 256 threads, 4 rows x 2 sets per
+// thread; with gsplit > 1 a block takes every gsplit-th chunk of the plane
+// waves and adds its sums into the zeroed Pi entries.
 // Rows r = (atom*nproj_max + p)*4 + x; Pi layout proj[((kbz*rows_tot) + r)*nsets + set],
 // nsets = nspin*nbnds*nspinor, set = (spin*nbnds + band)*nspinor + spinor.
 // T = float: beta, coefficients and products in FP32, each G chunk summed in
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
                                                      const long long* __restrict__ fk_off,
                                                      const double2* __restrict__ chat,
                                                      const long long* __restrict__ chat_off, NonlocalDesc nl,
-                                                     GeomDev gd, double2* __restrict__ proj)
+                                                     GeomDev gd, int gsplit, double2* __restrict__ proj)
 {
     typedef typename cplx_of<T>::type C2;
     constexpr int PG = PjCfg<T>::G;
@@ -145,7 +149,8 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
     const int nsets = gd.nspin * gd.nbnds * gd.nspinor;
     const int rows_tot = nl.natom * nl.nproj_max * 4;
     const int r0 = blockIdx.y * PJ_ROWS;
-    const int s0 = blockIdx.z * PJ_SETS;
+    const int gs = blockIdx.z % gsplit;  // this block's share of the plane waves: chunks gs, gs + gsplit, ...
+    const int s0 = (blockIdx.z / gsplit) * PJ_SETS;
     const int nr = min(PJ_ROWS, rows_tot - r0);
     const int ns = min(PJ_SETS, nsets - s0);
     const int a0 = r0 / (nl.nproj_max * 4);
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
     const double2* Cc = chat + chat_off[kbz];
     const int natom_blk = min(4, nl.natom - a0);
     const int nlm = (nl.lmax + 1) * (nl.lmax + 1);
-    for (int g0 = 0; g0 < npw; g0 += PG)
+    for (int g0 = gs * PG; g0 < npw; g0 += gsplit * PG)
     {
         const int ng = min(PG, npw - g0);
         __syncthreads();
@@ -296,7 +301,15 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
             {
                 double2 v = std::is_same<T, float>::value ? acc64[i][j]
                                                           : make_double2((double)acc[i][j].x, (double)acc[i][j].y);
-                proj[((size_t)kbz * rows_tot + r0 + rr) * nsets + s0 + ss] = v;
+                double2* o = proj + ((size_t)kbz * rows_tot + r0 + rr) * nsets + s0 + ss;
+                if (gsplit == 1)
+                    *o = v;
+                else
+                {
+                    // the plane-wave shares of one k add into the zeroed entry
+                    atomicAdd(&o->x, v.x);
+                    atomicAdd(&o->y, v.y);
+                }
             }
         }
 }
@@ -308,7 +321,17 @@ void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const d
 {
     const int nsets = g.nspin * g.nbnds * g.nspinor;
     const int rows = nl.natom * nl.nproj_max * 4;
-    dim3 grid(nk, (rows + PJ_ROWS - 1) / PJ_ROWS, (nsets + PJ_SETS - 1) / PJ_SETS);
+    const int rb = (rows + PJ_ROWS - 1) / PJ_ROWS, sb = (nsets + PJ_SETS - 1) / PJ_SETS;
+    // one block per (k, row block, set block) leaves most SMs idle for a few k:
+    // the plane waves of a k are shared by up to 8 blocks (about 4 blocks per SM)
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long long base = (long long)nk * rb * sb;
+    const int gsplit = (int)std::max(1LL, std::min(8LL, (4LL * nsm + base - 1) / base));
+    if (gsplit > 1)
+        cudaMemsetAsync(proj + (size_t)k0 * rows * nsets, 0, sizeof(double2) * (size_t)nk * rows * nsets, st);
+    dim3 grid(nk, rb, sb * gsplit);
     static bool attr = false;
     if (!attr)
     {
@@ -320,10 +343,11 @@ void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const d
     }
     if (f32acc)
         k_projections<float><<<grid, 256, pj_smem_bytes<float>(), st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk, fk_off,
-                                                                        chat, chat_off, nl, g, proj);
+                                                                        chat, chat_off, nl, g, gsplit, proj);
     else
         k_projections<double><<<grid, 256, pj_smem_bytes<double>(), st>>>(k0, ksym_dev, gvec, pw_off, npw, Fk,
-                                                                          fk_off, chat, chat_off, nl, g, proj);
+                                                                          fk_off, chat, chat_off, nl, g, gsplit,
+                                                                          proj);
 }
 
 // ------------------------------------------------------------------ finish
