@@ -56,11 +56,11 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
-    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf"],
+    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf", "configs"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
                         "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
-                        "file layout")
+                        "file layout; configs: mixed vs FP64 rate and error on every config's full size")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
     p.add_argument("--small", action="store_true",
                    help="star / dvscf workloads on the same cell with a 2x2x2 k grid (profiling cases)")
@@ -741,8 +741,100 @@ def run_dvscf(args):
     return 0
 
 
+CONFIG_NAMES = ["c0", "c1", "c2", "c3", "c4"]
+
+
+def run_configs(args):
+    """Every configuration at its full size: the mixed form on all (k, q) pairs
+    (device-resident, CUDA events), the FP64 form on a sample of pairs (its
+    full-BZ preparation plus the sampled pairs, scaled to the batch), and the
+    error of the mixed form on that sample with the metric's definition."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64, LelphError
+    build_library()
+    out = {}
+    for name in CONFIG_NAMES:
+        if name == "c4":
+            out[name] = {"status": "not run: the per-k operands of this design (split k+q rows and FP32 psi_k of "
+                                   "all 512 k, 200 bands, 60^3 product grid) need ~0.5 TB; k-batched preparation "
+                                   "and band tiling of the sandwich are not built"}
+            continue
+        t0 = time.perf_counter()
+        s = synth.make_system(name)
+        gen_s = time.perf_counter() - t0
+        nq, nk = len(s.qpts), s.nk_bz
+        qs = np.repeat(np.arange(nq), nk).astype(np.int32)
+        ks = np.tile(np.arange(nk), nq).astype(np.int32)
+        npairs = len(qs)
+        gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+        elems = g_elems(s, npairs)
+        rec = {"pairs": npairs, "g_elements": elems, "input_generation_s": gen_s}
+        try:
+            ctx = LelphGPU(s, args.precision, device=local)
+            for iq in range(nq):
+                ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+            gdev = torch.empty(npairs * gsz * 2, dtype=torch.float32, device="cuda")
+            stream = torch.cuda.ExternalStream(ctx.stream())
+
+            def step():
+                ctx.prepare()
+                ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+
+            for _ in range(2):
+                step()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = max(1, args.steps)
+            e0.record(stream)
+            for _ in range(reps):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            rng = np.random.default_rng(1)
+            sel = np.sort(rng.choice(npairs, size=min(args.fp64_pairs, npairs), replace=False))
+            gm = ctx.run(qs[sel], ks[sel], out=OUT_C64).astype(np.complex128)
+            ctx.close()
+            rec.update({"mixed_value": elems / (ms * 1e-3), "mixed_ms": ms})
+            with LelphGPU(s, "fp64", device=local) as c64:
+                for iq in range(nq):
+                    c64.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+                c64.prepare()
+                c64.run(qs[sel[:1]], ks[sel[:1]])
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                c64.prepare()
+                torch.cuda.synchronize()
+                t_prep = time.perf_counter() - t0
+                t0 = time.perf_counter()
+                g64 = c64.run(qs[sel], ks[sel])
+                torch.cuda.synchronize()
+                t_pairs = time.perf_counter() - t0
+            fp64_rate = elems / (t_prep + t_pairs * npairs / len(sel))
+            rec.update({"fp64_value": fp64_rate, "mixed_over_fp64": rec["mixed_value"] / fp64_rate,
+                        "error_vs_fp64": err_stats(gm, g64), "sample_pairs": len(sel)})
+        except LelphError as e:
+            rec["status"] = f"unsupported: {e}"
+        out[name] = rec
+        print(json.dumps({name: rec}), file=sys.stderr, flush=True)
+    line = {"metric": METRIC, "unit": "g_elements/s", "n_gpus": 1, "dtype": args.precision,
+            "data": "synthetic (seeded, the configurations' shapes)", "configs": out,
+            "error_definition": "e_i = ||g_mixed|-|g_fp64|| / max(|g_fp64|, 1e-6 max|g_fp64|); norm = "
+                                "||g_mixed - g_fp64||_2 / ||g_fp64||_2 (mixed output in complex64)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "configs":
+        return run_configs(args)
     if args.workload == "dvscf":
         return run_dvscf(args)
     if args.workload == "dmats":
