@@ -301,21 +301,26 @@ __global__ void k_dv_maxabs(const T2* __restrict__ dv, int nmodes, int nmag, lon
 {
     const int nu = blockIdx.y;
     const T2* d = dv + (size_t)nu * nmag * N;
+    // in the operand type: the result only picks a power-of-two scale with a margin
+    typedef decltype(T2().x) R;
     float m = 0.f;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x)
     {
-        double v;
+        R v;
         if (nmag == 4)
         {
-            double a0 = hypot((double)d[r].x, (double)d[r].y) + hypot((double)d[N + r].x, (double)d[N + r].y);
-            double a1 = hypot((double)d[2 * N + r].x, (double)d[2 * N + r].y) +
-                        hypot((double)d[3 * N + r].x, (double)d[3 * N + r].y);
-            v = fmax(a0, a1);
+            const R a0 = hypot(d[r].x, d[r].y) + hypot(d[N + r].x, d[N + r].y);
+            const R a1 = hypot(d[2 * N + r].x, d[2 * N + r].y) + hypot(d[3 * N + r].x, d[3 * N + r].y);
+            v = a0 > a1 ? a0 : a1;
         }
         else
         {
             v = 0;
-            for (int c = 0; c < nmag; ++c) v = fmax(v, hypot((double)d[c * N + r].x, (double)d[c * N + r].y));
+            for (int c = 0; c < nmag; ++c)
+            {
+                const R h = hypot(d[c * N + r].x, d[c * N + r].y);
+                v = h > v ? h : v;
+            }
         }
         m = fmaxf(m, (float)v);
     }
@@ -1184,7 +1189,8 @@ __global__ void k_dv_window(const T2* __restrict__ dvhat, int ncomp, int Nx, int
         int iy = ((dy + uy) % Ny + Ny) % Ny;
         int iz = ((dz + uz) % Nz + Nz) % Nz;
         const T2 v = src[((size_t)ix * Ny + iy) * Nz + iz];
-        dst[r] = mk2<T2>((double)v.x * invN, (double)v.y * invN);
+        const decltype(v.x) s = (decltype(v.x))invN;  // the operand type's 1/N
+        dst[r] = mk2<T2>(v.x * s, v.y * s);
     }
 }
 
