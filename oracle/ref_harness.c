@@ -269,6 +269,11 @@ int main(int argc, char** argv)
     memset(&comm, 0, sizeof(comm));
     comm.commW = comm.commQ = comm.commK = comm.commR = comm.commRq = MPI_COMM_WORLD;
     comm.nqpools = comm.nkpools = 1;
+    /* LELPH_REF_KPOOLS=n: the reference's own k-pool split (distribute_to_grps in
+     * compute_elph_matq.c:50-58) with this process as pool 0, so that only the
+     * first nk_BZ/n k-points of each q are computed (a timing sample) */
+    if (getenv("LELPH_REF_KPOOLS")) comm.nkpools = atoi(getenv("LELPH_REF_KPOOLS"));
+    if (comm.nkpools < 1) comm.nkpools = 1;
     comm.commW_size = comm.commQ_size = comm.commK_size = comm.commR_size = comm.commRq_size = 1;
 
     if (argc >= 6 && !strcmp(argv[3], "rotdv"))
