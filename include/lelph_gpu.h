@@ -43,6 +43,18 @@ extern "C" {
 #define LELPH_GPU_MIXED_F16 1  /* FP32 FFTs, split-f16 (hi,lo) tensor-core sandwich, FP64 phases/reduction */
 #define LELPH_GPU_MIXED_BF16 2 /* as above with split-bf16 */
 
+/* lelph_gpu_desc.route: the order of work of the local sandwich.
+ * REAL: psi(r) of every full-BZ k resident, one contraction over the grid per
+ *       pair (tensor cores in the mixed form; at most 64 bands there).
+ * GSPACE: the reference's order (elphLocal, src/dvloc/compute_Vbare_loc.c:264-310):
+ *       forward FFT of dV psi_k per (mode, band), pruned to the k+q sphere,
+ *       then a GEMM over the sphere; psi(r) is built per k when it is needed.
+ * AUTO: REAL unless its resident operands exceed half of the device memory or
+ *       the mixed form's tensor-core tile cannot hold the bands. */
+#define LELPH_GPU_ROUTE_AUTO 0
+#define LELPH_GPU_ROUTE_REAL 1
+#define LELPH_GPU_ROUTE_GSPACE 2
+
 /* element type of matrix-element outputs */
 #define LELPH_GPU_OUT_C128 0 /* double complex (reference built with -DCOMPILE_ELPH_DOUBLE) */
 #define LELPH_GPU_OUT_C64 1  /* float complex (reference default build, src/elphC.h:24-31) */
@@ -81,6 +93,7 @@ typedef struct lelph_gpu_desc
     /* library options */
     int precision;                 /* LELPH_GPU_FP64 / LELPH_GPU_MIXED_F16 / LELPH_GPU_MIXED_BF16 */
     int device;                    /* CUDA device ordinal */
+    int route;                     /* LELPH_GPU_ROUTE_* (0 = automatic) */
 } lelph_gpu_desc;
 
 typedef struct lelph_gpu_stats
@@ -99,6 +112,7 @@ typedef struct lelph_gpu_stats
     long long dmats_done;        /* Dmats computed */
     double qstar_ms;             /* device time of the q-star rotations (profiling on) */
     double dvscf_ms;             /* device time of the dV_scf ingest kernel (profiling on) */
+    int route;                   /* route in use: LELPH_GPU_ROUTE_REAL or LELPH_GPU_ROUTE_GSPACE */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

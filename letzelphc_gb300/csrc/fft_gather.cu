@@ -21,181 +21,7 @@
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
-
-// ------------------------------------------------------------- butterflies
-
-template <typename T2>
-__device__ __forceinline__ T2 mul_i(T2 a, int sign)  // multiply by sign * i
-{
-    T2 r;
-    r.x = -sign * a.y;
-    r.y = sign * a.x;
-    return r;
-}
-
-template <typename T2, typename T>
-__device__ __forceinline__ void dft2(T2* v)
-{
-    T2 a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
-}
-
-template <typename T2, typename T>
-__device__ __forceinline__ void dft4(T2* v, int sign)
-{
-    T2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-    T2 s13 = cadd(v[1], v[3]), d13 = mul_i(csub(v[1], v[3]), sign);
-    v[0] = cadd(s02, s13);
-    v[2] = csub(s02, s13);
-    v[1] = cadd(d02, d13);
-    v[3] = csub(d02, d13);
-}
-
-template <typename T2, typename T>
-__device__ __forceinline__ void dft3(T2* v, int sign)
-{
-    const T c = (T)-0.5;
-    const T s = (T)(sign * 0.86602540378443864676);  // sin(2 pi / 3)
-    T2 a = cadd(v[1], v[2]);
-    T2 d = csub(v[1], v[2]);
-    T2 t1;
-    t1.x = v[0].x + c * a.x;
-    t1.y = v[0].y + c * a.y;
-    T2 t2;  // i s d
-    t2.x = -s * d.y;
-    t2.y = s * d.x;
-    v[0] = cadd(v[0], a);
-    v[1] = cadd(t1, t2);
-    v[2] = csub(t1, t2);
-}
-
-template <typename T2, typename T>
-__device__ __forceinline__ void dft5(T2* v, int sign)
-{
-    const T c1 = (T)0.30901699437494742410;   // cos(2 pi / 5)
-    const T c2 = (T)-0.80901699437494742410;  // cos(4 pi / 5)
-    const T s1 = (T)(sign * 0.95105651629515357212);  // sin(2 pi / 5)
-    const T s2 = (T)(sign * 0.58778525229247312917);  // sin(4 pi / 5)
-    T2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
-    T2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
-    T2 x0 = v[0];
-    T2 r1, r2, i1, i2;
-    r1.x = x0.x + c1 * a1.x + c2 * a2.x;
-    r1.y = x0.y + c1 * a1.y + c2 * a2.y;
-    r2.x = x0.x + c2 * a1.x + c1 * a2.x;
-    r2.y = x0.y + c2 * a1.y + c1 * a2.y;
-    // i (s1 b1 + s2 b2) and i (s2 b1 - s1 b2)
-    T2 u, w;
-    u.x = s1 * b1.x + s2 * b2.x;
-    u.y = s1 * b1.y + s2 * b2.y;
-    w.x = s2 * b1.x - s1 * b2.x;
-    w.y = s2 * b1.y - s1 * b2.y;
-    i1.x = -u.y;
-    i1.y = u.x;
-    i2.x = -w.y;
-    i2.y = w.x;
-    v[0] = cadd(x0, cadd(a1, a2));
-    v[1] = cadd(r1, i1);
-    v[4] = csub(r1, i1);
-    v[2] = cadd(r2, i2);
-    v[3] = csub(r2, i2);
-}
-
-// One Stockham pass of radix R over nlines lines held in shared memory;
-// element e of line l lives at buf[l*ls + e*es].  Consecutive threads take
-// consecutive elements of a line when elements are contiguous (es == 1) and
-// consecutive lines otherwise (ls == 1), so that a warp's shared-memory
-// accesses fall into distinct banks either way.
-// Division by a run-time divisor d through its FP32 reciprocal: q = trunc(x/d)
-// is at most one off for 0 <= x < 2^24 and is corrected from the remainder
-// (the index arithmetic of the passes stays far below that bound).
-struct RecipDiv
-{
-    float inv;
-    int d;
-};
-__device__ __forceinline__ RecipDiv recip_div(int d) { return RecipDiv{__frcp_rn((float)d), d}; }
-__device__ __forceinline__ int div_rem(int x, const RecipDiv& f, int& r)
-{
-    int q = __float2int_rz((float)x * f.inv);
-    r = x - q * f.d;
-    if (r < 0)
-    {
-        --q;
-        r += f.d;
-    }
-    else if (r >= f.d)
-    {
-        ++q;
-        r -= f.d;
-    }
-    return q;
-}
-
-template <typename T2, typename T, int R>
-__device__ __forceinline__ void stockham_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int L,
-                                              int Ns, int es, int ls, const T2* tw, int sign)
-{
-    const int LR = L / R;
-    const int nwork = nlines * LR;
-    const int tstride = L / (Ns * R);
-    const bool line_fast = es != 1;
-    const RecipDiv dl = recip_div(line_fast ? nlines : LR), dn = recip_div(Ns);
-    for (int w = threadIdx.x; w < nwork; w += blockDim.x)
-    {
-        int line, j;
-        if (line_fast)
-            j = div_rem(w, dl, line);
-        else
-            line = div_rem(w, dl, j);
-        int k;
-        const int jq = div_rem(j, dn, k);
-        const T2* s = src + (size_t)line * ls;
-        T2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = s[(size_t)(j + r * LR) * es];
-        if (k != 0)
-        {
-#pragma unroll
-            for (int r = 1; r < R; ++r)
-            {
-                T2 t = tw[r * k * tstride];
-                if (sign < 0) t.y = -t.y;
-                v[r] = cmul(v[r], t);
-            }
-        }
-        if (R == 2) dft2<T2, T>(v);
-        if (R == 3) dft3<T2, T>(v, sign);
-        if (R == 4) dft4<T2, T>(v, sign);
-        if (R == 5) dft5<T2, T>(v, sign);
-        T2* d = dst + (size_t)line * ls;
-        int base = jq * Ns * R + k;
-#pragma unroll
-        for (int r = 0; r < R; ++r) d[(size_t)(base + r * Ns) * es] = v[r];
-    }
-}
-
-// Runs all passes; returns the buffer holding the result.
-template <typename T2, typename T>
-__device__ T2* fft_smem(T2* a, T2* b, int nlines, int es, int ls, const FftPlan1D& p, const T2* tw, int sign)
-{
-    int Ns = 1;
-    for (int st = 0; st < p.nstage; ++st)
-    {
-        int R = p.radix[st];
-        if (R == 4) stockham_pass<T2, T, 4>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
-        else if (R == 2) stockham_pass<T2, T, 2>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
-        else if (R == 3) stockham_pass<T2, T, 3>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
-        else stockham_pass<T2, T, 5>(a, b, nlines, p.L, Ns, es, ls, tw, sign);
-        __syncthreads();
-        T2* t = a;
-        a = b;
-        b = t;
-        Ns *= R;
-    }
-    return a;
-}
+#include "fft_smem.cuh"
 
 // ---------------------------------------------------- contiguous-line pass
 

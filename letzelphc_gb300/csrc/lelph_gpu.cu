@@ -60,6 +60,7 @@ struct lelph_gpu
     int ab_bf16 = 0;
     bool mixed = false;
     bool prepared = false;
+    bool gspace = false;  // G-space route of the local sandwich
     // host copies
     std::vector<double> alat, blat, kibz, kbz_crys, symR, symtau, atom_pos, PP, Fsign;
     std::vector<int> kmap, symtr, atom_type, npw;
@@ -109,6 +110,15 @@ struct lelph_gpu
     int vl_npts = 0, vl_dim2 = 0;
     double vl_dg = 0, vl_volume = 0;
     std::vector<double> vl_zval;
+    // G-space route: every full-BZ k's sphere (its k+q role) sorted by
+    // ((y, z) column, x) on the product grid, and the k+q coefficients stored
+    // in that order (Bp); psi(r) of one k at a time and the pass buffers
+    std::vector<int> gs_npad, gs_ncol;
+    std::vector<long long> gs_perm_off, gs_col_off, gs_cst_off, gs_bp_off;
+    int gs_npad_max = 0, gs_ncol_max = 0;
+    long long gs_bp_total = 0;
+    DevBuf d_gs_perm, d_gs_kcx, d_gs_cols, d_gs_cst, d_gs_npw, d_gs_npad, d_gs_permoff, d_gs_bpoff, d_gs_bp;
+    DevBuf d_gs_psi, d_gs_out1, d_gs_A, d_gs_part;
 };
 
 namespace
@@ -664,6 +674,119 @@ static int upload_wfc(lelph_gpu* h, const double* const* wfc)
     return LELPH_GPU_OK;
 }
 
+// G-space route: the sphere of every full-BZ k (as the k+q wavefunction of a
+// pair) on the product grid, sorted by ((y, z) column, x).  The sort order is
+// the K order of the route's GEMM: the x pass then writes each column's
+// sphere points as one contiguous run, and the k+q coefficients are stored
+// permuted to it once (k_gs_bperm).  The box position of a plane wave is the
+// one the scatter uses (W n modulo the grid), so no two plane waves of a
+// sphere share one (the product grid spans more than the sphere's diameter).
+static int gs_tables(lelph_gpu* h)
+{
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    const int nk = d.nkpts_BZ;
+    std::vector<std::vector<int>> perm(nk), kcx(nk), cols(nk), cst(nk);
+    std::vector<int> bad(nk, 0);
+    auto one = [&](int k) {
+        const KPointSym& ks = h->ksym[k];
+        const int npw = h->npw[ks.ik];
+        const int* mil = &h->miller[3 * h->pw_off[ks.ik]];
+        std::vector<std::pair<long long, int>> v(npw);
+        for (int p = 0; p < npw; ++p)
+        {
+            const int* n = mil + 3 * p;
+            int G[3], N3[3] = {g.Nx, g.Ny, g.Nz};
+            for (int r = 0; r < 3; ++r)
+            {
+                G[r] = (ks.W[3 * r] * n[0] + ks.W[3 * r + 1] * n[1] + ks.W[3 * r + 2] * n[2]) % N3[r];
+                if (G[r] < 0) G[r] += N3[r];
+            }
+            v[p] = {((long long)G[1] * g.Nz + G[2]) * g.Nx + G[0], p};
+        }
+        std::sort(v.begin(), v.end());
+        std::vector<int>& pm = perm[k];
+        std::vector<int>& kc = kcx[k];
+        std::vector<int>& cl = cols[k];
+        std::vector<int>& cs = cst[k];
+        pm.resize(npw);
+        kc.resize(npw);
+        long long last_col = -1;
+        for (int K = 0; K < npw; ++K)
+        {
+            if (K > 0 && v[K].first == v[K - 1].first) bad[k] = 1;
+            const long long col = v[K].first / g.Nx;
+            const int x = (int)(v[K].first - col * g.Nx);
+            if (col != last_col)
+            {
+                cl.push_back((int)col);
+                cs.push_back(K);
+                last_col = col;
+            }
+            pm[K] = v[K].second;
+            kc[K] = (int)(cl.size() - 1) * g.Nx + x;
+        }
+        cs.push_back(npw);
+    };
+    {
+        const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), nk));
+        std::vector<std::thread> pool;
+        for (int w = 1; w < nthr; ++w)
+            pool.emplace_back([&, w]() {
+                for (int k = w; k < nk; k += nthr) one(k);
+            });
+        for (int k = 0; k < nk; k += nthr) one(k);
+        for (auto& t : pool) t.join();
+    }
+    for (int k = 0; k < nk; ++k)
+        if (bad[k]) return fail(h, LELPH_GPU_ERR_GEOMETRY, "G-space route: two plane waves share a product-grid point");
+    const int nrowk = d.nspin * d.nbnds * d.nspinor;
+    h->gs_npad.resize(nk);
+    h->gs_ncol.resize(nk);
+    h->gs_perm_off.resize(nk);
+    h->gs_col_off.resize(nk);
+    h->gs_cst_off.resize(nk);
+    h->gs_bp_off.resize(nk);
+    std::vector<int> npw_k(nk);
+    long long po = 0, co = 0, so = 0, bo = 0;
+    h->gs_npad_max = h->gs_ncol_max = 0;
+    for (int k = 0; k < nk; ++k)
+    {
+        npw_k[k] = (int)perm[k].size();
+        h->gs_npad[k] = (npw_k[k] + 7) / 8 * 8;
+        h->gs_ncol[k] = (int)cols[k].size();
+        h->gs_perm_off[k] = po;
+        h->gs_col_off[k] = co;
+        h->gs_cst_off[k] = so;
+        h->gs_bp_off[k] = bo;
+        po += h->gs_npad[k];
+        co += h->gs_ncol[k];
+        so += h->gs_ncol[k] + 1;
+        bo += (long long)nrowk * h->gs_npad[k];
+        h->gs_npad_max = std::max(h->gs_npad_max, h->gs_npad[k]);
+        h->gs_ncol_max = std::max(h->gs_ncol_max, h->gs_ncol[k]);
+    }
+    h->gs_bp_total = bo;
+    std::vector<int> pall(po, 0), kall(po, 0), call(co), sall(so);
+    for (int k = 0; k < nk; ++k)
+    {
+        std::copy(perm[k].begin(), perm[k].end(), pall.begin() + h->gs_perm_off[k]);
+        std::copy(kcx[k].begin(), kcx[k].end(), kall.begin() + h->gs_perm_off[k]);
+        std::copy(cols[k].begin(), cols[k].end(), call.begin() + h->gs_col_off[k]);
+        std::copy(cst[k].begin(), cst[k].end(), sall.begin() + h->gs_cst_off[k]);
+    }
+    int rc;
+    if ((rc = upload(h, h->d_gs_perm, pall.data(), sizeof(int) * pall.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_kcx, kall.data(), sizeof(int) * kall.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_cols, call.data(), sizeof(int) * call.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_cst, sall.data(), sizeof(int) * sall.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_npw, npw_k.data(), sizeof(int) * nk))) return rc;
+    if ((rc = upload(h, h->d_gs_npad, h->gs_npad.data(), sizeof(int) * nk))) return rc;
+    if ((rc = upload(h, h->d_gs_permoff, h->gs_perm_off.data(), sizeof(long long) * nk))) return rc;
+    if ((rc = upload(h, h->d_gs_bpoff, h->gs_bp_off.data(), sizeof(long long) * nk))) return rc;
+    return LELPH_GPU_OK;
+}
+
 extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
 {
     if (!desc || !out) return LELPH_GPU_ERR_INVALID;
@@ -721,8 +844,11 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
             if (lelph_local_tc_stages(g3) < 3) h->g.kpts = 32;
         }
     }
-    if (h->mixed && (2 * h->g.nbp > 128 || !lelph_local_tc_supported(h->g)))
-        return bad(LELPH_GPU_ERR_UNSUPPORTED, "mixed form supports up to 64 bands");
+    if (d.route < LELPH_GPU_ROUTE_AUTO || d.route > LELPH_GPU_ROUTE_GSPACE) return bad(LELPH_GPU_ERR_INVALID, "route");
+    const bool tc_ok = !h->mixed || (2 * h->g.nbp <= 128 && lelph_local_tc_supported(h->g));
+    if (d.route == LELPH_GPU_ROUTE_REAL && !tc_ok)
+        return bad(LELPH_GPU_ERR_UNSUPPORTED, "the real-space route of the mixed form supports up to 64 bands");
+    h->gspace = d.route == LELPH_GPU_ROUTE_GSPACE || !tc_ok;
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
     // host copies
@@ -894,7 +1020,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                 for (int c : cand[2])
                 {
                     long long p = (long long)a * b * c;
-                    if (h->mixed && p % 32 != 0) continue;
+                    if (h->mixed && !h->gspace && p % 32 != 0) continue;
                     if (best < 0 || p < best)
                     {
                         best = p;
@@ -912,7 +1038,25 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
             if (!plan_1d(bm[r], h->plan[r])) return bad(LELPH_GPU_ERR_UNSUPPORTED, "product grid");
     }
     const long long N = (long long)h->g.Nx * h->g.Ny * h->g.Nz;
-    if (h->mixed)
+    if (d.route == LELPH_GPU_ROUTE_AUTO && !h->gspace)
+    {
+        // the real-space route keeps psi(r) of every full-BZ k resident (split
+        // k+q rows and FP32 psi in the mixed form, FP64 boxes in the plain form)
+        const double per_kpt = h->mixed ? 24.0 * h->g.nbp * d.nspin * d.nspinor
+                                        : 16.0 * d.nspin * d.nbnds * d.nspinor;
+        const double resident = per_kpt * (double)N * d.nkpts_BZ;
+        size_t fr = 0, tot = 0;
+        if (cudaSetDevice(d.device) == cudaSuccess && cudaMemGetInfo(&fr, &tot) == cudaSuccess &&
+            resident > 0.5 * (double)tot)
+            h->gspace = true;
+    }
+    if (h->gspace)
+    {
+        GsGeom gg{h->g.Nx, h->g.Ny, h->g.Nz, d.nbnds, d.nspinor, d.nmag, 0};
+        if (lelph_gs_plane_smem(gg, !h->mixed) > 220 * 1024 || lelph_gs_xpass_smem(gg, !h->mixed) > 220 * 1024)
+            return bad(LELPH_GPU_ERR_UNSUPPORTED, "G-space route: a (y, z) plane of the product grid exceeds shared memory");
+    }
+    if (h->mixed && !h->gspace)
     {
         if (N % 32 != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
         if (N % h->g.kpts != 0) h->g.kpts = 32;
@@ -945,7 +1089,9 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
-                      &h->d_qsitems, &h->d_dvraw};
+                      &h->d_qsitems, &h->d_dvraw, &h->d_gs_perm, &h->d_gs_kcx, &h->d_gs_cols, &h->d_gs_cst,
+                      &h->d_gs_npw, &h->d_gs_npad, &h->d_gs_permoff, &h->d_gs_bpoff, &h->d_gs_bp, &h->d_gs_psi,
+                      &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -1022,7 +1168,12 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     rc = ensure(h, h->d_status, 64);
     if (rc) return bad(rc, h->err);
     if (cudaMemsetAsync(h->d_status.p, 0, 64, h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "memset");
-    if (h->mixed)
+    if (h->gspace)
+    {
+        rc = gs_tables(h);
+        if (rc) return bad(rc, h->err);
+    }
+    if (h->mixed && !h->gspace)
     {
         const size_t Kr = 2 * (size_t)d.nspinor * N;
         const size_t rows = (size_t)d.nkpts_BZ * d.nspin * 2 * 2 * h->g.nbp;
@@ -1063,6 +1214,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     rc = upload_wfc(h, d.wfc);
     if (rc) return bad(rc, h->err);
     if (cudaStreamSynchronize(h->st) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "sync");
+    h->stats.route = h->gspace ? LELPH_GPU_ROUTE_GSPACE : LELPH_GPU_ROUTE_REAL;
     *out = h;
     return LELPH_GPU_OK;
 #undef UP
@@ -1088,7 +1240,27 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
     const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
     tstart(h);
     int rc;
-    if (!h->mixed)
+    if (h->gspace)
+    {
+        // G-space route: the unfolded coefficients of every full-BZ k (no
+        // boxes: psi(r) is made per k when its pairs run) and their copy in
+        // each sphere's sorted order, the GEMM operand of the k+q role
+        lelph_launch_scatter(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
+                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
+                             (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, !h->mixed, nullptr,
+                             (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st);
+        const size_t e = h->mixed ? sizeof(float2) : sizeof(double2);
+        rc = ensure(h, h->d_gs_bp, e * (size_t)h->gs_bp_total);
+        if (rc) return rc;
+        if (lelph_launch_gs_bperm(!h->mixed, (const double2*)h->d_chat.p, (const long long*)h->d_chatoff.p,
+                                  (const int*)h->d_gs_npw.p, (const int*)h->d_gs_npad.p,
+                                  (const long long*)h->d_gs_permoff.p, (const int*)h->d_gs_perm.p,
+                                  (const long long*)h->d_gs_bpoff.p, 0, d.nkpts_BZ, nbox_per_k, h->gs_npad_max,
+                                  h->d_gs_bp.p, h->st))
+            return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "G-space route: coefficient permutation grid");
+        h->stats.kernel_launches += 2;
+    }
+    else if (!h->mixed)
     {
         size_t bytes = sizeof(double2) * (size_t)d.nkpts_BZ * nbox_per_k * N;
         rc = ensure(h, h->d_psi64, bytes);
@@ -1695,6 +1867,15 @@ static int build_windows(lelph_gpu* h)
                                        (const float2*)h->d_tw32[1].p, +1, h->st);
             lelph_launch_fft_strided_f(tM, (long long)nu * ncomp, g.Ny * g.Nz, h->plan[0],
                                        (const float2*)h->d_tw32[0].p, +1, h->st);
+            if (h->gspace)
+            {
+                // the G-space route reads the windows as plain FP32 boxes
+                CUDA_TRY(h, cudaMemcpyAsync((float2*)h->d_win32.p + (size_t)h->win_base[s] * ncomp * M, tM,
+                                            sizeof(float2) * (size_t)nu * ncomp * M, cudaMemcpyDeviceToDevice, h->st));
+                h->stats.kernel_launches += 7;
+                CUDA_TRY(h, cudaGetLastError());
+                continue;
+            }
             unsigned* mx = (unsigned*)h->d_maxabs.p;
             float* sc = (float*)h->d_winscale.p + (size_t)h->win_base[s] * d.nmodes;
             CUDA_TRY(h, cudaMemsetAsync(mx, 0, sizeof(unsigned) * nu * d.nmodes, h->st));
@@ -1737,6 +1918,104 @@ static int build_windows(lelph_gpu* h)
         CUDA_TRY(h, cudaGetLastError());
     }
     h->windows_ok = true;
+    return LELPH_GPU_OK;
+}
+
+// Local term of pairs[0 .. n) on the G-space route, into glocal
+// (pair, spin, mode x band of k, band of k+q), FP64, 1/M applied.  Pairs are
+// visited grouped by their k so that psi(r) of a k is built once per group:
+// scatter of the unfolded coefficients and the inverse FFT (the reference's
+// invfft3D of the k wavefunction, src/dvloc/compute_Vbare_loc.c:206-238).
+static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
+{
+    const lelph_gpu_desc& d = h->d;
+    const GeomDev& g = h->g;
+    const bool f64 = !h->mixed;
+    const size_t e = f64 ? sizeof(double2) : sizeof(float2);
+    const long long M = (long long)g.Nx * g.Ny * g.Nz;
+    const int nb = d.nbnds, ns = d.nspinor, nm = d.nmodes;
+    const int nbox = d.nspin * nb * ns;
+    const int nrows = nm * nb;
+    const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
+    int rc = ensure(h, h->d_gs_psi, e * (size_t)nbox * M);
+    if (rc) return rc;
+    // modes per pass: the plane-pass output and the GEMM operand of a block of
+    // modes stay within ~2 GB
+    const size_t per_mode = e * (size_t)nb * ns * ((size_t)g.Nx * h->gs_ncol_max + h->gs_npad_max);
+    const int nub = (int)std::max<size_t>(1, std::min<size_t>((size_t)nm, (2ull << 30) / per_mode));
+    rc = ensure(h, h->d_gs_out1, e * (size_t)nub * nb * ns * g.Nx * h->gs_ncol_max);
+    if (rc) return rc;
+    rc = ensure(h, h->d_gs_A, e * (size_t)nub * nb * ns * h->gs_npad_max);
+    if (rc) return rc;
+    const int kchunk = 1024;
+    const int nch_max = (ns * h->gs_npad_max + kchunk - 1) / kchunk;
+    rc = ensure(h, h->d_gs_part, e * (size_t)nch_max * nrows * nb);
+    if (rc) return rc;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pairs[a].kbz_k < pairs[b].kbz_k; });
+    const void* tw[3];
+    for (int x = 0; x < 3; ++x) tw[x] = f64 ? h->d_tw64[x].p : h->d_tw32[x].p;
+    const void* winb = f64 ? h->d_win64.p : h->d_win32.p;
+    GsGeom gg{g.Nx, g.Ny, g.Nz, nb, ns, d.nmag, 0};
+    int cur = -1;
+    for (int oi = 0; oi < n; ++oi)
+    {
+        const int i = order[oi];
+        const PairInfo& P = pairs[i];
+        if (P.kbz_k != cur)
+        {
+            cur = P.kbz_k;
+            CUDA_TRY(h, cudaMemsetAsync(h->d_gs_psi.p, 0, e * (size_t)nbox * M, h->st));
+            lelph_launch_scatter(cur, 1, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
+                                 (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
+                                 (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, f64, h->d_gs_psi.p,
+                                 (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st);
+            if (f64)
+            {
+                double2* bx = (double2*)h->d_gs_psi.p;
+                lelph_launch_fft_contig_d(bx, (long long)nbox * g.Nx * g.Ny, h->plan[2], (const double2*)tw[2], +1, h->st);
+                lelph_launch_fft_strided_d(bx, (long long)nbox * g.Nx, g.Nz, h->plan[1], (const double2*)tw[1], +1, h->st);
+                lelph_launch_fft_strided_d(bx, nbox, g.Ny * g.Nz, h->plan[0], (const double2*)tw[0], +1, h->st);
+            }
+            else
+            {
+                float2* bx = (float2*)h->d_gs_psi.p;
+                lelph_launch_fft_contig_f(bx, (long long)nbox * g.Nx * g.Ny, h->plan[2], (const float2*)tw[2], +1, h->st);
+                lelph_launch_fft_strided_f(bx, (long long)nbox * g.Nx, g.Nz, h->plan[1], (const float2*)tw[1], +1, h->st);
+                lelph_launch_fft_strided_f(bx, nbox, g.Ny * g.Nz, h->plan[0], (const float2*)tw[0], +1, h->st);
+            }
+            h->stats.kernel_launches += 4;
+        }
+        const int kq = P.kbz_kq;
+        const int npad = h->gs_npad[kq], ncol = h->gs_ncol[kq];
+        const int Ktot = ns * npad;
+        const int nch = (Ktot + kchunk - 1) / kchunk;
+        const void* win = (const char*)winb + e * (size_t)P.dvslot * nm * d.nmag * M;
+        for (int spin = 0; spin < d.nspin; ++spin)
+        {
+            gg.spin = spin;
+            const void* psi = (const char*)h->d_gs_psi.p + e * (size_t)spin * nb * ns * M;
+            const void* B = (const char*)h->d_gs_bp.p + e * ((size_t)h->gs_bp_off[kq] + (size_t)spin * nb * ns * npad);
+            for (int nu0 = 0; nu0 < nm; nu0 += nub)
+            {
+                const int nmb = std::min(nub, nm - nu0);
+                if (lelph_launch_gs_plane(gg, f64, psi, win, nu0, nmb, h->plan[1], h->plan[2], tw[1], tw[2],
+                                          (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol, h->d_gs_out1.p, h->st) ||
+                    lelph_launch_gs_xpass(gg, f64, h->d_gs_out1.p, nmb * nb * ns, ncol, h->plan[0], tw[0],
+                                          (const int*)h->d_gs_cst.p + h->gs_cst_off[kq],
+                                          (const int*)h->d_gs_kcx.p + h->gs_perm_off[kq], npad, h->d_gs_A.p, h->st) ||
+                    lelph_launch_gs_gemm(f64, h->d_gs_A.p, B, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
+                                         h->d_gs_part.p, h->st))
+                    return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "G-space route: launch configuration");
+                h->stats.kernel_launches += 3;
+            }
+            lelph_launch_gs_reduce(f64, h->d_gs_part.p, (long long)nrows * nb, nch, 1.0 / (double)M,
+                                   glocal + ((size_t)i * d.nspin + spin) * nrows * nb, h->st);
+            h->stats.kernel_launches += 1;
+        }
+        CUDA_TRY(h, cudaGetLastError());
+    }
     return LELPH_GPU_OK;
 }
 
@@ -1794,7 +2073,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         gdev = h->d_gout.p;
     }
     NonlocalDesc nl = nl_desc(h);
-    if (h->mixed && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
+    if (h->mixed && !h->gspace && (h->tmapV_base != h->d_win32.p || h->tmapV_rows != h->nwin))
     {
         // dV windows, tile-major: blocks (window, 32-point block) of (mode, component) rows x 64 floats
         const long long M = (long long)g.Nx * g.Ny * g.Nz;
@@ -1809,17 +2088,23 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     const int nrows = d.nmodes * d.nbnds;
     // batch the pairs so the local workspace stays bounded (~4 GB)
     size_t per_pair;
-    if (!h->mixed) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
+    const bool fp64_local = !h->mixed || h->gspace;  // the local term arrives as FP64 sums (glocal)
+    if (fp64_local) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
     else per_pair = sizeof(float) * (size_t)d.nspin * ((nrows + 127) / 128) * h->nchunks * 128 * 2 * g.nbp;
     int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, (4ull << 30) / per_pair));
-    rc = ensure(h, h->mixed ? h->d_partials : h->d_glocal, per_pair * batch);
+    rc = ensure(h, fp64_local ? h->d_glocal : h->d_partials, per_pair * batch);
     if (rc) return rc;
     for (int p0 = 0; p0 < n; p0 += batch)
     {
         int nb = std::min(batch, n - p0);
         const PairInfo* dp = (const PairInfo*)h->d_pairs.p + p0;
         tstart(h);
-        if (!h->mixed)
+        if (h->gspace)
+        {
+            rc = gs_local(h, pairs.data() + p0, nb, (double2*)h->d_glocal.p);
+            if (rc) return rc;
+        }
+        else if (!h->mixed)
             lelph_launch_local_fp64(dp, nb, (const double2*)h->d_psi64.p, (const double2*)h->d_win64.p, g,
                                     (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
         else
@@ -1828,12 +2113,12 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
         tstart(h);
-        lelph_launch_finish(dp, nb, h->mixed ? 0 : 1, (const double2*)h->d_glocal.p, (const float*)h->d_partials.p,
+        lelph_launch_finish(dp, nb, fp64_local ? 1 : 0, (const double2*)h->d_glocal.p, (const float*)h->d_partials.p,
                             h->nchunks, (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
                             out_type == LELPH_GPU_OUT_C64, (char*)gdev + esz * gsz * p0, h->st);
         h->stats.finish_ms += tstop(h);
-        h->stats.kernel_launches += 2;
+        h->stats.kernel_launches += h->gspace ? 1 : 2;  // gs_local counts its own launches
         CUDA_TRY(h, cudaGetLastError());
     }
     if (!out_device) CUDA_TRY(h, cudaMemcpyAsync(g_out, gdev, esz * gsz * n, cudaMemcpyDeviceToHost, h->st));
@@ -2407,6 +2692,9 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
     CUDA_TRY(h, cudaSetDevice(h->device));
     if (!h->prepared || !h->windows_ok)
         return fail(h, LELPH_GPU_ERR_STATE, "lelph_gpu_prepare must run (after the last set_q) before the allocation-free call");
+    if (h->gspace)
+        return fail(h, LELPH_GPU_ERR_UNSUPPORTED,
+                    "the G-space route builds psi(r) per k in device buffers; it has no allocation-free form");
     unsigned char* scratch = nullptr;
     int rc = noalloc_scratch(h, &scratch);
     if (rc) return rc;

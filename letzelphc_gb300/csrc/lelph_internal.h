@@ -83,6 +83,29 @@ void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* 
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,
                        const GeomDev& g, const int* ulm, int* out, cudaStream_t st);
 
+// G-space route of the local sandwich (gspace.cu)
+struct GsGeom
+{
+    int Nx, Ny, Nz;  // product grid
+    int nb, nspinor, nmag, spin;
+};
+size_t lelph_gs_plane_smem(const GsGeom& gg, int fp64);
+size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64);
+// plane pass of modes nu0 .. nu0+nub-1: out [(nu - nu0) nb + m][s][x][ncol]
+int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const void* win, int nu0, int nub,
+                          const FftPlan1D& py, const FftPlan1D& pz, const void* twy, const void* twz, const int* cols,
+                          int ncol, void* out, cudaStream_t st);
+// x pass: A [rb][npad] (rb = row-box index of the block) in the sphere's sorted order
+int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, int ncol, const FftPlan1D& px,
+                          const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st);
+int lelph_launch_gs_gemm(int fp64, const void* A, const void* B, int nrows, int nb, int Ktot, int kchunk,
+                         int rowoff, int nrows_total, void* part, cudaStream_t st);
+void lelph_launch_gs_reduce(int fp64, const void* part, long long nel, int nchunks, double invM, double2* glocal,
+                            cudaStream_t st);
+int lelph_launch_gs_bperm(int fp64, const double2* chat, const long long* chat_off, const int* npw_k,
+                          const int* npad_k, const long long* perm_off, const int* perm, const long long* bp_off,
+                          int k0, int nk, int rows_per_k, int npad_max, void* Bp, cudaStream_t st);
+
 // local sandwich (sandwich.cu)
 void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* psi, const double2* dV,
                              const GeomDev& g, double2* glocal, unsigned* status, cudaStream_t st);

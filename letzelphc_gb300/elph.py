@@ -21,6 +21,8 @@ LIB_PATH = os.path.join(HERE, "_lib", "liblelph_gpu.so")
 FP64, MIXED_F16, MIXED_BF16 = 0, 1, 2
 OUT_C128, OUT_C64 = 0, 1
 PRECISIONS = {"fp64": FP64, "mixed": MIXED_F16, "mixed_f16": MIXED_F16, "mixed_bf16": MIXED_BF16}
+ROUTE_AUTO, ROUTE_REAL, ROUTE_GSPACE = 0, 1, 2  # LELPH_GPU_ROUTE_*
+ROUTES = {"auto": ROUTE_AUTO, "real": ROUTE_REAL, "gspace": ROUTE_GSPACE}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -39,7 +41,7 @@ class Desc(C.Structure):
         ("npw", _ip), ("gvec", C.POINTER(_dp)), ("wfc", C.POINTER(_dp)), ("Fk", C.POINTER(_dp)),
         ("ntype", C.c_int), ("nltimesj", C.c_int), ("lmax", C.c_int),
         ("PP_table", _dp), ("Fsign", _dp), ("fCoeff", C.POINTER(_dp)),
-        ("precision", C.c_int), ("device", C.c_int),
+        ("precision", C.c_int), ("device", C.c_int), ("route", C.c_int),
     ]
 
 
@@ -49,7 +51,7 @@ class Stats(C.Structure):
         ("prepare_ms", C.c_double), ("finish_ms", C.c_double), ("pairs_done", C.c_longlong),
         ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
         ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
-        ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double),
+        ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double), ("route", C.c_int),
     ]
 
 
@@ -124,7 +126,7 @@ class LelphGPU:
     """One device context holding a system (the reference's Lattice, WFC[],
     Pseudo) and any number of q slots."""
 
-    def __init__(self, s, precision="fp64", device=0):
+    def __init__(self, s, precision="fp64", device=0, route="auto"):
         L = load_library()
         self._L = L
         self._keep = []
@@ -171,6 +173,7 @@ class LelphGPU:
             d.fCoeff = C.POINTER(_dp)()
         d.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         d.device = device
+        d.route = ROUTES[route] if isinstance(route, str) else int(route)
         h = C.c_void_p()
         rc = L.lelph_gpu_create(C.byref(d), C.byref(h))
         if rc != 0:
