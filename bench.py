@@ -62,6 +62,7 @@ def parse():
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
                         "file layout; configs: mixed vs FP64 rate and error on every config's full size")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
+    p.add_argument("--configs", default="", help="configs workload: comma-separated subset (default: all)")
     p.add_argument("--small", action="store_true",
                    help="star / dvscf workloads on the same cell with a 2x2x2 k grid (profiling cases)")
     return p.parse_args()
@@ -748,7 +749,11 @@ def run_configs(args):
     """Every configuration at its full size: the mixed form on all (k, q) pairs
     (device-resident, CUDA events), the FP64 form on a sample of pairs (its
     full-BZ preparation plus the sampled pairs, scaled to the batch), and the
-    error of the mixed form on that sample with the metric's definition."""
+    error of the mixed form on that sample with the metric's definition.
+    Pairs run in blocks of k-points (every q of each k in one call, so a
+    route that builds psi(r) per k does so once per block) into an output
+    buffer of at most ~8 GB that each block overwrites: the 16-atom,
+    200-band configuration has 228 GB of complex64 g in all."""
     import torch
     rank, world, local = dist_env()
     if rank != 0:
@@ -758,64 +763,73 @@ def run_configs(args):
     from letzelphc_gb300.build import build_library
     from letzelphc_gb300.elph import LelphGPU, OUT_C64, LelphError
     build_library()
+    names = args.configs.split(",") if args.configs else CONFIG_NAMES
     out = {}
-    for name in CONFIG_NAMES:
-        if name == "c4":
-            out[name] = {"status": "not run: the per-k operands of this design (split k+q rows and FP32 psi_k of "
-                                   "all 512 k, 200 bands, 60^3 product grid) need ~0.5 TB; k-batched preparation "
-                                   "and band tiling of the sandwich are not built"}
-            continue
+    for name in names:
         t0 = time.perf_counter()
         s = synth.make_system(name)
         gen_s = time.perf_counter() - t0
         nq, nk = len(s.qpts), s.nk_bz
-        qs = np.repeat(np.arange(nq), nk).astype(np.int32)
-        ks = np.tile(np.arange(nk), nq).astype(np.int32)
-        npairs = len(qs)
         gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+        kb = int(max(1, min(nk, (8 << 30) // (8 * gsz * nq))))
+        blocks = []
+        for k0 in range(0, nk, kb):
+            kk = np.arange(k0, min(nk, k0 + kb))
+            blocks.append((np.repeat(np.arange(nq), len(kk)).astype(np.int32), np.tile(kk, nq).astype(np.int32)))
+        npairs = nq * nk
         elems = g_elems(s, npairs)
         rec = {"pairs": npairs, "g_elements": elems, "input_generation_s": gen_s}
         try:
             ctx = LelphGPU(s, args.precision, device=local)
+            st0 = ctx.stats()
+            rec["route"] = {1: "real-space", 2: "G-space"}.get(st0["route"], st0["route"])
+            rec["product_grid"] = list(st0["product_grid"])
             for iq in range(nq):
                 ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
-            gdev = torch.empty(npairs * gsz * 2, dtype=torch.float32, device="cuda")
+            gdev = torch.empty(len(blocks[0][0]) * gsz * 2, dtype=torch.float32, device="cuda")
             stream = torch.cuda.ExternalStream(ctx.stream())
+            big = npairs * gsz > 5e9
 
-            def step():
+            def step(bl):
                 ctx.prepare()
-                ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+                for qs, ks in bl:
+                    ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
 
-            for _ in range(2):
-                step()
+            # warm-up: the whole batch twice, or one block where the batch takes minutes
+            for _ in range(1 if big else 2):
+                step(blocks[:1] if big else blocks)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            reps = max(1, args.steps)
+            reps = 1 if big else max(1, args.steps)
             e0.record(stream)
             for _ in range(reps):
-                step()
+                step(blocks)
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
+            qs_all = np.concatenate([b[0] for b in blocks])
+            ks_all = np.concatenate([b[1] for b in blocks])
             rng = np.random.default_rng(1)
-            sel = np.sort(rng.choice(npairs, size=min(args.fp64_pairs, npairs), replace=False))
-            gm = ctx.run(qs[sel], ks[sel], out=OUT_C64).astype(np.complex128)
+            nsel = min(args.fp64_pairs if not big else 16, npairs)
+            sel = np.sort(rng.choice(npairs, size=nsel, replace=False))
+            gm = ctx.run(qs_all[sel], ks_all[sel], out=OUT_C64).astype(np.complex128)
             ctx.close()
             rec.update({"mixed_value": elems / (ms * 1e-3), "mixed_ms": ms})
             with LelphGPU(s, "fp64", device=local) as c64:
                 for iq in range(nq):
                     c64.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
                 c64.prepare()
-                c64.run(qs[sel[:1]], ks[sel[:1]])
+                c64.run(qs_all[sel[:1]], ks_all[sel[:1]])
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 c64.prepare()
                 torch.cuda.synchronize()
                 t_prep = time.perf_counter() - t0
                 t0 = time.perf_counter()
-                g64 = c64.run(qs[sel], ks[sel])
+                g64 = c64.run(qs_all[sel], ks_all[sel])
                 torch.cuda.synchronize()
                 t_pairs = time.perf_counter() - t0
+                rec["fp64_route"] = {1: "real-space", 2: "G-space"}.get(c64.stats()["route"])
             fp64_rate = elems / (t_prep + t_pairs * npairs / len(sel))
             rec.update({"fp64_value": fp64_rate, "mixed_over_fp64": rec["mixed_value"] / fp64_rate,
                         "error_vs_fp64": err_stats(gm, g64), "sample_pairs": len(sel)})
@@ -823,6 +837,7 @@ def run_configs(args):
             rec["status"] = f"unsupported: {e}"
         out[name] = rec
         print(json.dumps({name: rec}), file=sys.stderr, flush=True)
+        del s
     line = {"metric": METRIC, "unit": "g_elements/s", "n_gpus": 1, "dtype": args.precision,
             "data": "synthetic (seeded, the configurations' shapes)", "configs": out,
             "error_definition": "e_i = ||g_mixed|-|g_fp64|| / max(|g_fp64|, 1e-6 max|g_fp64|); norm = "

@@ -77,6 +77,207 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_plane(const T2* __restrict__ 
     }
 }
 
+// ------------------------------------------- plane pass, compile-time sizes
+// The same transform for square planes of the common product-grid sizes: the
+// radix schedule and the divisions of the index arithmetic are compile-time
+// constants; each pass takes the largest radix up to 16 that divides what is
+// left (two passes per axis for every size handled here: 60 = 15 x 4,
+// 48 = 16 x 3, ...), composite radices being done in registers as two
+// levels of radix-2/3/4/5 butterflies; the z lines sit at a padded stride
+// (Nz + 1) so that consecutive threads, taking consecutive lines, hit
+// distinct banks; the second (y) transform runs only on the z lines that hold
+// a column of the k+q sphere (their list zl; the result is compact, element
+// y of line l at l + y nzl).
+__host__ __device__ constexpr int ct_radix0(int L)
+{
+    return L % 16 == 0 ? 16 : L % 15 == 0 ? 15 : L % 12 == 0 ? 12 : L % 10 == 0 ? 10 : L % 9 == 0 ? 9
+         : L % 8 == 0 ? 8 : L % 6 == 0 ? 6 : L % 5 == 0 ? 5 : L % 4 == 0 ? 4 : L % 3 == 0 ? 3 : 2;
+}
+__host__ __device__ constexpr int ct_nstage(int L) { return L <= 1 ? 0 : 1 + ct_nstage(L / ct_radix0(L)); }
+__host__ __device__ constexpr int ct_radix_at(int L, int i) { return i == 0 ? ct_radix0(L) : ct_radix_at(L / ct_radix0(L), i - 1); }
+__host__ __device__ constexpr bool ct_smooth(int L) { return L == 1 || ((L % 2 == 0 || L % 3 == 0 || L % 5 == 0) && ct_smooth(L / ct_radix0(L))); }
+// first factor of a composite radix (the second is a radix-2/3/4/5)
+__host__ __device__ constexpr int ct_split(int R) { return R == 16 ? 4 : R == 15 ? 3 : R == 12 ? 4 : R == 10 ? 2 : R == 9 ? 3 : R == 8 ? 4 : R == 6 ? 2 : R; }
+
+template <typename T2, typename T, int R>
+__device__ __forceinline__ void dft_base(T2* v, int sign)
+{
+    if constexpr (R == 2) dft2<T2, T>(v);
+    if constexpr (R == 3) dft3<T2, T>(v, sign);
+    if constexpr (R == 4) dft4<T2, T>(v, sign);
+    if constexpr (R == 5) dft5<T2, T>(v, sign);
+}
+
+// DFT of R = R1 R2 points in registers: R2 DFTs of R1 points over the
+// stride-R2 subsets, twiddles w_R^(n2 k1) (w_R^m = tw[m L / R], tw holding
+// e^{+2 pi i t / L}), then R1 DFTs of R2 points; X[k1 + R1 k2].
+template <typename T2, typename T, int R, int L>
+__device__ __forceinline__ void dft_ct(T2* v, int sign, const T2* __restrict__ tw)
+{
+    constexpr int R1 = ct_split(R);
+    if constexpr (R1 == R)
+        dft_base<T2, T, R>(v, sign);
+    else
+    {
+        constexpr int R2 = R / R1;
+        T2 t[R];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2)
+        {
+            T2 u[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) u[n1] = v[R2 * n1 + n2];
+            dft_base<T2, T, R1>(u, sign);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; ++k1)
+            {
+                T2 x = u[k1];
+                if (n2 * k1 != 0)
+                {
+                    T2 w = tw[n2 * k1 * (L / R)];
+                    if (sign < 0) w.y = -w.y;
+                    x = cmul(x, w);
+                }
+                t[n2 * R1 + k1] = x;
+            }
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1)
+        {
+            T2 w2[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) w2[n2] = t[n2 * R1 + k1];
+            dft_base<T2, T, R2>(w2, sign);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = w2[k2];
+        }
+    }
+}
+
+// One Stockham pass of radix R (stage with NS = product of earlier radices).
+// Element e of source line l sits at src[(loff ? loff[l] : l*ls_s) + e*es_s],
+// of destination line l at dst[l*ls_d + e*es_d].  LINE_FAST: consecutive
+// threads take consecutive lines (lines interleaved in memory), else
+// consecutive elements of a line.
+template <typename T2, typename T, int L, int R, int NS, bool LINE_FAST, int NLC>
+__device__ __forceinline__ void ct_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int es_s,
+                                        int ls_s, const int* __restrict__ loff, int es_d, int ls_d,
+                                        const T2* __restrict__ tw, int sign)
+{
+    constexpr int LR = L / R;
+    constexpr int TS = L / (NS * R);
+    if (NLC > 0) nlines = NLC;
+    const int nwork = nlines * LR;
+    const RecipDiv dl = recip_div(LINE_FAST && NLC == 0 ? nlines : 1);
+    for (int w = threadIdx.x; w < nwork; w += blockDim.x)
+    {
+        int line, j;
+        if (LINE_FAST && NLC > 0)
+        {
+            j = w / NLC;
+            line = w - j * NLC;
+        }
+        else if (LINE_FAST)
+            j = div_rem(w, dl, line);
+        else
+        {
+            line = w / LR;
+            j = w - line * LR;
+        }
+        const int k = j % NS, jq = j / NS;
+        const T2* sp = src + (loff ? loff[line] : line * ls_s);
+        T2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = sp[(j + r * LR) * es_s];
+        if (NS > 1 && k != 0)
+        {
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+            {
+                T2 t = tw[r * k * TS];
+                if (sign < 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        dft_ct<T2, T, R, L>(v, sign, tw);
+        T2* dp = dst + line * ls_d;
+        const int base = jq * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dp[(base + r * NS) * es_d] = v[r];
+    }
+}
+
+// All passes; the first reads the source layout, the rest the destination
+// layout.  Returns the buffer holding the result.
+template <typename T2, typename T, int L, int STAGE, int NS, bool LINE_FAST, int NLC>
+__device__ __forceinline__ T2* ct_fft(T2* a, T2* b, int nlines, int es_s, int ls_s, const int* loff, int es, int ls,
+                                      const T2* tw, int sign)
+{
+    if constexpr (STAGE == ct_nstage(L))
+        return a;
+    else
+    {
+        constexpr int R = ct_radix_at(L, STAGE);
+        ct_pass<T2, T, L, R, NS, LINE_FAST, NLC>(a, b, nlines, es_s, ls_s, loff, es, ls, tw, sign);
+        __syncthreads();
+        return ct_fft<T2, T, L, STAGE + 1, NS * R, LINE_FAST, NLC>(b, a, nlines, es, ls, nullptr, es, ls, tw, sign);
+    }
+}
+
+// grid and output as k_gs_plane; cols2[c] = y nzl + l(z) indexes the compact
+// result of the pruned y transform.
+template <typename T2, typename T, int NY, int NZ>
+__global__ void __launch_bounds__(GS_THREADS) k_gs_plane_ct(const T2* __restrict__ psi, const T2* __restrict__ win,
+                                                            GsGeom gg, int nu0, const T2* __restrict__ twy,
+                                                            const T2* __restrict__ twz, const int* __restrict__ cols2,
+                                                            int ncol, const int* __restrict__ zl, int nzl,
+                                                            T2* __restrict__ out)
+{
+    static_assert(ct_smooth(NY) && ct_smooth(NZ), "2, 3, 5-smooth plane");
+    constexpr int NZP = NZ + 1;       // padded z-line stride
+    constexpr int NP = NY * NZP;
+    extern __shared__ __align__(16) unsigned char gsc_smem[];
+    T2* a = reinterpret_cast<T2*>(gsc_smem);
+    T2* b = a + NP;
+    T2* ty = b + NP;
+    T2* tz = ty + NY;
+    int* szl = reinterpret_cast<int*>(tz + NZ);
+    const int nul = blockIdx.x, m = blockIdx.y, x = blockIdx.z;
+    const int nu = nu0 + nul;
+    for (int t = threadIdx.x; t < NY; t += blockDim.x) ty[t] = twy[t];
+    for (int t = threadIdx.x; t < NZ; t += blockDim.x) tz[t] = twz[t];
+    for (int t = threadIdx.x; t < nzl; t += blockDim.x) szl[t] = zl[t];
+    constexpr int NPL = NY * NZ;      // points of a plane in global memory
+    const long long M = (long long)gg.Nx * NPL;
+    const size_t xoff = (size_t)x * NPL;
+    const T2* pm = psi + (size_t)m * gg.nspinor * M + xoff;
+    const T2* dv = win + (size_t)nu * gg.nmag * M + xoff;
+    for (int s = 0; s < gg.nspinor; ++s)
+    {
+        if (gg.nmag == 4)
+        {
+            const T2* d0 = dv + (size_t)(2 * s) * M;
+            const T2* d1 = d0 + M;
+            for (int e = threadIdx.x; e < NPL; e += GS_THREADS)
+                a[e + e / NZ] = cadd(cmul(d0[e], pm[e]), cmul(d1[e], pm[M + e]));
+        }
+        else
+        {
+            const T2* d0 = dv + (size_t)(gg.nmag == 2 ? gg.spin : 0) * M;
+            const T2* p0 = pm + (size_t)s * M;
+            for (int e = threadIdx.x; e < NPL; e += GS_THREADS) a[e + e / NZ] = cmul(d0[e], p0[e]);
+        }
+        __syncthreads();
+        // z lines (line y at y NZP), then the y transform of the sphere's z lines
+        T2* r = ct_fft<T2, T, NZ, 0, 1, true, NY>(a, b, NY, 1, NZP, nullptr, 1, NZP, tz, -1);
+        T2* o = r == a ? b : a;
+        r = ct_fft<T2, T, NY, 0, 1, true, 0>(r, o, nzl, NZP, 1, szl, nzl, 1, ty, -1);
+        T2* dst = out + (((size_t)(nul * gg.nb + m) * gg.nspinor + s) * gg.Nx + x) * ncol;
+        for (int c = threadIdx.x; c < ncol; c += GS_THREADS) dst[c] = r[cols2[c]];
+        __syncthreads();
+    }
+}
+
 // -------------------------------------------------------------------- x pass
 // grid: (ceil(ncol / GS_CB), rows of the block x nspinor); the tile [x][column]
 // is read along the columns (coalesced), transformed along x, and the sphere
@@ -194,6 +395,95 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_gemm(const T2* __restrict__ A
     }
 }
 
+// The same product for FP32 operands with a tile shaped to the band count:
+// 256 threads as 32 row groups x 8 column groups, TM rows x TN columns per
+// thread (columns tx + 8 j), BM = 32 TM rows, BN = 8 TN columns; BN is
+// picked at launch so that the bands fill whole tiles (200 bands: 5 tiles
+// of 40).
+template <int TM, int TN>
+__global__ void __launch_bounds__(GS_THREADS, 2) k_gs_gemm_f32(const float2* __restrict__ A, const float2* __restrict__ B,
+                                                            int nrows, int nb, int Ktot, int kchunk, int rowoff,
+                                                            int nrows_total, float2* __restrict__ part)
+{
+    constexpr int BM = 32 * TM, BN = 8 * TN;
+    constexpr int AL = BM * GS_BK / GS_THREADS;  // A elements each thread stages per K step
+    __shared__ float2 As[GS_BK][BM + 1];
+    __shared__ float2 Bs[GS_BK][BN + 1];
+    const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
+    const int lk = tid & 15, lr = tid >> 4;
+    const int r0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kbeg = blockIdx.z * kchunk, kend = min(Ktot, kbeg + kchunk);
+    float2 acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
+    float2 ra[AL], rb[(BN * GS_BK + GS_THREADS - 1) / GS_THREADS];
+    auto load = [&](int k0) {
+        const int k = k0 + lk;
+#pragma unroll
+        for (int i = 0; i < AL; ++i)
+        {
+            const int row = r0 + lr + 16 * i;
+            ra[i] = (row < nrows && k < kend) ? A[(size_t)row * Ktot + k] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int i = 0; i < (BN * GS_BK + GS_THREADS - 1) / GS_THREADS; ++i)
+        {
+            const int e = tid + i * GS_THREADS;
+            const int n = n0 + (e >> 4), kk = k0 + (e & 15);
+            rb[i] = (e < BN * GS_BK && n < nb && kk < kend) ? B[(size_t)n * Ktot + kk] : make_float2(0.f, 0.f);
+        }
+    };
+    load(kbeg);
+    for (int k0 = kbeg; k0 < kend; k0 += GS_BK)
+    {
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < AL; ++i) As[lk][lr + 16 * i] = ra[i];
+#pragma unroll
+        for (int i = 0; i < (BN * GS_BK + GS_THREADS - 1) / GS_THREADS; ++i)
+        {
+            const int e = tid + i * GS_THREADS;
+            if (e < BN * GS_BK) Bs[e & 15][e >> 4] = rb[i];
+        }
+        __syncthreads();
+        if (k0 + GS_BK < kend) load(k0 + GS_BK);
+#pragma unroll
+        for (int kk = 0; kk < GS_BK; ++kk)
+        {
+            float2 av[TM], bv[TN];
+#pragma unroll
+            for (int i = 0; i < TM; ++i) av[i] = As[kk][ty * TM + i];
+#pragma unroll
+            for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tx + 8 * j];
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j)
+                {
+                    acc[i][j].x = fmaf(av[i].x, bv[j].x, acc[i][j].x);
+                    acc[i][j].x = fmaf(av[i].y, bv[j].y, acc[i][j].x);
+                    acc[i][j].y = fmaf(av[i].y, bv[j].x, acc[i][j].y);
+                    acc[i][j].y = fmaf(-av[i].x, bv[j].y, acc[i][j].y);
+                }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+    {
+        const int row = r0 + ty * TM + i;
+        if (row >= nrows) continue;
+        float2* dst = part + ((size_t)blockIdx.z * nrows_total + rowoff + row) * nb;
+#pragma unroll
+        for (int j = 0; j < TN; ++j)
+        {
+            const int n = n0 + tx + 8 * j;
+            if (n < nb) dst[n] = acc[i][j];
+        }
+    }
+}
+
 // glocal[row][n] = invM * sum_c part[c][row][n], summed in FP64
 template <typename T2>
 __global__ void k_gs_reduce(const T2* __restrict__ part, long long nel, int nchunks, double invM,
@@ -250,12 +540,62 @@ size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64)
     return e * (2 * (size_t)gg.Nx * GS_CB + gg.Nx);
 }
 
+template <typename T2, typename T, int N>
+static int gs_plane_ct(const GsGeom& gg, const void* psi, const void* win, int nu0, int nub, const void* twy,
+                       const void* twz, const int* cols2, int ncol, const int* zl, int nzl, void* out, cudaStream_t st)
+{
+    const size_t smem = sizeof(T2) * (2 * (size_t)N * (N + 1) + 2 * N) + sizeof(int) * N;
+    static bool attr = false;
+    if (!attr)
+    {
+        if (cudaFuncSetAttribute(k_gs_plane_ct<T2, T, N, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    dim3 grid((unsigned)nub, (unsigned)gg.nb, (unsigned)gg.Nx);
+    k_gs_plane_ct<T2, T, N, N><<<grid, GS_THREADS, smem, st>>>((const T2*)psi, (const T2*)win, gg, nu0,
+                                                               (const T2*)twy, (const T2*)twz, cols2, ncol, zl, nzl,
+                                                               (T2*)out);
+    return 0;
+}
+
+bool lelph_gs_plane_fixed(const GsGeom& gg, int fp64)
+{
+    if (gg.Ny != gg.Nz) return false;
+    switch (gg.Ny)
+    {
+    case 36: case 48: case 60: case 64: case 72: case 80: return true;
+    case 96: return !fp64;  // two FP64 96 x 96 planes exceed shared memory
+    default: return false;
+    }
+}
+
 int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const void* win, int nu0, int nub,
                           const FftPlan1D& py, const FftPlan1D& pz, const void* twy, const void* twz, const int* cols,
-                          int ncol, void* out, cudaStream_t st)
+                          int ncol, const int* cols2, const int* zl, int nzl, void* out, cudaStream_t st)
 {
     const size_t smem = lelph_gs_plane_smem(gg, fp64);
     if (smem > 220 * 1024 || nub > 65535 || gg.nb > 65535 || gg.Nx > 65535) return -1;
+    if (lelph_gs_plane_fixed(gg, fp64) && cols2 && zl)
+    {
+#define GS_CT(N)                                                                                                       case N:                                                                                                                return fp64 ? gs_plane_ct<double2, double, N>(gg, psi, win, nu0, nub, twy, twz, cols2, ncol, zl, nzl, out, st)                     : gs_plane_ct<float2, float, N>(gg, psi, win, nu0, nub, twy, twz, cols2, ncol, zl, nzl, out, st);
+        switch (gg.Ny)
+        {
+            GS_CT(36)
+            GS_CT(48)
+            GS_CT(60)
+            GS_CT(64)
+            GS_CT(72)
+            GS_CT(80)
+        case 96:
+            if (fp64) break;
+            return gs_plane_ct<float2, float, 96>(gg, psi, win, nu0, nub, twy, twz, cols2, ncol, zl, nzl, out, st);
+        default:
+            break;
+        }
+#undef GS_CT
+    }
     dim3 grid((unsigned)nub, (unsigned)gg.nb, (unsigned)gg.Nx);
     if (fp64)
     {
@@ -312,11 +652,31 @@ int lelph_launch_gs_gemm(int fp64, const void* A, const void* B, int nrows, int 
     if (nch > 65535 || gy > 65535) return -1;
     dim3 grid((unsigned)((nrows + GS_BM - 1) / GS_BM), (unsigned)gy, (unsigned)nch);
     if (fp64)
+    {
         k_gs_gemm<double, double2><<<grid, GS_THREADS, 0, st>>>((const double2*)A, (const double2*)B, nrows, nb, Ktot,
                                                                 kchunk, rowoff, nrows_total, (double2*)part);
-    else
-        k_gs_gemm<float, float2><<<grid, GS_THREADS, 0, st>>>((const float2*)A, (const float2*)B, nrows, nb, Ktot,
-                                                              kchunk, rowoff, nrows_total, (float2*)part);
+        return 0;
+    }
+    // FP32: column tile of 32, 40, 48 or 64 bands, the one wasting the fewest columns
+    int best = 64, waste = 1 << 30;
+    for (int bn : {64, 48, 40, 32})
+    {
+        const int w = (nb + bn - 1) / bn * bn - nb;
+        if (w < waste)
+        {
+            waste = w;
+            best = bn;
+        }
+    }
+    dim3 g2((unsigned)((nrows + 127) / 128), (unsigned)((nb + best - 1) / best), (unsigned)nch);
+#define GS_G32(TN)                                                                                                 \
+    k_gs_gemm_f32<4, TN><<<g2, GS_THREADS, 0, st>>>((const float2*)A, (const float2*)B, nrows, nb, Ktot, kchunk, \
+                                                    rowoff, nrows_total, (float2*)part)
+    if (best == 64) GS_G32(8);
+    else if (best == 48) GS_G32(6);
+    else if (best == 40) GS_G32(5);
+    else GS_G32(4);
+#undef GS_G32
     return 0;
 }
 

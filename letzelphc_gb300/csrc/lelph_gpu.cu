@@ -113,12 +113,13 @@ struct lelph_gpu
     // G-space route: every full-BZ k's sphere (its k+q role) sorted by
     // ((y, z) column, x) on the product grid, and the k+q coefficients stored
     // in that order (Bp); psi(r) of one k at a time and the pass buffers
-    std::vector<int> gs_npad, gs_ncol;
-    std::vector<long long> gs_perm_off, gs_col_off, gs_cst_off, gs_bp_off;
+    std::vector<int> gs_npad, gs_ncol, gs_nzl;
+    std::vector<long long> gs_perm_off, gs_col_off, gs_cst_off, gs_bp_off, gs_zl_off;
     int gs_npad_max = 0, gs_ncol_max = 0;
     long long gs_bp_total = 0;
     DevBuf d_gs_perm, d_gs_kcx, d_gs_cols, d_gs_cst, d_gs_npw, d_gs_npad, d_gs_permoff, d_gs_bpoff, d_gs_bp;
     DevBuf d_gs_psi, d_gs_out1, d_gs_A, d_gs_part;
+    DevBuf d_gs_zl, d_gs_cols2;  // z lines holding a column of the sphere; column index into the pruned plane
 };
 
 namespace
@@ -686,7 +687,7 @@ static int gs_tables(lelph_gpu* h)
     const lelph_gpu_desc& d = h->d;
     const GeomDev& g = h->g;
     const int nk = d.nkpts_BZ;
-    std::vector<std::vector<int>> perm(nk), kcx(nk), cols(nk), cst(nk);
+    std::vector<std::vector<int>> perm(nk), kcx(nk), cols(nk), cst(nk), zls(nk), cols2(nk);
     std::vector<int> bad(nk, 0);
     auto one = [&](int k) {
         const KPointSym& ks = h->ksym[k];
@@ -727,6 +728,20 @@ static int gs_tables(lelph_gpu* h)
             kc[K] = (int)(cl.size() - 1) * g.Nx + x;
         }
         cs.push_back(npw);
+        // z lines of the sphere's columns, and each column's place in the
+        // result of the y transform run on those lines only
+        std::vector<int>& zl = zls[k];
+        std::vector<int> zpos(g.Nz, -1);
+        for (int c : cl) zpos[c % g.Nz] = 1;
+        for (int z = 0; z < g.Nz; ++z)
+            if (zpos[z] > 0)
+            {
+                zpos[z] = (int)zl.size();
+                zl.push_back(z);
+            }
+        std::vector<int>& c2 = cols2[k];
+        c2.resize(cl.size());
+        for (size_t c = 0; c < cl.size(); ++c) c2[c] = (cl[c] / g.Nz) * (int)zl.size() + zpos[cl[c] % g.Nz];
     };
     {
         const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), nk));
@@ -747,8 +762,10 @@ static int gs_tables(lelph_gpu* h)
     h->gs_col_off.resize(nk);
     h->gs_cst_off.resize(nk);
     h->gs_bp_off.resize(nk);
+    h->gs_nzl.resize(nk);
+    h->gs_zl_off.resize(nk);
     std::vector<int> npw_k(nk);
-    long long po = 0, co = 0, so = 0, bo = 0;
+    long long po = 0, co = 0, so = 0, bo = 0, zo = 0;
     h->gs_npad_max = h->gs_ncol_max = 0;
     for (int k = 0; k < nk; ++k)
     {
@@ -763,23 +780,30 @@ static int gs_tables(lelph_gpu* h)
         co += h->gs_ncol[k];
         so += h->gs_ncol[k] + 1;
         bo += (long long)nrowk * h->gs_npad[k];
+        h->gs_nzl[k] = (int)zls[k].size();
+        h->gs_zl_off[k] = zo;
+        zo += h->gs_nzl[k];
         h->gs_npad_max = std::max(h->gs_npad_max, h->gs_npad[k]);
         h->gs_ncol_max = std::max(h->gs_ncol_max, h->gs_ncol[k]);
     }
     h->gs_bp_total = bo;
-    std::vector<int> pall(po, 0), kall(po, 0), call(co), sall(so);
+    std::vector<int> pall(po, 0), kall(po, 0), call(co), sall(so), c2all(co), zall(std::max(1LL, zo));
     for (int k = 0; k < nk; ++k)
     {
         std::copy(perm[k].begin(), perm[k].end(), pall.begin() + h->gs_perm_off[k]);
         std::copy(kcx[k].begin(), kcx[k].end(), kall.begin() + h->gs_perm_off[k]);
         std::copy(cols[k].begin(), cols[k].end(), call.begin() + h->gs_col_off[k]);
         std::copy(cst[k].begin(), cst[k].end(), sall.begin() + h->gs_cst_off[k]);
+        std::copy(cols2[k].begin(), cols2[k].end(), c2all.begin() + h->gs_col_off[k]);
+        std::copy(zls[k].begin(), zls[k].end(), zall.begin() + h->gs_zl_off[k]);
     }
     int rc;
     if ((rc = upload(h, h->d_gs_perm, pall.data(), sizeof(int) * pall.size()))) return rc;
     if ((rc = upload(h, h->d_gs_kcx, kall.data(), sizeof(int) * kall.size()))) return rc;
     if ((rc = upload(h, h->d_gs_cols, call.data(), sizeof(int) * call.size()))) return rc;
     if ((rc = upload(h, h->d_gs_cst, sall.data(), sizeof(int) * sall.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_cols2, c2all.data(), sizeof(int) * c2all.size()))) return rc;
+    if ((rc = upload(h, h->d_gs_zl, zall.data(), sizeof(int) * zall.size()))) return rc;
     if ((rc = upload(h, h->d_gs_npw, npw_k.data(), sizeof(int) * nk))) return rc;
     if ((rc = upload(h, h->d_gs_npad, h->gs_npad.data(), sizeof(int) * nk))) return rc;
     if ((rc = upload(h, h->d_gs_permoff, h->gs_perm_off.data(), sizeof(long long) * nk))) return rc;
@@ -1091,7 +1115,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
                       &h->d_qsitems, &h->d_dvraw, &h->d_gs_perm, &h->d_gs_kcx, &h->d_gs_cols, &h->d_gs_cst,
                       &h->d_gs_npw, &h->d_gs_npad, &h->d_gs_permoff, &h->d_gs_bpoff, &h->d_gs_bp, &h->d_gs_psi,
-                      &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part};
+                      &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part, &h->d_gs_zl, &h->d_gs_cols2};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -2001,7 +2025,10 @@ static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
             {
                 const int nmb = std::min(nub, nm - nu0);
                 if (lelph_launch_gs_plane(gg, f64, psi, win, nu0, nmb, h->plan[1], h->plan[2], tw[1], tw[2],
-                                          (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol, h->d_gs_out1.p, h->st) ||
+                                          (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol,
+                                          (const int*)h->d_gs_cols2.p + h->gs_col_off[kq],
+                                          (const int*)h->d_gs_zl.p + h->gs_zl_off[kq], h->gs_nzl[kq],
+                                          h->d_gs_out1.p, h->st) ||
                     lelph_launch_gs_xpass(gg, f64, h->d_gs_out1.p, nmb * nb * ns, ncol, h->plan[0], tw[0],
                                           (const int*)h->d_gs_cst.p + h->gs_cst_off[kq],
                                           (const int*)h->d_gs_kcx.p + h->gs_perm_off[kq], npad, h->d_gs_A.p, h->st) ||

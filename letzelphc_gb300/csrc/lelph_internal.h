@@ -91,10 +91,12 @@ struct GsGeom
 };
 size_t lelph_gs_plane_smem(const GsGeom& gg, int fp64);
 size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64);
-// plane pass of modes nu0 .. nu0+nub-1: out [(nu - nu0) nb + m][s][x][ncol]
+// plane pass of modes nu0 .. nu0+nub-1: out [(nu - nu0) nb + m][s][x][ncol]; square planes of the
+// sizes lelph_gs_plane_fixed accepts run the compile-time kernel (cols2, zl: pruned y transform)
+bool lelph_gs_plane_fixed(const GsGeom& gg, int fp64);
 int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const void* win, int nu0, int nub,
                           const FftPlan1D& py, const FftPlan1D& pz, const void* twy, const void* twz, const int* cols,
-                          int ncol, void* out, cudaStream_t st);
+                          int ncol, const int* cols2, const int* zl, int nzl, void* out, cudaStream_t st);
 // x pass: A [rb][npad] (rb = row-box index of the block) in the sphere's sorted order
 int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, int ncol, const FftPlan1D& px,
                           const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st);
