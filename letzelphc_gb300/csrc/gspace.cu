@@ -540,11 +540,101 @@ size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64)
     return e * (2 * (size_t)gg.Nx * GS_CB + gg.Nx);
 }
 
+// FP32, one spinor component: each CTA takes one (band, x plane) and NUC
+// consecutive modes.  The psi plane stays in registers for all of them, and
+// the next mode's window plane is loaded into registers while the current
+// plane is transformed, so the loads (L2 hits, shared by the CTAs of
+// neighbouring bands and modes) are in flight during the FFT.
+template <int NY, int NZ, int NUC>
+__global__ void __launch_bounds__(GS_THREADS, 2) k_gs_plane_ct1(const float2* __restrict__ psi,
+                                                               const float2* __restrict__ win, GsGeom gg, int nu0,
+                                                               int nub, const float2* __restrict__ twy,
+                                                               const float2* __restrict__ twz,
+                                                               const int* __restrict__ cols2, int ncol,
+                                                               const int* __restrict__ zl, int nzl,
+                                                               float2* __restrict__ out)
+{
+    constexpr int NZP = NZ + 1;
+    constexpr int NP = NY * NZP;
+    constexpr int NPL = NY * NZ;
+    constexpr int PER = (NPL + GS_THREADS - 1) / GS_THREADS;
+    extern __shared__ __align__(16) unsigned char gs1_smem[];
+    float2* a = reinterpret_cast<float2*>(gs1_smem);
+    float2* b = a + NP;
+    float2* ty = b + NP;
+    float2* tz = ty + NY;
+    int* szl = reinterpret_cast<int*>(tz + NZ);
+    const int m = blockIdx.y, x = blockIdx.z;
+    const int nl0 = blockIdx.x * NUC, nl1 = min(nub, nl0 + NUC);
+    for (int t = threadIdx.x; t < NY; t += blockDim.x) ty[t] = twy[t];
+    for (int t = threadIdx.x; t < NZ; t += blockDim.x) tz[t] = twz[t];
+    for (int t = threadIdx.x; t < nzl; t += blockDim.x) szl[t] = zl[t];
+    const long long M = (long long)gg.Nx * NPL;
+    const size_t xoff = (size_t)x * NPL;
+    const float2* pm = psi + (size_t)m * M + xoff;
+    const int comp = gg.nmag == 2 ? gg.spin : 0;
+    float2 ps[PER], dvn[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+    {
+        const int e = threadIdx.x + i * GS_THREADS;
+        ps[i] = e < NPL ? pm[e] : make_float2(0.f, 0.f);
+    }
+    auto load_dv = [&](int nul) {
+        const float2* d0 = win + ((size_t)(nu0 + nul) * gg.nmag + comp) * M + xoff;
+#pragma unroll
+        for (int i = 0; i < PER; ++i)
+        {
+            const int e = threadIdx.x + i * GS_THREADS;
+            dvn[i] = e < NPL ? d0[e] : make_float2(0.f, 0.f);
+        }
+    };
+    load_dv(nl0);
+    for (int nul = nl0; nul < nl1; ++nul)
+    {
+#pragma unroll
+        for (int i = 0; i < PER; ++i)
+        {
+            const int e = threadIdx.x + i * GS_THREADS;
+            if (e < NPL) a[e + e / NZ] = cmul(dvn[i], ps[i]);
+        }
+        if (nul + 1 < nl1) load_dv(nul + 1);
+        __syncthreads();
+        float2* r = ct_fft<float2, float, NZ, 0, 1, true, NY>(a, b, NY, 1, NZP, nullptr, 1, NZP, tz, -1);
+        float2* o = r == a ? b : a;
+        r = ct_fft<float2, float, NY, 0, 1, true, 0>(r, o, nzl, NZP, 1, szl, nzl, 1, ty, -1);
+        float2* dst = out + ((size_t)(nul * gg.nb + m) * gg.Nx + x) * ncol;
+        for (int c = threadIdx.x; c < ncol; c += GS_THREADS) dst[c] = r[cols2[c]];
+        __syncthreads();
+    }
+}
+
 template <typename T2, typename T, int N>
 static int gs_plane_ct(const GsGeom& gg, const void* psi, const void* win, int nu0, int nub, const void* twy,
                        const void* twz, const int* cols2, int ncol, const int* zl, int nzl, void* out, cudaStream_t st)
 {
     const size_t smem = sizeof(T2) * (2 * (size_t)N * (N + 1) + 2 * N) + sizeof(int) * N;
+    // (planes up to 64 x 64: the psi and window planes of a thread fit its registers)
+    if constexpr (sizeof(T2) == sizeof(float2) && N * N <= 4096)
+    {
+        if (gg.nspinor == 1)
+        {
+            constexpr int NUC = 4;
+            static bool attr1 = false;
+            if (!attr1)
+            {
+                if (cudaFuncSetAttribute(k_gs_plane_ct1<N, N, NUC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem) != cudaSuccess)
+                    return -1;
+                attr1 = true;
+            }
+            dim3 g1((unsigned)((nub + NUC - 1) / NUC), (unsigned)gg.nb, (unsigned)gg.Nx);
+            k_gs_plane_ct1<N, N, NUC><<<g1, GS_THREADS, smem, st>>>((const float2*)psi, (const float2*)win, gg, nu0,
+                                                                    nub, (const float2*)twy, (const float2*)twz,
+                                                                    cols2, ncol, zl, nzl, (float2*)out);
+            return 0;
+        }
+    }
     static bool attr = false;
     if (!attr)
     {
