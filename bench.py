@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
-    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf", "configs"],
+    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf", "configs", "gspace"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
                         "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
@@ -742,6 +742,91 @@ def run_dvscf(args):
     return 0
 
 
+def run_gspace(args):
+    """The G-space route on the 16-atom, 200-band configuration (96^3 box, 60^3
+    product grid, npw ~12000): the first 8 irreducible q at a block of k
+    points (16 k; with --small a 2x2x2 k grid and 2 q, the profiling case),
+    device-resident output, CUDA events on the library stream; per-kernel
+    device times from the library's profiling counters in a separate pass."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64
+    build_library()
+    if args.small:
+        s = synth.make_system("c4", {"kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0), (0.5, 0.5, 0)]})
+        kk = np.arange(s.nk_bz)
+    else:
+        s = synth.make_system("c4", {"qpts": [tuple(q) for q in _c4_qpts()[:8]]})
+        kk = np.arange(16) * (s.nk_bz // 16)
+    nq = len(s.qpts)
+    qs = np.repeat(np.arange(nq), len(kk)).astype(np.int32)
+    ks = np.tile(kk, nq).astype(np.int32)
+    npairs = len(qs)
+    gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+    ctx = LelphGPU(s, args.precision, device=local)
+    for iq in range(nq):
+        ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+    ctx.prepare()
+    gdev = torch.empty(npairs * gsz * 2, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(max(3, args.warmup)):
+        ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    ctx.set_profiling(True)
+    p0 = ctx.stats()
+    ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)
+    p1 = ctx.stats()
+    ctx.set_profiling(False)
+    st = ctx.stats()
+    ctx.close()
+    d = {k: (p1[k] - p0[k]) / npairs for k in ("gs_plane_ms", "gs_xpass_ms", "gs_gemm_ms", "local_ms", "finish_ms")}
+    npw = int(np.mean([len(g) for g in s.gvec]))
+    gemm_flops = 8.0 * s.nmodes * s.nbnds * s.nbnds * s.nspinor * npw * s.nspin  # complex MACs x 8 per pair
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 (non-tensor) rate at the maximum SM clock
+    elems = npairs * gsz
+    line = {"metric": "g elements/s per GB300 on the G-space route (16-atom cell, 200 bands)",
+            "value": elems / (ms * 1e-3), "unit": "g_elements/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.precision, "data": "synthetic (seeded, configuration-4 shapes)",
+            "config": {"workload": f"{nq} q x {len(kk)} k of the 16-atom cell ({npairs} pairs, "
+                                   f"product grid {list(st['product_grid'])}, npw ~{npw})",
+                       "route": {1: "real-space", 2: "G-space"}.get(st["route"]),
+                       "timing": "CUDA events on the library stream, device-resident inputs and output"},
+            "ms_per_pair": ms / npairs, "kernel_ms_per_pair": d, "clocks": clk,
+            "gpu_launches": int(p1["kernel_launches"] - p0["kernel_launches"]),
+            "roofline": {"kernel": "k_gs_gemm_f32", "bound": "fp32",
+                         "achieved": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 if d["gs_gemm_ms"] else None,
+                         "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 / fp32_peak if d["gs_gemm_ms"] else None,
+                         "peak_source": "nominal GB300 FP32 SIMT rate at 2070 MHz (no measured FP32 peak)",
+                         "flops_per_pair": gemm_flops, "traffic": None}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _c4_qpts():
+    """The irreducible q of the 16-atom cell's 8x8x8 grid, as synth builds them."""
+    from letzelphc_gb300 import synth
+    cfg = synth.CONFIGS["c4"]
+    s = synth.make_system("c4", {"qpts": [(0, 0, 0)], "kgrid": cfg["kgrid"], "nbnds": 1, "npw": 50})
+    return synth.reduce_grid(cfg["kgrid"], s.sym_R, s.alat)
+
+
 CONFIG_NAMES = ["c0", "c1", "c2", "c3", "c4"]
 
 
@@ -850,6 +935,8 @@ def main():
     args = parse()
     if args.workload == "configs":
         return run_configs(args)
+    if args.workload == "gspace":
+        return run_gspace(args)
     if args.workload == "dvscf":
         return run_dvscf(args)
     if args.workload == "dmats":

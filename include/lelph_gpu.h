@@ -113,6 +113,9 @@ typedef struct lelph_gpu_stats
     double qstar_ms;             /* device time of the q-star rotations (profiling on) */
     double dvscf_ms;             /* device time of the dV_scf ingest kernel (profiling on) */
     int route;                   /* route in use: LELPH_GPU_ROUTE_REAL or LELPH_GPU_ROUTE_GSPACE */
+    double gs_plane_ms;          /* G-space route: device time of the plane, x-pass and GEMM kernels */
+    double gs_xpass_ms;          /*   (profiling on; each launch timed with events on the library stream) */
+    double gs_gemm_ms;
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

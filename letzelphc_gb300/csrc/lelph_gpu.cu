@@ -51,6 +51,7 @@ struct lelph_gpu
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evg0 = nullptr, evg1 = nullptr;  // per-kernel timing of the G-space route (profiling on)
     bool profiling = false;
     std::string err;
     lelph_gpu_stats stats;
@@ -622,6 +623,8 @@ extern "C" void lelph_gpu_destroy(lelph_gpu* h)
         if (b->p) cudaFree(b->p);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->evg0) cudaEventDestroy(h->evg0);
+    if (h->evg1) cudaEventDestroy(h->evg1);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
@@ -1103,6 +1106,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "stream");
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
+    cudaEventCreate(&h->evg0);
+    cudaEventCreate(&h->evg1);
     DevBuf* bufs[] = {&h->d_miller, &h->d_pwoff, &h->d_npw, &h->d_coef, &h->d_coefoff, &h->d_gvec, &h->d_fk,
                       &h->d_fkoff, &h->d_ksym, &h->d_chat, &h->d_chatoff, &h->d_psi64, &h->d_boxes32, &h->d_bsplit,
                       &h->d_psi32, &h->d_band_scale, &h->d_proj, &h->d_atype, &h->d_apos, &h->d_pp, &h->d_fsign, &h->d_fcoef,
@@ -1945,6 +1950,23 @@ static int build_windows(lelph_gpu* h)
     return LELPH_GPU_OK;
 }
 
+// Per-kernel device time of the G-space route while profiling: gs_tick marks
+// the start, each gs_tock returns the time since the last mark and re-marks.
+static void gs_tick(lelph_gpu* h)
+{
+    if (h->profiling) cudaEventRecord(h->evg0, h->st);
+}
+static double gs_tock(lelph_gpu* h)
+{
+    if (!h->profiling) return 0.0;
+    cudaEventRecord(h->evg1, h->st);
+    cudaEventSynchronize(h->evg1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->evg0, h->evg1);
+    std::swap(h->evg0, h->evg1);
+    return ms;
+}
+
 // Local term of pairs[0 .. n) on the G-space route, into glocal
 // (pair, spin, mode x band of k, band of k+q), FP64, 1/M applied.  Pairs are
 // visited grouped by their k so that psi(r) of a k is built once per group:
@@ -2024,17 +2046,23 @@ static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
             for (int nu0 = 0; nu0 < nm; nu0 += nub)
             {
                 const int nmb = std::min(nub, nm - nu0);
-                if (lelph_launch_gs_plane(gg, f64, psi, win, nu0, nmb, h->plan[1], h->plan[2], tw[1], tw[2],
-                                          (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol,
-                                          (const int*)h->d_gs_cols2.p + h->gs_col_off[kq],
-                                          (const int*)h->d_gs_zl.p + h->gs_zl_off[kq], h->gs_nzl[kq],
-                                          h->d_gs_out1.p, h->st) ||
-                    lelph_launch_gs_xpass(gg, f64, h->d_gs_out1.p, nmb * nb * ns, ncol, h->plan[0], tw[0],
-                                          (const int*)h->d_gs_cst.p + h->gs_cst_off[kq],
-                                          (const int*)h->d_gs_kcx.p + h->gs_perm_off[kq], npad, h->d_gs_A.p, h->st) ||
-                    lelph_launch_gs_gemm(f64, h->d_gs_A.p, B, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
-                                         h->d_gs_part.p, h->st))
-                    return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "G-space route: launch configuration");
+                int bad = 0;
+                gs_tick(h);
+                bad |= lelph_launch_gs_plane(gg, f64, psi, win, nu0, nmb, h->plan[1], h->plan[2], tw[1], tw[2],
+                                             (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol,
+                                             (const int*)h->d_gs_cols2.p + h->gs_col_off[kq],
+                                             (const int*)h->d_gs_zl.p + h->gs_zl_off[kq], h->gs_nzl[kq],
+                                             h->d_gs_out1.p, h->st);
+                h->stats.gs_plane_ms += gs_tock(h);
+                bad |= lelph_launch_gs_xpass(gg, f64, h->d_gs_out1.p, nmb * nb * ns, ncol, h->plan[0], tw[0],
+                                             (const int*)h->d_gs_cst.p + h->gs_cst_off[kq],
+                                             (const int*)h->d_gs_kcx.p + h->gs_perm_off[kq], npad, h->d_gs_A.p,
+                                             h->st);
+                h->stats.gs_xpass_ms += gs_tock(h);
+                bad |= lelph_launch_gs_gemm(f64, h->d_gs_A.p, B, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
+                                            h->d_gs_part.p, h->st);
+                h->stats.gs_gemm_ms += gs_tock(h);
+                if (bad) return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "G-space route: launch configuration");
                 h->stats.kernel_launches += 3;
             }
             lelph_launch_gs_reduce(f64, h->d_gs_part.p, (long long)nrows * nb, nch, 1.0 / (double)M,

@@ -52,6 +52,7 @@ class Stats(C.Structure):
         ("device_bytes", C.c_size_t), ("product_grid", C.c_int * 3), ("chunk_points", C.c_int),
         ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
         ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double), ("route", C.c_int),
+        ("gs_plane_ms", C.c_double), ("gs_xpass_ms", C.c_double), ("gs_gemm_ms", C.c_double),
     ]
 
 
