@@ -315,6 +315,52 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_xpass(const T2* __restrict__ 
     }
 }
 
+// x pass for the compile-time sizes: CB columns per CTA, every load of the
+// tile issued before the first is used (the generic pass waits on each), the
+// x transform with the compile-time schedule, consecutive threads on
+// consecutive columns (conflict-free).
+template <typename T2, typename T, int NX, int CB>
+__global__ void __launch_bounds__(GS_THREADS) k_gs_xpass_ct(const T2* __restrict__ in, int ncol,
+                                                            const T2* __restrict__ twx, const int* __restrict__ cst,
+                                                            const int* __restrict__ kcx, int npad,
+                                                            T2* __restrict__ A)
+{
+    constexpr int NE = NX * CB;
+    constexpr int PER = (NE + GS_THREADS - 1) / GS_THREADS;
+    extern __shared__ __align__(16) unsigned char gsxc_smem[];
+    T2* a = reinterpret_cast<T2*>(gsxc_smem);
+    T2* b = a + NE;
+    T2* tx = b + NE;
+    const int c0 = blockIdx.x * CB;
+    const int rb = blockIdx.y;
+    for (int t = threadIdx.x; t < NX; t += blockDim.x) tx[t] = twx[t];
+    const T2* src = in + (size_t)rb * NX * ncol + c0;
+    T2 v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+    {
+        const int e = threadIdx.x + i * GS_THREADS;
+        const int x = e / CB, cc = e - x * CB;
+        v[i] = (e < NE && c0 + cc < ncol) ? src[(size_t)x * ncol + cc] : mk2<T2>(0.0, 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+    {
+        const int e = threadIdx.x + i * GS_THREADS;
+        if (e < NE) a[e] = v[i];
+    }
+    __syncthreads();
+    T2* r = ct_fft<T2, T, NX, 0, 1, true, CB>(a, b, CB, CB, 1, nullptr, CB, 1, tx, -1);
+    const int k0 = cst[c0], k1 = cst[min(c0 + CB, ncol)];
+    T2* dst = A + (size_t)rb * npad;
+    for (int K = k0 + threadIdx.x; K < k1; K += blockDim.x)
+    {
+        const int w = kcx[K];
+        const int c = w / NX, x = w - c * NX;
+        dst[K] = r[x * CB + (c - c0)];
+    }
+}
+
 // ---------------------------------------------------------------------- GEMM
 // part[chunk][rowoff + row][n] = sum_{K in chunk} A[row][K] conj(B[n][K]);
 // A: nrows x Ktot, B: nb x Ktot, both K-contiguous.  64 x 64 tile, 16-deep K
@@ -708,11 +754,47 @@ int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const voi
     return 0;
 }
 
+template <typename T2, typename T, int NX, int CB>
+static int gs_xpass_ct(int nrb, int ncol, const void* twx, const int* cst, const int* kcx, int npad, const void* in,
+                       void* A, cudaStream_t st)
+{
+    const size_t smem = sizeof(T2) * (2 * (size_t)NX * CB + NX);
+    static bool attr = false;
+    if (!attr)
+    {
+        if (cudaFuncSetAttribute(k_gs_xpass_ct<T2, T, NX, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        attr = true;
+    }
+    dim3 grid((unsigned)((ncol + CB - 1) / CB), (unsigned)nrb);
+    k_gs_xpass_ct<T2, T, NX, CB><<<grid, GS_THREADS, smem, st>>>((const T2*)in, ncol, (const T2*)twx, cst, kcx, npad,
+                                                                (T2*)A);
+    return 0;
+}
+
 int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, int ncol, const FftPlan1D& px,
                           const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st)
 {
     const size_t smem = lelph_gs_xpass_smem(gg, fp64);
     if (smem > 220 * 1024 || nrb > 65535) return -1;
+#define GS_XC(N)                                                                                            \
+    case N:                                                                                                 \
+        return fp64 ? gs_xpass_ct<double2, double, N, 32>(nrb, ncol, twx, cst, kcx, npad, in, A, st)        \
+                    : gs_xpass_ct<float2, float, N, 64>(nrb, ncol, twx, cst, kcx, npad, in, A, st);
+    switch (gg.Nx)
+    {
+        GS_XC(36)
+        GS_XC(48)
+        GS_XC(60)
+        GS_XC(64)
+        GS_XC(72)
+        GS_XC(80)
+        GS_XC(96)
+    default:
+        break;
+    }
+#undef GS_XC
     dim3 grid((unsigned)((ncol + GS_CB - 1) / GS_CB), (unsigned)nrb);
     if (fp64)
     {
