@@ -2168,7 +2168,8 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
         tstart(h);
-        lelph_launch_finish(dp, nb, fp64_local ? 1 : 0, (const double2*)h->d_glocal.p, (const float*)h->d_partials.p,
+        lelph_launch_finish(dp, nb, !fp64_local ? 0 : (h->mixed ? 2 : 1), (const double2*)h->d_glocal.p,
+                            (const float*)h->d_partials.p,
                             h->nchunks, (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,
                             out_type == LELPH_GPU_OUT_C64, (char*)gdev + esz * gsz * p0, h->st);

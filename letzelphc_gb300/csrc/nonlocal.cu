@@ -688,12 +688,174 @@ static size_t finish_pair_smem(const NonlocalDesc& nl, const GeomDev& g, size_t 
            (size_t)nl.ntype * 8 * sizeof(double);
 }
 
+// Finish for many displacement components (3 natom > 24, where the
+// per-pair form's projection sets overflow shared memory): one CTA per
+// (16 x 16 band tile, pair, spin); the projections of the tile's 16 bands
+// of k and 16 bands of k+q, the pair's eigVec and the channel table sit in
+// shared memory; each thread owns one (m, n) and keeps its NJ displacement
+// sums in registers, then applies the mode transform.  glocal (FP64 local
+// term) is added in FP64; T is the arithmetic of the nonlocal term.
+#define FT_B 16
+template <int NJ, typename T>
+__global__ void __launch_bounds__(FT_B * FT_B) k_finish_tile(const PairInfo* __restrict__ pairs,
+                                                             const double2* __restrict__ glocal,
+                                                             const double2* __restrict__ proj,
+                                                             const double2* __restrict__ eig, int non_loc,
+                                                             NonlocalDesc nl, GeomDev gd, int out_c64,
+                                                             void* __restrict__ gout)
+{
+    typedef typename cplx_of<T>::type C2;
+    extern __shared__ __align__(16) unsigned char ftsm[];
+    const int ntile = (gd.nbnds + FT_B - 1) / FT_B;
+    const int tm = blockIdx.x / ntile, tn = blockIdx.x - tm * ntile;
+    const int zp = blockIdx.y;
+    const int pair = zp / gd.nspin, spin = zp - pair * gd.nspin;
+    const PairInfo P = pairs[pair];
+    const int nb = gd.nbnds, ns = gd.nspinor;
+    const int nsets = gd.nspin * nb * ns;
+    const int rows = nl.natom * nl.nproj_max * 4;
+    const int nj = 3 * nl.natom;
+    const int sets = FT_B * ns;                               // the tile's sets of one role
+    C2* sK = reinterpret_cast<C2*>(ftsm);                    // [rows][sets]  role k+q (bands n0 ..)
+    C2* sKp = sK + (size_t)rows * sets;                      // [rows][sets]  role k (bands m0 ..)
+    C2* sE = sKp + (size_t)rows * sets;                      // [nmodes][nj]
+    int* sch = reinterpret_cast<int*>(sE + (size_t)gd.nmodes * nj);
+    T* ssoc = reinterpret_cast<T*>(sch + nl.ntype * 8 * 4);
+    const int m0 = tm * FT_B, n0 = tn * FT_B;
+    if (non_loc)
+    {
+        const double2* PK = proj + (size_t)P.kbz_kq * rows * nsets + (size_t)spin * nb * ns;
+        const double2* PKp = proj + (size_t)P.kbz_k * rows * nsets + (size_t)spin * nb * ns;
+        for (int e = threadIdx.x; e < rows * sets; e += blockDim.x)
+        {
+            const int r = e / sets, c = e - r * sets;
+            const int bn = n0 * ns + c, bm = m0 * ns + c;
+            const double2 k1 = bn < nb * ns ? PK[(size_t)r * nsets + bn] : make_double2(0.0, 0.0);
+            const double2 k2 = bm < nb * ns ? PKp[(size_t)r * nsets + bm] : make_double2(0.0, 0.0);
+            sK[e] = mk2<C2>(k1.x, k1.y);
+            sKp[e] = mk2<C2>(k2.x, k2.y);
+        }
+        const double2* E = eig + (size_t)P.qslot * gd.nmodes * gd.nmodes;
+        for (int e = threadIdx.x; e < gd.nmodes * nj; e += blockDim.x)
+        {
+            const double2 v = E[(e / nj) * gd.nmodes + (e % nj)];
+            sE[e] = mk2<C2>(v.x, v.y);
+        }
+        if (threadIdx.x < nl.ntype)
+        {
+            const int it = threadIdx.x;
+            int nc = 0, pb = 0;
+            for (int lidx = 0; lidx < nl.nltimesj && nc < 8; ++lidx)
+            {
+                int l = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3] - 1.0);
+                if (l < 0) continue;
+                int twoj = (int)rint(nl.PP_table[(lidx * nl.ntype + it) * 3 + 1]);
+                int* ch = sch + (it * 8 + nc) * 4;
+                ch[0] = lidx;
+                ch[1] = l;
+                ch[2] = pb;
+                ch[3] = nl.fcoef ? nl.fcoef_off[lidx * nl.ntype + it] : -1;
+                ssoc[it * 8 + nc] = (T)((twoj != 0 && !nl.is_soc) ? (twoj + 1.0) / (4.0 * l + 2.0) : 1.0);
+                pb += 2 * l + 1;
+                ++nc;
+            }
+            for (; nc < 8; ++nc) sch[(it * 8 + nc) * 4 + 1] = -1;
+        }
+    }
+    __syncthreads();
+    const int ml = threadIdx.x / FT_B, nlc = threadIdx.x - ml * FT_B;
+    const int m = m0 + ml, n = n0 + nlc;  // m: band of k, n: band of k+q
+    if (m >= nb || n >= nb) return;
+    C2 out[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) out[j] = mk2<C2>(0.0, 0.0);
+    if (non_loc)
+    {
+#pragma unroll
+        for (int j = 0; j < NJ; ++j)
+        {
+            if (j >= nj) continue;
+            const int a = j / 3, x = j - 3 * a;
+            const int it = nl.atom_type[a];
+            const int rb = a * nl.nproj_max * 4;
+            C2 acc = mk2<C2>(0.0, 0.0);
+            for (int c = 0; c < 8; ++c)
+            {
+                const int* ch = sch + (it * 8 + c) * 4;
+                const int l = ch[1];
+                if (l < 0) break;
+                const int tl = 2 * l + 1, pb = ch[2], foff = ch[3];
+                const T soc = ssoc[it * 8 + c];
+                for (int im1 = 0; im1 < tl; ++im1)
+                    for (int im2 = 0; im2 < tl; ++im2)
+                    {
+                        if (foff < 0 && im1 != im2) continue;
+                        const int p1 = pb + im1, p2 = pb + im2;
+                        for (int s1 = 0; s1 < ns; ++s1)
+                            for (int s2 = 0; s2 < ns; ++s2)
+                            {
+                                C2 f;
+                                if (foff >= 0)
+                                {
+                                    const double* fc = nl.fcoef + 2 * ((size_t)foff + (im1 * tl + im2) * ns * ns + s1 * ns + s2);
+                                    f = mk2<C2>(fc[0], fc[1]);
+                                }
+                                else
+                                {
+                                    if (s1 != s2) continue;
+                                    f.x = soc;
+                                    f.y = 0;
+                                }
+                                const C2 K0 = sK[(size_t)(rb + p1 * 4 + 0) * sets + nlc * ns + s1];
+                                const C2 Kx = sK[(size_t)(rb + p1 * 4 + 1 + x) * sets + nlc * ns + s1];
+                                const C2 Kp0 = cconj(sKp[(size_t)(rb + p2 * 4 + 0) * sets + ml * ns + s2]);
+                                C2 Kpx = sKp[(size_t)(rb + p2 * 4 + 1 + x) * sets + ml * ns + s2];
+                                Kpx.x = -Kpx.x;  // -conj
+                                acc = cadd(acc, cmul(f, cadd(cmul(Kx, Kp0), cmul(K0, Kpx))));
+                            }
+                    }
+            }
+            out[j] = acc;
+        }
+    }
+    const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
+    for (int nu = 0; nu < gd.nmodes; ++nu)
+    {
+        const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
+        double2 v = glocal[((size_t)zp * gd.nmodes * nb + nu * nb + m) * nb + n];
+        if (non_loc)
+        {
+            C2 sacc = mk2<C2>(0.0, 0.0);
+#pragma unroll
+            for (int j = 0; j < NJ; ++j)
+                if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
+            v = cadd(v, cmul(pre, make_double2((double)sacc.x, (double)sacc.y)));
+        }
+        if (out_c64)
+            reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)v.x, (float)v.y);
+        else
+            reinterpret_cast<double2*>(gout)[oidx] = v;
+    }
+}
+
+static size_t finish_tile_smem(const NonlocalDesc& nl, const GeomDev& g, size_t csz)
+{
+    const size_t rows = (size_t)nl.natom * nl.nproj_max * 4;
+    const size_t sets = (size_t)FT_B * g.nspinor;
+    return 2 * rows * sets * csz + (size_t)g.nmodes * 3 * nl.natom * csz + (size_t)nl.ntype * 8 * 4 * sizeof(int) +
+           (size_t)nl.ntype * 8 * sizeof(double);
+}
+
 void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const double2* glocal,
                          const float* partials, int nchunks, const float* mode_scale, const float* band_scale,
                          const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,
                          const GeomDev& g, int out_c64, void* gout, cudaStream_t st)
 {
-    const size_t smem = finish_pair_smem(nl, g, mode_fp64 ? sizeof(double2) : sizeof(float2));
+    // mode_fp64: 0 = K-chunk partials (mixed real-space route), 1 = FP64 local
+    // term and FP64 nonlocal arithmetic (plain form), 2 = FP64 local term and
+    // FP32 nonlocal arithmetic (mixed form on the G-space route)
+    const bool t64 = mode_fp64 == 1;
+    const size_t smem = finish_pair_smem(nl, g, t64 ? sizeof(double2) : sizeof(float2));
     const int nj = 3 * nl.natom;
     if (smem <= 160 * 1024 && nj <= 24)
     {
@@ -711,7 +873,7 @@ void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const
     k_finish_pair<NJ, T><<<nz, NJ <= 12 ? 256 : 128, smem, st>>>(pairs, mode_fp64, glocal, partials, nchunks,    \
                                                                   mode_scale, band_scale, proj, eig, non_loc, nl, g, \
                                                                   out_c64, gout)
-        if (mode_fp64)
+        if (t64)
         {
             if (nj <= 12) FINL(12, double);
             else FINL(24, double);
@@ -722,6 +884,26 @@ void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const
             else FINL(24, float);
         }
 #undef FINL
+        return;
+    }
+    const size_t tsm = finish_tile_smem(nl, g, t64 ? sizeof(double2) : sizeof(float2));
+    if (mode_fp64 && nj <= 48 && tsm <= 200 * 1024)
+    {
+        static bool tattr = false;
+        if (!tattr)
+        {
+            cudaFuncSetAttribute(k_finish_tile<48, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_finish_tile<48, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            tattr = true;
+        }
+        const int nt = (g.nbnds + FT_B - 1) / FT_B;
+        dim3 tg((unsigned)(nt * nt), (unsigned)(npairs * g.nspin));
+        if (t64)
+            k_finish_tile<48, double><<<tg, FT_B * FT_B, tsm, st>>>(pairs, glocal, proj, eig, non_loc, nl, g, out_c64,
+                                                                  gout);
+        else
+            k_finish_tile<48, float><<<tg, FT_B * FT_B, tsm, st>>>(pairs, glocal, proj, eig, non_loc, nl, g, out_c64,
+                                                                 gout);
         return;
     }
     dim3 grid((g.nbnds * g.nbnds + FIN_MN - 1) / FIN_MN, npairs * g.nspin);

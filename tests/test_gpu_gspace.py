@@ -111,3 +111,20 @@ def test_gspace_batch_order_independent():
         perm = np.random.default_rng(3).permutation(len(qs))
         gp = ctx.run(qs[perm], ks[perm])
     assert np.array_equal(gp, g[perm])
+
+
+@pytest.mark.parametrize("route", ["real", "gspace"])
+def test_sixteen_atoms_against_oracle(route):
+    """48 displacement components: the finish runs tiled over bands (the
+    per-pair form holds at most 24); both routes, both forms, vs the oracle."""
+    s = synth.make_system("c4", {"nbnds": 6, "npw": 300, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)],
+                                 "fft": (24, 24, 24)})
+    ks = list(range(s.nk_bz))
+    ref = O.compute_elphq(s, 0, k_list=ks)
+    with LelphGPU(s, "fp64", route=route) as c64, LelphGPU(s, "mixed", route=route) as cm:
+        c64.set_q(0, s.qpts[0], s.eigVec[0], s.dVscf[0])
+        cm.set_q(0, s.qpts[0], s.eigVec[0], s.dVscf[0])
+        g = c64.run([0] * len(ks), ks)
+        gm = cm.run([0] * len(ks), ks)
+    assert np.abs(g - ref).max() / np.abs(ref).max() < FP64_TOL
+    assert np.linalg.norm((gm - ref).ravel()) / np.linalg.norm(ref.ravel()) < 2e-6
