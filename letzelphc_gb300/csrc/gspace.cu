@@ -445,16 +445,29 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_gemm(const T2* __restrict__ A
 // 256 threads as 32 row groups x 8 column groups, TM rows x TN columns per
 // thread (columns tx + 8 j), BM = 32 TM rows, BN = 8 TN columns; BN is
 // picked at launch so that the bands fill whole tiles (200 bands: 5 tiles
-// of 40).
+// of 40).  The K steps are double-buffered in shared memory by cp.async
+// (8-byte copies into the K-major tiles; out-of-range elements are
+// zero-filled), so no registers hold staged tiles.
+__device__ __forceinline__ void gs_cp8(uint32_t dst, const void* src, bool valid)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void gs_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void gs_cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void gs_cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 template <int TM, int TN>
 __global__ void __launch_bounds__(GS_THREADS, 2) k_gs_gemm_f32(const float2* __restrict__ A, const float2* __restrict__ B,
-                                                            int nrows, int nb, int Ktot, int kchunk, int rowoff,
-                                                            int nrows_total, float2* __restrict__ part)
+                                                               int nrows, int nb, int Ktot, int kchunk, int rowoff,
+                                                               int nrows_total, float2* __restrict__ part)
 {
     constexpr int BM = 32 * TM, BN = 8 * TN;
-    constexpr int AL = BM * GS_BK / GS_THREADS;  // A elements each thread stages per K step
-    __shared__ float2 As[GS_BK][BM + 1];
-    __shared__ float2 Bs[GS_BK][BN + 1];
+    constexpr int AL = BM * GS_BK / GS_THREADS;                      // A elements each thread copies per K step
+    constexpr int BL = (BN * GS_BK + GS_THREADS - 1) / GS_THREADS;   // B elements (last round partial)
+    extern __shared__ __align__(16) unsigned char gsg_smem[];
+    auto As = reinterpret_cast<float2(*)[GS_BK][BM + 1]>(gsg_smem);                           // [2][BK][BM+1]
+    auto Bs = reinterpret_cast<float2(*)[GS_BK][BN + 1]>(gsg_smem + sizeof(float2) * 2 * GS_BK * (BM + 1));
     const int tid = threadIdx.x, tx = tid & 7, ty = tid >> 3;
     const int lk = tid & 15, lr = tid >> 4;
     const int r0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
@@ -464,45 +477,50 @@ __global__ void __launch_bounds__(GS_THREADS, 2) k_gs_gemm_f32(const float2* __r
     for (int i = 0; i < TM; ++i)
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
-    float2 ra[AL], rb[(BN * GS_BK + GS_THREADS - 1) / GS_THREADS];
-    auto load = [&](int k0) {
+    auto issue = [&](int k0, int buf) {
         const int k = k0 + lk;
 #pragma unroll
         for (int i = 0; i < AL; ++i)
         {
             const int row = r0 + lr + 16 * i;
-            ra[i] = (row < nrows && k < kend) ? A[(size_t)row * Ktot + k] : make_float2(0.f, 0.f);
+            const bool ok = row < nrows && k < kend;
+            gs_cp8((uint32_t)__cvta_generic_to_shared(&As[buf][lk][lr + 16 * i]),
+                   ok ? (const void*)(A + (size_t)row * Ktot + k) : (const void*)A, ok);
         }
 #pragma unroll
-        for (int i = 0; i < (BN * GS_BK + GS_THREADS - 1) / GS_THREADS; ++i)
+        for (int i = 0; i < BL; ++i)
         {
             const int e = tid + i * GS_THREADS;
-            const int n = n0 + (e >> 4), kk = k0 + (e & 15);
-            rb[i] = (e < BN * GS_BK && n < nb && kk < kend) ? B[(size_t)n * Ktot + kk] : make_float2(0.f, 0.f);
+            if (e < BN * GS_BK)
+            {
+                const int n = n0 + (e >> 4), kk = k0 + (e & 15);
+                const bool ok = n < nb && kk < kend;
+                gs_cp8((uint32_t)__cvta_generic_to_shared(&Bs[buf][e & 15][e >> 4]),
+                       ok ? (const void*)(B + (size_t)n * Ktot + kk) : (const void*)B, ok);
+            }
         }
+        gs_cp_commit();
     };
-    load(kbeg);
-    for (int k0 = kbeg; k0 < kend; k0 += GS_BK)
+    issue(kbeg, 0);
+    int buf = 0;
+    for (int k0 = kbeg; k0 < kend; k0 += GS_BK, buf ^= 1)
     {
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < AL; ++i) As[lk][lr + 16 * i] = ra[i];
-#pragma unroll
-        for (int i = 0; i < (BN * GS_BK + GS_THREADS - 1) / GS_THREADS; ++i)
+        if (k0 + GS_BK < kend)
         {
-            const int e = tid + i * GS_THREADS;
-            if (e < BN * GS_BK) Bs[e & 15][e >> 4] = rb[i];
+            issue(k0 + GS_BK, buf ^ 1);
+            gs_cp_wait1();
         }
+        else
+            gs_cp_wait0();
         __syncthreads();
-        if (k0 + GS_BK < kend) load(k0 + GS_BK);
 #pragma unroll
         for (int kk = 0; kk < GS_BK; ++kk)
         {
             float2 av[TM], bv[TN];
 #pragma unroll
-            for (int i = 0; i < TM; ++i) av[i] = As[kk][ty * TM + i];
+            for (int i = 0; i < TM; ++i) av[i] = As[buf][kk][ty * TM + i];
 #pragma unroll
-            for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tx + 8 * j];
+            for (int j = 0; j < TN; ++j) bv[j] = Bs[buf][kk][tx + 8 * j];
 #pragma unroll
             for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -514,6 +532,7 @@ __global__ void __launch_bounds__(GS_THREADS, 2) k_gs_gemm_f32(const float2* __r
                     acc[i][j].y = fmaf(-av[i].x, bv[j].y, acc[i][j].y);
                 }
         }
+        __syncthreads();
     }
 #pragma unroll
     for (int i = 0; i < TM; ++i)
@@ -840,14 +859,29 @@ int lelph_launch_gs_gemm(int fp64, const void* A, const void* B, int nrows, int 
             best = bn;
         }
     }
-    dim3 g2((unsigned)((nrows + 127) / 128), (unsigned)((nb + best - 1) / best), (unsigned)nch);
-#define GS_G32(TN)                                                                                                 \
-    k_gs_gemm_f32<4, TN><<<g2, GS_THREADS, 0, st>>>((const float2*)A, (const float2*)B, nrows, nb, Ktot, kchunk, \
-                                                    rowoff, nrows_total, (float2*)part)
-    if (best == 64) GS_G32(8);
-    else if (best == 48) GS_G32(6);
-    else if (best == 40) GS_G32(5);
-    else GS_G32(4);
+    // 256-row tiles (8 rows per thread) for the narrow column tiles when the rows fill them
+    const bool tall = best <= 40 && nrows >= 2048;
+    const int bm = tall ? 256 : 128;
+    dim3 g2((unsigned)((nrows + bm - 1) / bm), (unsigned)((nb + best - 1) / best), (unsigned)nch);
+#define GS_G32(TM, TN)                                                                                          \
+    do                                                                                                          \
+    {                                                                                                           \
+        const int sm = (int)(sizeof(float2) * 2 * GS_BK * (32 * TM + 1 + 8 * TN + 1));                           \
+        static bool at = false;                                                                                 \
+        if (!at)                                                                                                \
+        {                                                                                                       \
+            if (cudaFuncSetAttribute(k_gs_gemm_f32<TM, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != \
+                cudaSuccess)                                                                                    \
+                return -1;                                                                                      \
+            at = true;                                                                                          \
+        }                                                                                                       \
+        k_gs_gemm_f32<TM, TN><<<g2, GS_THREADS, sm, st>>>((const float2*)A, (const float2*)B, nrows, nb, Ktot,   \
+                                                          kchunk, rowoff, nrows_total, (float2*)part);          \
+    } while (0)
+    if (best == 64) GS_G32(4, 8);
+    else if (best == 48) GS_G32(4, 6);
+    else if (best == 40) { if (tall) GS_G32(8, 5); else GS_G32(4, 5); }
+    else { if (tall) GS_G32(8, 4); else GS_G32(4, 4); }
 #undef GS_G32
     return 0;
 }
