@@ -606,12 +606,14 @@ size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64)
 }
 
 // FP32, one spinor component: each CTA takes one (band, x plane) and NUC
-// consecutive modes.  The psi plane stays in registers for all of them, and
-// the next mode's window plane is loaded into registers while the current
-// plane is transformed, so the loads (L2 hits, shared by the CTAs of
-// neighbouring bands and modes) are in flight during the FFT.
+// consecutive modes; the psi plane stays in registers for all of them.  At
+// most 85 registers, so three CTAs share an SM (their shared memory fits
+// too) and hide each other's barriers and window loads.  (Measured: keeping
+// the next window plane in registers as well, two CTAs per SM, was 9 %
+// slower; two planes per CTA with 512 threads, 4 % slower; the y transform
+// with radices <= 5, 12 % slower.)
 template <int NY, int NZ, int NUC>
-__global__ void __launch_bounds__(GS_THREADS, 2) k_gs_plane_ct1(const float2* __restrict__ psi,
+__global__ void __launch_bounds__(GS_THREADS, 3) k_gs_plane_ct1(const float2* __restrict__ psi,
                                                                const float2* __restrict__ win, GsGeom gg, int nu0,
                                                                int nub, const float2* __restrict__ twy,
                                                                const float2* __restrict__ twz,
@@ -638,32 +640,22 @@ __global__ void __launch_bounds__(GS_THREADS, 2) k_gs_plane_ct1(const float2* __
     const size_t xoff = (size_t)x * NPL;
     const float2* pm = psi + (size_t)m * M + xoff;
     const int comp = gg.nmag == 2 ? gg.spin : 0;
-    float2 ps[PER], dvn[PER];
+    float2 ps[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i)
     {
         const int e = threadIdx.x + i * GS_THREADS;
         ps[i] = e < NPL ? pm[e] : make_float2(0.f, 0.f);
     }
-    auto load_dv = [&](int nul) {
+    for (int nul = nl0; nul < nl1; ++nul)
+    {
         const float2* d0 = win + ((size_t)(nu0 + nul) * gg.nmag + comp) * M + xoff;
 #pragma unroll
         for (int i = 0; i < PER; ++i)
         {
             const int e = threadIdx.x + i * GS_THREADS;
-            dvn[i] = e < NPL ? d0[e] : make_float2(0.f, 0.f);
+            if (e < NPL) a[e + e / NZ] = cmul(d0[e], ps[i]);
         }
-    };
-    load_dv(nl0);
-    for (int nul = nl0; nul < nl1; ++nul)
-    {
-#pragma unroll
-        for (int i = 0; i < PER; ++i)
-        {
-            const int e = threadIdx.x + i * GS_THREADS;
-            if (e < NPL) a[e + e / NZ] = cmul(dvn[i], ps[i]);
-        }
-        if (nul + 1 < nl1) load_dv(nul + 1);
         __syncthreads();
         float2* r = ct_fft<float2, float, NZ, 0, 1, true, NY>(a, b, NY, 1, NZP, nullptr, 1, NZP, tz, -1);
         float2* o = r == a ? b : a;
@@ -685,6 +677,7 @@ static int gs_plane_ct(const GsGeom& gg, const void* psi, const void* win, int n
         if (gg.nspinor == 1)
         {
             constexpr int NUC = 4;
+            dim3 g1((unsigned)((nub + NUC - 1) / NUC), (unsigned)gg.nb, (unsigned)gg.Nx);
             static bool attr1 = false;
             if (!attr1)
             {
@@ -693,10 +686,9 @@ static int gs_plane_ct(const GsGeom& gg, const void* psi, const void* win, int n
                     return -1;
                 attr1 = true;
             }
-            dim3 g1((unsigned)((nub + NUC - 1) / NUC), (unsigned)gg.nb, (unsigned)gg.Nx);
-            k_gs_plane_ct1<N, N, NUC><<<g1, GS_THREADS, smem, st>>>((const float2*)psi, (const float2*)win, gg, nu0,
-                                                                    nub, (const float2*)twy, (const float2*)twz,
-                                                                    cols2, ncol, zl, nzl, (float2*)out);
+            k_gs_plane_ct1<N, N, NUC><<<g1, GS_THREADS, smem, st>>>((const float2*)psi, (const float2*)win, gg, nu0, nub,
+                                                                    (const float2*)twy, (const float2*)twz, cols2, ncol,
+                                                                    zl, nzl, (float2*)out);
             return 0;
         }
     }
