@@ -809,7 +809,7 @@ def run_gspace(args):
                        "timing": "CUDA events on the library stream, device-resident inputs and output"},
             "ms_per_pair": ms / npairs, "kernel_ms_per_pair": d, "clocks": clk,
             "gpu_launches": int(p1["kernel_launches"] - p0["kernel_launches"]),
-            "roofline": {"kernel": "k_gs_gemm_f32", "bound": "fp32",
+            "roofline": {"kernel": "k_gs_gemm_f32x2", "bound": "fp32",
                          "achieved": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 if d["gs_gemm_ms"] else None,
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 / fp32_peak if d["gs_gemm_ms"] else None,
