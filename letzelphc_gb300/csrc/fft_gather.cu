@@ -27,7 +27,9 @@
 
 // With a box mask, only the lines of occupied (x, y) columns are read,
 // transformed and written back; the others are all zero and stay so.
-template <typename T2, typename T>
+// CTL > 0: the line length is the compile-time constant CTL (== p.L) and the
+// compile-time Stockham schedule runs (ct_fft); 0: the run-time plan.
+template <typename T2, typename T, int CTL>
 __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long long nlines, FftPlan1D p,
                                                     const T2* __restrict__ tw, int sign, int lpc, BoxMask mk)
 {
@@ -65,7 +67,11 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
             a[i] = g[(size_t)act[j] * p.L + e];
         }
         __syncthreads();
-        T2* r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
+        T2* r;
+        if constexpr (CTL > 0)
+            r = ct_fft<T2, T, CTL, 0, 1, false, 0>(a, b, na, 1, CTL, nullptr, 1, CTL, tws, sign);
+        else
+            r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
         for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
         {
             int e;
@@ -77,7 +83,11 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
     int n = nl * p.L;
     for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = g[i];
     __syncthreads();
-    T2* r = fft_smem<T2, T>(a, b, nl, 1, p.L, p, tws, sign);
+    T2* r;
+    if constexpr (CTL > 0)
+        r = ct_fft<T2, T, CTL, 0, 1, false, 0>(a, b, nl, 1, CTL, nullptr, 1, CTL, tws, sign);
+    else
+        r = fft_smem<T2, T>(a, b, nl, 1, p.L, p, tws, sign);
     for (int i = threadIdx.x; i < n; i += blockDim.x) g[i] = r[i];
 }
 
@@ -86,7 +96,8 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
 // of `ich` inner positions, loaded as an [L][ich] tile (coalesced in inner).
 
 // With a box mask (y pass: outer = (box, x)), empty x planes are skipped.
-template <typename T2, typename T>
+// CTL as in k_fft_contig.
+template <typename T2, typename T, int CTL>
 __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long long nouter, int inner, int ich,
                                                      int nchunk, FftPlan1D p, const T2* __restrict__ tw, int sign,
                                                      BoxMask mk)
@@ -116,7 +127,11 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
         a[l * ic + i] = g[(size_t)l * inner + i];
     }
     __syncthreads();
-    T2* r = fft_smem<T2, T>(a, b, ic, ic, 1, p, tws, sign);
+    T2* r;
+    if constexpr (CTL > 0)
+        r = ct_fft<T2, T, CTL, 0, 1, true, 0>(a, b, ic, ic, 1, nullptr, ic, 1, tws, sign);
+    else
+        r = fft_smem<T2, T>(a, b, ic, ic, 1, p, tws, sign);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
     {
         int i;
@@ -151,7 +166,7 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
     }
 }
 
-template <int BF16>
+template <int BF16, int CTL>
 __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ boxes, int nbox, int k0, int ich,
                                                      int nchunk, FftPlan1D p, const float2* __restrict__ tw,
                                                      int sign, GeomDev gd, const float* __restrict__ band_scale,
@@ -181,7 +196,11 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
         a[l * ic + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : g[(size_t)l * inner + i];
     }
     __syncthreads();
-    float2* r = fft_smem<float2, float>(a, b, ic, ic, 1, p, tws, sign);
+    float2* r;
+    if constexpr (CTL > 0)
+        r = ct_fft<float2, float, CTL, 0, 1, true, 0>(a, b, ic, ic, 1, nullptr, ic, 1, tws, sign);
+    else
+        r = fft_smem<float2, float>(a, b, ic, ic, 1, p, tws, sign);
     // box o -> (kslot, spin, band, spinor)
     int sp = o % gd.nspinor;
     int t = o / gd.nspinor;
@@ -353,9 +372,12 @@ static int ich_for(int L, int inner, int elems)
     return ich;
 }
 
-template <typename T2, typename T>
-static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st,
-                          const BoxMask& mk)
+// Line lengths with a compile-time FFT instance (FP32 passes of the mixed form)
+#define LELPH_CT_SIZES(X) X(24) X(36) X(48) X(60) X(64) X(72) X(96)
+
+template <typename T2, typename T, int CTL>
+static void launch_contig_l(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st,
+                            const BoxMask& mk)
 {
     const int elems = sizeof(T) == 8 ? 2048 : 4096;
     int lpc = elems / p.L;
@@ -364,16 +386,16 @@ static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const 
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaFuncSetAttribute(k_fft_contig<T2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_fft_contig<T2, T, CTL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     long long nb = (nlines + lpc - 1) / lpc;
-    k_fft_contig<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nlines, p, tw, sign, lpc, mk);
+    k_fft_contig<T2, T, CTL><<<(unsigned)nb, 256, smem, st>>>(data, nlines, p, tw, sign, lpc, mk);
 }
 
-template <typename T2, typename T>
-static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1D& p, const T2* tw, int sign,
-                           cudaStream_t st, const BoxMask& mk)
+template <typename T2, typename T, int CTL>
+static void launch_strided_l(T2* data, long long nouter, int inner, const FftPlan1D& p, const T2* tw, int sign,
+                             cudaStream_t st, const BoxMask& mk)
 {
     const int elems = sizeof(T) == 8 ? 2048 : 4096;
     int ich = ich_for(p.L, inner, elems);
@@ -382,11 +404,47 @@ static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaFuncSetAttribute(k_fft_strided<T2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_fft_strided<T2, T, CTL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     long long nb = nouter * nchunk;
-    k_fft_strided<T2, T><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign, mk);
+    k_fft_strided<T2, T, CTL><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign, mk);
+}
+
+template <typename T2, typename T>
+static void launch_contig(T2* data, long long nlines, const FftPlan1D& p, const T2* tw, int sign, cudaStream_t st,
+                          const BoxMask& mk)
+{
+    if constexpr (sizeof(T) == 4)
+    {
+        switch (p.L)
+        {
+#define LELPH_CT_CASE(N) \
+    case N: launch_contig_l<T2, T, N>(data, nlines, p, tw, sign, st, mk); return;
+            LELPH_CT_SIZES(LELPH_CT_CASE)
+#undef LELPH_CT_CASE
+        default: break;
+        }
+    }
+    launch_contig_l<T2, T, 0>(data, nlines, p, tw, sign, st, mk);
+}
+
+template <typename T2, typename T>
+static void launch_strided(T2* data, long long nouter, int inner, const FftPlan1D& p, const T2* tw, int sign,
+                           cudaStream_t st, const BoxMask& mk)
+{
+    if constexpr (sizeof(T) == 4)
+    {
+        switch (p.L)
+        {
+#define LELPH_CT_CASE(N) \
+    case N: launch_strided_l<T2, T, N>(data, nouter, inner, p, tw, sign, st, mk); return;
+            LELPH_CT_SIZES(LELPH_CT_CASE)
+#undef LELPH_CT_CASE
+        default: break;
+        }
+    }
+    launch_strided_l<T2, T, 0>(data, nouter, inner, p, tw, sign, st, mk);
 }
 
 void lelph_launch_fft_contig_d(double2* data, long long nlines, const FftPlan1D& p, const double2* tw, int sign,
@@ -410,6 +468,42 @@ void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const
     launch_strided<float2, float>(data, nouter, inner, p, tw, sign, st, mk);
 }
 
+template <int BF16, int CTL>
+static void launch_x_split_l(unsigned nb, size_t smem, const float2* boxes, int nbox, int k0, int ich, int nchunk,
+                             const FftPlan1D& p, const float2* tw, int sign, const GeomDev& g,
+                             const float* band_scale, uint16_t* Bsplit, float2* psi32, cudaStream_t st,
+                             const BoxMask& mk)
+{
+    static bool attr_set = false;
+    if (!attr_set)
+    {
+        cudaFuncSetAttribute(k_fft_x_split<BF16, CTL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    k_fft_x_split<BF16, CTL><<<nb, 256, smem, st>>>(boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
+                                                    psi32, mk);
+}
+
+template <int BF16>
+static void launch_x_split(unsigned nb, size_t smem, const float2* boxes, int nbox, int k0, int ich, int nchunk,
+                           const FftPlan1D& p, const float2* tw, int sign, const GeomDev& g, const float* band_scale,
+                           uint16_t* Bsplit, float2* psi32, cudaStream_t st, const BoxMask& mk)
+{
+    switch (p.L)
+    {
+#define LELPH_CT_CASE(N)                                                                                         \
+    case N:                                                                                                      \
+        launch_x_split_l<BF16, N>(nb, smem, boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit, psi32, \
+                                  st, mk);                                                                       \
+        return;
+        LELPH_CT_SIZES(LELPH_CT_CASE)
+#undef LELPH_CT_CASE
+    default: break;
+    }
+    launch_x_split_l<BF16, 0>(nb, smem, boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit, psi32, st,
+                              mk);
+}
+
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
                                  float2* psi32, cudaStream_t st, const BoxMask& mk)
@@ -419,20 +513,13 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
     int nchunk = (inner + ich - 1) / ich;
     size_t smem = (size_t)(2 * ich * p.L + p.L) * sizeof(float2);
     long long nbox = (long long)nbox_k * g.nspin * g.nbnds * g.nspinor;
-    static bool attr_set = false;
-    if (!attr_set)
-    {
-        cudaFuncSetAttribute(k_fft_x_split<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(k_fft_x_split<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
     unsigned nb = (unsigned)(nbox * nchunk);
     if (ab_bf16)
-        k_fft_x_split<1><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
-                                                psi32, mk);
+        launch_x_split<1>(nb, smem, boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit, psi32, st,
+                          mk);
     else
-        k_fft_x_split<0><<<nb, 256, smem, st>>>(boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
-                                                psi32, mk);
+        launch_x_split<0>(nb, smem, boxes, (int)nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit, psi32, st,
+                          mk);
 }
 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,

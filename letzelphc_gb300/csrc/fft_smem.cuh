@@ -182,3 +182,146 @@ __device__ T2* fft_smem(T2* a, T2* b, int nlines, int es, int ls, const FftPlan1
     }
     return a;
 }
+
+// ---------------------------------------------- compile-time line length
+// Stockham FFT of lines whose length L is a compile-time constant: the radix
+// schedule and the divisions of the index arithmetic are constants; each
+// pass takes the largest radix up to 16 that divides what is left (two
+// passes for the common grid sizes: 36 = 12 x 3, 48 = 16 x 3, 60 = 15 x 4,
+// ...), composite radices being done in registers as two levels of
+// radix-2/3/4/5 butterflies.
+__host__ __device__ constexpr int ct_radix0(int L)
+{
+    return L % 16 == 0 ? 16 : L % 15 == 0 ? 15 : L % 12 == 0 ? 12 : L % 10 == 0 ? 10 : L % 9 == 0 ? 9
+         : L % 8 == 0 ? 8 : L % 6 == 0 ? 6 : L % 5 == 0 ? 5 : L % 4 == 0 ? 4 : L % 3 == 0 ? 3 : 2;
+}
+__host__ __device__ constexpr int ct_nstage(int L) { return L <= 1 ? 0 : 1 + ct_nstage(L / ct_radix0(L)); }
+__host__ __device__ constexpr int ct_radix_at(int L, int i) { return i == 0 ? ct_radix0(L) : ct_radix_at(L / ct_radix0(L), i - 1); }
+__host__ __device__ constexpr bool ct_smooth(int L) { return L == 1 || ((L % 2 == 0 || L % 3 == 0 || L % 5 == 0) && ct_smooth(L / ct_radix0(L))); }
+// first factor of a composite radix (the second is a radix-2/3/4/5)
+__host__ __device__ constexpr int ct_split(int R) { return R == 16 ? 4 : R == 15 ? 3 : R == 12 ? 4 : R == 10 ? 2 : R == 9 ? 3 : R == 8 ? 4 : R == 6 ? 2 : R; }
+
+template <typename T2, typename T, int R>
+__device__ __forceinline__ void dft_base(T2* v, int sign)
+{
+    if constexpr (R == 2) dft2<T2, T>(v);
+    if constexpr (R == 3) dft3<T2, T>(v, sign);
+    if constexpr (R == 4) dft4<T2, T>(v, sign);
+    if constexpr (R == 5) dft5<T2, T>(v, sign);
+}
+
+// DFT of R = R1 R2 points in registers: R2 DFTs of R1 points over the
+// stride-R2 subsets, twiddles w_R^(n2 k1) (w_R^m = tw[m L / R], tw holding
+// e^{+2 pi i t / L}), then R1 DFTs of R2 points; X[k1 + R1 k2].
+template <typename T2, typename T, int R, int L>
+__device__ __forceinline__ void dft_ct(T2* v, int sign, const T2* __restrict__ tw)
+{
+    constexpr int R1 = ct_split(R);
+    if constexpr (R1 == R)
+        dft_base<T2, T, R>(v, sign);
+    else
+    {
+        constexpr int R2 = R / R1;
+        T2 t[R];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2)
+        {
+            T2 u[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) u[n1] = v[R2 * n1 + n2];
+            dft_base<T2, T, R1>(u, sign);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; ++k1)
+            {
+                T2 x = u[k1];
+                if (n2 * k1 != 0)
+                {
+                    T2 w = tw[n2 * k1 * (L / R)];
+                    if (sign < 0) w.y = -w.y;
+                    x = cmul(x, w);
+                }
+                t[n2 * R1 + k1] = x;
+            }
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1)
+        {
+            T2 w2[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) w2[n2] = t[n2 * R1 + k1];
+            dft_base<T2, T, R2>(w2, sign);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = w2[k2];
+        }
+    }
+}
+
+// One Stockham pass of radix R (stage with NS = product of earlier radices).
+// Element e of source line l sits at src[(loff ? loff[l] : l*ls_s) + e*es_s],
+// of destination line l at dst[l*ls_d + e*es_d].  LINE_FAST: consecutive
+// threads take consecutive lines (lines interleaved in memory), else
+// consecutive elements of a line.
+template <typename T2, typename T, int L, int R, int NS, bool LINE_FAST, int NLC>
+__device__ __forceinline__ void ct_pass(const T2* __restrict__ src, T2* __restrict__ dst, int nlines, int es_s,
+                                        int ls_s, const int* __restrict__ loff, int es_d, int ls_d,
+                                        const T2* __restrict__ tw, int sign)
+{
+    constexpr int LR = L / R;
+    constexpr int TS = L / (NS * R);
+    if (NLC > 0) nlines = NLC;
+    const int nwork = nlines * LR;
+    const RecipDiv dl = recip_div(LINE_FAST && NLC == 0 ? nlines : 1);
+    for (int w = threadIdx.x; w < nwork; w += blockDim.x)
+    {
+        int line, j;
+        if constexpr (LINE_FAST && NLC > 0)
+        {
+            j = w / NLC;
+            line = w - j * NLC;
+        }
+        else if constexpr (LINE_FAST)
+            j = div_rem(w, dl, line);
+        else
+        {
+            line = w / LR;
+            j = w - line * LR;
+        }
+        const int k = j % NS, jq = j / NS;
+        const T2* sp = src + (loff ? loff[line] : line * ls_s);
+        T2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = sp[(j + r * LR) * es_s];
+        if (NS > 1 && k != 0)
+        {
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+            {
+                T2 t = tw[r * k * TS];
+                if (sign < 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        dft_ct<T2, T, R, L>(v, sign, tw);
+        T2* dp = dst + line * ls_d;
+        const int base = jq * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dp[(base + r * NS) * es_d] = v[r];
+    }
+}
+
+// All passes; the first reads the source layout, the rest the destination
+// layout.  Returns the buffer holding the result.
+template <typename T2, typename T, int L, int STAGE, int NS, bool LINE_FAST, int NLC>
+__device__ __forceinline__ T2* ct_fft(T2* a, T2* b, int nlines, int es_s, int ls_s, const int* loff, int es, int ls,
+                                      const T2* tw, int sign)
+{
+    if constexpr (STAGE == ct_nstage(L))
+        return a;
+    else
+    {
+        constexpr int R = ct_radix_at(L, STAGE);
+        ct_pass<T2, T, L, R, NS, LINE_FAST, NLC>(a, b, nlines, es_s, ls_s, loff, es, ls, tw, sign);
+        __syncthreads();
+        return ct_fft<T2, T, L, STAGE + 1, NS * R, LINE_FAST, NLC>(b, a, nlines, es, ls, nullptr, es, ls, tw, sign);
+    }
+}
