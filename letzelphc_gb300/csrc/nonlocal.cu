@@ -645,16 +645,33 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
                 const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
                 T sre = 0, ere = 0, sim = 0, eim = 0;
-                for (int c = 0; c < nchunks; ++c)
+                auto two_sum = [](T& s, T& e, T x) {
+                    const T t = s + x, z = t - s;
+                    e += (s - (t - z)) + (x - z);
+                    s = t;
+                };
+                // four chunks' loads in flight before their (dependent) compensated adds
+                int c = 0;
+                for (; c + 4 <= nchunks; c += 4)
                 {
-                    const T xr = (T)pp[(size_t)c * 128 * NT + n], xi = (T)pp[(size_t)c * 128 * NT + gd.nbp + n];
-                    T t = sre + xr, z = t - sre;
-                    ere += (sre - (t - z)) + (xr - z);
-                    sre = t;
-                    t = sim + xi;
-                    z = t - sim;
-                    eim += (sim - (t - z)) + (xi - z);
-                    sim = t;
+                    T xr[4], xi[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                    {
+                        xr[u] = (T)pp[(size_t)(c + u) * 128 * NT + n];
+                        xi[u] = (T)pp[(size_t)(c + u) * 128 * NT + gd.nbp + n];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                    {
+                        two_sum(sre, ere, xr[u]);
+                        two_sum(sim, eim, xi[u]);
+                    }
+                }
+                for (; c < nchunks; ++c)
+                {
+                    two_sum(sre, ere, (T)pp[(size_t)c * 128 * NT + n]);
+                    two_sum(sim, eim, (T)pp[(size_t)c * 128 * NT + gd.nbp + n]);
                 }
                 const float sc = mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
                                  band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
