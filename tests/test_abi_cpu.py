@@ -44,9 +44,10 @@ def test_descriptor_layout_matches_c():
 #include <stddef.h>
 #include "lelph_gpu.h"
 int main(void){
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(lelph_gpu_desc), offsetof(lelph_gpu_desc, alat_vec),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(lelph_gpu_desc), offsetof(lelph_gpu_desc, alat_vec),
          offsetof(lelph_gpu_desc, npw), offsetof(lelph_gpu_desc, ntype), offsetof(lelph_gpu_desc, precision),
-         sizeof(lelph_gpu_stats), offsetof(lelph_gpu_stats, product_grid));
+         sizeof(lelph_gpu_stats), offsetof(lelph_gpu_stats, product_grid), offsetof(lelph_gpu_desc, route),
+         offsetof(lelph_gpu_stats, route), offsetof(lelph_gpu_stats, gs_plane_ms), offsetof(lelph_gpu_stats, gs_gemm_ms));
   return 0; }
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -56,8 +57,17 @@ int main(void){
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         out = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     D = elph.Desc
+    S = elph.Stats
     assert out == [ctypes.sizeof(D), D.alat_vec.offset, D.npw.offset, D.ntype.offset, D.precision.offset,
-                   ctypes.sizeof(elph.Stats), elph.Stats.product_grid.offset]
+                   ctypes.sizeof(S), S.product_grid.offset, D.route.offset, S.route.offset, S.gs_plane_ms.offset,
+                   S.gs_gemm_ms.offset]
+
+
+def test_route_constants_match_header():
+    import re
+    hdr = open(os.path.join(ROOT, "include", "lelph_gpu.h")).read()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define LELPH_GPU_ROUTE_(\w+) (\d+)", hdr)}
+    assert vals == {"AUTO": elph.ROUTE_AUTO, "REAL": elph.ROUTE_REAL, "GSPACE": elph.ROUTE_GSPACE}
 
 
 def test_strerror_covers_status_codes():
