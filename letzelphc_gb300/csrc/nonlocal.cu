@@ -121,7 +121,8 @@ template <typename T> static constexpr size_t pj_smem_bytes()
 // nsets = nspin*nbnds*nspinor, set = (spin*nbnds + band)*nspinor + spinor.
 // T = float: beta, coefficients and products in FP32, each G chunk summed in
 // FP32 and the chunk sums in FP64; the K vectors, Y_lm and the structure-factor
-// phases e^{-i 2pi K.tau} are evaluated in FP64 in both forms.
+// phases e^{-i 2pi K.tau} are evaluated in FP64 (the mixed form reduces the
+// phase angle to one turn in FP64 and takes sine and cosine in FP32).
 template <typename T>
 __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __restrict__ ks,
                                                      const double* __restrict__ gvec,
@@ -229,9 +230,21 @@ __global__ void __launch_bounds__(256) k_projections(int k0, const KPointSym* __
                 {
                     const double* tau = nl.atom_pos + 3 * (a0 + part);
                     double dot = K0 * tau[0] + K1 * tau[1] + K2 * tau[2];
-                    double sn, cs;
-                    sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
-                    ph_s[part * PG + t] = mk2<C2>(cs, -sn);
+                    if constexpr (std::is_same<T, float>::value)
+                    {
+                        // mixed form: the angle 2 pi_T dot is reduced to one turn in FP64
+                        // (pi_T the reference's truncated pi) and the phase taken in FP32
+                        const double turns = dot * (LELPH_PI_T / 3.14159265358979323846);
+                        float sn, cs;
+                        sincospif(2.0f * (float)(turns - rint(turns)), &sn, &cs);
+                        ph_s[part * PG + t] = mk2<C2>(cs, -sn);
+                    }
+                    else
+                    {
+                        double sn, cs;
+                        sincos(2.0 * LELPH_PI_T * dot, &sn, &cs);
+                        ph_s[part * PG + t] = mk2<C2>(cs, -sn);
+                    }
                 }
             }
         }
