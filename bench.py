@@ -461,6 +461,7 @@ def run_ours(args):
                 "data": "synthetic (seeded; no public dataset)",
                 "config": {"workload": WORKLOAD, "pairs_per_step": npairs, "g_elements_per_step": elems,
                            "precision": args.precision, "parallelism": f"q-sharded x{world}",
+                           "route": {1: "real-space", 2: "G-space"}.get(st1["route"], st1["route"]),
                            "l2": f"inputs larger than L2 ({st1['device_bytes'] / 1e9:.1f} GB resident on the device)"},
                 "e2e": {"value": world * elems / (e2e_step_ms * 1e-3), "unit": "g_elements/s",
                         "ms_per_step": e2e_step_ms, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
