@@ -489,7 +489,7 @@ size_t lelph_gs_xpass_smem(const GsGeom& gg, int fp64)
     return e * (2 * (size_t)gg.Nx * GS_CB + gg.Nx);
 }
 
-// FP32, one spinor component: each CTA takes one (band, x plane) and NUC
+// FP32, one spinor component: each CTA takes one (band, x plane) and NUC (8)
 // consecutive modes; the psi plane stays in registers for all of them.  At
 // most 85 registers, so three CTAs share an SM (their shared memory fits
 // too) and hide each other's barriers and window loads.  (Measured: keeping
@@ -560,7 +560,7 @@ static int gs_plane_ct(const GsGeom& gg, const void* psi, const void* win, int n
     {
         if (gg.nspinor == 1)
         {
-            constexpr int NUC = 4;
+            constexpr int NUC = 8;
             dim3 g1((unsigned)((nub + NUC - 1) / NUC), (unsigned)gg.nb, (unsigned)gg.Nx);
             static bool attr1 = false;
             if (!attr1)
