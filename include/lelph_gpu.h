@@ -50,7 +50,9 @@ extern "C" {
  *       forward FFT of dV psi_k per (mode, band), pruned to the k+q sphere,
  *       then a GEMM over the sphere; psi(r) is built per k when it is needed.
  * AUTO: REAL unless its resident operands exceed half of the device memory or
- *       the mixed form's tensor-core tile cannot hold the bands. */
+ *       the mixed form's tensor-core tile cannot hold the bands; when both fit,
+ *       the mixed form takes the route a cost model per pair (rates measured on
+ *       GB300) finds cheaper. */
 #define LELPH_GPU_ROUTE_AUTO 0
 #define LELPH_GPU_ROUTE_REAL 1
 #define LELPH_GPU_ROUTE_GSPACE 2

@@ -1076,6 +1076,24 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         if (cudaSetDevice(d.device) == cudaSuccess && cudaMemGetInfo(&fr, &tot) == cudaSuccess &&
             resident > 0.5 * (double)tot)
             h->gspace = true;
+        // Mixed form, both routes fit: the cheaper per pair by a cost model with
+        // rates measured on GB300 (one pair and spin; rows = modes x bands x
+        // spinors): real-space, the split sandwich, 12 rows (2 nbp) M tensor flops
+        // at 7.6e14/s; G-space, the pruned plane and x passes at 3.6e-12 s per grid
+        // point of a row plus the GEMM over the sphere, 8 rows nb npw flops at
+        // 4.7e13/s.  (The plain form stays on the real-space route when it fits:
+        // it is the validation form, and the allocation-free entry point runs
+        // only that route; LELPH_GPU_ROUTE_GSPACE selects the other.)
+        if (!h->gspace && h->mixed)
+        {
+            double npw_avg = 0;
+            for (int ik = 0; ik < d.nkpts_iBZ; ++ik) npw_avg += h->npw[ik];
+            npw_avg /= d.nkpts_iBZ;
+            const double rows = (double)d.nmodes * d.nbnds * d.nspinor;
+            const double t_real = 12.0 * rows * (2.0 * h->g.nbp) * (double)N / 7.6e14;
+            const double t_gs = rows * (double)N * 3.6e-12 + 8.0 * rows * d.nbnds * npw_avg / 4.7e13;
+            if (t_gs < t_real) h->gspace = true;
+        }
     }
     if (h->gspace)
     {
