@@ -1,6 +1,6 @@
 // G-space route of the local sandwich: the reference's own order of work
 // (elphLocal, src/dvloc/compute_Vbare_loc.c:264-310, with fft_convolution3D,
-// src/fft/convolution.c:13-...): for each mode nu and band m of k,
+// src/fft/convolution.c:13-189): for each mode nu and band m of k,
 //   F_{nu m s}(G) = sum_r e^{-i G.r} P_{nu m s}(r),
 //   P_{nu m s} = dV_nu psi_{k m}  (nmag 1/2)  or  sum_s' dV_nu[s s'] psi_{k m s'}  (nmag 4),
 // then one GEMM over the k+q sphere,
@@ -8,16 +8,19 @@
 // Everything runs on the product grid with the pair's dV window (as in the
 // real-space route), so F is needed only on the k+q sphere, and the forward
 // transform is pruned accordingly:
-// * k_gs_plane: one (x plane, band, mode) per CTA: the product plane is formed
-//   on load, transformed along z then y in shared memory, and only the (y, z)
-//   columns that hold a plane wave of the k+q sphere are written out;
-// * k_gs_xpass: the x transform of those columns, whose epilogue writes the
-//   sphere's values in the sphere's sorted order (column, x) -- the K order of
-//   the GEMM; the k+q coefficients are stored permuted to the same order;
-// * k_gs_gemm: SIMT complex GEMM over one K chunk (FP32 in the mixed form,
-//   FP64 in the plain form); chunk partials are summed in FP64 by k_gs_reduce,
-//   which also applies 1/M and writes the FP64 local term the finish kernel
-//   consumes.
+// * plane pass (k_gs_plane; k_gs_plane_ct / k_gs_plane_ct1 for square planes
+//   of the common sizes): the product plane dV psi_k of one x is formed on
+//   load, transformed along z then y in shared memory (y only on the z lines
+//   the sphere reaches), and only the (y, z) columns that hold a plane wave
+//   of the k+q sphere are written out;
+// * x pass (k_gs_xpass; k_gs_xpass_ct): the x transform of those columns,
+//   whose epilogue writes the sphere's values in the sphere's sorted order
+//   (column, x) -- the K order of the GEMM; the k+q coefficients are stored
+//   permuted to the same order (k_gs_bperm);
+// * GEMM (k_gs_gemm_f32x2 in the mixed form, k_gs_gemm in FP64): complex
+//   product over one K chunk; chunk partials are summed in FP64 by
+//   k_gs_reduce, which also applies 1/M and writes the FP64 local term the
+//   finish kernel consumes.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
