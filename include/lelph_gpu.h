@@ -165,8 +165,10 @@ int lelph_gpu_run_device(lelph_gpu* h, int n, const int* qslot, const int* kbz, 
  * lelph_gpu_run.  Items are processed in batches that fit the array; a size
  * whose single (k, q) pair needs more than the array returns
  * LELPH_GPU_ERR_UNSUPPORTED.  The first call on a device looks the array up
- * (cudaGetSymbolAddress) with that device current, so that first call should
- * come before any stream capture.  All calls share the one array and every
+ * (cudaGetSymbolAddress) with that device current, and so does the first call
+ * after the device's context was destroyed and re-created (cudaDeviceReset
+ * reloads the array elsewhere); such a first call should come before any
+ * stream capture.  All calls share the one array and every
  * call overwrites what it uses, so calls that overlap on the GPU (several
  * contexts or threads at once on one device) race and must be serialised by
  * the caller. */
@@ -268,7 +270,24 @@ int lelph_gpu_compute_elphq_star(lelph_gpu* h, const double qpt_crys[3], const d
  * rotateGvecs + Sort_pw (src/wfc/rotate_Gvecs.c:15-81, src/wfc/sortpw.c:95-315). */
 int lelph_gpu_debug_gvec_map(lelph_gpu* h, int kbz, const int ulm[3], int* out);
 
+/* Layout check of the partial sums of the mixed form's real-space sandwich
+ * (host arithmetic only, no device work; the output size nmodes * nspin *
+ * nb^2 per pair of elphLocal, src/dvloc/compute_Vbare_loc.c:286-341, is
+ * assembled from them): for nmodes, nbnds (<= 64), nspin and nchunks K chunks
+ * per pair, out[0] = floats the library allocates for npairs pairs, out[1] =
+ * one past the highest float the tensor-core sandwich writes, out[2] = one
+ * past the highest float the finish kernel reads. */
+int lelph_gpu_debug_partials_extent(int nmodes, int nbnds, int nspin, int nchunks, int npairs,
+                                    unsigned long long out[3]);
+
 int lelph_gpu_set_profiling(lelph_gpu* h, int on);
+/* Limit, in nanoseconds, of every wait between the roles of the tensor-core
+ * sandwich's pipeline (0: the default, 1.5 s).  A wait that runs out makes the
+ * kernel stop, let its copies and MMAs in flight finish, release its tensor
+ * memory and report LELPH_GPU_ERR_TIMEOUT; the context stays usable.  (No
+ * counterpart in the reference, which has no device waits; a short limit lets
+ * a test exercise that path.) */
+int lelph_gpu_set_wait_limit(lelph_gpu* h, unsigned long long ns);
 int lelph_gpu_stats_get(lelph_gpu* h, lelph_gpu_stats* s);
 /* the CUDA stream (cudaStream_t) every kernel of the context runs on */
 void* lelph_gpu_stream(lelph_gpu* h);

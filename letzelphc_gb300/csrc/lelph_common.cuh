@@ -95,14 +95,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 
 // Bounded wait: returns false (and leaves the barrier alone) when the phase
 // did not complete within LELPH_WAIT_LIMIT_NS.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  unsigned long long limit_ns = LELPH_WAIT_LIMIT_NS)
 {
     if (mbar_try_wait(bar, parity)) return true;
     unsigned long long t0 = gtimer_ns();
     while (true)
     {
         if (mbar_try_wait(bar, parity)) return true;
-        if (gtimer_ns() - t0 > LELPH_WAIT_LIMIT_NS) return false;
+        if (gtimer_ns() - t0 > limit_ns) return false;
     }
 }
 

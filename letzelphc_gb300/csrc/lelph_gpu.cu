@@ -59,6 +59,7 @@ struct lelph_gpu
     int nltimesj = 0, ntype = 0;
     int nproj_max = 0;
     int ab_bf16 = 0;
+    unsigned long long wait_ns = 0;  // limit of each pipeline wait of the tensor-core sandwich (0: default)
     bool mixed = false;
     bool prepared = false;
     bool gspace = false;  // G-space route of the local sandwich
@@ -600,6 +601,13 @@ extern "C" int lelph_gpu_set_profiling(lelph_gpu* h, int on)
     return LELPH_GPU_OK;
 }
 
+extern "C" int lelph_gpu_set_wait_limit(lelph_gpu* h, unsigned long long ns)
+{
+    if (!h) return LELPH_GPU_ERR_INVALID;
+    h->wait_ns = ns;
+    return LELPH_GPU_OK;
+}
+
 extern "C" int lelph_gpu_stats_get(lelph_gpu* h, lelph_gpu_stats* s)
 {
     if (!h || !s) return LELPH_GPU_ERR_INVALID;
@@ -858,7 +866,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     h->g.nbp = (d.nbnds + 7) / 8 * 8;
     h->g.nmag = d.nmag;
     h->g.nmodes = d.nmodes;
-    h->g.mt_modes = std::min(d.nmodes, std::max(1, 128 / d.nbnds));
+    h->g.mt_modes = lelph_tc_tile_modes(d.nmodes, d.nbnds);
     // 64-point pipeline stages when three stages and two A slots fit, else 32
     h->g.kpts = 64;
     if (!lelph_local_tc_supported(h->g)) h->g.kpts = 32;
@@ -2163,7 +2171,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     size_t per_pair;
     const bool fp64_local = !h->mixed || h->gspace;  // the local term arrives as FP64 sums (glocal)
     if (fp64_local) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
-    else per_pair = sizeof(float) * (size_t)d.nspin * ((nrows + 127) / 128) * h->nchunks * 128 * 2 * g.nbp;
+    else per_pair = sizeof(float) * lelph_tc_partials_per_pair(g, h->nchunks);
     int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, (4ull << 30) / per_pair));
     rc = ensure(h, fp64_local ? h->d_glocal : h->d_partials, per_pair * batch);
     if (rc) return rc;
@@ -2182,7 +2190,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
                                     (double2*)h->d_glocal.p, (unsigned*)h->d_status.p, h->st);
         else
             lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapP, &h->tmapV, g, h->ab_bf16, h->chunk_pts, h->nchunks,
-                                  (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st);
+                                  (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st, h->wait_ns);
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
         tstart(h);
@@ -2696,6 +2704,34 @@ extern "C" int lelph_gpu_debug_gvec_map(lelph_gpu* h, int kbz, const int ulm[3],
     return LELPH_GPU_OK;
 }
 
+extern "C" int lelph_gpu_debug_partials_extent(int nmodes, int nbnds, int nspin, int nchunks, int npairs,
+                                               unsigned long long out[3])
+{
+    if (!out || nmodes < 1 || nbnds < 1 || nbnds > 64 || nspin < 1 || nchunks < 1 || npairs < 1)
+        return LELPH_GPU_ERR_INVALID;
+    GeomDev g{};
+    g.nmodes = nmodes;
+    g.nbnds = nbnds;
+    g.nbp = (nbnds + 7) / 8 * 8;
+    g.nspin = nspin;
+    g.mt_modes = lelph_tc_tile_modes(nmodes, nbnds);
+    const long long zlast = (long long)npairs * nspin - 1;
+    // the sandwich writes 128 rows x 2 nbp columns of every (pair, spin, mode tile, K chunk)
+    const size_t wr = lelph_tc_partial_offset(g, nchunks, zlast, lelph_tc_mode_tiles(g) - 1, nchunks - 1, 127) +
+                      2 * (size_t)g.nbp;
+    // the finish reads row (nu - mt mt_modes) nb + m of tile mt = nu / mt_modes, columns n and nbp + n
+    size_t rd = 0;
+    for (int nu = 0; nu < nmodes; ++nu)
+    {
+        const int mt = nu / g.mt_modes, rr = (nu - mt * g.mt_modes) * nbnds + (nbnds - 1);
+        rd = std::max(rd, lelph_tc_partial_offset(g, nchunks, zlast, mt, nchunks - 1, rr) + g.nbp + nbnds);
+    }
+    out[0] = lelph_tc_partials_per_pair(g, nchunks) * (size_t)npairs;
+    out[1] = wr;
+    out[2] = rd;
+    return LELPH_GPU_OK;
+}
+
 // ============================================ allocation-free variant of run
 
 // Callers that cannot allocate device memory once set-up is over -- a host
@@ -2713,23 +2749,61 @@ static __device__ __align__(256) unsigned char lelph_noalloc_scratch[LELPH_NOALL
 namespace
 {
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[256] = {};
+struct NoallocAddr
+{
+    unsigned long long ctx_id;  // unique id of the context the address belongs to (0: none yet)
+    void* p;
+};
+NoallocAddr g_noalloc_addr[256] = {};
 
-// Device address of the scratch array on h->device, looked up once per device
-// with that device current (the first call on a device does this set-up).
+// Unique id of the calling thread's current context (cuCtxGetId, reached
+// through the runtime's driver entry points); 0 if the driver cannot say.
+unsigned long long current_ctx_id()
+{
+    using PFN_cur = CUresult (*)(CUcontext*);
+    using PFN_id = CUresult (*)(CUcontext, unsigned long long*);
+    static PFN_cur cur = nullptr;
+    static PFN_id cid = nullptr;
+    static bool looked = false;
+    if (!looked)
+    {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            cur = reinterpret_cast<PFN_cur>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            cid = reinterpret_cast<PFN_id>(p);
+        looked = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!cur || !cid || cur(&c) != CUDA_SUCCESS || !c || cid(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on h->device (current when this runs),
+// looked up once per device and context: the first call on a device does this
+// set-up, and so does the first call after the device's context was destroyed
+// and re-created (cudaDeviceReset), when the module and its array are loaded
+// anew at another address.
 int noalloc_scratch(lelph_gpu* h, unsigned char** out)
 {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     if (h->device < 0 || h->device >= 256) return fail(h, LELPH_GPU_ERR_INVALID, "device ordinal");
-    if (!g_noalloc_addr[h->device])
+    NoallocAddr& a = g_noalloc_addr[h->device];
+    const unsigned long long id = current_ctx_id();
+    if (!a.p || id == 0 || id != a.ctx_id)
     {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, lelph_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return fail(h, LELPH_GPU_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_noalloc_addr[h->device] = p;
+        a.p = p;
+        a.ctx_id = id;
     }
-    *out = static_cast<unsigned char*>(g_noalloc_addr[h->device]);
+    *out = static_cast<unsigned char*>(a.p);
     return LELPH_GPU_OK;
 }
 
@@ -2775,10 +2849,9 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
     const lelph_gpu_desc& d = h->d;
     const GeomDev& g = h->g;
     const int nrows = d.nmodes * d.nbnds;
-    const int mtiles = (d.nmodes + g.mt_modes - 1) / g.mt_modes;
     size_t per_pair;
     if (!h->mixed) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
-    else per_pair = sizeof(float) * (size_t)d.nspin * mtiles * h->nchunks * 128 * 2 * g.nbp;
+    else per_pair = sizeof(float) * lelph_tc_partials_per_pair(g, h->nchunks);
     const size_t room = LELPH_NOALLOC_BYTES - LELPH_NOALLOC_PAIR_BYTES;
     if (per_pair > room)
         return fail(h, LELPH_GPU_ERR_UNSUPPORTED,
@@ -2822,7 +2895,7 @@ extern "C" int lelph_gpu_run_device_noalloc(lelph_gpu* h, int n, const int* qslo
                                     (double2*)work, (unsigned*)h->d_status.p, h->st);
         else
             lelph_launch_local_tc(dpairs, nb, &h->tmapB, &h->tmapP, &h->tmapV, g, h->ab_bf16, h->chunk_pts,
-                                  h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st);
+                                  h->nchunks, (float*)work, (unsigned*)h->d_status.p, h->st, h->wait_ns);
         lelph_launch_finish(dpairs, nb, h->mixed ? 0 : 1, (const double2*)work, (const float*)work, h->nchunks,
                             (const float*)h->d_winscale.p, (const float*)h->d_band_scale.p,
                             (const double2*)h->d_proj.p, (const double2*)h->d_eig.p, non_loc, nl, g,

@@ -48,6 +48,31 @@ struct GeomDev
     int kpts;      // grid points per pipeline stage of the tensor-core sandwich (64, or 32 for wide tiles)
 };
 
+// Partial sums of the tensor-core sandwich, laid out
+// [pair * nspin + spin][mode tile][K chunk][128 rows][2 nbp] (FP32).  A mode
+// tile holds mt_modes whole modes, so there are ceil(nmodes / mt_modes) tiles
+// per (pair, spin) -- more than ceil(nmodes * nbnds / 128) whenever 128 is not
+// a multiple of nbnds.  The kernel that writes the partials, the finish that
+// reads them and every allocation of them use these helpers.
+inline int lelph_tc_tile_modes(int nmodes, int nbnds)  // mt_modes; a tile row is one (mode, band of k)
+{
+    const int m = 128 / nbnds > 1 ? 128 / nbnds : 1;
+    return nmodes < m ? nmodes : m;
+}
+__host__ __device__ inline int lelph_tc_mode_tiles(const GeomDev& g)
+{
+    return (g.nmodes + g.mt_modes - 1) / g.mt_modes;
+}
+__host__ __device__ inline size_t lelph_tc_partial_offset(const GeomDev& g, int nchunks, long long zp, int mt,
+                                                          int chunk, int row)
+{
+    return ((((size_t)zp * lelph_tc_mode_tiles(g) + mt) * nchunks + chunk) * 128 + row) * (size_t)(2 * g.nbp);
+}
+inline size_t lelph_tc_partials_per_pair(const GeomDev& g, int nchunks)
+{
+    return (size_t)g.nspin * lelph_tc_mode_tiles(g) * nchunks * 128 * (size_t)(2 * g.nbp);
+}
+
 // Occupancy of the boxes of a chunk of k-points after the sphere -> box
 // scatter: col[(kslot*Nx + x)*Ny + y] != 0 when the z-column (x, y) holds a
 // plane wave of k, xpl[kslot*Nx + x] != 0 when the plane x does.  Every band
@@ -117,7 +142,8 @@ int lelph_local_tc_tile_modes(const GeomDev& g);
 int lelph_local_tc_supported(const GeomDev& g);
 void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapP,
                            const void* tmapV, const GeomDev& g, int ab_bf16, int chunk_pts, int nchunks,
-                           float* partials, unsigned* status, cudaStream_t st);
+                           float* partials, unsigned* status, cudaStream_t st,
+                           unsigned long long wait_ns = 0);  // limit of each pipeline wait (0: the default)
 
 // nonlocal + finish (nonlocal.cu)
 struct NonlocalDesc

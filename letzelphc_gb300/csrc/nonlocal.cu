@@ -451,7 +451,6 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
     }
     const double invN = 1.0 / ((double)gd.Nx * gd.Ny * gd.Nz);
     const int nrows = gd.nmodes * nb;
-    const int mtiles = (gd.nmodes + gd.mt_modes - 1) / gd.mt_modes;
     const int NT = 2 * gd.nbp;
     // pre-factor -2 pi i e2 (src/nonloc/Vbare_nloc.c:547)
     const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
@@ -471,7 +470,7 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
         else
         {
             int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
-            const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
+            const float* pp = partials + lelph_tc_partial_offset(gd, nchunks, zp, mt, 0, rr);
             double re = 0.0, im = 0.0;
             for (int c = 0; c < nchunks; ++c)
             {
@@ -569,7 +568,6 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
         __syncthreads();
     }
     const double invN = 1.0 / ((double)gd.Nx * gd.Ny * gd.Nz);
-    const int mtiles = (gd.nmodes + gd.mt_modes - 1) / gd.mt_modes;
     const int NT = 2 * gd.nbp;
     const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
     const C2 preT = mk2<C2>(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
@@ -656,7 +654,7 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 // term in FP64: a few FP64 operations per element instead of one
                 // FP64 addition per chunk
                 const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
-                const float* pp = partials + (((size_t)zp * mtiles + mt) * nchunks * 128 + rr) * NT;
+                const float* pp = partials + lelph_tc_partial_offset(gd, nchunks, zp, mt, 0, rr);
                 T sre = 0, ere = 0, sim = 0, eim = 0;
                 auto two_sum = [](T& s, T& e, T x) {
                     const T t = s + x, z = t - s;

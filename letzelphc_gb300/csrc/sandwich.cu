@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
                int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
-               unsigned* __restrict__ status)
+               unsigned* __restrict__ status, unsigned long long wait_ns)
 {
     extern __shared__ __align__(1024) uint8_t smraw[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 const long long r00 = kc0 - (long long)sp * N;
                 for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u)
                 {
-                    if (!mbar_wait_bounded(&empty[s], ph ^ 1u))
+                    if (!mbar_wait_bounded(&empty[s], ph ^ 1u, wait_ns))
                     {
                         *abort_flag = 1;
                         atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
@@ -458,6 +458,8 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             int s = 0, a = 0, b = 0;
             uint32_t pha = 0, phb = 0;
             bool stop = false;
+            uint64_t* last_commit = nullptr;  // the A-slot barrier of the latest commit, and its phase parity
+            uint32_t last_par = 0;
             for (int u = blockIdx.x; u < nunits && !stop; u += gridDim.x)
             {
                 for (int it = 0; it < nstage; ++it)
@@ -468,8 +470,8 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     // per stage: the producers arrive on aready[a] only after they saw the
                     // stage's TMA tiles land (full[s]), which orders B for the MMAs too
                     bool ok = true;
-                    if (first) ok = mbar_wait_bounded(&acce[b], phb ^ 1u);
-                    ok = ok && mbar_wait_bounded(&aready[a], pha);
+                    if (first) ok = mbar_wait_bounded(&acce[b], phb ^ 1u, wait_ns);
+                    ok = ok && mbar_wait_bounded(&aready[a], pha, wait_ns);
                     if (!ok)
                     {
                         *abort_flag = 1;
@@ -503,6 +505,8 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     }
                     umma_commit(&empty[s]);
                     umma_commit(&afree[a]);
+                    last_commit = &afree[a];
+                    last_par = pha;
                     if (last) umma_commit(&accf[b]);
                     s = (s + 1 == NST) ? 0 : s + 1;
                     if (++a == NA)
@@ -517,6 +521,9 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                     }
                 }
             }
+            // every MMA this thread issued completes before the tensor memory is
+            // released, also when a wait above gave up (the commit tracks them all)
+            if (last_commit) mbar_wait_bounded(last_commit, last_par);
         }
     }
     else if (warp < 10)
@@ -555,7 +562,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             for (int it = 0; it < nstage; ++it, s = (s + 1 == NST) ? 0 : s + 1, ph ^= (s == 0) ? 1u : 0u,
                      a = (a + 1 == NA) ? 0 : a + 1, pha ^= (a == 0) ? 1u : 0u)
             {
-                bool ok = mbar_wait_bounded(&afree[a], pha ^ 1u) && mbar_wait_bounded(&full[s], ph);
+                bool ok = mbar_wait_bounded(&afree[a], pha ^ 1u, wait_ns) && mbar_wait_bounded(&full[s], ph, wait_ns);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok && lane == 0)
                 {
@@ -626,7 +633,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             for (int i = 0; i < 64; ++i) acc[i] = 0.f;
             for (int grp = 0; grp < ngroup; ++grp, b = (b + 1 == NACC) ? 0 : b + 1, phb ^= (b == 0) ? 1u : 0u)
             {
-                bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], phb);
+                bool ok = (*abort_flag == 0) && mbar_wait_bounded(&accf[b], phb, wait_ns);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok)
                 {
@@ -664,7 +671,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             if (stop) break;
             const TcUnit w = tc_unit(u, nchunks, mtiles, gd.nspin, pairs);
             const int row = q * 32 + lane;
-            float* out = partials + ((((size_t)w.zp * mtiles + w.mt) * nchunks + w.chunk) * 128 + row) * NT + c0;
+            float* out = partials + lelph_tc_partial_offset(gd, nchunks, w.zp, w.mt, w.chunk, row) + c0;
 #pragma unroll
             for (int c = 0; c < 64; c += 4)
                 if (c < nc) *reinterpret_cast<float4*>(out + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
@@ -681,9 +688,10 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
 
 void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB, const void* tmapP,
                            const void* tmapV, const GeomDev& g, int ab_bf16, int chunk_pts, int nchunks,
-                           float* partials, unsigned* status, cudaStream_t st)
+                           float* partials, unsigned* status, cudaStream_t st, unsigned long long wait_ns)
 {
-    const int mtiles = (g.nmodes + g.mt_modes - 1) / g.mt_modes;
+    if (wait_ns == 0) wait_ns = LELPH_WAIT_LIMIT_NS;
+    const int mtiles = lelph_tc_mode_tiles(g);
     const long long units = (long long)npairs * g.nspin * mtiles * nchunks;
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
@@ -700,7 +708,7 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     {                                                                                                            \
         cudaFuncSetAttribute(k_local_tc<BF, KPV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
         k_local_tc<BF, KPV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles,     \
-                                                         (int)units, partials, status);                          \
+                                                         (int)units, partials, status, wait_ns);                 \
     } while (0)
     if (ab_bf16)
     {

@@ -63,6 +63,7 @@ EXPORTS = [
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
     "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
     "lelph_gpu_dmats", "lelph_gpu_compute_elphq_star", "lelph_gpu_set_q_dvscf_qe",
+    "lelph_gpu_debug_partials_extent", "lelph_gpu_set_wait_limit",
 ]
 
 _lib = None
@@ -87,6 +88,8 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_set_q_induced.argtypes = [vp, C.c_int, _dp, _dp, _dp]
     L.lelph_gpu_rotate_dvscf.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp]
     L.lelph_gpu_dmats.argtypes = [vp, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_longlong, _dp]
+    L.lelph_gpu_debug_partials_extent.argtypes = [C.c_int] * 5 + [C.POINTER(C.c_ulonglong)]
+    L.lelph_gpu_set_wait_limit.argtypes = [vp, C.c_ulonglong]
     L.lelph_gpu_set_q_dvscf_qe.argtypes = [vp, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp]
     L.lelph_gpu_compute_elphq_star.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int,
                                                _ip, C.c_int, vp]
@@ -365,6 +368,10 @@ class LelphGPU:
 
     def set_profiling(self, on=True):
         self._check(self._L.lelph_gpu_set_profiling(self.h, int(on)))
+
+    def set_wait_limit(self, ns=0):
+        """Limit of every pipeline wait of the tensor-core sandwich (0: default)."""
+        self._check(self._L.lelph_gpu_set_wait_limit(self.h, int(ns)))
 
     def stats(self):
         st = Stats()

@@ -8,6 +8,10 @@
  * star.  The netCDF writes of elph_mat are captured in memory and written out
  * as complex128 (nq, nk_BZ, nmodes, nspin, nb, nb).
  *
+ * Timing samples: LELPH_REF_KPOOLS=P splits the full-BZ k-points into the
+ * reference's P k pools and LELPH_REF_KPOOL=i makes this process pool i (pool
+ * 0 by default); LELPH_REF_QPT=i runs only the i-th q of the file.
+ *
  * usage: lelph_ref <system.bin> <g_out.bin> [rotate <D_in.bin> <g_rot_out.bin>]
  *        lelph_ref <system.bin> <g_out.bin> dvloc <v_out.bin>
  *        lelph_ref <system.bin> <unused> rotdv <spec.bin> <dv_out.bin>
@@ -42,6 +46,11 @@
  * layout: (patterns, nmag, Nz, Ny, Nx) complex128) with the spec's eig and
  * pats records; dv_out.bin is the dV in the mode basis (nmodes, nmag, Nx, Ny, Nz).
  *
+ * Built with -DCOMPILE_ELPH_DOUBLE (the parity build) every input is used as
+ * written; built without it (the reference's default single-precision build,
+ * src/elphC.h:21-31) every real and complex input is rounded once to float on
+ * load, and g is widened back to complex128 on output.
+ *
  * TEST INFRASTRUCTURE ONLY (the compiled reference is the checker's checker). */
 #include <complex.h>
 #include <math.h>
@@ -50,6 +59,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "common/ELPH_timers.h"
 #include "common/dtypes.h"
@@ -99,6 +109,19 @@ static void load(const char* path)
         r.nbytes = n * es;
         r.data = malloc(r.nbytes ? r.nbytes : 1);
         if (fread(r.data, 1, r.nbytes, f) != r.nbytes) die("truncated data");
+        if (sizeof(ELPH_float) == 4 && r.code != 1)
+        {
+            /* the reference's default build reads every real and complex
+             * input in single precision: round each value once */
+            const size_t nv = r.code == 0 ? n : 2 * n;
+            const double* src = r.data;
+            float* dst = malloc(nv * sizeof(float) + 1);
+            if (!dst) die("out of memory");
+            for (size_t i = 0; i < nv; ++i) dst[i] = (float)src[i];
+            free(r.data);
+            r.data = dst;
+            r.nbytes = nv * sizeof(float);
+        }
         if (nrec >= 4096) die("too many records");
         recs[nrec++] = r;
     }
@@ -118,17 +141,17 @@ static struct rec* get(const char* name, int required)
 }
 
 /* elph_mat slices land here: (nq, nk, nmodes, nspin, nb, nb) */
-static double _Complex* g_all = NULL;
+static ELPH_cmplx* g_all = NULL;
 static size_t g_slice = 0;
 static size_t g_nk = 0;
 /* Dmats served to nc_get_vara: (nsym, nk, nspin, nb, nb) */
-static double _Complex* dmats = NULL;
+static ELPH_cmplx* dmats = NULL;
 static size_t dmat_slice = 0, dmat_nk = 0;
 
 int nc_put_vara(int ncid, int varid, const size_t* startp, const size_t* countp, const void* op)
 {
     (void)ncid; (void)varid; (void)countp;
-    memcpy(g_all + (startp[0] * g_nk + startp[1]) * g_slice, op, sizeof(double _Complex) * g_slice);
+    memcpy(g_all + (startp[0] * g_nk + startp[1]) * g_slice, op, sizeof(ELPH_cmplx) * g_slice);
     return 0;
 }
 
@@ -136,7 +159,7 @@ int nc_get_vara(int ncid, int varid, const size_t* startp, const size_t* countp,
 {
     (void)ncid; (void)varid; (void)countp;
     if (!dmats) return 1;
-    memcpy(ip, dmats + (startp[0] * dmat_nk + startp[1]) * dmat_slice, sizeof(double _Complex) * dmat_slice);
+    memcpy(ip, dmats + (startp[0] * dmat_nk + startp[1]) * dmat_slice, sizeof(ELPH_cmplx) * dmat_slice);
     return 0;
 }
 
@@ -179,14 +202,14 @@ int main(int argc, char** argv)
     lat.fft_dims[2] = Nz;
     lat.nfftz_loc = Nz;
     lat.nfftz_loc_shift = 0;
-    memcpy(lat.alat_vec, get("alat", 1)->data, 9 * sizeof(double));
-    memcpy(lat.blat_vec, get("blat", 1)->data, 9 * sizeof(double));
+    memcpy(lat.alat_vec, get("alat", 1)->data, 9 * sizeof(ELPH_float));
+    memcpy(lat.blat_vec, get("blat", 1)->data, 9 * sizeof(ELPH_float));
     lat.volume = 0;
     lat.atomic_pos = get("atom_pos", 1)->data;
     lat.atom_type = get("atom_type", 1)->data;
     lat.kpt_iredBZ = get("kibz", 1)->data;
     lat.kpt_fullBZ_crys = get("kbz_crys", 1)->data;
-    lat.kpt_fullBZ = malloc(sizeof(double) * 3 * (size_t)nkbz);
+    lat.kpt_fullBZ = malloc(sizeof(ELPH_float) * 3 * (size_t)nkbz);
     for (int i = 0; i < nkbz; ++i)
         for (int x = 0; x < 3; ++x)
         {
@@ -197,13 +220,13 @@ int main(int argc, char** argv)
     lat.kmap = get("kmap", 1)->data;
     lat.is_soc_present = soc != 0;
     lat.syms = malloc(sizeof(struct symmetry) * (size_t)nsym);
-    const double* R = get("sym_R", 1)->data;
-    const double* T = get("sym_tau", 1)->data;
+    const ELPH_float* R = get("sym_R", 1)->data;
+    const ELPH_float* T = get("sym_tau", 1)->data;
     const int* TR = get("sym_trev", 1)->data;
     for (int i = 0; i < nsym; ++i)
     {
-        memcpy(lat.syms[i].Rmat, R + 9 * i, 9 * sizeof(double));
-        memcpy(lat.syms[i].tau, T + 3 * i, 3 * sizeof(double));
+        memcpy(lat.syms[i].Rmat, R + 9 * i, 9 * sizeof(ELPH_float));
+        memcpy(lat.syms[i].tau, T + 3 * i, 3 * sizeof(ELPH_float));
         lat.syms[i].time_rev = TR[i] != 0;
     }
 
@@ -237,7 +260,7 @@ int main(int argc, char** argv)
     ps.fCoeff = NULL;
     if (soc && nspinor == 2)
     {
-        ps.fCoeff = calloc((size_t)(nltimesj * ntype), sizeof(double _Complex*));
+        ps.fCoeff = calloc((size_t)(nltimesj * ntype), sizeof(ELPH_cmplx*));
         for (int i = 0; i < nltimesj * ntype; ++i)
         {
             char nm[32];
@@ -274,8 +297,15 @@ int main(int argc, char** argv)
      * first nk_BZ/n k-points of each q are computed (a timing sample) */
     if (getenv("LELPH_REF_KPOOLS")) comm.nkpools = atoi(getenv("LELPH_REF_KPOOLS"));
     if (comm.nkpools < 1) comm.nkpools = 1;
+    /* LELPH_REF_KPOOL=i: this process is pool i instead (the pool index is
+     * commQ_rank / commK_size, compute_elph_matq.c:52-54) */
+    if (getenv("LELPH_REF_KPOOL")) comm.commQ_rank = atoi(getenv("LELPH_REF_KPOOL"));
+    if (comm.commQ_rank < 0 || comm.commQ_rank >= comm.nkpools) die("LELPH_REF_KPOOL out of range");
     comm.commW_size = comm.commQ_size = comm.commK_size = comm.commR_size = comm.commRq_size = 1;
 
+    if (sizeof(ELPH_float) == 4 && argc >= 4 && strcmp(argv[3], "star"))
+        die("the single-precision build runs the matrix elements (and the star mode) only");
+#ifdef COMPILE_ELPH_DOUBLE
     if (argc >= 6 && !strcmp(argv[3], "rotdv"))
     {
         nrec = 0;
@@ -327,6 +357,7 @@ int main(int argc, char** argv)
         fclose(fd);
         return 0;
     }
+#endif
     g_slice = (size_t)nmodes * nspin * nbnds * nbnds;
     g_nk = (size_t)nkbz;
     size_t nq_bz = (size_t)nq;
@@ -355,17 +386,18 @@ int main(int argc, char** argv)
         ph.nq_BZ = (ND_int)nq_bz;
         dmat_slice = (size_t)nspin * nbnds * nbnds;
         dmat_nk = (size_t)nkbz;
-        dmats = malloc(sizeof(double _Complex) * (size_t)nsym * dmat_nk * dmat_slice);
+        dmats = malloc(sizeof(ELPH_cmplx) * (size_t)nsym * dmat_nk * dmat_slice);
         if (!dmats) die("out of memory for Dmats");
         for (int is = 0; is < nsym; ++is)
             for (int ik = 0; ik < nkbz; ++ik)
                 electronic_reps(wfcs, &lat, lat.syms[is].Rmat, lat.syms[is].tau, lat.syms[is].time_rev, ik,
                                 dmats + ((size_t)is * dmat_nk + ik) * dmat_slice, &comm);
     }
-    g_all = calloc(nq_bz * g_nk * g_slice, sizeof(double _Complex));
-    double _Complex* eig = get("eigVec", 1)->data;
-    double _Complex* dv = get("dVscf", 1)->data;
+    g_all = calloc(nq_bz * g_nk * g_slice, sizeof(ELPH_cmplx));
+    ELPH_cmplx* eig = get("eigVec", 1)->data;
+    ELPH_cmplx* dv = get("dVscf", 1)->data;
     size_t nfft = (size_t)Nx * Ny * Nz;
+#ifdef COMPILE_ELPH_DOUBLE
     if (argc >= 5 && !strcmp(argv[3], "dvloc"))
     {
         const double* A = lat.alat_vec;
@@ -414,17 +446,32 @@ int main(int argc, char** argv)
         fclose(fv);
         free(vloc);
     }
+#endif
+    /* LELPH_REF_QPT=i: only the i-th q of the file (a timing sample) */
+    const int q_only = getenv("LELPH_REF_QPT") ? atoi(getenv("LELPH_REF_QPT")) : -1;
+    if (q_only >= nq) die("LELPH_REF_QPT out of range");
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
     for (int iq = 0; iq < nq; ++iq)
     {
+        if (q_only >= 0 && iq != q_only) continue;
         compute_and_write_elphq(wfcs, &lat, &ps, &ph, iq, eig + (size_t)iq * nmodes * nmodes,
                                 dv + (size_t)iq * nmodes * nmag * nfft, 0, 0, 0, 0, non_loc != 0,
                                 kminusq != 0, &comm);
     }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    /* wall time of the stage calls alone (no input loading), for timing samples */
+    fprintf(stderr, "lelph_ref: stage_seconds %.6f\n", (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec));
     FILE* fo = fopen(argv[2], "wb");
     if (!fo) die("cannot write output");
-    fwrite(g_all, sizeof(double _Complex), nq_bz * g_nk * g_slice, fo);
+    for (size_t i = 0; i < nq_bz * g_nk * g_slice; ++i)
+    {
+        const double v[2] = {creal(g_all[i]), cimag(g_all[i])};  /* complex128 in either build */
+        fwrite(v, sizeof(double), 2, fo);
+    }
     fclose(fo);
 
+#ifdef COMPILE_ELPH_DOUBLE
     if (argc >= 6 && !strcmp(argv[3], "rotate"))
     {
         /* elph_q_rotate on (g, Dl, Dr, time_rev) records of a separate file */
@@ -440,5 +487,6 @@ int main(int argc, char** argv)
         fwrite(out, 1, gq->nbytes, fr);
         fclose(fr);
     }
+#endif
     return 0;
 }

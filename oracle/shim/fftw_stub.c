@@ -4,8 +4,11 @@
  *   X[k + m q] = sum_{r<p} W_n^{r (k + m q)} Y_r[k],  n = p m,
  * with Y_r the length-m transforms of x[r], x[r+p], ...  Twiddles
  * W_n^t = exp(sign 2 pi i t / n) are evaluated in long double from the exact
- * reduced fraction t/n.  Every transform is computed in double; the float
- * entry points convert at the boundary.  Oracle build only. */
+ * reduced fraction t/n and rounded once to the working precision.  The
+ * double entry points compute in double; the float entry points compute every
+ * butterfly in float, as FFTW's single-precision library does, so that the
+ * reference's default (FP32) build carries the rounding of a float FFT.
+ * Oracle build only. */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -21,6 +24,9 @@ struct lelph_dft_plan
     double _Complex* tw; /* tw[t] = exp(sign 2 pi i t / n), t < n */
     double _Complex* buf;
     double _Complex* scratch;
+    float _Complex* twf; /* the same in float (float plans) */
+    float _Complex* buff;
+    float _Complex* scratchf;
 };
 
 static const long double TWO_PI_L = 6.283185307179586476925286766559005768L;
@@ -33,41 +39,42 @@ static int smallest_factor(int n)
 }
 
 /* in: n elements with stride s; out: n contiguous elements; tw: table of the
- * full length N (W_N^t), twstride = N / n. */
-static void dft_rec(const double _Complex* in, double _Complex* out, int n, int s, const double _Complex* tw,
-                    int twstride, int N, double _Complex* scratch)
-{
-    if (n == 1)
-    {
-        out[0] = in[0];
-        return;
+ * full length N (W_N^t), twstride = N / n.  Instantiated for double and float. */
+#define LELPH_DFT_REC(NAME, CT)                                                                        \
+    static void NAME(const CT* in, CT* out, int n, int s, const CT* tw, int twstride, int N, CT* scratch) \
+    {                                                                                                  \
+        if (n == 1)                                                                                    \
+        {                                                                                              \
+            out[0] = in[0];                                                                            \
+            return;                                                                                    \
+        }                                                                                              \
+        int p = smallest_factor(n);                                                                    \
+        int m = n / p;                                                                                 \
+        for (int r = 0; r < p; ++r)                                                                    \
+            NAME(in + (size_t)r * s, out + (size_t)r * m, m, s * p, tw, twstride * p, N, scratch + n); \
+        CT* t = scratch;                                                                               \
+        for (int k = 0; k < m; ++k)                                                                    \
+        {                                                                                              \
+            for (int r = 0; r < p; ++r)                                                                \
+            {                                                                                          \
+                long long e = ((long long)r * k * twstride) % N;                                       \
+                t[r] = out[(size_t)r * m + k] * tw[e];                                                 \
+            }                                                                                          \
+            for (int q = 0; q < p; ++q)                                                                \
+            {                                                                                          \
+                CT acc = 0;                                                                            \
+                for (int r = 0; r < p; ++r)                                                            \
+                {                                                                                      \
+                    long long e = ((long long)r * q * m * twstride) % N;                               \
+                    acc += t[r] * tw[e];                                                               \
+                }                                                                                      \
+                t[p + q] = acc;                                                                        \
+            }                                                                                          \
+            for (int q = 0; q < p; ++q) out[(size_t)q * m + k] = t[p + q];                             \
+        }                                                                                              \
     }
-    int p = smallest_factor(n);
-    int m = n / p;
-    for (int r = 0; r < p; ++r)
-        dft_rec(in + (size_t)r * s, out + (size_t)r * m, m, s * p, tw, twstride * p, N, scratch + n);
-    /* combine */
-    double _Complex* t = scratch;
-    for (int k = 0; k < m; ++k)
-    {
-        for (int r = 0; r < p; ++r)
-        {
-            long long e = ((long long)r * k * twstride) % N;
-            t[r] = out[(size_t)r * m + k] * tw[e];
-        }
-        for (int q = 0; q < p; ++q)
-        {
-            double _Complex acc = 0;
-            for (int r = 0; r < p; ++r)
-            {
-                long long e = ((long long)r * q * m * twstride) % N;
-                acc += t[r] * tw[e];
-            }
-            t[p + q] = acc;
-        }
-        for (int q = 0; q < p; ++q) out[(size_t)q * m + k] = t[p + q];
-    }
-}
+LELPH_DFT_REC(dft_rec, double _Complex)
+LELPH_DFT_REC(dft_rec_f, float _Complex)
 
 static struct lelph_dft_plan* make_plan(int rank, const int* n, int howmany, void* in, int istride, int idist,
                                         void* out, int ostride, int odist, int sign, int is_float)
@@ -88,38 +95,39 @@ static struct lelph_dft_plan* make_plan(int rank, const int* n, int howmany, voi
     p->tw = malloc(sizeof(double _Complex) * (size_t)p->n);
     p->buf = malloc(sizeof(double _Complex) * (size_t)p->n * 2);
     p->scratch = malloc(sizeof(double _Complex) * (size_t)p->n * 8 + 64);
+    p->twf = malloc(sizeof(float _Complex) * (size_t)p->n);
+    p->buff = malloc(sizeof(float _Complex) * (size_t)p->n * 2);
+    p->scratchf = malloc(sizeof(float _Complex) * (size_t)p->n * 8 + 64);
     for (int t = 0; t < p->n; ++t)
     {
         long double ang = TWO_PI_L * (long double)t / (long double)p->n;
         p->tw[t] = (double)cosl(ang) + (double)(sign * sinl(ang)) * I;
+        p->twf[t] = (float)cosl(ang) + (float)(sign * sinl(ang)) * I;
     }
     return p;
 }
 
 static void run_plan(const struct lelph_dft_plan* p, void* in, void* out)
 {
-    double _Complex* x = p->buf;
-    double _Complex* y = p->buf + p->n;
     for (int h = 0; h < p->howmany; ++h)
     {
         if (p->is_float)
         {
+            float _Complex* x = p->buff;
+            float _Complex* y = p->buff + p->n;
             const float _Complex* src = (const float _Complex*)in + (size_t)h * p->idist;
             for (int i = 0; i < p->n; ++i) x[i] = src[(size_t)i * p->istride];
+            dft_rec_f(x, y, p->n, 1, p->twf, 1, p->n, p->scratchf);
+            float _Complex* dst = (float _Complex*)out + (size_t)h * p->odist;
+            for (int i = 0; i < p->n; ++i) dst[(size_t)i * p->ostride] = y[i];
         }
         else
         {
+            double _Complex* x = p->buf;
+            double _Complex* y = p->buf + p->n;
             const double _Complex* src = (const double _Complex*)in + (size_t)h * p->idist;
             for (int i = 0; i < p->n; ++i) x[i] = src[(size_t)i * p->istride];
-        }
-        dft_rec(x, y, p->n, 1, p->tw, 1, p->n, p->scratch);
-        if (p->is_float)
-        {
-            float _Complex* dst = (float _Complex*)out + (size_t)h * p->odist;
-            for (int i = 0; i < p->n; ++i) dst[(size_t)i * p->ostride] = (float _Complex)y[i];
-        }
-        else
-        {
+            dft_rec(x, y, p->n, 1, p->tw, 1, p->n, p->scratch);
             double _Complex* dst = (double _Complex*)out + (size_t)h * p->odist;
             for (int i = 0; i < p->n; ++i) dst[(size_t)i * p->ostride] = y[i];
         }
@@ -132,6 +140,9 @@ static void free_plan(struct lelph_dft_plan* p)
     free(p->tw);
     free(p->buf);
     free(p->scratch);
+    free(p->twf);
+    free(p->buff);
+    free(p->scratchf);
     free(p);
 }
 

@@ -10,7 +10,7 @@ split, LELPH_REF_KPOOLS); the rate is g elements / wall time of the run.
 
 TEST INFRASTRUCTURE ONLY: it needs the reference tree and an x86 build here.
 
-    make -C oracle OUT=_ref/o3 CFLAGS="-O3 -march=native -std=gnu11 -fopenmp -DELPH_OMP_PARALLEL_BUILD"
+    make -C oracle REF=<reference tree> OUT=_ref/o3 CFLAGS="-O3 -march=native -std=gnu11 -fopenmp -DELPH_OMP_PARALLEL_BUILD"
     python oracle/time_reference.py [c0 c1 ...]
 """
 import json

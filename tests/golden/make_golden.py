@@ -12,13 +12,18 @@ matrix elements computed from the summed dV; rotate_dvscf.npz pins
 rotate_dvscf, dmats.npz the electronic representation matrices
 (electronic_reps, src/symmetries/elec_reps.c:16) and star_*.npz the stage's
 q-star expansion (src/elph/compute_elph_matq.c:159-217); dvscf_qe.npz pins
-the dV_scf ingest (read_dvscf_qe, src/io/qe/read_dvscf.c:15).
+the dV_scf ingest (read_dvscf_qe, src/io/qe/read_dvscf.c:15); ref_f32.npz
+holds the output of the reference's default single-precision build
+(oracle/_ref/f32/lelph_ref, no -DCOMPILE_ELPH_DOUBLE, src/elphC.h:21-31) on two
+systems, the yardstick for the error of the mixed form.
 
 Run from the repo root after ``make -C oracle``:
     python tests/golden/make_golden.py            (every fixture)
     python tests/golden/make_golden.py dmats      (only dmats.npz)
     python tests/golden/make_golden.py star       (only star_*.npz)
     python tests/golden/make_golden.py dvscf      (only dvscf_qe.npz)
+    python tests/golden/make_golden.py f32        (only ref_f32.npz; needs
+        make -C oracle OUT=_ref/f32 DEFS= as well)
 """
 import json
 import os
@@ -305,6 +310,73 @@ def dvscf_fixture(tmp):
                         sample=np.array(DVSCF_SAMPLE), **rec)
 
 
+# the reference's single-precision build on every system of GOLDEN and on the
+# first k-points of one q of the 4-atom c1 system (32 bands, 48^3 grid, its own
+# k-pool split LELPH_REF_KPOOLS); name -> (base, overrides, kminusq, non_loc, k pools)
+F32_SYS = dict({n: (b, o, kmq, nl, 1) for n, (b, o, kmq, nl) in GOLDEN.items()},
+               c1s=("c1", {"qpts": [(0.125, 0, 0)]}, False, True, 128))
+
+
+# systems at the shapes of the benchmark configurations and of tensor-core
+# tiles that hold whole modes (48 bands x 12 modes, 36 bands x 24 modes): both
+# builds of the reference run the first nk_BZ / kpools k-points of one q and
+# only the error statistics of the single-precision build against the double
+# one are stored (the metric's definition: max and RMS of e_i, complex norm);
+# name -> (base, overrides, k pools)
+F32_STATS = {
+    "tile48": ("c1", {"nbnds": 48, "kgrid": (4, 4, 4), "qpts": [(0.25, 0, 0)]}, 32),
+    "tile36": ("c3", {"nbnds": 36, "nspinor": 1, "nmag": 1, "soc": False, "ls": (0, 1), "npw": 1500,
+                      "fft": (40, 40, 40), "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}, 4),
+    "c2s": ("c2", {"qpts": [(1 / 12, 0, 0)]}, 36),
+    "c3s": ("c3", {"qpts": [(1 / 6, 0, 0)]}, 54),
+    "c4s": ("c4", {"nbnds": 80, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]}, 8),
+}
+
+
+def f32_stats(name, base, ov, kpools, tmp):
+    s = synth.make_system(base, dict(ov))
+    sysf = os.path.join(tmp, "f32s_" + name + ".bin")
+    synth.write_system(s, sysf)
+    env = dict(os.environ, LELPH_REF_KPOOLS=str(kpools))
+    nk = s.nk_bz // kpools + (1 if s.nk_bz % kpools else 0)
+    g = {}
+    for tag, exe in (("64", REF), ("32", os.path.join(ROOT, "oracle", "_ref", "f32", "lelph_ref"))):
+        gf = os.path.join(tmp, "f32s_" + name + tag + ".bin")
+        subprocess.run([exe, sysf, gf], check=True, env=env, stdout=subprocess.DEVNULL)
+        g[tag] = synth.read_g(gf, s, len(s.qpts))[:, :nk]
+    a, b = np.abs(g["32"]), np.abs(g["64"])
+    e = np.abs(a - b) / np.maximum(b, 1e-6 * b.max())
+    st = np.array([e.max(), np.sqrt(np.mean(e * e)),
+                   np.linalg.norm((g["32"] - g["64"]).ravel()) / np.linalg.norm(g["64"].ravel())])
+    print("f32 stats", name, nk, st.tolist(), flush=True)
+    return {name + "_stats": st, name + "_nk": np.array(nk),
+            name + "_spec": np.array(json.dumps({"base": base, "overrides": ov, "kminusq": False, "non_loc": True})),
+            name + "_wfc_sum": np.array([np.abs(w).sum() for w in s.wfc]), name + "_dv_sum": np.abs(s.dVscf).sum()}
+
+
+def f32_fixture(tmp):
+    ref32 = os.path.join(ROOT, "oracle", "_ref", "f32", "lelph_ref")
+    rec = {}
+    for name, (base, ov, kpools) in F32_STATS.items():
+        rec.update(f32_stats(name, base, ov, kpools, tmp))
+    for name, (base, ov, kmq, nl, kpools) in F32_SYS.items():
+        s = synth.make_system(base, dict(ov))
+        sysf = os.path.join(tmp, "f32_" + name + ".bin")
+        synth.write_system(s, sysf, kminusq=kmq, non_loc=nl)
+        gf = os.path.join(tmp, "f32_" + name + "_g.bin")
+        env = dict(os.environ, LELPH_REF_KPOOLS=str(kpools))
+        subprocess.run([ref32, sysf, gf], check=True, env=env, stdout=subprocess.DEVNULL)
+        nk = s.nk_bz // kpools + (1 if s.nk_bz % kpools else 0)
+        g = synth.read_g(gf, s, len(s.qpts))[:, :nk]
+        rec[name + "_g32"] = g.astype(np.complex64)
+        rec[name + "_spec"] = np.array(json.dumps({"base": base, "overrides": ov, "kminusq": kmq,
+                                                   "non_loc": nl}))
+        rec[name + "_wfc_sum"] = np.array([np.abs(w).sum() for w in s.wfc])
+        rec[name + "_dv_sum"] = np.abs(s.dVscf).sum()
+        print("f32", name, g.shape, float(np.abs(g).max()))
+    np.savez(os.path.join(ROOT, "tests", "golden", "ref_f32.npz"), **rec)
+
+
 if __name__ == "__main__":
     only = sys.argv[1:]
     with tempfile.TemporaryDirectory() as tmp:
@@ -321,3 +393,5 @@ if __name__ == "__main__":
             star_fixture(tmp)
         if not only or "dvscf" in only:
             dvscf_fixture(tmp)
+        if not only or "f32" in only:
+            f32_fixture(tmp)

@@ -78,3 +78,44 @@ def load_dvscf_qe():
         pats = np.linalg.qr(rng.standard_normal((nm, nm)) + 1j * rng.standard_normal((nm, nm)))[0]
         out[name] = (s, raw, pats)
     return z, out
+
+
+def load_f32(name):
+    """(system, g32, kminusq, non_loc) of one system of tests/golden/ref_f32.npz:
+    the output of the reference's default single-precision build (complex64,
+    the first nk k-points of each q when the fixture was a k-pool sample)."""
+    z = np.load(os.path.join(GOLDEN_DIR, "ref_f32.npz"))
+    spec = json.loads(str(z[name + "_spec"]))
+    ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls") else v)
+          for k, v in spec["overrides"].items()}
+    if "qpts" in ov:
+        ov["qpts"] = [tuple(q) for q in ov["qpts"]]
+    s = synth.make_system(spec["base"], ov)
+    assert np.allclose([np.abs(w).sum() for w in s.wfc], z[name + "_wfc_sum"], rtol=1e-12)
+    assert np.isclose(np.abs(s.dVscf).sum(), float(z[name + "_dv_sum"]), rtol=1e-12)
+    return s, z[name + "_g32"], bool(spec["kminusq"]), bool(spec["non_loc"])
+
+
+def errors(g, ref):
+    """The metric's error of g against ref: e_i = ||g_i| - |ref_i|| /
+    max(|ref_i|, 1e-6 max|ref|); returns (max e, RMS e, ||g - ref|| / ||ref||)."""
+    a, b = np.abs(g), np.abs(ref)
+    e = np.abs(a - b) / np.maximum(b, 1e-6 * b.max())
+    return float(e.max()), float(np.sqrt(np.mean(e * e))), float(np.linalg.norm((g - ref).ravel()) /
+                                                                np.linalg.norm(ref.ravel()))
+
+
+def load_f32_stats(name):
+    """(system, (max, RMS, norm), nk) of a stats-only entry of ref_f32.npz: the
+    error of the reference's single-precision build against its double build
+    on the first nk k-points of the system's q."""
+    z = np.load(os.path.join(GOLDEN_DIR, "ref_f32.npz"))
+    spec = json.loads(str(z[name + "_spec"]))
+    ov = {k: (tuple(v) if isinstance(v, list) and k in ("kgrid", "fft", "ls") else v)
+          for k, v in spec["overrides"].items()}
+    if "qpts" in ov:
+        ov["qpts"] = [tuple(q) for q in ov["qpts"]]
+    s = synth.make_system(spec["base"], ov)
+    assert np.allclose([np.abs(w).sum() for w in s.wfc], z[name + "_wfc_sum"], rtol=1e-12)
+    assert np.isclose(np.abs(s.dVscf).sum(), float(z[name + "_dv_sum"]), rtol=1e-12)
+    return s, z[name + "_stats"], int(z[name + "_nk"])

@@ -74,3 +74,47 @@ def test_strerror_covers_status_codes():
     lib = elph.load_library(build_library())
     for code in range(0, -8, -1):
         assert lib.lelph_gpu_strerror(code).decode() not in ("", "unknown status")
+
+
+def test_partials_allocation_covers_kernel_indices():
+    """The mixed real-space route's partial sums: for every band count the
+    tensor-core tile takes and the mode counts of 1-16 atom cells, the bytes
+    the library allocates cover the highest float the sandwich writes and the
+    finish reads (host arithmetic of the library itself, no device work).  A
+    tile holds whole modes, so 128 % nbnds != 0 needs more tiles than
+    ceil(nmodes * nbnds / 128)."""
+    lib = elph.load_library(build_library())
+    out = (ctypes.c_ulonglong * 3)()
+    short = 0
+    for nb in range(1, 65):
+        for nm in (3, 6, 9, 12, 24, 36, 48):
+            for ns, nch, npairs in ((1, 1, 1), (2, 3, 5)):
+                assert lib.lelph_gpu_debug_partials_extent(nm, nb, ns, nch, npairs, out) == 0
+                alloc, wr, rd = out[0], out[1], out[2]
+                assert wr <= alloc and rd <= alloc, (nb, nm, ns, nch, npairs, alloc, wr, rd)
+                assert wr == alloc  # the last unit's block ends the buffer exactly
+                nbp = (nb + 7) // 8 * 8
+                short += alloc > ns * ((nm * nb + 127) // 128) * nch * 128 * 2 * nbp * npairs
+    assert short > 0   # shapes where whole-mode tiles need more than ceil(nm nb / 128) tiles exist
+    assert lib.lelph_gpu_debug_partials_extent(12, 65, 1, 1, 1, out) != 0
+
+
+def test_reference_binding_compiles_into_the_reference():
+    """The binding a LetzElPhC maintainer compiles in place of
+    src/elph/compute_elph_matq.c builds against the reference's own headers in
+    both of its precisions and defines the stage's symbol (build() makes these
+    objects when the reference sources are at hand)."""
+    import platform
+    import shutil
+    import pytest
+    if not shutil.which("nm"):
+        pytest.skip("nm is not installed")
+    for sub in ("", "-f32"):
+        d = os.path.join(ROOT, "oracle", "_ref", platform.machine() + sub)
+        obj, exe = os.path.join(d, "binding.o"), os.path.join(d, "lelph_ref_gpu")
+        if not os.path.exists(obj):
+            pytest.skip("the reference sources were not available to build()")
+        syms = subprocess.run(["nm", obj], capture_output=True, text=True, check=True).stdout
+        assert re.search(r"\bT compute_and_write_elphq\b", syms)
+        assert "lelph_gpu_compute_elphq_star" in syms and "nc_put_vara" in syms
+        assert os.access(exe, os.X_OK)

@@ -137,3 +137,19 @@ def test_dvscf_ingest_matches_reference():
         assert np.abs(out[::st] - smp).max() < 1e-12 * np.abs(smp).max(), name
         nrm = np.linalg.norm(out.reshape(s.nmodes, -1), axis=1)
         assert np.abs(nrm - z[name + "_norm"]).max() < 1e-12 * nrm.max(), name
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_reference_single_precision_build_fixture(name):
+    """ref_f32.npz holds the reference's default single-precision build
+    (src/elphC.h:21-31) on the inputs of the FP64 fixtures: it must differ from
+    the FP64 build like a single-precision result does (not be an FP64 copy,
+    not be wrong), since the GPU tests use its error as the yardstick of the
+    mixed form."""
+    from golden_util import errors, load_f32
+    s, g32, _, _ = load_f32(name)
+    _, g64, _, _ = load(name)
+    emax, erms, enorm = errors(g32, g64)
+    assert g32.dtype == np.complex64 and g32.shape == g64.shape
+    assert 1e-8 < enorm < 1e-5, enorm
+    assert erms < 1e-4 and emax > 1e-7, (emax, erms)

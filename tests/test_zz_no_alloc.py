@@ -42,12 +42,26 @@ def test_noalloc_matches_run_device(name, ov, prec):
         ctx.run_device(qs, ks, ref.data_ptr(), out=OUT_C128)
         torch.cuda.synchronize()
         scale = ref.abs().max().item()
+        warm = torch.empty_like(ref)
+        outs = [torch.full_like(ref, float("nan")) for _ in range(2)]
+        # a warm-up call loads every kernel the entry point launches (modules load
+        # lazily, on first launch, into device memory), so that free device
+        # memory is steady around the two checked calls
+        rc = L.lelph_gpu_run_device_noalloc(ctx.h, n, _ptr(qs), _ptr(ks), 1, 0, OUT_C128,
+                                            C.c_void_p(warm.data_ptr()))
+        assert rc == 0, L.lelph_gpu_last_error(ctx.h).decode()
+        held0 = ctx.stats()["device_bytes"]
         for call in range(2):
-            out = torch.full_like(ref, float("nan"))
+            out = outs[call]
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             rc = L.lelph_gpu_run_device_noalloc(ctx.h, n, _ptr(qs), _ptr(ks), 1, 0, OUT_C128,
                                                 C.c_void_p(out.data_ptr()))
             assert rc == 0, L.lelph_gpu_last_error(ctx.h).decode()
             torch.cuda.synchronize()
+            # nothing was allocated during the call: neither by the context nor on the device
+            assert torch.cuda.mem_get_info()[0] == free0
+            assert ctx.stats()["device_bytes"] == held0
             err = (out - ref).abs().max().item() / scale
             assert err < TOL, (call, err)
 
