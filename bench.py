@@ -59,11 +59,13 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
-    p.add_argument("--workload", default="elph", choices=["elph", "dmats", "star", "dvscf", "configs", "gspace"],
+    p.add_argument("--workload", default="elph",
+                   choices=["elph", "dmats", "star", "dvscf", "configs", "gspace", "batch"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
                         "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
-                        "file layout; configs: mixed vs FP64 rate and error on every config's full size")
+                        "file layout; configs: mixed vs FP64 rate and error on every config's full size; "
+                        "batch: the batched uneven workload in one call, per q and per (k, q) call")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
     p.add_argument("--configs", default="", help="configs workload: comma-separated subset (default: all)")
     p.add_argument("--small", action="store_true",
@@ -1007,8 +1009,98 @@ def run_configs(args):
     return 0
 
 
+def run_batch(args):
+    """The batched uneven workload (3-atom hexagonal slab, 36x36x216 grid,
+    12x12x1 k, 64 q, 9 modes, 40 bands, npw 1800-2600 across k) three ways on
+    the mixed form, device-resident, CUDA events on the library stream:
+    * batch: every (k, q) pair of the 64 q in one call (the tensor-core
+      sandwich is one persistent launch over all pairs);
+    * per q: one call per q-point (144 pairs each), the reference's per-q
+      stage granularity (compute_and_write_elphq, src/elph/elph_driver.c:200-307);
+    * per (k, q): one call per pair, the granularity of the reference's k
+      loop (src/elph/compute_elph_matq.c:116-150), on a sample of the pairs
+      and scaled to the batch.
+    The full-BZ preparation (unfold, FFTs, projections) is timed once and
+    counted in every rate."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import LelphGPU, OUT_C64
+    build_library()
+    s = synth.make_system("c2")
+    nq, nk = len(s.qpts), s.nk_bz
+    gsz = s.nmodes * s.nspin * s.nbnds * s.nbnds
+    npairs = nq * nk
+    elems = g_elems(s, npairs)
+    qs = np.repeat(np.arange(nq), nk).astype(np.int32)
+    ks = np.tile(np.arange(nk), nq).astype(np.int32)
+    ctx = LelphGPU(s, args.precision, device=local)
+    for iq in range(nq):
+        ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
+    gdev = torch.empty(npairs * gsz * 2, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    es = 8 * gsz  # bytes of one pair's complex64 output
+
+    def timed(fn, reps=1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, 1e3 * (time.perf_counter() - t0) / reps
+
+    ctx.prepare()
+    ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64)   # warm-up (windows, kernels loaded)
+    prep_ms, _ = timed(ctx.prepare, 3)
+    batch_ms, batch_wall = timed(lambda: ctx.run_device(qs, ks, gdev.data_ptr(), out=OUT_C64), max(3, args.steps))
+
+    def per_q():
+        for iq in range(nq):
+            sl = slice(iq * nk, (iq + 1) * nk)
+            ctx.run_device(qs[sl], ks[sl], gdev.data_ptr() + iq * nk * es, out=OUT_C64)
+    perq_ms, perq_wall = timed(per_q)
+    nsamp = min(npairs, 4 * nk)
+    rng = np.random.default_rng(2)
+    sel = np.sort(rng.choice(npairs, size=nsamp, replace=False))
+
+    def per_pair():
+        for i in sel:
+            ctx.run_device(qs[i:i + 1], ks[i:i + 1], gdev.data_ptr() + int(i) * es, out=OUT_C64)
+    pp_ms, pp_wall = timed(per_pair)
+    pp_full_ms = pp_ms * npairs / nsamp
+    pp_full_wall = pp_wall * npairs / nsamp
+    st = ctx.stats()
+    ctx.close()
+    rate = lambda ms: elems / ((prep_ms + ms) * 1e-3)  # noqa: E731
+    line = {"metric": METRIC, "unit": "g_elements/s", "n_gpus": 1, "dtype": args.precision,
+            "data": "synthetic (seeded, the batched uneven workload's shapes)",
+            "config": {"workload": "3-atom hexagonal slab, 36x36x216 grid, 12x12x1 k, 64 q, 9 modes, 40 bands, "
+                                   "npw 1800-2600", "pairs": npairs, "g_elements": elems,
+                       "route": {1: "real-space", 2: "G-space"}.get(st["route"], st["route"]),
+                       "product_grid": list(st["product_grid"])},
+            "prepare_ms": prep_ms,
+            "batch": {"value": rate(batch_ms), "pairs_ms": batch_ms, "wall_ms": batch_wall, "calls": 1},
+            "per_q": {"value": rate(perq_ms), "pairs_ms": perq_ms, "wall_ms": perq_wall, "calls": nq},
+            "per_pair": {"value": rate(pp_full_ms), "pairs_ms": pp_full_ms, "wall_ms": pp_full_wall,
+                         "calls": npairs, "sample_pairs": int(nsamp),
+                         "note": "timed on the sample, scaled to every pair of the batch"},
+            "batch_over_per_pair": (prep_ms + pp_full_ms) / (prep_ms + batch_ms),
+            "batch_over_per_q": (prep_ms + perq_ms) / (prep_ms + batch_ms)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "batch":
+        return run_batch(args)
     if args.workload == "configs":
         return run_configs(args)
     if args.workload == "gspace":

@@ -142,6 +142,26 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_plane_ct(const T2* __restrict
     }
 }
 
+// Epilogue store of one sphere value: as it is, or (FP32 operand of the
+// tensor-core GEMM, lo given) as its TF32-rounded value and the TF32-rounded
+// remainder.
+__device__ __forceinline__ void gs_store(double2* hi, double2* lo, int K, double2 v)
+{
+    (void)lo;
+    hi[K] = v;
+}
+__device__ __forceinline__ void gs_store(float2* hi, float2* lo, int K, float2 v)
+{
+    if (!lo)
+    {
+        hi[K] = v;
+        return;
+    }
+    const float2 h = make_float2(tf32_rn(v.x), tf32_rn(v.y));
+    hi[K] = h;
+    lo[K] = make_float2(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y));
+}
+
 // -------------------------------------------------------------------- x pass
 // grid: (ceil(ncol / GS_CB), rows of the block x nspinor); the tile [x][column]
 // is read along the columns (coalesced), transformed along x, and the sphere
@@ -151,7 +171,7 @@ template <typename T2, typename T>
 __global__ void __launch_bounds__(GS_THREADS) k_gs_xpass(const T2* __restrict__ in, int Nx, int ncol,
                                                          FftPlan1D px, const T2* __restrict__ twx,
                                                          const int* __restrict__ cst, const int* __restrict__ kcx,
-                                                         int npad, T2* __restrict__ A)
+                                                         int npad, T2* __restrict__ A, T2* __restrict__ A_lo)
 {
     extern __shared__ __align__(16) unsigned char gsx_smem[];
     T2* a = reinterpret_cast<T2*>(gsx_smem);
@@ -175,7 +195,7 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_xpass(const T2* __restrict__ 
     {
         const int v = kcx[K];
         const int c = v / Nx, x = v - c * Nx;
-        dst[K] = r[x * GS_CB + (c - c0)];
+        gs_store(dst, A_lo ? A_lo + (size_t)rb * npad : nullptr, K, r[x * GS_CB + (c - c0)]);
     }
 }
 
@@ -187,7 +207,7 @@ template <typename T2, typename T, int NX, int CB>
 __global__ void __launch_bounds__(GS_THREADS) k_gs_xpass_ct(const T2* __restrict__ in, int ncol,
                                                             const T2* __restrict__ twx, const int* __restrict__ cst,
                                                             const int* __restrict__ kcx, int npad,
-                                                            T2* __restrict__ A)
+                                                            T2* __restrict__ A, T2* __restrict__ A_lo)
 {
     constexpr int NE = NX * CB;
     constexpr int PER = (NE + GS_THREADS - 1) / GS_THREADS;
@@ -217,11 +237,12 @@ __global__ void __launch_bounds__(GS_THREADS) k_gs_xpass_ct(const T2* __restrict
     T2* r = ct_fft<T2, T, NX, 0, 1, true, CB>(a, b, CB, CB, 1, nullptr, CB, 1, tx, -1);
     const int k0 = cst[c0], k1 = cst[min(c0 + CB, ncol)];
     T2* dst = A + (size_t)rb * npad;
+    T2* dlo = A_lo ? A_lo + (size_t)rb * npad : nullptr;
     for (int K = k0 + threadIdx.x; K < k1; K += blockDim.x)
     {
         const int w = kcx[K];
         const int c = w / NX, x = w - c * NX;
-        dst[K] = r[x * CB + (c - c0)];
+        gs_store(dst, dlo, K, r[x * CB + (c - c0)]);
     }
 }
 
@@ -654,7 +675,7 @@ int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const voi
 
 template <typename T2, typename T, int NX, int CB>
 static int gs_xpass_ct(int nrb, int ncol, const void* twx, const int* cst, const int* kcx, int npad, const void* in,
-                       void* A, cudaStream_t st)
+                       void* A, void* A_lo, cudaStream_t st)
 {
     const size_t smem = sizeof(T2) * (2 * (size_t)NX * CB + NX);
     static bool attr = false;
@@ -667,19 +688,21 @@ static int gs_xpass_ct(int nrb, int ncol, const void* twx, const int* cst, const
     }
     dim3 grid((unsigned)((ncol + CB - 1) / CB), (unsigned)nrb);
     k_gs_xpass_ct<T2, T, NX, CB><<<grid, GS_THREADS, smem, st>>>((const T2*)in, ncol, (const T2*)twx, cst, kcx, npad,
-                                                                (T2*)A);
+                                                                (T2*)A, (T2*)A_lo);
     return 0;
 }
 
 int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, int ncol, const FftPlan1D& px,
-                          const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st)
+                          const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st,
+                          void* A_lo)
 {
+    if (fp64) A_lo = nullptr;
     const size_t smem = lelph_gs_xpass_smem(gg, fp64);
     if (smem > 220 * 1024 || nrb > 65535) return -1;
 #define GS_XC(N)                                                                                            \
     case N:                                                                                                 \
-        return fp64 ? gs_xpass_ct<double2, double, N, 32>(nrb, ncol, twx, cst, kcx, npad, in, A, st)        \
-                    : gs_xpass_ct<float2, float, N, 64>(nrb, ncol, twx, cst, kcx, npad, in, A, st);
+        return fp64 ? gs_xpass_ct<double2, double, N, 32>(nrb, ncol, twx, cst, kcx, npad, in, A, A_lo, st)  \
+                    : gs_xpass_ct<float2, float, N, 64>(nrb, ncol, twx, cst, kcx, npad, in, A, A_lo, st);
     switch (gg.Nx)
     {
         GS_XC(36)
@@ -701,7 +724,7 @@ int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, i
             return -1;
         k_gs_xpass<double2, double><<<grid, GS_THREADS, smem, st>>>((const double2*)in, gg.Nx, ncol, px,
                                                                     (const double2*)twx, cst, kcx, npad,
-                                                                    (double2*)A);
+                                                                    (double2*)A, nullptr);
     }
     else
     {
@@ -709,7 +732,8 @@ int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, i
                                  (int)smem) != cudaSuccess)
             return -1;
         k_gs_xpass<float2, float><<<grid, GS_THREADS, smem, st>>>((const float2*)in, gg.Nx, ncol, px,
-                                                                  (const float2*)twx, cst, kcx, npad, (float2*)A);
+                                                                  (const float2*)twx, cst, kcx, npad, (float2*)A,
+                                                                  (float2*)A_lo);
     }
     return 0;
 }

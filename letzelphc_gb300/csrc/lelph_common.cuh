@@ -54,6 +54,15 @@ __device__ __forceinline__ unsigned long long gtimer_ns()
     return t;
 }
 
+// nearest TF32 value of x (10 explicit significand bits, the low 13 bits of
+// the FP32 word cleared; ties away from zero)
+__device__ __forceinline__ float tf32_rn(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
 // ---------------------------------------------------------------- mbarrier
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)

@@ -121,6 +121,8 @@ struct lelph_gpu
     long long gs_bp_total = 0;
     DevBuf d_gs_perm, d_gs_kcx, d_gs_cols, d_gs_cst, d_gs_npw, d_gs_npad, d_gs_permoff, d_gs_bpoff, d_gs_bp;
     DevBuf d_gs_psi, d_gs_out1, d_gs_A, d_gs_part;
+    DevBuf d_gs_bq;      // mixed form on the tensor cores: the pair's k+q operand split into TF32 hi / lo
+    bool gs_tc = false;  // mixed G-space GEMM on the tensor cores (gspace_tc.cu)
     DevBuf d_gs_zl, d_gs_cols2;  // z lines holding a column of the sphere; column index into the pruned plane
 };
 
@@ -884,6 +886,11 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     if (d.route == LELPH_GPU_ROUTE_REAL && !tc_ok)
         return bad(LELPH_GPU_ERR_UNSUPPORTED, "the real-space route of the mixed form supports up to 64 bands");
     h->gspace = d.route == LELPH_GPU_ROUTE_GSPACE || !tc_ok;
+    {
+        // the mixed G-space GEMM on the tensor cores (LELPH_GS_TC=0: the FP32 SIMT GEMM)
+        const char* e = std::getenv("LELPH_GS_TC");
+        h->gs_tc = h->mixed && lelph_gs_tc_supported(d.nbnds) && !(e && e[0] == '0');
+    }
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
     // host copies
@@ -1146,7 +1153,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
                       &h->d_qsitems, &h->d_dvraw, &h->d_gs_perm, &h->d_gs_kcx, &h->d_gs_cols, &h->d_gs_cst,
                       &h->d_gs_npw, &h->d_gs_npad, &h->d_gs_permoff, &h->d_gs_bpoff, &h->d_gs_bp, &h->d_gs_psi,
-                      &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part, &h->d_gs_zl, &h->d_gs_cols2};
+                      &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part, &h->d_gs_zl, &h->d_gs_cols2, &h->d_gs_bq};
     for (DevBuf* b : bufs) h->owned.push_back(b);
     int rc = 0;
 #define UP(buf, ptr, bytes)                              \
@@ -2013,12 +2020,29 @@ static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
     if (rc) return rc;
     // modes per pass: the plane-pass output and the GEMM operand of a block of
     // modes stay within ~2 GB
-    const size_t per_mode = e * (size_t)nb * ns * ((size_t)g.Nx * h->gs_ncol_max + h->gs_npad_max);
+    // (the tensor-core GEMM of the mixed form takes the sphere values as two
+    // arrays, TF32 hi and lo, and the k+q coefficients split the same way)
+    const bool tc = !f64 && h->gs_tc;
+    const size_t na = tc ? 2 : 1;
+    const size_t per_mode = e * (size_t)nb * ns * ((size_t)g.Nx * h->gs_ncol_max + na * h->gs_npad_max);
     const int nub = (int)std::max<size_t>(1, std::min<size_t>((size_t)nm, (2ull << 30) / per_mode));
     rc = ensure(h, h->d_gs_out1, e * (size_t)nub * nb * ns * g.Nx * h->gs_ncol_max);
     if (rc) return rc;
-    rc = ensure(h, h->d_gs_A, e * (size_t)nub * nb * ns * h->gs_npad_max);
+    const size_t a_cap = (size_t)nub * nb * ns * h->gs_npad_max;  // complex elements of one A array
+    void* prev_A = h->d_gs_A.p;
+    rc = ensure(h, h->d_gs_A, e * na * a_cap);
     if (rc) return rc;
+    // a row's positions past its sphere (npw .. npad) meet zero k+q coefficients
+    // and must hold finite values: clear a fresh buffer once
+    if (h->d_gs_A.p != prev_A) CUDA_TRY(h, cudaMemsetAsync(h->d_gs_A.p, 0, h->d_gs_A.n, h->st));
+    int ntile_count = 0;
+    const int NT = tc ? lelph_gs_tc_ntile(nb, &ntile_count) : 0;
+    if (tc)
+    {
+        rc = ensure(h, h->d_gs_bq, sizeof(float) * 2 * (size_t)(2 * nb) * (2 * (size_t)ns * h->gs_npad_max));
+        if (rc) return rc;
+    }
+    void* A_lo = tc ? (void*)((float2*)h->d_gs_A.p + a_cap) : nullptr;
     const int kchunk = 1024;
     const int nch_max = (ns * h->gs_npad_max + kchunk - 1) / kchunk;
     rc = ensure(h, h->d_gs_part, e * (size_t)nch_max * nrows * nb);
@@ -2069,10 +2093,29 @@ static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
             gg.spin = spin;
             const void* psi = (const char*)h->d_gs_psi.p + e * (size_t)spin * nb * ns * M;
             const void* B = (const char*)h->d_gs_bp.p + e * ((size_t)h->gs_bp_off[kq] + (size_t)spin * nb * ns * npad);
+            CUtensorMap tm[4];
+            if (tc)
+            {
+                // B rows 2n = (br, bi), 2n + 1 = (-bi, br) over K = 2 Ktot, hi plane then lo plane
+                float* bq = (float*)h->d_gs_bq.p;
+                lelph_launch_gs_bsplit((const float2*)B, nb, Ktot, bq, h->st);
+                h->stats.kernel_launches += 1;
+                const size_t plane = (size_t)(2 * nb) * 2 * Ktot;
+                rc = make_tmap(h, &tm[2], bq, 2ull * Ktot, 2ull * nb, (unsigned)NT, true, true, 32);
+                if (!rc) rc = make_tmap(h, &tm[3], bq + plane, 2ull * Ktot, 2ull * nb, (unsigned)NT, true, true, 32);
+                if (rc) return rc;
+            }
             for (int nu0 = 0; nu0 < nm; nu0 += nub)
             {
                 const int nmb = std::min(nub, nm - nu0);
                 int bad = 0;
+                if (tc)
+                {
+                    rc = make_tmap(h, &tm[0], h->d_gs_A.p, 2ull * Ktot, (unsigned long long)nmb * nb, 128, true, true,
+                                   32);
+                    if (!rc) rc = make_tmap(h, &tm[1], A_lo, 2ull * Ktot, (unsigned long long)nmb * nb, 128, true, true, 32);
+                    if (rc) return rc;
+                }
                 gs_tick(h);
                 bad |= lelph_launch_gs_plane(gg, f64, psi, win, nu0, nmb, h->plan[1], h->plan[2], tw[1], tw[2],
                                              (const int*)h->d_gs_cols.p + h->gs_col_off[kq], ncol,
@@ -2083,10 +2126,15 @@ static int gs_local(lelph_gpu* h, const PairInfo* pairs, int n, double2* glocal)
                 bad |= lelph_launch_gs_xpass(gg, f64, h->d_gs_out1.p, nmb * nb * ns, ncol, h->plan[0], tw[0],
                                              (const int*)h->d_gs_cst.p + h->gs_cst_off[kq],
                                              (const int*)h->d_gs_kcx.p + h->gs_perm_off[kq], npad, h->d_gs_A.p,
-                                             h->st);
+                                             h->st, A_lo);
                 h->stats.gs_xpass_ms += gs_tock(h);
-                bad |= lelph_launch_gs_gemm(f64, h->d_gs_A.p, B, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
-                                            h->d_gs_part.p, h->st);
+                if (tc)
+                    bad |= lelph_launch_gs_gemm_tc(tm, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
+                                                   (float2*)h->d_gs_part.p, (unsigned*)h->d_status.p, h->wait_ns,
+                                                   h->st);
+                else
+                    bad |= lelph_launch_gs_gemm(f64, h->d_gs_A.p, B, nmb * nb, nb, Ktot, kchunk, nu0 * nb, nrows,
+                                                h->d_gs_part.p, h->st);
                 h->stats.gs_gemm_ms += gs_tock(h);
                 if (bad) return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "G-space route: launch configuration");
                 h->stats.kernel_launches += 3;

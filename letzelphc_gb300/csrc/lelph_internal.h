@@ -122,9 +122,21 @@ bool lelph_gs_plane_fixed(const GsGeom& gg, int fp64);
 int lelph_launch_gs_plane(const GsGeom& gg, int fp64, const void* psi, const void* win, int nu0, int nub,
                           const FftPlan1D& py, const FftPlan1D& pz, const void* twy, const void* twz, const int* cols,
                           int ncol, const int* cols2, const int* zl, int nzl, void* out, cudaStream_t st);
-// x pass: A [rb][npad] (rb = row-box index of the block) in the sphere's sorted order
+// x pass: A [rb][npad] (rb = row-box index of the block) in the sphere's sorted order;
+// with A_lo (FP32 only) A receives the TF32-rounded values and A_lo the rounded remainders
 int lelph_launch_gs_xpass(const GsGeom& gg, int fp64, const void* in, int nrb, int ncol, const FftPlan1D& px,
-                          const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st);
+                          const void* twx, const int* cst, const int* kcx, int npad, void* A, cudaStream_t st,
+                          void* A_lo = nullptr);
+// tensor-core GEMM of the mixed form (gspace_tc.cu): tmaps = CUtensorMap[4] of
+// A hi, A lo (nrows x 2 Ktot FP32, box 32 x 128), B hi, B lo (2 nb x 2 Ktot,
+// box 32 x NT); B from lelph_launch_gs_bsplit
+int lelph_gs_tc_ntile(int nb, int* ntiles);
+int lelph_gs_tc_supported(int nb);
+size_t lelph_gs_tc_smem(int nb);
+void lelph_launch_gs_bsplit(const float2* Bp, int nb, int Ktot, float* Bq, cudaStream_t st);
+int lelph_launch_gs_gemm_tc(const void* tmaps, int nrows, int nb, int Ktot, int kchunk, int rowoff,
+                            int nrows_total, float2* part, unsigned* status, unsigned long long wait_ns,
+                            cudaStream_t st);
 int lelph_launch_gs_gemm(int fp64, const void* A, const void* B, int nrows, int nb, int Ktot, int kchunk,
                          int rowoff, int nrows_total, void* part, cudaStream_t st);
 void lelph_launch_gs_reduce(int fp64, const void* part, long long nel, int nchunks, double invM, double2* glocal,
