@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="mixed_f16")
     p.add_argument("--fp64-pairs", type=int, default=64)
-    p.add_argument("--cpu-pairs", type=int, default=3)
+    p.add_argument("--cpu-pairs", type=int, default=16)
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--profile-case", type=int, default=0,
@@ -247,30 +247,53 @@ def ref_binary(single=True):
     return exe if os.access(exe, os.X_OK) else None
 
 
-class RefRunner:
-    """Runs the compiled reference on single (q, k) pairs of a system: one
-    process per pair, the k-point chosen through the reference's own k-pool
-    split (one pool per full-BZ k, this process = pool k), OpenMP over every
-    host core; the time is the harness's wall time of the stage calls (input
-    loading excluded)."""
+def openblas_path():
+    """An OpenBLAS shared library for the reference's GEMMs (its recipe links
+    -lopenblas): the one SciPy ships, if SciPy is installed."""
+    import glob
+    try:
+        import scipy
+    except ImportError:
+        return ""
+    d = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    libs = sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))
+    return libs[0] if libs else ""
 
-    def __init__(self, s, exe, threads):
+
+class RefRunner:
+    """Runs the compiled reference on (q, k) pairs of a system the way an MPI
+    run of it with one k pool per rank does (nkpools = ranks, one rank per
+    core, src/elph/compute_elph_matq.c:51-54): one process per pair, all of a
+    batch at once, each the pool of its k-point (one pool per full-BZ k) with
+    one thread; the time of a batch is the longest of the harness's wall
+    times of the stage calls (input loading excluded)."""
+
+    def __init__(self, s, exe):
         import tempfile
         from letzelphc_gb300 import synth
-        self.s, self.exe, self.threads = s, exe, threads
+        self.s, self.exe = s, exe
         self.dir = tempfile.mkdtemp(prefix="lelph_ref_")
         self.sysf = os.path.join(self.dir, "system.bin")
         synth.write_system(s, self.sysf)
+        self.blas = openblas_path()
 
-    def pair(self, iq, k):
-        env = dict(os.environ, OMP_NUM_THREADS=str(self.threads), LELPH_REF_QPT=str(iq),
-                   LELPH_REF_KPOOLS=str(self.s.nk_bz), LELPH_REF_KPOOL=str(k))
-        r = subprocess.run([self.exe, self.sysf, os.path.join(self.dir, "g.bin")], env=env, check=True,
-                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
-        for line in r.stderr.splitlines():
-            if "stage_seconds" in line:
-                return float(line.split()[-1])
-        raise RuntimeError("the reference harness printed no stage time")
+    def pairs(self, items):
+        procs = []
+        for i, (iq, k) in enumerate(items):
+            env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", LELPH_REF_QPT=str(iq),
+                       LELPH_REF_KPOOLS=str(self.s.nk_bz), LELPH_REF_KPOOL=str(k), LELPH_REF_BLAS=self.blas)
+            procs.append(subprocess.Popen([self.exe, self.sysf, os.path.join(self.dir, f"g{i}.bin")], env=env,
+                                          stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True))
+        worst = 0.0
+        for p in procs:
+            _, err = p.communicate()
+            if p.returncode != 0:
+                raise RuntimeError(f"the reference harness failed: {err[-400:]}")
+            t = [float(line.split()[-1]) for line in err.splitlines() if "stage_seconds" in line]
+            if not t:
+                raise RuntimeError("the reference harness printed no stage time")
+            worst = max(worst, t[0])
+        return worst
 
     def close(self):
         import shutil
@@ -288,21 +311,23 @@ def run_reference(args):
     rng = np.random.default_rng(0)
     ts, es = [], []
     if exe:
-        # the reference's compiled stage, one (k, q) pair of the workload per step
-        rr = RefRunner(s, exe, cores)
+        # the reference's compiled stage: per step one random (k, q) pair of the
+        # workload on every host core, one process (k pool) per core
+        rr = RefRunner(s, exe)
         try:
-            rr.pair(0, 0)   # warm-up: page cache, OpenMP start-up (a new process each step)
+            rr.pairs([(0, k) for k in range(cores)])   # warm-up: page cache, library loading
             for _ in range(args.steps):
-                iq, k = int(rng.integers(len(s.qpts))), int(rng.integers(s.nk_bz))
-                ts.append(rr.pair(iq, k))
-                es.append(g_elems(s, 1))
+                items = [(int(rng.integers(len(s.qpts))), int(rng.integers(s.nk_bz))) for _ in range(cores)]
+                ts.append(rr.pairs(items))
+                es.append(g_elems(s, cores))
         finally:
             rr.close()
         warm = 1
-        kind, sample = "reference", f"1 random (k, q) pair per step, {args.steps} steps"
+        kind, sample = "reference", f"{cores} random (k, q) pairs per step (one per core), {args.steps} steps"
         build = ("the reference's own per-q stage (compute_and_write_elphq and its callees, unmodified sources) "
-                 "in its default single-precision build, gcc -O3 -fopenmp -DELPH_OMP_PARALLEL_BUILD, against "
-                 "single-rank MPI / FFTW-API / CBLAS stand-ins, OpenMP on every host core")
+                 "in its default single-precision build, gcc -O3 -fopenmp -DELPH_OMP_PARALLEL_BUILD, one "
+                 "process per core as the k pools of an MPI run, against single-rank MPI, FFTW-API (in-house "
+                 "mixed-radix FFT) and CBLAS (OpenBLAS when SciPy ships one) stand-ins")
         dtype = "f32"
     else:
         import multiprocessing as mp
@@ -517,14 +542,15 @@ def run_ours(args):
         exe = ref_binary(single=True)
         if exe:
             cores = os.cpu_count() or 1
-            rr = RefRunner(s, exe, cores)
+            items = [(i % nq, (37 * i + 5) % nk) for i in range(cores * max(1, args.cpu_pairs // cores))]
+            rr = RefRunner(s, exe)
             try:
-                t = sum(rr.pair(iq, k) for iq, k in pairs)
+                t = sum(rr.pairs(items[i:i + cores]) for i in range(0, len(items), cores))
             finally:
                 rr.close()
-            cpu = {"value": g_elems(s, len(pairs)) / t, "unit": "g_elements/s", "cores": cores, "kind": "reference",
-                   "sample": f"{len(pairs)} (k,q) pairs of the workload, the reference's default single-precision "
-                             f"build, OpenMP on every host core, one process per pair"}
+            cpu = {"value": g_elems(s, len(items)) / t, "unit": "g_elements/s", "cores": cores, "kind": "reference",
+                   "sample": f"{len(items)} (k,q) pairs of the workload, the reference's default single-precision "
+                             f"build, one process (k pool) per core"}
         else:
             t, e = cpu_port_sample(s, pairs)
             cpu = {"value": e / t, "unit": "g_elements/s", "cores": 1, "kind": "port",
@@ -877,6 +903,27 @@ def run_gspace(args):
     gemm_flops = 8.0 * s.nmodes * s.nbnds * s.nbnds * s.nspinor * npw * s.nspin  # complex MACs x 8 per pair
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 (non-tensor) rate at the maximum SM clock
     elems = npairs * gsz
+    tc = args.precision != "fp64" and os.environ.get("LELPH_GS_TC", "1") != "0"
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    if tc:
+        # three TF32 products (hi hi, hi lo, lo hi) of the real GEMM; TF32 runs at
+        # half the bf16 rate of the tensor cores
+        tflops = 3 * gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 if d["gs_gemm_ms"] else None
+        tpeak = (peaks.get("bf16_tflops") or 1900.0) / 2
+        roof = {"kernel": "k_gs_gemm_tc (split-TF32 tcgen05 GEMM)", "bound": "tensor", "achieved": tflops,
+                "peak": tpeak, "unit": "TFLOP/s", "frac": tflops / tpeak if tflops else None,
+                "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (of measured): TF32 tensor rate"
+                if peaks else "half of the fallback bf16 peak", "flops_per_pair": 3 * gemm_flops, "traffic": None}
+    else:
+        roof = {"kernel": "k_gs_gemm_f32x2", "bound": "fp32",
+                "achieved": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 if d["gs_gemm_ms"] else None,
+                "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 / fp32_peak if d["gs_gemm_ms"] else None,
+                "peak_source": "nominal GB300 FP32 SIMT rate at 2070 MHz (no measured FP32 peak)",
+                "flops_per_pair": gemm_flops, "traffic": None}
     line = {"metric": "g elements/s per GB300 on the G-space route (16-atom cell, 200 bands)",
             "value": elems / (ms * 1e-3), "unit": "g_elements/s", "n_gpus": 1, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -887,12 +934,7 @@ def run_gspace(args):
                        "timing": "CUDA events on the library stream, device-resident inputs and output"},
             "ms_per_pair": ms / npairs, "kernel_ms_per_pair": d, "clocks": clk,
             "gpu_launches": int(p1["kernel_launches"] - p0["kernel_launches"]),
-            "roofline": {"kernel": "k_gs_gemm_f32x2", "bound": "fp32",
-                         "achieved": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 if d["gs_gemm_ms"] else None,
-                         "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": gemm_flops / (d["gs_gemm_ms"] * 1e-3) / 1e12 / fp32_peak if d["gs_gemm_ms"] else None,
-                         "peak_source": "nominal GB300 FP32 SIMT rate at 2070 MHz (no measured FP32 peak)",
-                         "flops_per_pair": gemm_flops, "traffic": None}}
+            "roofline": roof}
     print(json.dumps(line), flush=True)
     return 0
 
