@@ -60,12 +60,13 @@ def parse():
     p.add_argument("--profile-case", type=int, default=0,
                    help="profiling case for ncu: this many (k, q) pairs of one q, one step, no extras")
     p.add_argument("--workload", default="elph",
-                   choices=["elph", "dmats", "star", "dvscf", "configs", "gspace", "batch"],
+                   choices=["elph", "dmats", "star", "dvscf", "configs", "gspace", "batch", "tune"],
                    help="elph: the per-q stage (default); dmats: the electronic representation matrices "
                         "of the same system (every symmetry x full-BZ k); star: the per-q stage with the "
                         "q-star expansion of each of the 8 q; dvscf: the dV_scf ingest of the 8 q from QE's "
                         "file layout; configs: mixed vs FP64 rate and error on every config's full size; "
-                        "batch: the batched uneven workload in one call, per q and per (k, q) call")
+                        "batch: the batched uneven workload in one call, per q and per (k, q) call; "
+                        "tune: the measured route and tile choice on every config's shape")
     p.add_argument("--dmat-syms", type=int, default=0, help="dmats profiling case: only this many symmetries")
     p.add_argument("--configs", default="", help="configs workload: comma-separated subset (default: all)")
     p.add_argument("--small", action="store_true",
@@ -1139,10 +1140,42 @@ def run_batch(args):
     return 0
 
 
+def run_tune(args):
+    """lelph_gpu_tune on every configuration's shape (its first q, the first
+    four full-BZ k-points as the sample): the measured time per pair of each
+    candidate and the choice -- the route table of the library."""
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from letzelphc_gb300 import synth
+    from letzelphc_gb300.build import build_library
+    from letzelphc_gb300.elph import tune
+    build_library()
+    names = args.configs.split(",") if args.configs else CONFIG_NAMES
+    out = {}
+    for name in names:
+        ov = {"qpts": [tuple(q) for q in _c4_qpts()[1:2]]} if name == "c4" else {}
+        s = synth.make_system(name, ov)
+        iq = 1 if len(s.qpts) > 1 else 0
+        rec = {}
+        for prec in (args.precision, "fp64"):
+            rec[prec] = tune(s, prec, iq=iq, npairs=4, device=local)
+        out[name] = rec
+        print(json.dumps({name: rec}), file=sys.stderr, flush=True)
+        del s
+    print(json.dumps({"workload": "lelph_gpu_tune on every configuration's shape (first q with a nonzero "
+                                  "vector, 4 full-BZ k-points per candidate)", "configs": out}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "tune":
+        return run_tune(args)
     if args.workload == "configs":
         return run_configs(args)
     if args.workload == "gspace":

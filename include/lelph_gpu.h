@@ -96,7 +96,26 @@ typedef struct lelph_gpu_desc
     int precision;                 /* LELPH_GPU_FP64 / LELPH_GPU_MIXED_F16 / LELPH_GPU_MIXED_BF16 */
     int device;                    /* CUDA device ordinal */
     int route;                     /* LELPH_GPU_ROUTE_* (0 = automatic) */
+    int tile_points;               /* real-space route, mixed form: grid points per stage of the tensor-core
+                                      pipeline, 64 or 32 (0 = the library's choice) */
+    int gs_gemm;                   /* G-space route, mixed form: LELPH_GPU_GS_GEMM_* (0 = tensor cores where
+                                      the band count allows) */
 } lelph_gpu_desc;
+
+#define LELPH_GPU_GS_GEMM_TENSOR 1 /* split-TF32 tcgen05 GEMM */
+#define LELPH_GPU_GS_GEMM_SIMT 2   /* FP32 SIMT GEMM */
+
+/* What lelph_gpu_tune measured and chose. */
+typedef struct lelph_gpu_tuning
+{
+    int route;                     /* chosen LELPH_GPU_ROUTE_REAL / LELPH_GPU_ROUTE_GSPACE */
+    int tile_points;               /* chosen stage size of the real-space route (0 on the G-space route) */
+    int gs_gemm;                   /* chosen GEMM of the G-space route (0 on the real-space route) */
+    int cached;                    /* 1: read from the cache file, nothing was measured */
+    double ms_per_pair[4];         /* device time per (k, q) pair of each candidate: real-space with 64- and
+                                      32-point stages, G-space with the tensor-core and the SIMT GEMM
+                                      (negative: not a candidate for this system or form) */
+} lelph_gpu_tuning;
 
 typedef struct lelph_gpu_stats
 {
@@ -125,6 +144,22 @@ typedef struct lelph_gpu_stats
  * Replaces the per-call setup of elphLocal / add_elphNonLocal
  * (src/dvloc/compute_Vbare_loc.c:93-205, src/nonloc/Vbare_nloc.c:96-245). */
 int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out);
+
+/* Measured choice of the route and the tile options for a system (no
+ * counterpart in the reference, whose FFTW plans are measured per call with
+ * FFTW_MEASURE, src/fft/planner.c:224-306): every candidate the system and
+ * precision allow -- the real-space route with 64- and 32-point stages of the
+ * tensor-core pipeline (when its resident operands fit in half of the device
+ * memory), the G-space route with the tensor-core and the SIMT GEMM -- runs
+ * as its own context on the caller's q (qpt_crys, eigVec, dVscf as in
+ * lelph_gpu_set_q) and the first npairs full-BZ k-points, is timed after a
+ * warm-up, and the fastest is returned; route, tile_points and gs_gemm of
+ * *out fill the same fields of a descriptor.  desc->route, tile_points and
+ * gs_gemm are ignored.  With cache_path (may be NULL) the result is looked up
+ * in, and otherwise appended to, that text file under a key of the system's
+ * sizes, precision and device name. */
+int lelph_gpu_tune(const lelph_gpu_desc* desc, const double qpt_crys[3], const double* eigVec, const double* dVscf,
+                   int npairs, const char* cache_path, lelph_gpu_tuning* out);
 
 /* Replace the plane-wave coefficients of every iBZ k-point
  * ([ik] -> (nspin, nbnds, nspinor, npw) complex); invalidates lelph_gpu_prepare. */

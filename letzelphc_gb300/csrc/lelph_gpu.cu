@@ -887,9 +887,14 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         return bad(LELPH_GPU_ERR_UNSUPPORTED, "the real-space route of the mixed form supports up to 64 bands");
     h->gspace = d.route == LELPH_GPU_ROUTE_GSPACE || !tc_ok;
     {
-        // the mixed G-space GEMM on the tensor cores (LELPH_GS_TC=0: the FP32 SIMT GEMM)
+        // the mixed G-space GEMM on the tensor cores unless the descriptor asks for
+        // the SIMT GEMM (or LELPH_GS_TC=0)
+        if (d.gs_gemm < 0 || d.gs_gemm > LELPH_GPU_GS_GEMM_SIMT) return bad(LELPH_GPU_ERR_INVALID, "gs_gemm");
+        if (d.gs_gemm == LELPH_GPU_GS_GEMM_TENSOR && h->mixed && !lelph_gs_tc_supported(d.nbnds))
+            return bad(LELPH_GPU_ERR_UNSUPPORTED, "the tensor-core G-space GEMM does not take this band count");
         const char* e = std::getenv("LELPH_GS_TC");
-        h->gs_tc = h->mixed && lelph_gs_tc_supported(d.nbnds) && !(e && e[0] == '0');
+        h->gs_tc = h->mixed && lelph_gs_tc_supported(d.nbnds) && d.gs_gemm != LELPH_GPU_GS_GEMM_SIMT &&
+                   !(e && e[0] == '0');
     }
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
@@ -1120,7 +1125,12 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
     {
         if (N % 32 != 0) return bad(LELPH_GPU_ERR_UNSUPPORTED, "grid size must be a multiple of 32");
         if (N % h->g.kpts != 0) h->g.kpts = 32;
-        // override for tests and tuning: LELPH_TC_STAGE = 32 forces 32-point stages
+        // the descriptor's stage size (a tuned choice), or LELPH_TC_STAGE = 32 (tests)
+        if (d.tile_points == 32) h->g.kpts = 32;
+        else if (d.tile_points == 64 && h->g.kpts != 64)
+            return bad(LELPH_GPU_ERR_UNSUPPORTED, "64-point stages do not fit this tile");
+        else if (d.tile_points != 0 && d.tile_points != 64)
+            return bad(LELPH_GPU_ERR_INVALID, "tile_points must be 0, 32 or 64");
         if (const char* e = getenv("LELPH_TC_STAGE"))
             if (atoi(e) == 32) h->g.kpts = 32;
         if (lelph_local_tc_smem_bytes(h->g) > 227 * 1024) return bad(LELPH_GPU_ERR_UNSUPPORTED, "shared memory");
@@ -2777,6 +2787,141 @@ extern "C" int lelph_gpu_debug_partials_extent(int nmodes, int nbnds, int nspin,
     out[0] = lelph_tc_partials_per_pair(g, nchunks) * (size_t)npairs;
     out[1] = wr;
     out[2] = rd;
+    return LELPH_GPU_OK;
+}
+
+// ============================================================== tuning
+
+namespace
+{
+// device time per pair of one candidate context: a warm-up call (preparation,
+// dV windows, kernels loaded), then two timed calls; negative on failure
+double tune_candidate(const lelph_gpu_desc& dc, const double* q, const double* eig, const double* dv, int n)
+{
+    lelph_gpu* h = nullptr;
+    if (lelph_gpu_create(&dc, &h) != LELPH_GPU_OK)
+    {
+        lelph_gpu_destroy(h);
+        return -1.0;
+    }
+    double ms = -1.0;
+    void* gout = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<int> qs(n, 0), ks(n);
+    for (int i = 0; i < n; ++i) ks[i] = i;
+    const size_t bytes = sizeof(float2) * (size_t)n * dc.nmodes * dc.nspin * dc.nbnds * dc.nbnds;
+    if (!h->gspace && h->mixed)
+    {
+        // the real-space route keeps psi(r) of every full-BZ k resident: skip it where
+        // that would take more than half of the device memory (as the automatic route does)
+        const double per_kpt = 24.0 * h->g.nbp * dc.nspin * dc.nspinor;
+        const double resident = per_kpt * (double)h->g.Nx * h->g.Ny * h->g.Nz * dc.nkpts_BZ;
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || resident > 0.5 * (double)tot) goto done;
+    }
+    if (lelph_gpu_set_q(h, 0, q, eig, dv) != LELPH_GPU_OK) goto done;
+    if (cudaMalloc(&gout, bytes) != cudaSuccess)
+    {
+        cudaGetLastError();
+        goto done;
+    }
+    if (run_impl(h, n, qs.data(), ks.data(), 1, 0, LELPH_GPU_OUT_C64, gout, true) != LELPH_GPU_OK) goto done;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) goto done;
+    cudaEventRecord(e0, h->st);
+    for (int r = 0; r < 2; ++r)
+        if (run_impl(h, n, qs.data(), ks.data(), 1, 0, LELPH_GPU_OUT_C64, gout, true) != LELPH_GPU_OK) goto done;
+    cudaEventRecord(e1, h->st);
+    if (cudaEventSynchronize(e1) == cudaSuccess)
+    {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, e0, e1) == cudaSuccess) ms = (double)t / (2.0 * n);
+    }
+done:
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (gout) cudaFree(gout);
+    cudaGetLastError();
+    lelph_gpu_destroy(h);
+    return ms;
+}
+
+std::string tune_key(const lelph_gpu_desc& d)
+{
+    long long npw = 0;
+    for (int i = 0; i < d.nkpts_iBZ; ++i) npw += d.npw[i];
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, d.device);
+    char buf[512];
+    snprintf(buf, sizeof buf, "prec=%d spin=%d spinor=%d mag=%d bands=%d modes=%d fft=%dx%dx%d kBZ=%d npw=%lld dev=%s",
+             d.precision, d.nspin, d.nspinor, d.nmag, d.nbnds, d.nmodes, d.fft_dims[0], d.fft_dims[1],
+             d.fft_dims[2], d.nkpts_BZ, d.nkpts_iBZ ? npw / d.nkpts_iBZ : 0, prop.name);
+    for (char* c = buf; *c; ++c)
+        if (*c == '|' || *c == '\n') *c = '_';
+    return buf;
+}
+}  // namespace
+
+extern "C" int lelph_gpu_tune(const lelph_gpu_desc* desc, const double qpt_crys[3], const double* eigVec,
+                              const double* dVscf, int npairs, const char* cache_path, lelph_gpu_tuning* out)
+{
+    if (!desc || !qpt_crys || !eigVec || !dVscf || !out || npairs < 1) return LELPH_GPU_ERR_INVALID;
+    lelph_gpu_desc d = *desc;
+    if (cudaSetDevice(d.device) != cudaSuccess) return LELPH_GPU_ERR_CUDA;
+    npairs = std::min(npairs, d.nkpts_BZ);
+    memset(out, 0, sizeof(*out));
+    const std::string key = tune_key(d);
+    if (cache_path)
+        if (FILE* f = fopen(cache_path, "r"))
+        {
+            char line[1024];
+            bool hit = false;
+            while (!hit && fgets(line, sizeof line, f))
+            {
+                char* bar = strchr(line, '|');
+                if (!bar || std::string(line, bar - line) != key) continue;
+                hit = sscanf(bar + 1, "%d %d %d %lf %lf %lf %lf", &out->route, &out->tile_points, &out->gs_gemm,
+                             &out->ms_per_pair[0], &out->ms_per_pair[1], &out->ms_per_pair[2],
+                             &out->ms_per_pair[3]) == 7;
+            }
+            fclose(f);
+            if (hit)
+            {
+                out->cached = 1;
+                return LELPH_GPU_OK;
+            }
+        }
+    struct Cand
+    {
+        int route, tile, gemm;
+    };
+    const bool mixed = d.precision != LELPH_GPU_FP64;
+    const Cand cands[4] = {{LELPH_GPU_ROUTE_REAL, 64, 0},
+                           {LELPH_GPU_ROUTE_REAL, 32, 0},
+                           {LELPH_GPU_ROUTE_GSPACE, 0, LELPH_GPU_GS_GEMM_TENSOR},
+                           {LELPH_GPU_ROUTE_GSPACE, 0, LELPH_GPU_GS_GEMM_SIMT}};
+    int best = -1;
+    for (int c = 0; c < 4; ++c)
+    {
+        out->ms_per_pair[c] = -1.0;
+        // the plain form has one real-space kernel and one G-space GEMM
+        if (!mixed && (c == 1 || c == 2)) continue;
+        d.route = cands[c].route;
+        d.tile_points = mixed ? cands[c].tile : 0;
+        d.gs_gemm = mixed ? cands[c].gemm : 0;
+        out->ms_per_pair[c] = tune_candidate(d, qpt_crys, eigVec, dVscf, npairs);
+        if (out->ms_per_pair[c] > 0 && (best < 0 || out->ms_per_pair[c] < out->ms_per_pair[best])) best = c;
+    }
+    if (best < 0) return LELPH_GPU_ERR_UNSUPPORTED;
+    out->route = cands[best].route;
+    out->tile_points = mixed ? cands[best].tile : 0;
+    out->gs_gemm = mixed ? cands[best].gemm : 0;
+    if (cache_path)
+        if (FILE* f = fopen(cache_path, "a"))
+        {
+            fprintf(f, "%s|%d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), out->route, out->tile_points, out->gs_gemm,
+                    out->ms_per_pair[0], out->ms_per_pair[1], out->ms_per_pair[2], out->ms_per_pair[3]);
+            fclose(f);
+        }
     return LELPH_GPU_OK;
 }
 

@@ -42,7 +42,16 @@ class Desc(C.Structure):
         ("ntype", C.c_int), ("nltimesj", C.c_int), ("lmax", C.c_int),
         ("PP_table", _dp), ("Fsign", _dp), ("fCoeff", C.POINTER(_dp)),
         ("precision", C.c_int), ("device", C.c_int), ("route", C.c_int),
+        ("tile_points", C.c_int), ("gs_gemm", C.c_int),
     ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("route", C.c_int), ("tile_points", C.c_int), ("gs_gemm", C.c_int), ("cached", C.c_int),
+                ("ms_per_pair", C.c_double * 4)]
+
+
+GS_GEMMS = {"auto": 0, "tensor": 1, "simt": 2}
 
 
 class Stats(C.Structure):
@@ -63,7 +72,7 @@ EXPORTS = [
     "lelph_gpu_last_error", "lelph_gpu_destroy", "lelph_gpu_run_device_noalloc",
     "lelph_gpu_set_local_pseudo", "lelph_gpu_dvlocq", "lelph_gpu_set_q_induced", "lelph_gpu_rotate_dvscf",
     "lelph_gpu_dmats", "lelph_gpu_compute_elphq_star", "lelph_gpu_set_q_dvscf_qe",
-    "lelph_gpu_debug_partials_extent", "lelph_gpu_set_wait_limit",
+    "lelph_gpu_debug_partials_extent", "lelph_gpu_set_wait_limit", "lelph_gpu_tune",
 ]
 
 _lib = None
@@ -90,6 +99,7 @@ def load_library(path: str = LIB_PATH):
     L.lelph_gpu_dmats.argtypes = [vp, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_longlong, _dp]
     L.lelph_gpu_debug_partials_extent.argtypes = [C.c_int] * 5 + [C.POINTER(C.c_ulonglong)]
     L.lelph_gpu_set_wait_limit.argtypes = [vp, C.c_ulonglong]
+    L.lelph_gpu_tune.argtypes = [C.POINTER(Desc), _dp, _dp, _dp, C.c_int, C.c_char_p, C.POINTER(Tuning)]
     L.lelph_gpu_set_q_dvscf_qe.argtypes = [vp, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _dp]
     L.lelph_gpu_compute_elphq_star.argtypes = [vp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int,
                                                _ip, C.c_int, vp]
@@ -126,58 +136,90 @@ def _ptr(a, t=_dp):
     return a.ctypes.data_as(t)
 
 
+def describe(s, precision="fp64", device=0, route="auto", tile_points=0, gs_gemm="auto", keep=None):
+    """lelph_gpu_desc of a system (the fields of the reference's Lattice, WFC[]
+    and Pseudo under their own names); every array it points to is appended
+    to `keep`, which must outlive the descriptor's use."""
+    keep = [] if keep is None else keep
+    d = Desc()
+
+    def arr(x, dt):
+        a = np.ascontiguousarray(x, dtype=dt)
+        keep.append(a)
+        return a
+
+    d.natom, d.nsym, d.timerev = s.natom, len(s.sym_R), int(s.timerev)
+    d.nspin, d.nspinor, d.nbnds, d.nmag, d.nmodes = s.nspin, s.nspinor, s.nbnds, s.nmag, s.nmodes
+    d.nkpts_iBZ, d.nkpts_BZ = s.nk_ibz, s.nk_bz
+    d.fft_dims[:] = list(s.fft_dims)
+    d.alat_vec = _ptr(arr(s.alat, np.float64))
+    d.blat_vec = _ptr(arr(s.blat, np.float64))
+    d.atomic_pos = _ptr(arr(s.atom_pos, np.float64))
+    d.atom_type = _ptr(arr(s.atom_type, np.int32), _ip)
+    d.kpt_iredBZ = _ptr(arr(s.kibz, np.float64))
+    d.kpt_fullBZ_crys = _ptr(arr(s.kbz_crys, np.float64))
+    d.kmap = _ptr(arr(s.kmap, np.int32), _ip)
+    d.sym_Rmat = _ptr(arr(s.sym_R, np.float64))
+    d.sym_tau = _ptr(arr(s.sym_tau, np.float64))
+    d.sym_time_rev = _ptr(arr(s.sym_trev, np.int32), _ip)
+    d.is_soc_present = int(s.is_soc_present)
+    d.npw = _ptr(arr([len(g) for g in s.gvec], np.int32), _ip)
+    gv = (_dp * s.nk_ibz)(*[_ptr(arr(g, np.float64)) for g in s.gvec])
+    fk = (_dp * s.nk_ibz)(*[_ptr(arr(f, np.float64)) for f in s.Fk])
+    keep += [gv, fk]
+    d.gvec, d.Fk = gv, fk
+    wf = (_dp * s.nk_ibz)(*[_ptr(arr(w, np.complex128)) for w in s.wfc])
+    keep.append(wf)
+    d.wfc = wf
+    d.ntype, d.nltimesj, d.lmax = s.ntype, s.nltimesj, s.lmax
+    d.PP_table = _ptr(arr(s.PP_table, np.float64))
+    d.Fsign = _ptr(arr(s.Fsign, np.float64))
+    if s.fCoeff is not None:
+        fc = (_dp * len(s.fCoeff))(*[(_ptr(arr(f, np.complex128)) if f is not None else _dp()) for f in s.fCoeff])
+        keep.append(fc)
+        d.fCoeff = fc
+    else:
+        d.fCoeff = C.POINTER(_dp)()
+    d.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    d.device = device
+    d.route = ROUTES[route] if isinstance(route, str) else int(route)
+    d.tile_points = int(tile_points)
+    d.gs_gemm = GS_GEMMS[gs_gemm] if isinstance(gs_gemm, str) else int(gs_gemm)
+    return d
+
+
+def tune(s, precision="mixed", iq=0, npairs=4, device=0, cache_path=None):
+    """lelph_gpu_tune on the system's q-point iq and its first npairs full-BZ
+    k-points: {"route", "tile_points", "gs_gemm", "cached", "ms_per_pair"}
+    (route as a name; pass the three to LelphGPU)."""
+    L = load_library()
+    keep = []
+    d = describe(s, precision, device, keep=keep)
+    q = np.ascontiguousarray(s.qpts[iq], dtype=np.float64)
+    e = np.ascontiguousarray(s.eigVec[iq], dtype=np.complex128)
+    v = np.ascontiguousarray(s.dVscf[iq], dtype=np.complex128)
+    t = Tuning()
+    rc = L.lelph_gpu_tune(C.byref(d), _ptr(q), _ptr(e), _ptr(v), int(npairs),
+                          cache_path.encode() if cache_path else None, C.byref(t))
+    if rc != 0:
+        raise LelphError(rc, L.lelph_gpu_strerror(rc).decode())
+    names = {v: k for k, v in ROUTES.items()}
+    return {"route": names[t.route], "tile_points": t.tile_points, "gs_gemm": t.gs_gemm, "cached": bool(t.cached),
+            "ms_per_pair": {"real-space, 64-point stages": t.ms_per_pair[0],
+                            "real-space, 32-point stages": t.ms_per_pair[1],
+                            "G-space, tensor-core GEMM": t.ms_per_pair[2],
+                            "G-space, SIMT GEMM": t.ms_per_pair[3]}}
+
+
 class LelphGPU:
     """One device context holding a system (the reference's Lattice, WFC[],
     Pseudo) and any number of q slots."""
 
-    def __init__(self, s, precision="fp64", device=0, route="auto"):
+    def __init__(self, s, precision="fp64", device=0, route="auto", tile_points=0, gs_gemm="auto"):
         L = load_library()
         self._L = L
         self._keep = []
-        d = Desc()
-        keep = self._keep
-
-        def arr(x, dt):
-            a = np.ascontiguousarray(x, dtype=dt)
-            keep.append(a)
-            return a
-
-        d.natom, d.nsym, d.timerev = s.natom, len(s.sym_R), int(s.timerev)
-        d.nspin, d.nspinor, d.nbnds, d.nmag, d.nmodes = s.nspin, s.nspinor, s.nbnds, s.nmag, s.nmodes
-        d.nkpts_iBZ, d.nkpts_BZ = s.nk_ibz, s.nk_bz
-        d.fft_dims[:] = list(s.fft_dims)
-        d.alat_vec = _ptr(arr(s.alat, np.float64))
-        d.blat_vec = _ptr(arr(s.blat, np.float64))
-        d.atomic_pos = _ptr(arr(s.atom_pos, np.float64))
-        d.atom_type = _ptr(arr(s.atom_type, np.int32), _ip)
-        d.kpt_iredBZ = _ptr(arr(s.kibz, np.float64))
-        d.kpt_fullBZ_crys = _ptr(arr(s.kbz_crys, np.float64))
-        d.kmap = _ptr(arr(s.kmap, np.int32), _ip)
-        d.sym_Rmat = _ptr(arr(s.sym_R, np.float64))
-        d.sym_tau = _ptr(arr(s.sym_tau, np.float64))
-        d.sym_time_rev = _ptr(arr(s.sym_trev, np.int32), _ip)
-        d.is_soc_present = int(s.is_soc_present)
-        d.npw = _ptr(arr([len(g) for g in s.gvec], np.int32), _ip)
-        gv = (_dp * s.nk_ibz)(*[_ptr(arr(g, np.float64)) for g in s.gvec])
-        fk = (_dp * s.nk_ibz)(*[_ptr(arr(f, np.float64)) for f in s.Fk])
-        keep += [gv, fk]
-        d.gvec, d.Fk = gv, fk
-        self._wfc_arrays = [arr(w, np.complex128) for w in s.wfc]
-        wf = (_dp * s.nk_ibz)(*[_ptr(w) for w in self._wfc_arrays])
-        keep.append(wf)
-        d.wfc = wf
-        d.ntype, d.nltimesj, d.lmax = s.ntype, s.nltimesj, s.lmax
-        d.PP_table = _ptr(arr(s.PP_table, np.float64))
-        d.Fsign = _ptr(arr(s.Fsign, np.float64))
-        if s.fCoeff is not None:
-            fc = (_dp * len(s.fCoeff))(*[(_ptr(arr(f, np.complex128)) if f is not None else _dp()) for f in s.fCoeff])
-            keep.append(fc)
-            d.fCoeff = fc
-        else:
-            d.fCoeff = C.POINTER(_dp)()
-        d.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-        d.device = device
-        d.route = ROUTES[route] if isinstance(route, str) else int(route)
+        d = self.desc = describe(s, precision, device, route, tile_points, gs_gemm, self._keep)
         h = C.c_void_p()
         rc = L.lelph_gpu_create(C.byref(d), C.byref(h))
         if rc != 0:
