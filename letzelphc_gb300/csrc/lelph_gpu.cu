@@ -2810,11 +2810,12 @@ double tune_candidate(const lelph_gpu_desc& dc, const double* q, const double* e
     std::vector<int> qs(n, 0), ks(n);
     for (int i = 0; i < n; ++i) ks[i] = i;
     const size_t bytes = sizeof(float2) * (size_t)n * dc.nmodes * dc.nspin * dc.nbnds * dc.nbnds;
-    if (!h->gspace && h->mixed)
+    if (!h->gspace)
     {
         // the real-space route keeps psi(r) of every full-BZ k resident: skip it where
         // that would take more than half of the device memory (as the automatic route does)
-        const double per_kpt = 24.0 * h->g.nbp * dc.nspin * dc.nspinor;
+        const double per_kpt = h->mixed ? 24.0 * h->g.nbp * dc.nspin * dc.nspinor
+                                        : 16.0 * dc.nspin * dc.nbnds * dc.nspinor;
         const double resident = per_kpt * (double)h->g.Nx * h->g.Ny * h->g.Nz * dc.nkpts_BZ;
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || resident > 0.5 * (double)tot) goto done;
