@@ -1101,18 +1101,28 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         // spinors): real-space, the split sandwich, 12 rows (2 nbp) M tensor flops
         // at 7.6e14/s; G-space, the pruned plane and x passes at 3.6e-12 s per grid
         // point of a row plus the GEMM over the sphere, 8 rows nb npw flops at
-        // 4.7e13/s.  (The plain form stays on the real-space route when it fits:
-        // it is the validation form, and the allocation-free entry point runs
-        // only that route; LELPH_GPU_ROUTE_GSPACE selects the other.)
+        // 1.8e14/s (the tensor-core GEMM; 4.7e13/s with the SIMT one).
+        // lelph_gpu_tune measures instead of modelling.
         if (!h->gspace && h->mixed)
         {
             double npw_avg = 0;
             for (int ik = 0; ik < d.nkpts_iBZ; ++ik) npw_avg += h->npw[ik];
             npw_avg /= d.nkpts_iBZ;
             const double rows = (double)d.nmodes * d.nbnds * d.nspinor;
+            const double gemm_rate = lelph_gs_tc_supported(d.nbnds) ? 1.8e14 : 4.7e13;
             const double t_real = 12.0 * rows * (2.0 * h->g.nbp) * (double)N / 7.6e14;
-            const double t_gs = rows * (double)N * 3.6e-12 + 8.0 * rows * d.nbnds * npw_avg / 4.7e13;
+            const double t_gs = rows * (double)N * 3.6e-12 + 8.0 * rows * d.nbnds * npw_avg / gemm_rate;
             if (t_gs < t_real) h->gspace = true;
+        }
+        // Plain (FP64) form: the G-space route wherever its planes fit in shared
+        // memory; measured 4-5x faster per pair than the FP64 real-space sandwich
+        // on every configuration's shape (the FP64 SIMT contraction over the whole
+        // grid costs more than the pruned FP64 transforms plus the sphere GEMM).
+        if (!h->gspace && !h->mixed)
+        {
+            GsGeom gg{h->g.Nx, h->g.Ny, h->g.Nz, d.nbnds, d.nspinor, d.nmag, 0};
+            if (lelph_gs_plane_smem(gg, 1) <= 220 * 1024 && lelph_gs_xpass_smem(gg, 1) <= 220 * 1024)
+                h->gspace = true;
         }
     }
     if (h->gspace)

@@ -29,7 +29,7 @@ def test_noalloc_matches_run_device(name, ov, prec):
     torch = pytest.importorskip("torch")
     s = synth.make_system(name, ov)
     L = load_library()
-    with LelphGPU(s, prec) as ctx:
+    with LelphGPU(s, prec, route="real") as ctx:   # the route whose buffers are all set up in advance
         for iq in range(len(s.qpts)):
             ctx.set_q(iq, s.qpts[iq], s.eigVec[iq], s.dVscf[iq])
         ctx.prepare()
@@ -69,7 +69,7 @@ def test_noalloc_matches_run_device(name, ov, prec):
 def test_noalloc_requires_prepare():
     s = synth.make_system("c0", {"kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)], "nbnds": 2})
     L = load_library()
-    with LelphGPU(s, "fp64") as ctx:
+    with LelphGPU(s, "fp64", route="real") as ctx:
         ctx.set_q(0, s.qpts[0], s.eigVec[0], s.dVscf[0])
         qs = np.zeros(1, np.int32)
         ks = np.zeros(1, np.int32)
