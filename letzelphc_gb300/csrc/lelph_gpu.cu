@@ -50,6 +50,8 @@ struct lelph_gpu
     lelph_gpu_desc d;
     int device = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t st_copy = nullptr;    // copies of finished output batches to the host (run)
+    cudaEvent_t evc[2] = {nullptr, nullptr};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evg0 = nullptr, evg1 = nullptr;  // per-kernel timing of the G-space route (profiling on)
     bool profiling = false;
@@ -635,6 +637,10 @@ extern "C" void lelph_gpu_destroy(lelph_gpu* h)
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->evg0) cudaEventDestroy(h->evg0);
     if (h->evg1) cudaEventDestroy(h->evg1);
+    if (h->st_copy) cudaStreamSynchronize(h->st_copy);
+    for (cudaEvent_t e : h->evc)
+        if (e) cudaEventDestroy(e);
+    if (h->st_copy) cudaStreamDestroy(h->st_copy);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
 }
@@ -1150,7 +1156,11 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
 
     // ---- device
     if (cudaSetDevice(h->device) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "cudaSetDevice");
-    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return bad(LELPH_GPU_ERR_CUDA, "stream");
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->st_copy, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->evc[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->evc[1], cudaEventDisableTiming) != cudaSuccess)
+        return bad(LELPH_GPU_ERR_CUDA, "stream");
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
     cudaEventCreate(&h->evg0);
@@ -2235,9 +2245,22 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     if (fp64_local) per_pair = sizeof(double2) * (size_t)d.nspin * nrows * d.nbnds;
     else per_pair = sizeof(float) * lelph_tc_partials_per_pair(g, h->nchunks);
     int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)n, (4ull << 30) / per_pair));
+    // Output to host memory: the pairs go in four or more batches, and each
+    // batch's result is copied on the copy stream while the next one computes
+    // (the copy of batch i is issued after batch i + 1 is launched, so a
+    // pageable destination, whose copy blocks the host, still overlaps).
+    const bool overlap = !out_device && n >= 256;
+    if (overlap) batch = std::min(batch, (n + 3) / 4);
     rc = ensure(h, fp64_local ? h->d_glocal : h->d_partials, per_pair * batch);
     if (rc) return rc;
-    for (int p0 = 0; p0 < n; p0 += batch)
+    auto copy_batch = [&](int q0, int qn, int ev) -> int {
+        CUDA_TRY(h, cudaStreamWaitEvent(h->st_copy, h->evc[ev], 0));
+        CUDA_TRY(h, cudaMemcpyAsync((char*)g_out + esz * gsz * q0, (const char*)gdev + esz * gsz * q0,
+                                    esz * gsz * qn, cudaMemcpyDeviceToHost, h->st_copy));
+        return LELPH_GPU_OK;
+    };
+    int prev0 = -1, prevn = 0, ib = 0;
+    for (int p0 = 0; p0 < n; p0 += batch, ++ib)
     {
         int nb = std::min(batch, n - p0);
         const PairInfo* dp = (const PairInfo*)h->d_pairs.p + p0;
@@ -2264,8 +2287,26 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         h->stats.finish_ms += tstop(h);
         h->stats.kernel_launches += h->gspace ? 1 : 2;  // gs_local counts its own launches
         CUDA_TRY(h, cudaGetLastError());
+        if (overlap)
+        {
+            CUDA_TRY(h, cudaEventRecord(h->evc[ib & 1], h->st));
+            if (prev0 >= 0)
+            {
+                rc = copy_batch(prev0, prevn, (ib - 1) & 1);
+                if (rc) return rc;
+            }
+            prev0 = p0;
+            prevn = nb;
+        }
     }
-    if (!out_device) CUDA_TRY(h, cudaMemcpyAsync(g_out, gdev, esz * gsz * n, cudaMemcpyDeviceToHost, h->st));
+    if (overlap)
+    {
+        rc = copy_batch(prev0, prevn, (ib - 1) & 1);
+        if (rc) return rc;
+        CUDA_TRY(h, cudaStreamSynchronize(h->st_copy));
+    }
+    else if (!out_device)
+        CUDA_TRY(h, cudaMemcpyAsync(g_out, gdev, esz * gsz * n, cudaMemcpyDeviceToHost, h->st));
     rc = check_status(h);
     if (rc) return rc;
     h->stats.pairs_done += n;
