@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
@@ -322,8 +323,10 @@ __device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int ns
     return w;
 }
 
-template <int BF16, int KP>
-__global__ void __launch_bounds__(TC_MAX_THREADS, 1)
+// PW producer warps (8, or 16 with 64-point stages): PW / 4 per TMEM lane
+// quadrant, each forming KP / (PW / 4) points of every stage.
+template <int BF16, int KP, int PW>
+__global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
                int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
@@ -358,11 +361,11 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
         for (int s = 0; s < NST; ++s)
         {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1 + 8);
+            mbar_init(&empty[s], 1 + PW);
         }
         for (int a = 0; a < NA; ++a)
         {
-            mbar_init(&aready[a], 8);
+            mbar_init(&aready[a], PW);
             mbar_init(&afree[a], 1);
         }
         for (int b = 0; b < NACC; ++b)
@@ -526,10 +529,10 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             if (last_commit) mbar_wait_bounded(last_commit, last_par);
         }
     }
-    else if (warp < 10)
+    else if (warp < 2 + PW)
     {
         // ---------------- A producers: lane quadrant q = warp % 4 (rows 32q..32q+31),
-        // half h of the stage's 64 points
+        // part h of PW / 4 of the stage's points
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
@@ -576,11 +579,12 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 }
                 tc_fence_after();
                 const uint8_t* st = sm + s * L.stage_bytes;
-                // points h*KP/2 .. (h+1)*KP/2 - 1 of the stage, in 16-point blocks
+                // points h KP / NQ .. (h + 1) KP / NQ - 1 of the stage, in 16-point blocks
+                constexpr int NQ = PW / 4;
 #pragma unroll 1
-                for (int b = 0; b < KP / 32; ++b)
+                for (int b = 0; b < KP / (16 * NQ); ++b)
                 {
-                    const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
+                    const int p0 = h * (KP / NQ) + 16 * b;  // first point of the block in the stage
                     const int pb = p0 >> 4;                // 16-point psi block
                     const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
                     const uint8_t* pp[2];
@@ -616,10 +620,10 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
             }
         }
     }
-    else if (warp < 10 + ndrain)
+    else if (warp < 2 + PW + ndrain)
     {
         // ---------------- drain warps: TMEM lane quadrant warp%4, 64-column half
-        const int dw = warp - 10;
+        const int dw = warp - (2 + PW);
         const int q = warp & 3;
         const int c0 = (dw >> 2) * 64;
         const int nc = min(64, NT - c0);
@@ -698,27 +702,34 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(units, std::max(1, nsm));
     const int smem = lelph_local_tc_smem_bytes(g);
-    const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
+    const int ndrain = 4 * ((2 * g.nbp + 63) / 64);
+    // sixteen producer warps where the tile has one column group of drains and
+    // 64-point stages (LELPH_TC_PRODUCERS = 16), else eight
+    int pw = 8;
+    if (const char* e = getenv("LELPH_TC_PRODUCERS"))
+        if (atoi(e) == 16 && ndrain == 4 && g.kpts == 64 && !ab_bf16) pw = 16;
+    const int threads = 32 * (2 + pw + ndrain);
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (units <= 0) return;
-#define TC_LAUNCH(BF, KPV)                                                                                       \
+#define TC_LAUNCH(BF, KPV, PWV)                                                                                  \
     do                                                                                                           \
     {                                                                                                            \
-        cudaFuncSetAttribute(k_local_tc<BF, KPV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
-        k_local_tc<BF, KPV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles,     \
-                                                         (int)units, partials, status, wait_ns);                 \
+        cudaFuncSetAttribute(k_local_tc<BF, KPV, PWV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);        \
+        k_local_tc<BF, KPV, PWV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, \
+                                                              (int)units, partials, status, wait_ns);            \
     } while (0)
     if (ab_bf16)
     {
-        if (g.kpts == 64) TC_LAUNCH(1, 64);
-        else TC_LAUNCH(1, 32);
+        if (g.kpts == 64) TC_LAUNCH(1, 64, 8);
+        else TC_LAUNCH(1, 32, 8);
     }
     else
     {
-        if (g.kpts == 64) TC_LAUNCH(0, 64);
-        else TC_LAUNCH(0, 32);
+        if (g.kpts == 64 && pw == 16) TC_LAUNCH(0, 64, 16);
+        else if (g.kpts == 64) TC_LAUNCH(0, 64, 8);
+        else TC_LAUNCH(0, 32, 8);
     }
 #undef TC_LAUNCH
 }
