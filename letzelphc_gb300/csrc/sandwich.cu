@@ -24,7 +24,6 @@
 #include <stdint.h>
 
 #include <algorithm>
-#include <cstdlib>
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
@@ -292,6 +291,94 @@ __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const floa
     }
 }
 
+// One pipeline stage of the merged split product (NT <= 64): per 16-wide K
+// step k, A_hi [B_hi; B_lo] (N = 2 NT) into dacc and A_lo B_hi (N = NT) into
+// dacc2.  B's descriptor advances by 32 bytes per step inside a 128-byte K
+// atom (d0: atom 0, d1: atom 1) and A's tensor-memory column by 8, all by
+// immediates inside one asm block, so that the issuing thread spends about
+// three instructions per MMA pair: it shares its SM sub-partition with FMA-bound
+// producer warps, and every instruction of it waits for an issue slot.
+template <int KP>
+__device__ __forceinline__ void umma_stage_merged(uint32_t dacc, uint32_t dacc2, uint32_t ahi, uint64_t d0,
+                                                  uint64_t d1, uint32_t idesc2, uint32_t idesc, uint32_t en);
+template <>
+__device__ __forceinline__ void umma_stage_merged<64>(uint32_t dacc, uint32_t dacc2, uint32_t ahi, uint64_t d0,
+                                                      uint64_t d1, uint32_t idesc2, uint32_t idesc, uint32_t en)
+{
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t.reg .b64 d;\n\t.reg .b32 a;\n\t"
+        "setp.ne.b32 p, %7, 0;\n\tsetp.eq.b32 q, %7, %7;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%2], %3, %5, p;\n\t"
+        "add.u32 a, %2, 64;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], %3, %6, q;\n\t"
+        "add.s64 d, %3, 2;\n\t"
+        "add.u32 a, %2, 8;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 72;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %3, 4;\n\t"
+        "add.u32 a, %2, 16;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 80;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %3, 6;\n\t"
+        "add.u32 a, %2, 24;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 88;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.u32 a, %2, 32;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], %4, %5, q;\n\t"
+        "add.u32 a, %2, 96;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], %4, %6, q;\n\t"
+        "add.s64 d, %4, 2;\n\t"
+        "add.u32 a, %2, 40;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 104;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %4, 4;\n\t"
+        "add.u32 a, %2, 48;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 112;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %4, 6;\n\t"
+        "add.u32 a, %2, 56;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 120;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "}"
+        ::"r"(dacc), "r"(dacc2), "r"(ahi), "l"(d0), "l"(d1), "r"(idesc2), "r"(idesc), "r"(en)
+        : "memory");
+}
+template <>
+__device__ __forceinline__ void umma_stage_merged<32>(uint32_t dacc, uint32_t dacc2, uint32_t ahi, uint64_t d0,
+                                                      uint64_t d1, uint32_t idesc2, uint32_t idesc, uint32_t en)
+{
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t.reg .b64 d;\n\t.reg .b32 a;\n\t"
+        "setp.ne.b32 p, %7, 0;\n\tsetp.eq.b32 q, %7, %7;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%2], %3, %5, p;\n\t"
+        "add.u32 a, %2, 32;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], %3, %6, q;\n\t"
+        "add.s64 d, %3, 2;\n\t"
+        "add.u32 a, %2, 8;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 40;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %3, 4;\n\t"
+        "add.u32 a, %2, 16;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 48;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "add.s64 d, %3, 6;\n\t"
+        "add.u32 a, %2, 24;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [a], d, %5, q;\n\t"
+        "add.u32 a, %2, 56;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%1], [a], d, %6, q;\n\t"
+        "}"
+        ::"r"(dacc), "r"(dacc2), "r"(ahi), "l"(d0), "l"(d1), "r"(idesc2), "r"(idesc), "r"(en)
+        : "memory");
+}
+
 // Persistent grid: one CTA per SM; CTA c takes the work units u = c, c + G,
 // c + 2G, ... with u = (pair*nspin + spin, mode tile, K chunk), chunk fastest.
 // The barrier rings, the tensor memory and the TMA pipeline carry over from
@@ -323,10 +410,8 @@ __device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int ns
     return w;
 }
 
-// PW producer warps (8, or 16 with 64-point stages): PW / 4 per TMEM lane
-// quadrant, each forming KP / (PW / 4) points of every stage.
-template <int BF16, int KP, int PW>
-__global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS, 1)
+template <int BF16, int KP>
+__global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
                int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
@@ -361,11 +446,11 @@ __global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS,
         for (int s = 0; s < NST; ++s)
         {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1 + PW);
+            mbar_init(&empty[s], 1 + 8);
         }
         for (int a = 0; a < NA; ++a)
         {
-            mbar_init(&aready[a], PW);
+            mbar_init(&aready[a], 8);
             mbar_init(&afree[a], 1);
         }
         for (int b = 0; b < NACC; ++b)
@@ -486,19 +571,21 @@ __global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS,
                     const uint32_t base = smem_u32(sm + s * L.stage_bytes);
                     const uint32_t dacc = tmem + (uint32_t)b * L.accw;
                     const uint32_t ahi = tmem + L.a_col0 + (uint32_t)a * (2u * KP);
+                    if (merged)
+                    {
+                        // rows [0, NT) of each atom's 2*NT-row tile are B_hi, [NT, 2NT) B_lo
+                        const uint64_t d0 = umma_desc_sw128(base + L.b_hi);
+                        const uint64_t d1 = d0 + (uint64_t)(L.b_atom >> 4);
+                        umma_stage_merged<KP>(dacc, dacc + (uint32_t)NT, ahi, d0, d1, idesc2, idesc,
+                                              first ? 0u : 1u);
+                    }
+                    else
 #pragma unroll
                     for (int k = 0; k < KP / 8; ++k)
                     {
                         const uint32_t atom = base + (uint32_t)(k >> 2) * L.b_atom + 32u * (uint32_t)(k & 3);
                         const uint64_t bh = umma_desc_sw128(atom + L.b_hi);
                         const uint32_t en = (first && k == 0) ? 0u : 1u;
-                        if (merged)
-                        {
-                            // rows [0, NT) of the atom's 2*NT-row tile are B_hi, [NT, 2NT) B_lo
-                            umma_f16_ta(dacc, ahi + 8 * k, bh, idesc2, en);
-                            umma_f16_ta(dacc + (uint32_t)NT, ahi + KP + 8 * k, bh, idesc, 1u);
-                        }
-                        else
                         {
                             const uint64_t bl = umma_desc_sw128(atom + L.b_lo);
                             umma_f16_ta(dacc, ahi + 8 * k, bh, idesc, en);
@@ -529,10 +616,10 @@ __global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS,
             if (last_commit) mbar_wait_bounded(last_commit, last_par);
         }
     }
-    else if (warp < 2 + PW)
+    else if (warp < 10)
     {
         // ---------------- A producers: lane quadrant q = warp % 4 (rows 32q..32q+31),
-        // part h of PW / 4 of the stage's points
+        // half h of the stage's points
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
@@ -579,12 +666,11 @@ __global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS,
                 }
                 tc_fence_after();
                 const uint8_t* st = sm + s * L.stage_bytes;
-                // points h KP / NQ .. (h + 1) KP / NQ - 1 of the stage, in 16-point blocks
-                constexpr int NQ = PW / 4;
+                // points h*KP/2 .. (h+1)*KP/2 - 1 of the stage, in 16-point blocks
 #pragma unroll 1
-                for (int b = 0; b < KP / (16 * NQ); ++b)
+                for (int b = 0; b < KP / 32; ++b)
                 {
-                    const int p0 = h * (KP / NQ) + 16 * b;  // first point of the block in the stage
+                    const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
                     const int pb = p0 >> 4;                // 16-point psi block
                     const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
                     const uint8_t* pp[2];
@@ -620,10 +706,10 @@ __global__ void __launch_bounds__(PW == 16 ? 32 * (2 + 16 + 4) : TC_MAX_THREADS,
             }
         }
     }
-    else if (warp < 2 + PW + ndrain)
+    else if (warp < 10 + ndrain)
     {
         // ---------------- drain warps: TMEM lane quadrant warp%4, 64-column half
-        const int dw = warp - (2 + PW);
+        const int dw = warp - 10;
         const int q = warp & 3;
         const int c0 = (dw >> 2) * 64;
         const int nc = min(64, NT - c0);
@@ -702,34 +788,27 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(units, std::max(1, nsm));
     const int smem = lelph_local_tc_smem_bytes(g);
-    const int ndrain = 4 * ((2 * g.nbp + 63) / 64);
-    // sixteen producer warps where the tile has one column group of drains and
-    // 64-point stages (LELPH_TC_PRODUCERS = 16), else eight
-    int pw = 8;
-    if (const char* e = getenv("LELPH_TC_PRODUCERS"))
-        if (atoi(e) == 16 && ndrain == 4 && g.kpts == 64 && !ab_bf16) pw = 16;
-    const int threads = 32 * (2 + pw + ndrain);
+    const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (units <= 0) return;
-#define TC_LAUNCH(BF, KPV, PWV)                                                                                  \
+#define TC_LAUNCH(BF, KPV)                                                                                       \
     do                                                                                                           \
     {                                                                                                            \
-        cudaFuncSetAttribute(k_local_tc<BF, KPV, PWV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);        \
-        k_local_tc<BF, KPV, PWV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles, \
-                                                              (int)units, partials, status, wait_ns);            \
+        cudaFuncSetAttribute(k_local_tc<BF, KPV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
+        k_local_tc<BF, KPV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles,     \
+                                                         (int)units, partials, status, wait_ns);                 \
     } while (0)
     if (ab_bf16)
     {
-        if (g.kpts == 64) TC_LAUNCH(1, 64, 8);
-        else TC_LAUNCH(1, 32, 8);
+        if (g.kpts == 64) TC_LAUNCH(1, 64);
+        else TC_LAUNCH(1, 32);
     }
     else
     {
-        if (g.kpts == 64 && pw == 16) TC_LAUNCH(0, 64, 16);
-        else if (g.kpts == 64) TC_LAUNCH(0, 64, 8);
-        else TC_LAUNCH(0, 32, 8);
+        if (g.kpts == 64) TC_LAUNCH(0, 64);
+        else TC_LAUNCH(0, 32);
     }
 #undef TC_LAUNCH
 }
