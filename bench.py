@@ -475,6 +475,33 @@ def run_ours(args):
                 "step_share": local_ms / (local_ms + prep_ms + fin_ms),
                 "prepare_ms": prep_ms, "finish_ms": fin_ms}
 
+    # HBM rooflines of the preparation's memory-bound kernels (per step, from the
+    # library's per-role profiling events): algorithmic bytes / device time
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    Mp = int(np.prod(p1["product_grid"]))
+    nsets = s.nspin * s.nbnds * s.nspinor
+    nbp = (s.nbnds + 7) // 8 * 8
+    npw_k = np.array([len(s.gvec[int(ik)]) for ik in s.kmap[:, 0]], dtype=np.float64)
+    box_bytes = s.nk_bz * nsets * Mp * 8.0            # FP32 boxes of every full-BZ k
+    prep_roles = {
+        "k_scatter (+ box clears)": (p1["prep_scatter_ms"] - p0["prep_scatter_ms"],
+                                     float((npw_k * (nsets * (16 + 8 + 16) + 12)).sum()) + box_bytes,
+                                     "FP64 iBZ coefficients and Miller indices read, FP32 box entries and FP64 "
+                                     "unfolded coefficients written, boxes cleared"),
+        "k_fft_x_split": (p1["prep_xsplit_ms"] - p0["prep_xsplit_ms"],
+                          box_bytes + s.nk_bz * s.nspin * s.nspinor * Mp * (2 * 2 * nbp * 4 + nbp * 8.0),
+                          "FP32 boxes read (an upper bound: only occupied planes are read), split k+q rows "
+                          "(hi, lo) and FP32 psi_k tiles written"),
+        "k_fft_contig + k_fft_strided (z, y)": (p1["prep_fft_ms"] - p0["prep_fft_ms"], 4 * box_bytes,
+                                                 "FP32 boxes read and written once per pass (an upper bound: "
+                                                 "the passes skip unoccupied columns and planes)"),
+    }
+    hbm_roofs = [{"kernel": k, "bound": "hbm", "ms": ms, "traffic_model_bytes": by,
+                  "achieved": by / (ms * 1e-3) / 1e9 if ms > 0 else None, "peak": hbm, "unit": "GB/s",
+                  "frac": by / (ms * 1e-3) / 1e9 / hbm if ms > 0 else None, "bytes": what}
+                 for k, (ms, by, what) in prep_roles.items()]
+    roofline["memory_bound_kernels"] = hbm_roofs
+
     # ------------------------------------------------ end to end (host buffers)
     wfc_pin = [torch.empty(w.shape, dtype=torch.complex128, pin_memory=True) for w in s.wfc]
     for t, w in zip(wfc_pin, s.wfc):

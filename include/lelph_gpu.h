@@ -137,6 +137,11 @@ typedef struct lelph_gpu_stats
     double gs_plane_ms;          /* G-space route: device time of the plane, x-pass and GEMM kernels */
     double gs_xpass_ms;          /*   (profiling on; each launch timed with events on the library stream) */
     double gs_gemm_ms;
+    double prep_scatter_ms;      /* real-space route, mixed form, profiling on: device time of the */
+    double prep_fft_ms;          /*   preparation's roles -- sphere -> box scatter, z and y FFT passes, */
+    double prep_xsplit_ms;       /*   x pass writing the tensor-core operands, KB projections, and the */
+    double prep_proj_ms;         /*   dV windows (prepare) */
+    double windows_ms;
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

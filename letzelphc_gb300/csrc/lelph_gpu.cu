@@ -543,6 +543,24 @@ int check_status(lelph_gpu* h)
     return LELPH_GPU_OK;
 }
 
+// Per-kernel device time while profiling (the G-space route's kernels, the
+// preparation's roles): gs_tick marks
+// the start, each gs_tock returns the time since the last mark and re-marks.
+static void gs_tick(lelph_gpu* h)
+{
+    if (h->profiling) cudaEventRecord(h->evg0, h->st);
+}
+static double gs_tock(lelph_gpu* h)
+{
+    if (!h->profiling) return 0.0;
+    cudaEventRecord(h->evg1, h->st);
+    cudaEventSynchronize(h->evg1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->evg0, h->evg1);
+    std::swap(h->evg0, h->evg1);
+    return ms;
+}
+
 void tstart(lelph_gpu* h)
 {
     if (h->profiling) cudaEventRecord(h->ev0, h->st);
@@ -1382,12 +1400,14 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
         for (int k0 = 0; k0 < d.nkpts_BZ; k0 += nkc)
         {
             int nk = std::min(nkc, d.nkpts_BZ - k0);
+            gs_tick(h);
             CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
             CUDA_TRY(h, cudaMemsetAsync(h->d_colmask.p, 0, mask_k * nkc, h->st));
             lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
                                  (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
                                  (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p,
                                  (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st, mk);
+            h->stats.prep_scatter_ms += gs_tock(h);
             const long long nbox = (long long)nk * nbox_per_k;
             float2* bx = (float2*)h->d_boxes32.p;
             // z pass on the occupied columns, y pass on the occupied x planes, x pass
@@ -1396,21 +1416,26 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
                                       mk);
             lelph_launch_fft_strided_f(bx, nbox * g.Nx, g.Nz, h->plan[1], (const float2*)h->d_tw32[1].p, +1, h->st,
                                        mk);
+            h->stats.prep_fft_ms += gs_tock(h);
             lelph_launch_fft_x_to_split(bx, nk, k0, h->plan[0], (const float2*)h->d_tw32[0].p, +1, g,
                                         (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p,
                                         (float2*)h->d_psi32.p, h->st, mk);
+            h->stats.prep_xsplit_ms += gs_tock(h);
             h->stats.kernel_launches += 4;
         }
     }
     NonlocalDesc nl = nl_desc(h);
+    gs_tick(h);
     lelph_launch_projections(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
                              (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double*)h->d_fk.p,
                              (const long long*)h->d_fkoff.p, (const double2*)h->d_chat.p,
                              (const long long*)h->d_chatoff.p, nl, g, h->mixed ? 1 : 0, (double2*)h->d_proj.p, h->st);
+    h->stats.prep_proj_ms += gs_tock(h);
     h->stats.kernel_launches += 1;
     CUDA_TRY(h, cudaGetLastError());
     int wr = build_windows(h);
     if (wr) return wr;
+    h->stats.windows_ms += gs_tock(h);
     h->stats.prepare_ms += tstop(h);
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->prepared = true;
@@ -2007,22 +2032,6 @@ static int build_windows(lelph_gpu* h)
     return LELPH_GPU_OK;
 }
 
-// Per-kernel device time of the G-space route while profiling: gs_tick marks
-// the start, each gs_tock returns the time since the last mark and re-marks.
-static void gs_tick(lelph_gpu* h)
-{
-    if (h->profiling) cudaEventRecord(h->evg0, h->st);
-}
-static double gs_tock(lelph_gpu* h)
-{
-    if (!h->profiling) return 0.0;
-    cudaEventRecord(h->evg1, h->st);
-    cudaEventSynchronize(h->evg1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, h->evg0, h->evg1);
-    std::swap(h->evg0, h->evg1);
-    return ms;
-}
 
 // Local term of pairs[0 .. n) on the G-space route, into glocal
 // (pair, spin, mode x band of k, band of k+q), FP64, 1/M applied.  Pairs are

@@ -62,6 +62,8 @@ class Stats(C.Structure):
         ("dmats_ms", C.c_double), ("dmats_host_ms", C.c_double), ("dmats_done", C.c_longlong),
         ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double), ("route", C.c_int),
         ("gs_plane_ms", C.c_double), ("gs_xpass_ms", C.c_double), ("gs_gemm_ms", C.c_double),
+        ("prep_scatter_ms", C.c_double), ("prep_fft_ms", C.c_double), ("prep_xsplit_ms", C.c_double),
+        ("prep_proj_ms", C.c_double), ("windows_ms", C.c_double),
     ]
 
 
