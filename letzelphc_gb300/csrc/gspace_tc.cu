@@ -105,7 +105,10 @@ __global__ void __launch_bounds__(GT_THREADS, 1)
                  float2* __restrict__ part, unsigned* __restrict__ status, unsigned long long wait_ns)
 {
     extern __shared__ __align__(1024) uint8_t gt_raw[];
-    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gt_raw) + 1023) & ~uintptr_t(1023));
+    // aligned by pointer arithmetic on the shared array itself (not through an
+    // integer), so that the compiler keeps the shared address space and emits
+    // shared-memory loads with 32-bit addresses rather than generic ones
+    uint8_t* sm = gt_raw + ((1024u - (smem_u32(gt_raw) & 1023u)) & 1023u);
     const GtLayout L = gt_layout(NT);
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
     uint64_t* empty = full + GT_NST_MAX;

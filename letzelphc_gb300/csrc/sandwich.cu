@@ -169,7 +169,8 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 // A pipeline stage is KP grid points (KP/32 K atoms of 128 bytes); one TMEM
 // accumulator chains 64 points (two 32-point stages or one 64-point stage)
 // before it is drained.
-#define TC_MAX_THREADS 576 // 10 role warps + up to 8 drain warps
+// 10 role warps + 4 drain warps per 64 accumulator columns (NDR groups)
+#define TC_THREADS(NDR) (32 * (10 + 4 * (NDR)))
 
 struct TcSmemLayout
 {
@@ -253,24 +254,63 @@ __device__ __forceinline__ void split_pair(float re, float im, uint32_t& h, uint
     }
 }
 
-// A operand for SUB grid points of one row (one lane): a = sum_c dV^{c} psi^{c},
-// split and stored to the lane's TMEM row.  pp[c] points at the lane's psi row
-// (128-byte swizzled half tile), dvp[c] at the row's dV (16 points of the half).
+// Tensor-memory stores of the A producers.  No "memory" clobber: they write
+// tensor memory only, and a clobber would keep the compiler from issuing the
+// next points' shared-memory loads before them.  The stage's
+// tcgen05.wait::st (a volatile asm with a clobber) stays after them.
+__device__ __forceinline__ void tmem_st8_a(uint32_t taddr, const uint32_t* r)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]));
+}
+__device__ __forceinline__ void tmem_st4_a(uint32_t taddr, const uint32_t* r)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
+                 "r"(r[2]), "r"(r[3]));
+}
+
+// The operands of SUB grid points of one row (one lane), NC dV components:
+// psi (16-byte chunks of two points) and dV.
+template <int SUB, int NC>
+struct ProdFrag
+{
+    float4 ps[SUB / 2][NC];
+    float4 dv[SUB / 2][NC];
+};
+
+// pp[c] points at the lane's psi row (128-byte swizzled half tile), dvp[c] at
+// the row's dV (16 points of the half); j0 is the first point of the SUB.
+template <int SUB, int NC>
+__device__ __forceinline__ void prod_load(ProdFrag<SUB, NC>& f, const uint8_t* const* pp, const float4* const* dvp,
+                                          uint32_t swz, int j0)
+{
+#pragma unroll
+    for (int jj = 0; jj < SUB / 2; ++jj)
+    {
+        const int j = j0 / 2 + jj;  // 16-byte chunk = 2 points
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+        {
+            f.ps[jj][c] = *reinterpret_cast<const float4*>(pp[c] + ((((uint32_t)j) ^ swz) << 4));
+            f.dv[jj][c] = dvp[c][j];
+        }
+    }
+}
+
+// A operand of the SUB points: a = sum_c dV^{c} psi^{c}, split and stored to
+// the lane's TMEM row.
 template <int BF16, int SUB, int NC>
-__device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const float4* const* dvp, uint32_t swz, int j0,
-                                            uint32_t tcol_hi, uint32_t tcol_lo)
+__device__ __forceinline__ void prod_store(const ProdFrag<SUB, NC>& f, uint32_t tcol_hi, uint32_t tcol_lo)
 {
     uint32_t hi[SUB], lo[SUB];
 #pragma unroll
     for (int jj = 0; jj < SUB / 2; ++jj)
     {
-        const int j = j0 / 2 + jj;  // 16-byte chunk = 2 points
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int c = 0; c < NC; ++c)
         {
-            const float4 ps = *reinterpret_cast<const float4*>(pp[c] + ((((uint32_t)j) ^ swz) << 4));
-            const float4 dv = dvp[c][j];
+            const float4 ps = f.ps[jj][c], dv = f.dv[jj][c];
             acc.x += dv.x * ps.x - dv.y * ps.y;
             acc.y += dv.x * ps.y + dv.y * ps.x;
             acc.z += dv.z * ps.z - dv.w * ps.w;
@@ -281,13 +321,71 @@ __device__ __forceinline__ void produce_sub(const uint8_t* const* pp, const floa
     }
     if (SUB == 8)
     {
-        tmem_st8(tcol_hi, hi);
-        tmem_st8(tcol_lo, lo);
+        tmem_st8_a(tcol_hi, hi);
+        tmem_st8_a(tcol_lo, lo);
     }
     else
     {
-        tmem_st4(tcol_hi, hi);
-        tmem_st4(tcol_lo, lo);
+        tmem_st4_a(tcol_hi, hi);
+        tmem_st4_a(tcol_lo, lo);
+    }
+}
+
+// A producer's share of one pipeline stage: points h*KP/2 .. (h+1)*KP/2 - 1,
+// in 16-point psi blocks of 16/SUB pieces of SUB points each.  The pieces are
+// software-pipelined: the shared-memory loads of piece t+1 are issued before
+// piece t is formed and stored, so that their latency overlaps the work.
+template <int BF16, int KP, int SUB, int NC, int PF>
+__device__ __forceinline__ void produce_stage(const uint8_t* st, const TcSmemLayout& L, const float4* zero_dv,
+                                              bool in_tile, int h, int m, int ml, int nmag, int comp0, int comp1,
+                                              int nsp, uint32_t swz, uint32_t col_base)
+{
+    constexpr int NATOM = KP / 32;
+    constexpr int PER_BLOCK = 16 / SUB;
+    constexpr int NPIECE = (KP / 32) * PER_BLOCK;
+    const uint8_t* pp[NPIECE / PER_BLOCK][2];
+    const float4* dvp[NPIECE / PER_BLOCK][2];
+#pragma unroll
+    for (int b = 0; b < KP / 32; ++b)
+    {
+        const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
+        const int pb = p0 >> 4;                // 16-point psi block
+        const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
+        pp[b][0] = st + L.p + (0 * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
+        pp[b][1] = st + L.p + ((nsp - 1) * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
+        dvp[b][0] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * nmag + comp0) * 32 + (p0 & 31)) * 2)
+                            : zero_dv;
+        dvp[b][1] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * nmag + comp1) * 32 + (p0 & 31)) * 2)
+                            : zero_dv;
+    }
+    if (PF)
+    {
+        ProdFrag<SUB, NC> f[2];
+        prod_load<SUB, NC>(f[0], pp[0], dvp[0], swz, 0);
+#pragma unroll
+        for (int t = 0; t < NPIECE; ++t)
+        {
+            if (t + 1 < NPIECE)
+            {
+                const int bn = (t + 1) / PER_BLOCK;
+                prod_load<SUB, NC>(f[(t + 1) & 1], pp[bn], dvp[bn], swz, ((t + 1) % PER_BLOCK) * SUB);
+            }
+            const int b = t / PER_BLOCK, j0 = (t % PER_BLOCK) * SUB;
+            const uint32_t col_hi = col_base + (uint32_t)(h * (KP / 2) + 16 * b + j0);
+            prod_store<BF16, SUB, NC>(f[t & 1], col_hi, col_hi + KP);
+        }
+    }
+    else
+    {
+#pragma unroll
+        for (int t = 0; t < NPIECE; ++t)
+        {
+            ProdFrag<SUB, NC> f;
+            const int b = t / PER_BLOCK, j0 = (t % PER_BLOCK) * SUB;
+            prod_load<SUB, NC>(f, pp[b], dvp[b], swz, j0);
+            const uint32_t col_hi = col_base + (uint32_t)(h * (KP / 2) + 16 * b + j0);
+            prod_store<BF16, SUB, NC>(f, col_hi, col_hi + KP);
+        }
     }
 }
 
@@ -410,15 +508,18 @@ __device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int ns
     return w;
 }
 
-template <int BF16, int KP>
-__global__ void __launch_bounds__(TC_MAX_THREADS, 1)
+template <int BF16, int KP, int NDR>
+__global__ void __launch_bounds__(TC_THREADS(NDR), 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
                int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
                unsigned* __restrict__ status, unsigned long long wait_ns)
 {
     extern __shared__ __align__(1024) uint8_t smraw[];
-    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    // aligned by pointer arithmetic on the shared array itself (not through an
+    // integer), so that the compiler keeps the shared address space and emits
+    // shared-memory loads with 32-bit addresses rather than generic ones
+    uint8_t* sm = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
     const TcSmemLayout L = tc_layout(gd);
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
     uint64_t* empty = full + TC_NST_MAX;    // TMA slot consumed: MMA commit + 8 producer warps
@@ -439,7 +540,7 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
     const int nstage = chunk_pts / KP;
     const int ngroup = (nstage + TC_GROUP - 1) / TC_GROUP;
     const int nsp = (gd.nmag == 4) ? 2 : 1;
-    const int ndrain = 4 * ((NT + 63) / 64);
+    const int ndrain = 4 * NDR;  // = 4 * ceil(NT / 64), chosen by the launcher
 
     if (threadIdx.x == 0)
     {
@@ -666,35 +767,13 @@ __global__ void __launch_bounds__(TC_MAX_THREADS, 1)
                 }
                 tc_fence_after();
                 const uint8_t* st = sm + s * L.stage_bytes;
-                // points h*KP/2 .. (h+1)*KP/2 - 1 of the stage, in 16-point blocks
-#pragma unroll 1
-                for (int b = 0; b < KP / 32; ++b)
-                {
-                    const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
-                    const int pb = p0 >> 4;                // 16-point psi block
-                    const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
-                    const uint8_t* pp[2];
-                    const float4* dvp[2];
-                    pp[0] = st + L.p + (0 * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
-                    pp[1] = st + L.p + ((nsp - 1) * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
-                    dvp[0] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * gd.nmag + comp0) * 32 + (p0 & 31)) * 2)
-                                     : zero_dv;
-                    dvp[1] = in_tile ? reinterpret_cast<const float4*>(dvs + ((size_t)(ml * gd.nmag + comp1) * 32 + (p0 & 31)) * 2)
-                                     : zero_dv;
-                    const uint32_t col_hi = lane_base + L.a_col0 + (uint32_t)a * (2u * KP) + (uint32_t)p0;
-                    if (gd.nmag == 4)
-                    {
-#pragma unroll
-                        for (int j0 = 0; j0 < 16; j0 += 4)
-                            produce_sub<BF16, 4, 2>(pp, dvp, swz, j0, col_hi + j0, col_hi + KP + j0);
-                    }
-                    else
-                    {
-#pragma unroll
-                        for (int j0 = 0; j0 < 16; j0 += 8)
-                            produce_sub<BF16, 8, 1>(pp, dvp, swz, j0, col_hi + j0, col_hi + KP + j0);
-                    }
-                }
+                const uint32_t col_base = lane_base + L.a_col0 + (uint32_t)a * (2u * KP);
+                if (gd.nmag == 4)
+                    produce_stage<BF16, KP, 4, 2, 1>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
+                                                     swz, col_base);
+                else
+                    produce_stage<BF16, KP, 8, 1, 1>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
+                                                     swz, col_base);
                 tmem_wait_st();
                 tc_fence_before();
                 __syncwarp();
@@ -788,27 +867,35 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = (int)std::min<long long>(units, std::max(1, nsm));
     const int smem = lelph_local_tc_smem_bytes(g);
-    const int threads = 32 * (10 + 4 * ((2 * g.nbp + 63) / 64));
+    const int ndr = (2 * g.nbp + 63) / 64;  // drain groups of 64 accumulator columns (1 or 2)
     const CUtensorMap* tB = static_cast<const CUtensorMap*>(tmapB);
     const CUtensorMap* tP = static_cast<const CUtensorMap*>(tmapP);
     const CUtensorMap* tV = static_cast<const CUtensorMap*>(tmapV);
     if (units <= 0) return;
-#define TC_LAUNCH(BF, KPV)                                                                                       \
+#define TC_LAUNCH(BF, KPV, NDR)                                                                                  \
     do                                                                                                           \
     {                                                                                                            \
-        cudaFuncSetAttribute(k_local_tc<BF, KPV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
-        k_local_tc<BF, KPV><<<grid, threads, smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, mtiles,     \
-                                                         (int)units, partials, status, wait_ns);                 \
+        cudaFuncSetAttribute(k_local_tc<BF, KPV, NDR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);        \
+        k_local_tc<BF, KPV, NDR><<<grid, TC_THREADS(NDR), smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, \
+                                                                     mtiles, (int)units, partials, status,       \
+                                                                     wait_ns);                                   \
+    } while (0)
+#define TC_LAUNCH_NDR(BF, KPV)                                                                                   \
+    do                                                                                                           \
+    {                                                                                                            \
+        if (ndr == 1) TC_LAUNCH(BF, KPV, 1);                                                                     \
+        else TC_LAUNCH(BF, KPV, 2);                                                                              \
     } while (0)
     if (ab_bf16)
     {
-        if (g.kpts == 64) TC_LAUNCH(1, 64);
-        else TC_LAUNCH(1, 32);
+        if (g.kpts == 64) TC_LAUNCH_NDR(1, 64);
+        else TC_LAUNCH_NDR(1, 32);
     }
     else
     {
-        if (g.kpts == 64) TC_LAUNCH(0, 64);
-        else TC_LAUNCH(0, 32);
+        if (g.kpts == 64) TC_LAUNCH_NDR(0, 64);
+        else TC_LAUNCH_NDR(0, 32);
     }
+#undef TC_LAUNCH_NDR
 #undef TC_LAUNCH
 }
