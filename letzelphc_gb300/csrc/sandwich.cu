@@ -246,8 +246,9 @@ __device__ __forceinline__ void split_pair(float re, float im, uint32_t& h, uint
     {
         __half2 hv = __floats2half2_rn(re, im);
         float2 hf = __half22float2(hv);
-        // both residuals in one packed FP32x2 FMA: (re, im) - hi, exactly rounded
-        const float2 d = __ffma2_rn(hf, make_float2(-1.f, -1.f), make_float2(re, im));
+        // the residuals (re, im) - hi, exact; two scalar subtractions, which
+        // measured faster than one packed FP32x2 FMA here
+        const float2 d = make_float2(re - hf.x, im - hf.y);
         __half2 lv = __floats2half2_rn(d.x, d.y);
         h = *reinterpret_cast<uint32_t*>(&hv);
         l = *reinterpret_cast<uint32_t*>(&lv);
@@ -262,6 +263,12 @@ __device__ __forceinline__ void tmem_st8_a(uint32_t taddr, const uint32_t* r)
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
                  "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]));
+}
+__device__ __forceinline__ void tmem_st16_a(uint32_t taddr, const uint32_t* r)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+                 ::"r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+                 "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]));
 }
 __device__ __forceinline__ void tmem_st4_a(uint32_t taddr, const uint32_t* r)
 {
@@ -306,9 +313,18 @@ __device__ __forceinline__ void prod_store(const ProdFrag<SUB, NC>& f, uint32_t 
 #pragma unroll
     for (int jj = 0; jj < SUB / 2; ++jj)
     {
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        // the first component's product initialises the sum: 0 + x is not
+        // foldable to x in IEEE arithmetic (-0), so a zero start costs an add
+        float4 acc;
+        {
+            const float4 ps = f.ps[jj][0], dv = f.dv[jj][0];
+            acc.x = dv.x * ps.x - dv.y * ps.y;
+            acc.y = dv.x * ps.y + dv.y * ps.x;
+            acc.z = dv.z * ps.z - dv.w * ps.w;
+            acc.w = dv.z * ps.w + dv.w * ps.z;
+        }
 #pragma unroll
-        for (int c = 0; c < NC; ++c)
+        for (int c = 1; c < NC; ++c)
         {
             const float4 ps = f.ps[jj][c], dv = f.dv[jj][c];
             acc.x += dv.x * ps.x - dv.y * ps.y;
@@ -319,7 +335,12 @@ __device__ __forceinline__ void prod_store(const ProdFrag<SUB, NC>& f, uint32_t 
         split_pair<BF16>(acc.x, acc.y, hi[2 * jj], lo[2 * jj]);
         split_pair<BF16>(acc.z, acc.w, hi[2 * jj + 1], lo[2 * jj + 1]);
     }
-    if (SUB == 8)
+    if (SUB == 16)
+    {
+        tmem_st16_a(tcol_hi, hi);
+        tmem_st16_a(tcol_lo, lo);
+    }
+    else if (SUB == 8)
     {
         tmem_st8_a(tcol_hi, hi);
         tmem_st8_a(tcol_lo, lo);
