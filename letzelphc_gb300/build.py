@@ -14,7 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liblelph_gpu.so")
 SOURCES = ["fft_gather.cu", "sandwich.cu", "nonlocal.cu", "dvloc.cu", "rotate_dv.cu", "dmats.cu", "qstar.cu",
-           "dvscf.cu", "gspace.cu", "gspace_tc.cu", "lelph_gpu.cu", "ndb_elph.cpp"]
+           "dvscf.cu", "gspace.cu", "gspace_tc.cu", "projections_tc.cu", "lelph_gpu.cu",
+           "ndb_elph.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 

@@ -281,7 +281,8 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
                                                  const int* __restrict__ npw_arr, const double2* __restrict__ coef,
                                                  const long long* __restrict__ coef_off, GeomDev gd,
                                                  T2* __restrict__ boxes, double2* __restrict__ chat,
-                                                 const long long* __restrict__ chat_off, BoxMask mk)
+                                                 float2* __restrict__ chat32, const long long* __restrict__ chat_off,
+                                                 BoxMask mk)
 {
     const int kslot = blockIdx.y;
     const int kbz = k0 + kslot;
@@ -316,7 +317,9 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
     const double2 u0 = make_double2(s.su2[0], s.su2[1]), u1 = make_double2(s.su2[2], s.su2[3]);
     const double2 u2 = make_double2(s.su2[4], s.su2[5]), u3 = make_double2(s.su2[6], s.su2[7]);
     const double2* cbase = coef + coef_off[s.ik];
-    double2* chb = chat + chat_off[kbz];
+    // the unfolded coefficients in FP64, or in FP32 (chat32) for the tensor-core projections
+    double2* chb = chat32 ? nullptr : chat + chat_off[kbz];
+    float2* chb32 = chat32 ? chat32 + chat_off[kbz] : nullptr;
     T2* bxb = boxes ? boxes + (size_t)kslot * nsets * gd.nspinor * N : nullptr;
     for (int set = 0; set < nsets; ++set)
     {
@@ -332,12 +335,13 @@ __global__ void __launch_bounds__(256) k_scatter(int k0, const KPointSym* __rest
         {
             v[0] = c[g];
         }
-        double2* ch = chb + (size_t)set * gd.nspinor * npw;
+        const size_t co = (size_t)set * gd.nspinor * npw;
         for (int sp = 0; sp < gd.nspinor; ++sp)
         {
             double2 w = cmul(v[sp], ph);
             if (s.trev) w.y = -w.y;
-            ch[(size_t)sp * npw + g] = w;
+            if (chb32) chb32[co + (size_t)sp * npw + g] = make_float2((float)w.x, (float)w.y);
+            else chb[co + (size_t)sp * npw + g] = w;
             if (bxb) bxb[((size_t)set * gd.nspinor + sp) * N + bidx] = mk2<T2>(w.x, w.y);
         }
     }
@@ -525,15 +529,15 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
                           const int* npw, int npw_max, const double2* coef, const long long* coef_off,
                           const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
-                          cudaStream_t st, const BoxMask& mk)
+                          cudaStream_t st, const BoxMask& mk, float2* chat32)
 {
     dim3 grid((unsigned)((npw_max + 255) / 256), nk);
     if (box_fp64)
         k_scatter<double2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
-                                                 (double2*)boxes, chat, chat_off, mk);
+                                                 (double2*)boxes, chat, chat32, chat_off, mk);
     else
         k_scatter<float2><<<grid, 256, 0, st>>>(k0, ksym_dev, miller, pw_off, npw, coef, coef_off, g,
-                                                (float2*)boxes, chat, chat_off, mk);
+                                                (float2*)boxes, chat, chat32, chat_off, mk);
 }
 
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,

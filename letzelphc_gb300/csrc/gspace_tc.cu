@@ -40,23 +40,6 @@
 #define GT_NST_MAX 8
 #define GT_SMEM_LIMIT (227 * 1024)
 
-__host__ __device__ constexpr uint32_t umma_idesc_tf32(uint32_t M, uint32_t N)
-{
-    // f32 accumulate (bits 4-5 = 1), A and B TF32 (format 2 at bits 7-9 and
-    // 10-12), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
-}
-
-__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
 struct GtLayout
 {
     uint32_t a_bytes, b_bytes, stage_bytes, nst, bar_off, total, acc_stride, tmem_cols;

@@ -65,6 +65,7 @@ struct lelph_gpu
     bool mixed = false;
     bool prepared = false;
     bool gspace = false;  // G-space route of the local sandwich
+    bool proj_tc = false;  // KB projections on the tensor cores (mixed form)
     // host copies
     std::vector<double> alat, blat, kibz, kbz_crys, symR, symtau, atom_pos, PP, Fsign;
     std::vector<int> kmap, symtr, atom_type, npw;
@@ -919,6 +920,9 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
         const char* e = std::getenv("LELPH_GS_TC");
         h->gs_tc = h->mixed && lelph_gs_tc_supported(d.nbnds) && d.gs_gemm != LELPH_GPU_GS_GEMM_SIMT &&
                    !(e && e[0] == '0');
+        // the mixed form's KB projections on the tensor cores unless LELPH_PROJ_TC=0
+        const char* ep = std::getenv("LELPH_PROJ_TC");
+        h->proj_tc = h->mixed && !(ep && ep[0] == '0');
     }
     h->ntype = d.ntype;
     h->nltimesj = d.nltimesj;
@@ -1344,6 +1348,10 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
     const int npw_max = *std::max_element(h->npw.begin(), h->npw.end());
     tstart(h);
     int rc;
+    // KB projections on the tensor cores (mixed form); on the real-space route they
+    // read an FP32 copy of the unfolded coefficients, which nothing else uses there
+    const bool proj_tc = h->proj_tc && lelph_projections_tc_supported(nl_desc(h));
+    const bool chat_f32 = proj_tc && !h->gspace;
     if (h->gspace)
     {
         // G-space route: the unfolded coefficients of every full-BZ k (no
@@ -1406,7 +1414,8 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
             lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
                                  (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
                                  (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p,
-                                 (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st, mk);
+                                 (double2*)h->d_chat.p, (const long long*)h->d_chatoff.p, h->st, mk,
+                                 proj_tc ? (float2*)h->d_chat.p : nullptr);
             h->stats.prep_scatter_ms += gs_tock(h);
             const long long nbox = (long long)nk * nbox_per_k;
             float2* bx = (float2*)h->d_boxes32.p;
@@ -1426,10 +1435,24 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
     }
     NonlocalDesc nl = nl_desc(h);
     gs_tick(h);
-    lelph_launch_projections(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
-                             (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double*)h->d_fk.p,
-                             (const long long*)h->d_fkoff.p, (const double2*)h->d_chat.p,
-                             (const long long*)h->d_chatoff.p, nl, g, h->mixed ? 1 : 0, (double2*)h->d_proj.p, h->st);
+    if (proj_tc)
+    {
+        CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+        if (lelph_launch_projections_tc(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
+                                        (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p,
+                                        (const double*)h->d_fk.p, (const long long*)h->d_fkoff.p, h->d_chat.p,
+                                        chat_f32 ? 1 : 0, (const long long*)h->d_chatoff.p, nl, g,
+                                        (double2*)h->d_proj.p, (unsigned*)h->d_status.p, h->wait_ns, h->st))
+            return fail(h, LELPH_GPU_ERR_CUDA, "projection launch failed");
+        const int rs = check_status(h);
+        if (rs) return rs;
+    }
+    else
+        lelph_launch_projections(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
+                                 (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const double*)h->d_fk.p,
+                                 (const long long*)h->d_fkoff.p, (const double2*)h->d_chat.p,
+                                 (const long long*)h->d_chatoff.p, nl, g, h->mixed ? 1 : 0, (double2*)h->d_proj.p,
+                                 h->st);
     h->stats.prep_proj_ms += gs_tock(h);
     h->stats.kernel_launches += 1;
     CUDA_TRY(h, cudaGetLastError());

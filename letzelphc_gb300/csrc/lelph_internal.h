@@ -102,7 +102,7 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,
                           const int* npw, int npw_max, const double2* coef, const long long* coef_off,
                           const GeomDev& g, int box_fp64, void* boxes, double2* chat, const long long* chat_off,
-                          cudaStream_t st, const BoxMask& mk = BoxMask());
+                          cudaStream_t st, const BoxMask& mk = BoxMask(), float2* chat32 = nullptr);
 
 // debugging / parity: box index of each rotated plane wave of one full-BZ k
 void lelph_launch_gmap(const KPointSym* ks, int kbz, const int* miller, const long long* pw_off, const int* npw,
@@ -172,6 +172,15 @@ void lelph_launch_projections(int k0, int nk, const KPointSym* ksym_dev, const d
                               const int* npw, const double* Fk, const long long* fk_off, const double2* chat,
                               const long long* chat_off, const NonlocalDesc& nl, const GeomDev& g, int f32acc,
                               double2* proj, cudaStream_t st);
+// the same projections on the tensor cores (mixed form; projections_tc.cu):
+// TF32 split operands built in shared memory, FP64 sums; proj is overwritten
+// (chat: the unfolded coefficients as double2, or as float2 with chat_f32)
+int lelph_projections_tc_supported(const NonlocalDesc& nl);
+int lelph_launch_projections_tc(int k0, int nk, const KPointSym* ksym_dev, const double* gvec,
+                                const long long* pw_off, const int* npw, const double* Fk, const long long* fk_off,
+                                const void* chat, int chat_f32, const long long* chat_off, const NonlocalDesc& nl,
+                                const GeomDev& g, double2* proj, unsigned* status, unsigned long long wait_ns,
+                                cudaStream_t st);
 void lelph_launch_finish(const PairInfo* pairs, int npairs, int mode_fp64, const double2* glocal,
                          const float* partials, int nchunks, const float* mode_scale, const float* band_scale,
                          const double2* proj, const double2* eig, int non_loc, const NonlocalDesc& nl,

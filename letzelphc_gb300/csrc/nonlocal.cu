@@ -22,28 +22,7 @@
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
-
-__device__ __forceinline__ double ylm_legendre(int l, int m, double x)
-{
-    // associated Legendre function without the Condon-Shortley phase, m >= 0
-    double val = 1.0;
-    if (l == 0 && m == 0) return 1.0;
-    if (m > l) return 0.0;
-    double sq = sqrt(1.0 - x * x);
-    for (int im = 1; im <= m; ++im) val *= (2 * im - 1) * sq;
-    if (l == m) return val;
-    double vmm = val;
-    val *= (2 * m + 1) * x;
-    if (l == m + 1) return val;
-    for (int im = m + 2; im <= l; ++im)
-    {
-        double tmp = val;
-        val = (2 * im - 1) * x * val - (im + m - 1) * vmm;
-        val = val / (im - m);
-        vmm = tmp;
-    }
-    return val;
-}
+#include "ylm.cuh"
 
 // real spherical harmonics of Blanco, Florez and Bermejo (J. Mol. Struct.
 // THEOCHEM 419, 19 (1997)), the convention of src/common/numerical_func.c:97-152
@@ -67,41 +46,6 @@ __device__ __forceinline__ double ylm_real(int l, int m, double vx, double vy, d
 #define PJ_MAXP 24
 #define PJ_ROWS 64   // (atom, projector, component) rows per block
 #define PJ_SETS 32   // coefficient sets per block
-
-// Real spherical harmonics of all (l, m), l <= lmax, at K, written to y[l*l + l + m]:
-// cos(m phi), sin(m phi) by the angle-addition recurrence from cos(phi), sin(phi).
-__device__ __forceinline__ void ylm_all(int lmax, double vx, double vy, double vz, double* y)
-{
-    const double fact[8] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0};
-    const double norm = sqrt(vx * vx + vy * vy + vz * vz);
-    if (norm < 1e-6)
-    {
-        for (int i = 0; i < (lmax + 1) * (lmax + 1); ++i) y[i] = 0.0;
-        y[0] = 1.0 / sqrt(4 * LELPH_PI_T);
-        return;
-    }
-    const double cost = vz / norm;
-    const double rxy = sqrt(vx * vx + vy * vy);
-    const double c1 = rxy > 0.0 ? vx / rxy : 1.0, s1 = rxy > 0.0 ? vy / rxy : 0.0;
-    double cm = 1.0, sm = 0.0;  // cos(m phi), sin(m phi)
-    for (int m = 0; m <= lmax; ++m)
-    {
-        for (int l = m; l <= lmax; ++l)
-        {
-            double p = ylm_legendre(l, m, cost) * sqrt(fact[l - m] * (2 * l + 1) / (4 * LELPH_PI_T * fact[l + m]));
-            if (m == 0)
-                y[l * l + l] = p;
-            else
-            {
-                y[l * l + l + m] = sqrt(2.0) * cm * p;
-                y[l * l + l - m] = sqrt(2.0) * sm * p;
-            }
-        }
-        const double cn = cm * c1 - sm * s1, sn = sm * c1 + cm * s1;
-        cm = cn;
-        sm = sn;
-    }
-}
 
 template <typename T> struct PjCfg;
 template <> struct PjCfg<float> { static constexpr int G = 64; };
