@@ -485,8 +485,8 @@ def run_ours(args):
     box_bytes = s.nk_bz * nsets * Mp * 8.0            # FP32 boxes of every full-BZ k
     prep_roles = {
         "k_scatter (+ box clears)": (p1["prep_scatter_ms"] - p0["prep_scatter_ms"],
-                                     float((npw_k * (nsets * (16 + 8 + 16) + 12)).sum()) + box_bytes,
-                                     "FP64 iBZ coefficients and Miller indices read, FP32 box entries and FP64 "
+                                     float((npw_k * (nsets * (16 + 8 + 8) + 12)).sum()) + box_bytes,
+                                     "FP64 iBZ coefficients and Miller indices read, FP32 box entries and FP32 "
                                      "unfolded coefficients written, boxes cleared"),
         "k_fft_x_split": (p1["prep_xsplit_ms"] - p0["prep_xsplit_ms"],
                           box_bytes + s.nk_bz * s.nspin * s.nspinor * Mp * (2 * 2 * nbp * 4 + nbp * 8.0),
@@ -501,6 +501,21 @@ def run_ours(args):
                   "frac": by / (ms * 1e-3) / 1e9 / hbm if ms > 0 else None, "bytes": what}
                  for k, (ms, by, what) in prep_roles.items()]
     roofline["memory_bound_kernels"] = hbm_roofs
+    # the KB projections on the tensor cores: three TF32 products of the real GEMM
+    # (2 nsets coefficient rows) x (projector rows) x (2 npw), per full-BZ k
+    lsh = np.rint(np.asarray(s.PP_table)[:, :, 0] - 1.0).astype(int)  # [l shell, type] -> l (< 0: none)
+    nproj_max = int(max(sum(2 * l + 1 for l in lsh[:, t] if l >= 0) for t in range(lsh.shape[1])))
+    proj_rows = s.natom * nproj_max * 4
+    proj_ms = p1["prep_proj_ms"] - p0["prep_proj_ms"]
+    if proj_rows and proj_ms > 0:
+        pf = float(3 * 2 * (2 * nsets) * proj_rows * (2 * npw_k).sum())
+        tf32 = (peaks.get("bf16_tflops") or 1900.0) / 2
+        roofline["tensor_kernels"] = [{
+            "kernel": "k_projections_tc (KB projections, split-TF32 tcgen05)", "bound": "tensor", "ms": proj_ms,
+            "flops": pf, "achieved": pf / (proj_ms * 1e-3) / 1e12, "peak": tf32, "unit": "TFLOP/s",
+            "frac": pf / (proj_ms * 1e-3) / 1e12 / tf32,
+            "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (of measured): TF32 tensor rate",
+            "note": "bound by forming its operands (tables in FP64, TF32 splits), not by the tensor pipe"}]
 
     # ------------------------------------------------ end to end (host buffers)
     wfc_pin = [torch.empty(w.shape, dtype=torch.complex128, pin_memory=True) for w in s.wfc]

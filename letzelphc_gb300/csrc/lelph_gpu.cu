@@ -102,6 +102,8 @@ struct lelph_gpu
     // Dmats: Miller -> position tables of the iBZ lists, the job table and the
     // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
     DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32, d_dmstar, d_gstar, d_qsitems;
+    DevBuf d_dmgroups, d_dmperm, d_dmcoefT;  // job groups, plane-wave-major FP32 coefficients (tensor-core Dmats)
+    bool dm_coefT_ready = false;
     DevBuf d_dvraw;  // QE-layout dV_scf of the last ingest and eig pats^H
     bool dm_coef32_ready = false;
     long long coef_total = 0;  // complex coefficients of every iBZ k
@@ -710,6 +712,7 @@ static int upload_wfc(lelph_gpu* h, const double* const* wfc)
     CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->prepared = false;
     h->dm_coef32_ready = false;
+    h->dm_coefT_ready = false;
     return LELPH_GPU_OK;
 }
 
@@ -1197,6 +1200,7 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
                       &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
+                      &h->d_dmgroups, &h->d_dmperm, &h->d_dmcoefT,
                       &h->d_qsitems, &h->d_dvraw, &h->d_gs_perm, &h->d_gs_kcx, &h->d_gs_cols, &h->d_gs_cst,
                       &h->d_gs_npw, &h->d_gs_npad, &h->d_gs_permoff, &h->d_gs_bpoff, &h->d_gs_bp, &h->d_gs_psi,
                       &h->d_gs_out1, &h->d_gs_A, &h->d_gs_part, &h->d_gs_zl, &h->d_gs_cols2, &h->d_gs_bq};
@@ -2650,6 +2654,66 @@ static int dmats_run(lelph_gpu* h, int nsym, const double* Rmat, const double* t
         h->stats.kernel_launches += 1;
         CUDA_TRY(h, cudaGetLastError());
         h->dm_coef32_ready = true;
+    }
+    // mixed form on the tensor cores with LELPH_DMATS_TC=1: about four times more
+    // accurate than the SIMT kernel, but slower at every band count measured
+    // (operand formation, not the contraction, bounds it), so not the default
+    const char* etc = std::getenv("LELPH_DMATS_TC");
+    if (!fp64 && etc && etc[0] == '1' && lelph_dmats_tc_supported(dg))
+    {
+        // groups of jobs sharing (ik1, conj_w), at most JB each
+        int JB, nbt, NT, ntiles;
+        lelph_dmats_tc_config(dg.nb, &JB, &nbt, &NT, &ntiles);
+        std::vector<int> perm((size_t)count);
+        for (long long i = 0; i < count; ++i) perm[(size_t)i] = (int)i;
+        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) {
+            const DmatJob &a = jobs[(size_t)x], &b = jobs[(size_t)y];
+            return a.ik1 != b.ik1 ? a.ik1 < b.ik1 : a.conj_w < b.conj_w;
+        });
+        std::vector<DmatGroup> groups;
+        for (long long i = 0; i < count;)
+        {
+            const DmatJob& J = jobs[(size_t)perm[(size_t)i]];
+            DmatGroup gr{(int)i, 0, J.ik1, J.conj_w};
+            while (i < count && gr.count < JB && jobs[(size_t)perm[(size_t)i]].ik1 == J.ik1 &&
+                   jobs[(size_t)perm[(size_t)i]].conj_w == J.conj_w)
+            {
+                ++gr.count;
+                ++i;
+            }
+            groups.push_back(gr);
+        }
+        if (!h->dm_coefT_ready)
+        {
+            rc = ensure(h, h->d_dmcoefT, sizeof(float2) * (size_t)h->coef_total);
+            if (rc) return rc;
+            lelph_launch_dm_c64t((const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p,
+                                 (const int*)h->d_npw.p, d.nkpts_iBZ, d.nspin, d.nbnds, d.nspinor,
+                                 (float2*)h->d_dmcoefT.p, h->st);
+            h->stats.kernel_launches += 1;
+            CUDA_TRY(h, cudaGetLastError());
+            h->dm_coefT_ready = true;
+        }
+        rc = upload(h, h->d_dmperm, perm.data(), sizeof(int) * perm.size());
+        if (rc) return rc;
+        rc = upload(h, h->d_dmgroups, groups.data(), sizeof(DmatGroup) * groups.size());
+        if (rc) return rc;
+        CUDA_TRY(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned), h->st));
+        tstart(h);
+        if (lelph_launch_dmats_tc((const DmatJob*)h->d_dmjobs.p, count, (const DmatGroup*)h->d_dmgroups.p,
+                                  (const int*)h->d_dmperm.p, (int)groups.size(), dg, (const float2*)h->d_dmcoef32.p,
+                                  (const float2*)h->d_dmcoefT.p, (const long long*)h->d_coefoff.p,
+                                  (const int*)h->d_miller.p,
+                                  (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, (const int*)h->d_dmgtab.p,
+                                  npw_max, (int*)h->d_dmmap.p, out, (unsigned*)h->d_status.p, h->wait_ns, h->st))
+            return fail(h, LELPH_GPU_ERR_UNSUPPORTED, "Dmat launch configuration");
+        h->stats.kernel_launches += 2;
+        CUDA_TRY(h, cudaGetLastError());
+        h->stats.dmats_ms += tstop(h);
+        rc = check_status(h);
+        if (rc) return rc;
+        h->stats.dmats_done += count;
+        return LELPH_GPU_OK;
     }
     tstart(h);
     if (lelph_launch_dmats((const DmatJob*)h->d_dmjobs.p, count, dg, (const double2*)h->d_coef.p,

@@ -246,6 +246,23 @@ struct DmatJob
     double2 M[4];    // 2x2 spinor matrix (row-major)
 };
 static_assert(sizeof(DmatJob) == 208, "DmatJob layout");
+// jobs perm[first .. first + count) share ik1 and conj_w (tensor-core form)
+struct DmatGroup
+{
+    int first, count, ik1, conj_w;
+};
+// tensor-core form of the mixed Dmats (dmats.cu): jobs grouped by (ik1, conj_w)
+// into groups of at most JB (lelph_dmats_tc_config); out is overwritten
+void lelph_dmats_tc_config(int nb, int* JB, int* nbt, int* NT, int* ntiles);
+int lelph_dmats_tc_supported(const DmatGeom& dg);
+// coef32t: the FP32 coefficients in the plane-wave-major order of lelph_launch_dm_c64t
+void lelph_launch_dm_c64t(const double2* in, const long long* coef_off, const int* npw, int nk, int nspin, int nb,
+                          int ns, float2* out, cudaStream_t st);
+int lelph_launch_dmats_tc(const DmatJob* jobs, long long njobs, const DmatGroup* groups, const int* perm,
+                          int ngroups, const DmatGeom& dg, const float2* coef32, const float2* coef32t,
+                          const long long* coef_off, const int* miller, const long long* pw_off, const int* npw,
+                          const int* gtab, int npw_max, int* map, double2* out, unsigned* status,
+                          unsigned long long wait_ns, cudaStream_t st);
 size_t lelph_dmats_smem_bytes(const DmatGeom& dg, int fp64);
 void lelph_launch_dm_gtab(const int* miller, const long long* pw_off, const int* npw, int nk, int npw_max, int Nx,
                           int Ny, int Nz, int* gtab, cudaStream_t st);

@@ -16,9 +16,10 @@
 // Both operands are built in shared memory by producer warps, one 16-plane-
 // wave stage (32 real K elements, one 128-byte K atom) at a time, as TF32
 // (hi, lo) pairs in the 128-byte swizzled K-major layout the MMA descriptors
-// read: per stage the producers tabulate K, Y_lm (FP64, stored FP32), the
-// structure-factor phases (angle reduced to one turn in FP64, sine and cosine
-// in FP32) and F, then form beta and the expanded coefficient rows; the
+// read: per stage the producers tabulate K and Y_lm (FP32, the recurrences of
+// the FP64 form), the structure-factor phases (K.tau = (k + G).(R^T tau) and
+// the angle reduced to one turn in FP64, sine and cosine in FP32) and F, then
+// form beta and the expanded coefficient rows; the
 // tables cover a group of up to 8 stages, so that the serial FP64 work of a
 // table phase is shared by the group.  One thread issues per stage three
 // products of four K = 8 steps (kind::tf32): hi hi into one tensor-memory
@@ -42,20 +43,20 @@
 
 #define PT_G 16           // plane waves per stage
 #define PT_CH 16          // stages per FP32 sum
-#define PT_PWARPS 8       // producer warps
-#define PT_PTHREADS (32 * PT_PWARPS)
+// producer warps: 8, or 7 with two drain groups (512 threads: 128 registers a thread)
+#define PT_PW(NDR) ((NDR) == 1 ? 8 : 7)
 #define PT_NST_MAX 6
 #define PT_SMEM_LIMIT (227 * 1024)
 #define PT_MAXLM 16       // lmax <= 3
 #define PT_MAXATOM 64     // atoms per projector tile
 #define PT_MAXLT 32       // (l shell, type) pairs
-#define PT_THREADS(NDR) (32 * (1 + PT_PWARPS + 4 * (NDR)))
+#define PT_THREADS(NDR) (32 * (1 + PT_PW(NDR) + 4 * (NDR)))
 
 struct PtLayout
 {
     uint32_t a_bytes, b_bytes, stage_bytes, nst;
     uint32_t tab_off, tab_bytes, ylm, kx, f, ph;  // table buffer offsets (two buffers)
-    uint32_t rinfo_off, bar_off, total;
+    uint32_t rinfo_off, taup_off, bar_off, total;
 };
 
 // tables of TG = tgs * PT_G plane waves: Y_lm (nlm rows), K (3 rows), F (nlt rows)
@@ -72,12 +73,13 @@ __host__ __device__ inline PtLayout pt_layout(int NTB, int nlm, int nlt, int nat
     L.f = L.kx + 3 * TG * 4;
     L.ph = L.f + (uint32_t)nlt * TG * 4;
     L.tab_bytes = (L.ph + (uint32_t)natmax * TG * 8 + 15) / 16 * 16;
-    const uint32_t other = 2 * L.tab_bytes + 128 * 5 * 4 + 256 + 1024;
+    const uint32_t other = 2 * L.tab_bytes + 128 * 5 * 4 + (PT_MAXATOM * 3 + 12) * 8 + 256 + 1024;
     L.nst = other < PT_SMEM_LIMIT ? (PT_SMEM_LIMIT - other) / L.stage_bytes : 0;
     if (L.nst > PT_NST_MAX) L.nst = PT_NST_MAX;
     L.tab_off = L.nst * L.stage_bytes;
     L.rinfo_off = L.tab_off + 2 * L.tab_bytes;
-    L.bar_off = L.rinfo_off + 128 * 5 * 4;
+    L.taup_off = L.rinfo_off + 128 * 5 * 4;  // k (3), R (9), R^T tau of the tile's atoms (FP64)
+    L.bar_off = L.taup_off + (PT_MAXATOM * 3 + 12) * 8;
     L.total = L.bar_off + 256 + 1024;  // barriers, alignment slack
     return L;
 }
@@ -99,6 +101,7 @@ __device__ __forceinline__ void pt_split4(float4 v, float4& h, float4& l)
 
 // barrier of the producer warps (id 1) that also ORs a per-thread flag over them:
 // every producer gets the same answer, so they leave their loops together
+template <int NTHR>
 __device__ __forceinline__ bool pt_bar_any(bool v)
 {
     uint32_t r;
@@ -106,7 +109,7 @@ __device__ __forceinline__ bool pt_bar_any(bool v)
         "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)v), "n"(PT_PTHREADS)
+        : "r"((uint32_t)v), "n"(NTHR)
         : "memory");
     return r != 0;
 }
@@ -131,7 +134,7 @@ __device__ __forceinline__ PtUnit pt_unit(int u, int k0, int mtiles, int ntiles)
 
 // Persistent grid: one CTA per SM over units (k, set tile, projector tile),
 // projector tile fastest.  Warp 0: tensor memory and MMA issue; warps
-// 1..PT_PWARPS: producers; then 4*NDR drain warps (lane quadrant warp % 4,
+// 1..PW: producers; then 4*NDR drain warps (lane quadrant warp % 4,
 // 64 accumulator columns each).  proj must be zero on entry.
 template <int NDR, typename CT>
 __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
@@ -149,6 +152,8 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
     const int nlm = (nl.lmax + 1) * (nl.lmax + 1);
     const PtLayout L = pt_layout(NTB, nlm, nlt, natmax, tgs);
     const int TG = tgs * PT_G;
+    constexpr int PW = PT_PW(NDR), PTH = 32 * PW;
+    constexpr int NA = (512 + PTH - 1) / PTH;  // coefficient tasks (64 sets x 8 chunks) per producer thread
     uint64_t* sfull = reinterpret_cast<uint64_t*>(sm + L.bar_off);  // stage written (producer warps)
     uint64_t* sfree = sfull + PT_NST_MAX;                           // stage read (MMA commit)
     uint64_t* accf = sfree + PT_NST_MAX;                            // [2] accumulator complete (MMA commit)
@@ -168,7 +173,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
     {
         for (int s = 0; s < NST; ++s)
         {
-            mbar_init(&sfull[s], PT_PWARPS);
+            mbar_init(&sfull[s], PW);
             mbar_init(&sfree[s], 1);
         }
         for (int b = 0; b < 2; ++b)
@@ -246,7 +251,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
             if (last_commit) mbar_wait_bounded(last_commit, last_par);
         }
     }
-    else if (warp <= PT_PWARPS)
+    else if (warp <= PW)
     {
         // ---------------- producers
         const int p = threadIdx.x - 32;
@@ -256,7 +261,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
         for (int u = blockIdx.x; u < nunits; u += gridDim.x)
         {
             const PtUnit w = pt_unit(u, k0, mtiles, ntiles);
-            const KPointSym S = ks[w.kbz];
+            const KPointSym& S = ks[w.kbz];
             const int npw = npw_arr[S.ik];
             const int nstage = (npw + PT_G - 1) / PT_G;
             const double* G = gvec + 3 * pw_off[S.ik];
@@ -268,7 +273,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
             const int natom_t = a_last - a_first + 1;
             // the previous unit's stages have been formed by every producer before the
             // row table is replaced
-            if (pt_bar_any(failed)) break;
+            if (pt_bar_any<PTH>(failed)) break;
             if (p < NTB)
             {
                 const int rg = row0 + p;
@@ -297,17 +302,45 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                 for (int c = 0; c < 4; ++c) rinfo[p * 5 + c] = info[c];
                 rinfo[p * 5 + 4] = __float_as_int(sg);
             }
+            // k and R of the unit, and R^T tau: K.tau = (k + G).(R^T tau) needs one
+            // FP64 dot product per atom
+            double* kR = reinterpret_cast<double*>(sm + L.taup_off);
+            double* taup = kR + 12;
+            if (p < 3) kR[p] = S.kcart[p];
+            else if (p < 12) kR[p] = S.R[p - 3];
+            else if (p < 12 + 3 * natom_t)
+            {
+                const int a = (p - 12) / 3, x = (p - 12) % 3;
+                const double* ta = nl.atom_pos + 3 * (a_first + a);
+                taup[p - 12] = S.R[x] * ta[0] + S.R[3 + x] * ta[1] + S.R[6 + x] * ta[2];
+            }
+            if (pt_bar_any<PTH>(failed)) break;
             const float* ylm_s = nullptr;
             const float* kx_s = nullptr;
             const float* f_s = nullptr;
             const float2* ph_s = nullptr;
+            float2 cvn[NA][2];
+            auto load_cv = [&](int st_i) {
+                const int g0 = st_i * PT_G;
+#pragma unroll
+                for (int i = 0; i < NA; ++i)
+                {
+                    const int tau = min(p + PTH * i, 511);
+                    const int sl = tau >> 3, c = tau & 7;
+                    const int set = set0 + sl, g = g0 + 2 * c;
+                    cvn[i][0] = (set < nsets && g < npw) ? pt_c32(Cc[(size_t)set * npw + g]) : make_float2(0.f, 0.f);
+                    cvn[i][1] =
+                        (set < nsets && g + 1 < npw) ? pt_c32(Cc[(size_t)set * npw + g + 1]) : make_float2(0.f, 0.f);
+                }
+            };
+            load_cv(0);
             bool leave = false;
             for (int it = 0; it < nstage; ++it)
             {
                 const int gi = it % tgs;  // stage within its table group
                 if (gi == 0)
                 {
-                    // tables of the group's TG plane waves (K, Y_lm in FP64, phases, F)
+                    // tables of the group's TG plane waves (K and Y_lm in FP32, phases, F)
                     uint8_t* tab = sm + L.tab_off + (uint32_t)(ngroup & 1) * L.tab_bytes;
                     ++ngroup;
                     float* ylm_w = reinterpret_cast<float*>(tab + L.ylm);
@@ -316,34 +349,38 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     float2* ph_w = reinterpret_cast<float2*>(tab + L.ph);
                     const int gbase = it * PT_G;
                     const int ntask = TG * (1 + natom_t + nlt);
-                    for (int tau = p; tau < ntask; tau += PT_PTHREADS)
+                    for (int tau = p; tau < ntask; tau += PTH)
                     {
                         const int gg = tau % TG, kind = tau / TG;
                         const int g = gbase + gg;
                         if (kind < 1 + natom_t)
                         {
-                            double K0 = 0.0, K1 = 0.0, K2 = 0.0;
+                            double v0 = 0.0, v1 = 0.0, v2 = 0.0;
                             if (g < npw)
                             {
-                                const double v0 = S.kcart[0] + G[3 * g], v1 = S.kcart[1] + G[3 * g + 1],
-                                             v2 = S.kcart[2] + G[3 * g + 2];
-                                K0 = S.R[0] * v0 + S.R[1] * v1 + S.R[2] * v2;
-                                K1 = S.R[3] * v0 + S.R[4] * v1 + S.R[5] * v2;
-                                K2 = S.R[6] * v0 + S.R[7] * v1 + S.R[8] * v2;
+                                v0 = kR[0] + G[3 * g];
+                                v1 = kR[1] + G[3 * g + 1];
+                                v2 = kR[2] + G[3 * g + 2];
                             }
                             if (kind == 0)
                             {
-                                double y[PT_MAXLM];
-                                ylm_all(nl.lmax, K0, K1, K2, y);
-                                for (int i = 0; i < nlm; ++i) ylm_w[i * TG + gg] = g < npw ? (float)y[i] : 0.f;
-                                kx_w[0 * TG + gg] = (float)K0;
-                                kx_w[1 * TG + gg] = (float)K1;
-                                kx_w[2 * TG + gg] = (float)K2;
+                                // K = R (k + G) and Y_lm(K) in FP32
+                                const float f0 = (float)v0, f1 = (float)v1, f2 = (float)v2;
+                                const double* R = kR + 3;
+                                const float K0 = (float)R[0] * f0 + (float)R[1] * f1 + (float)R[2] * f2;
+                                const float K1 = (float)R[3] * f0 + (float)R[4] * f1 + (float)R[5] * f2;
+                                const float K2 = (float)R[6] * f0 + (float)R[7] * f1 + (float)R[8] * f2;
+                                if (g < npw) ylm_all_f(nl.lmax, K0, K1, K2, ylm_w + gg, TG);
+                                else
+                                    for (int i = 0; i < nlm; ++i) ylm_w[i * TG + gg] = 0.f;
+                                kx_w[0 * TG + gg] = K0;
+                                kx_w[1 * TG + gg] = K1;
+                                kx_w[2 * TG + gg] = K2;
                             }
                             else
                             {
-                                const double* tau_a = nl.atom_pos + 3 * (a_first + kind - 1);
-                                const double dot = K0 * tau_a[0] + K1 * tau_a[1] + K2 * tau_a[2];
+                                const double* tp = taup + 3 * (kind - 1);
+                                const double dot = v0 * tp[0] + v1 * tp[1] + v2 * tp[2];
                                 // the angle 2 pi_T dot reduced to one turn in FP64 (pi_T the
                                 // reference's truncated pi), sine and cosine in FP32
                                 const double turns = dot * (LELPH_PI_T / 3.14159265358979323846);
@@ -363,25 +400,23 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     f_s = f_w;
                     ph_s = ph_w;
                     // tables complete; every producer leaves together when any one's wait ran out
-                    if (pt_bar_any(failed))
+                    if (pt_bar_any<PTH>(failed))
                     {
                         leave = true;
                         break;
                     }
                 }
-                const int g0 = it * PT_G;
-                // coefficient loads first: tasks (set, 2-plane-wave chunk), 2 per thread
-                float2 cv[2][2];
+                // this stage's coefficients (loaded one stage ahead) and the next
+                // stage's loads, in flight while this stage is formed: tasks (set,
+                // 2-plane-wave chunk)
+                float2 cv[NA][2];
 #pragma unroll
-                for (int i = 0; i < 2; ++i)
+                for (int i = 0; i < NA; ++i)
                 {
-                    const int tau = p + PT_PTHREADS * i;
-                    const int sl = tau >> 3, c = tau & 7;
-                    const int set = set0 + sl, g = g0 + 2 * c;
-                    cv[i][0] = (set < nsets && g < npw) ? pt_c32(Cc[(size_t)set * npw + g]) : make_float2(0.f, 0.f);
-                    cv[i][1] =
-                        (set < nsets && g + 1 < npw) ? pt_c32(Cc[(size_t)set * npw + g + 1]) : make_float2(0.f, 0.f);
+                    cv[i][0] = cvn[i][0];
+                    cv[i][1] = cvn[i][1];
                 }
+                if (it + 1 < nstage) load_cv(it + 1);
                 if (!failed && !mbar_wait_bounded(&sfree[s], phs ^ 1u, wait_ns))
                 {
                     failed = true;
@@ -396,9 +431,15 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     uint8_t* Bhi = st + 2 * L.a_bytes;
                     uint8_t* Blo = Bhi + L.b_bytes;
                     // B: projector rows n, chunk c = plane waves 2c, 2c + 1 of the stage
-                    for (int tau = p; tau < NTB * 8; tau += PT_PTHREADS)
+                    // eight lanes per row, consecutive plane waves: a warp's table reads
+                    // fall in consecutive words (no bank conflicts between rows)
+                    constexpr int NBT = (128 * 8 + PTH - 1) / PTH;
+#pragma unroll
+                    for (int i = 0; i < NBT; ++i)
                     {
-                        const int n = tau % NTB, c = tau / NTB;
+                        const int tau = p + PTH * i;
+                        if (tau >= NTB * 8) break;
+                        const int n = tau >> 3, c = tau & 7;
                         const int* ri = rinfo + n * 5;
                         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                         if (ri[0] >= 0)
@@ -424,9 +465,10 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     }
                     // A: the coefficient rows 2 sl (cr, ci) and 2 sl + 1 (-ci, cr)
 #pragma unroll
-                    for (int i = 0; i < 2; ++i)
+                    for (int i = 0; i < NA; ++i)
                     {
-                        const int tau = p + PT_PTHREADS * i;
+                        const int tau = p + PTH * i;
+                        if (tau >= 512) break;
                         const int sl = tau >> 3, c = tau & 7;
                         const float cr0 = cv[i][0].x, ci0 = cv[i][0].y, cr1 = cv[i][1].x, ci1 = cv[i][1].y;
                         float4 h, l;
@@ -451,10 +493,10 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
             if (leave) break;
         }
     }
-    else if (warp < 1 + PT_PWARPS + ndrain)
+    else if (warp < 1 + PW + ndrain)
     {
         // ---------------- drains: lane quadrant warp % 4, columns [64 cg, 64 cg + 64)
-        const int dw = warp - 1 - PT_PWARPS;
+        const int dw = warp - 1 - PW;
         const int q = warp & 3, cg = dw >> 2;
         const int r = q * 32 + lane;  // accumulator row: set 2 sl + part
         const int sl = r >> 1, part = r & 1;

@@ -60,3 +60,61 @@ __device__ __forceinline__ void ylm_all(int lmax, double vx, double vy, double v
     }
 }
 
+
+// The same in FP32 (the mixed form's tensor-core projections): identical
+// recurrences and normalisation, evaluated in single precision as the
+// reference's default single-precision build does.
+__device__ __forceinline__ float ylm_legendre_f(int l, int m, float x)
+{
+    float val = 1.f;
+    if (l == 0 && m == 0) return 1.f;
+    if (m > l) return 0.f;
+    const float sq = sqrtf(fmaxf(1.f - x * x, 0.f));
+    for (int im = 1; im <= m; ++im) val *= (float)(2 * im - 1) * sq;
+    if (l == m) return val;
+    float vmm = val;
+    val *= (float)(2 * m + 1) * x;
+    if (l == m + 1) return val;
+    for (int im = m + 2; im <= l; ++im)
+    {
+        const float tmp = val;
+        val = ((float)(2 * im - 1) * x * val - (float)(im + m - 1) * vmm) / (float)(im - m);
+        vmm = tmp;
+    }
+    return val;
+}
+
+// y[(l*l + l + m) * stride] (y in shared memory: no local array)
+__device__ __forceinline__ void ylm_all_f(int lmax, float vx, float vy, float vz, float* y, int stride)
+{
+    const float norm = sqrtf(vx * vx + vy * vy + vz * vz);
+    if (norm < 1e-6f)
+    {
+        for (int i = 0; i < (lmax + 1) * (lmax + 1); ++i) y[i * stride] = 0.f;
+        y[0] = 1.f / sqrtf(4.f * (float)LELPH_PI_T);
+        return;
+    }
+    const float cost = vz / norm;
+    const float rxy = sqrtf(vx * vx + vy * vy);
+    const float c1 = rxy > 0.f ? vx / rxy : 1.f, s1 = rxy > 0.f ? vy / rxy : 0.f;
+    float cm = 1.f, sm = 0.f;
+    for (int m = 0; m <= lmax; ++m)
+    {
+        for (int l = m; l <= lmax; ++l)
+        {
+            float ratio = 1.f;  // (l - m)! / (l + m)!
+            for (int i = l - m + 1; i <= l + m; ++i) ratio /= (float)i;
+            const float p = ylm_legendre_f(l, m, cost) * sqrtf(ratio * (float)(2 * l + 1) / (4.f * (float)LELPH_PI_T));
+            if (m == 0)
+                y[(l * l + l) * stride] = p;
+            else
+            {
+                y[(l * l + l + m) * stride] = 1.41421356f * cm * p;
+                y[(l * l + l - m) * stride] = 1.41421356f * sm * p;
+            }
+        }
+        const float cn = cm * c1 - sm * s1, sn = sm * c1 + cm * s1;
+        cm = cn;
+        sm = sn;
+    }
+}

@@ -72,3 +72,53 @@ def test_dmats_reject_bad_operations(golden):
         assert e.value.status == -5
         with pytest.raises(LelphError):
             ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev, first=len(s.sym_R) * s.nk_bz - 2, count=5)
+
+
+# ---- the mixed form on the tensor cores (k_dmats_tc, LELPH_DMATS_TC=1) against
+# the SIMT kernel (the default): groups of jobs that share k1 (up to 4 jobs of
+# 32 bands per unit), one job per unit in band tiles above 64 bands, both
+# spinor counts, two spins, ragged plane-wave counts.
+def _dmats_both(s, monkeypatch, **kw):
+    monkeypatch.setenv("LELPH_DMATS_TC", "0")
+    with LelphGPU(s, "mixed") as ctx:
+        d_simt = ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev, **kw)
+    monkeypatch.setenv("LELPH_DMATS_TC", "1")
+    with LelphGPU(s, "mixed") as ctx:
+        d_tc = ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev, **kw)
+    return d_tc, d_simt
+
+
+@pytest.mark.parametrize("name", ["c0", "l12", "soc_tr", "lsda", "hex_ragged"])
+def test_dmats_tensor_cores_match_simt(golden, name, monkeypatch):
+    z, systems = golden
+    s = systems[name]
+    ref = O.dmats(s).reshape(-1, s.nspin, s.nbnds, s.nbnds)
+    d_tc, d_simt = _dmats_both(s, monkeypatch)
+    e_tc, e_simt = np.abs(d_tc - ref).max(), np.abs(d_simt - ref).max()
+    print(f"{name}: max|D - D_fp64| tensor cores {e_tc:.2e}, SIMT {e_simt:.2e}")
+    assert e_tc < MIXED_TOL, (name, e_tc)
+    assert np.abs(d_tc - d_simt).max() < MIXED_TOL, name
+
+
+@pytest.mark.parametrize("nbnds", [80, 136])
+def test_dmats_tensor_cores_band_tiles(monkeypatch, nbnds):
+    from letzelphc_gb300 import synth
+    s = synth.make_system("c0", {"nbnds": nbnds, "npw": 600, "kgrid": (2, 2, 2)})
+    with LelphGPU(s, "fp64") as ctx:
+        ref = ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev)
+    d_tc, d_simt = _dmats_both(s, monkeypatch)
+    e_tc, e_simt = np.abs(d_tc - ref).max(), np.abs(d_simt - ref).max()
+    print(f"{nbnds} bands: max|D - D_fp64| tensor cores {e_tc:.2e}, SIMT {e_simt:.2e}")
+    assert e_tc < MIXED_TOL, e_tc
+
+
+def test_dmats_tensor_cores_block_equals_table(golden, monkeypatch):
+    # a block groups its jobs differently from the whole table; each job's
+    # matrix does not depend on its group
+    z, systems = golden
+    s = systems["l12"]
+    monkeypatch.setenv("LELPH_DMATS_TC", "1")
+    with LelphGPU(s, "mixed") as ctx:
+        full = ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev)
+        part = ctx.dmats(s.sym_R, s.sym_tau, s.sym_trev, first=37, count=101)
+    assert np.abs(part - full[37:138]).max() < 1e-12
