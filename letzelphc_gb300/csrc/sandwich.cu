@@ -152,8 +152,8 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 // ============================================================= mixed form
 //
 // Warp roles: warp 0 issues TMA, warp 1 owns tensor memory and issues the
-// MMAs, warps 2-9 build the A operand directly in tensor memory, warps
-// 10.. drain the accumulators.
+// MMAs, warps 2 .. 2 + 4 PQ - 1 build the A operand directly in tensor
+// memory, the next warps drain the accumulators.
 //
 // Tensor memory (512 columns): NACC (4, or 2 for wide tiles) accumulators,
 // then NA A-operand slots of 128 columns (A_hi: 64 columns, A_lo: 64 columns;
@@ -169,8 +169,13 @@ void lelph_launch_local_fp64(const PairInfo* pairs, int npairs, const double2* p
 // A pipeline stage is KP grid points (KP/32 K atoms of 128 bytes); one TMEM
 // accumulator chains 64 points (two 32-point stages or one 64-point stage)
 // before it is drained.
-// 10 role warps + 4 drain warps per 64 accumulator columns (NDR groups)
-#define TC_THREADS(NDR) (32 * (10 + 4 * (NDR)))
+// producer warps per TMEM lane quadrant (each forms KP / PQ points of a stage,
+// at least one 16-point block)
+#define TC_PQ 2
+template <int KP> __host__ __device__ constexpr int tc_pq() { return KP >= 16 * TC_PQ ? TC_PQ : KP / 16; }
+// TMA and MMA warps, 4 PQ producer warps, 4 drain warps per 64 accumulator
+// columns (NDR groups)
+#define TC_THREADS(KP, NDR) (32 * (2 + 4 * tc_pq<KP>() + 4 * (NDR)))
 
 struct TcSmemLayout
 {
@@ -352,7 +357,7 @@ __device__ __forceinline__ void prod_store(const ProdFrag<SUB, NC>& f, uint32_t 
     }
 }
 
-// A producer's share of one pipeline stage: points h*KP/2 .. (h+1)*KP/2 - 1,
+// A producer's share of one pipeline stage: points h*KP/PQ .. (h+1)*KP/PQ - 1,
 // in 16-point psi blocks of 16/SUB pieces of SUB points each.  The pieces are
 // software-pipelined: the shared-memory loads of piece t+1 are issued before
 // piece t is formed and stored, so that their latency overlaps the work.
@@ -362,14 +367,17 @@ __device__ __forceinline__ void produce_stage(const uint8_t* st, const TcSmemLay
                                               int nsp, uint32_t swz, uint32_t col_base)
 {
     constexpr int NATOM = KP / 32;
+    constexpr int PPW = KP / tc_pq<KP>();  // points of this warp
+    static_assert(PPW % 16 == 0, "a producer warp forms whole 16-point blocks");
+    constexpr int NBW = PPW / 16;    // 16-point blocks of this warp
     constexpr int PER_BLOCK = 16 / SUB;
-    constexpr int NPIECE = (KP / 32) * PER_BLOCK;
-    const uint8_t* pp[NPIECE / PER_BLOCK][2];
-    const float4* dvp[NPIECE / PER_BLOCK][2];
+    constexpr int NPIECE = NBW * PER_BLOCK;
+    const uint8_t* pp[NBW][2];
+    const float4* dvp[NBW][2];
 #pragma unroll
-    for (int b = 0; b < KP / 32; ++b)
+    for (int b = 0; b < NBW; ++b)
     {
-        const int p0 = h * (KP / 2) + 16 * b;  // first point of the block in the stage
+        const int p0 = h * PPW + 16 * b;  // first point of the block in the stage
         const int pb = p0 >> 4;                // 16-point psi block
         const float* dvs = reinterpret_cast<const float*>(st + L.dv + (uint32_t)(p0 >> 5) * L.dv_block);
         pp[b][0] = st + L.p + (0 * 2 * NATOM + pb) * L.p_half + (uint32_t)m * 128;
@@ -392,7 +400,7 @@ __device__ __forceinline__ void produce_stage(const uint8_t* st, const TcSmemLay
                 prod_load<SUB, NC>(f[(t + 1) & 1], pp[bn], dvp[bn], swz, ((t + 1) % PER_BLOCK) * SUB);
             }
             const int b = t / PER_BLOCK, j0 = (t % PER_BLOCK) * SUB;
-            const uint32_t col_hi = col_base + (uint32_t)(h * (KP / 2) + 16 * b + j0);
+            const uint32_t col_hi = col_base + (uint32_t)(h * PPW + 16 * b + j0);
             prod_store<BF16, SUB, NC>(f[t & 1], col_hi, col_hi + KP);
         }
     }
@@ -404,7 +412,7 @@ __device__ __forceinline__ void produce_stage(const uint8_t* st, const TcSmemLay
             ProdFrag<SUB, NC> f;
             const int b = t / PER_BLOCK, j0 = (t % PER_BLOCK) * SUB;
             prod_load<SUB, NC>(f, pp[b], dvp[b], swz, j0);
-            const uint32_t col_hi = col_base + (uint32_t)(h * (KP / 2) + 16 * b + j0);
+            const uint32_t col_hi = col_base + (uint32_t)(h * PPW + 16 * b + j0);
             prod_store<BF16, SUB, NC>(f, col_hi, col_hi + KP);
         }
     }
@@ -502,7 +510,7 @@ __device__ __forceinline__ void umma_stage_merged<32>(uint32_t dacc, uint32_t da
 // c + 2G, ... with u = (pair*nspin + spin, mode tile, K chunk), chunk fastest.
 // The barrier rings, the tensor memory and the TMA pipeline carry over from
 // one unit to the next, so a unit's first tiles are in flight while the
-// previous unit drains.  32*(10 + ndrain) threads.
+// previous unit drains.  TC_THREADS(KP, NDR) threads.
 //
 // The tensor-core accumulator loses low-order bits on every accumulation
 // (its error grows linearly with the number of MMAs chained into one FP32
@@ -530,7 +538,7 @@ __device__ __forceinline__ TcUnit tc_unit(int u, int nchunks, int mtiles, int ns
 }
 
 template <int BF16, int KP, int NDR>
-__global__ void __launch_bounds__(TC_THREADS(NDR), 1)
+__global__ void __launch_bounds__(TC_THREADS(KP, NDR), 1)
     k_local_tc(const __grid_constant__ CUtensorMap tmapB, const __grid_constant__ CUtensorMap tmapP,
                const __grid_constant__ CUtensorMap tmapV, const PairInfo* __restrict__ pairs, GeomDev gd,
                int chunk_pts, int nchunks, int mtiles, int nunits, float* __restrict__ partials,
@@ -543,7 +551,7 @@ __global__ void __launch_bounds__(TC_THREADS(NDR), 1)
     uint8_t* sm = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
     const TcSmemLayout L = tc_layout(gd);
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar_off);
-    uint64_t* empty = full + TC_NST_MAX;    // TMA slot consumed: MMA commit + 8 producer warps
+    uint64_t* empty = full + TC_NST_MAX;    // TMA slot consumed: MMA commit + 4 PQ producer warps
     uint64_t* aready = empty + TC_NST_MAX;  // A slot written (producers -> MMA)
     uint64_t* afree = aready + TC_NA_MAX;   // A slot read (MMA commit -> producers)
     uint64_t* accf = afree + TC_NA_MAX;     // [nacc] accumulator b complete (MMA -> drain)
@@ -568,11 +576,11 @@ __global__ void __launch_bounds__(TC_THREADS(NDR), 1)
         for (int s = 0; s < NST; ++s)
         {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1 + 8);
+            mbar_init(&empty[s], 1 + 4 * tc_pq<KP>());
         }
         for (int a = 0; a < NA; ++a)
         {
-            mbar_init(&aready[a], 8);
+            mbar_init(&aready[a], 4 * tc_pq<KP>());
             mbar_init(&afree[a], 1);
         }
         for (int b = 0; b < NACC; ++b)
@@ -738,10 +746,10 @@ __global__ void __launch_bounds__(TC_THREADS(NDR), 1)
             if (last_commit) mbar_wait_bounded(last_commit, last_par);
         }
     }
-    else if (warp < 10)
+    else if (warp < 2 + 4 * tc_pq<KP>())
     {
         // ---------------- A producers: lane quadrant q = warp % 4 (rows 32q..32q+31),
-        // half h of the stage's points
+        // share h of the stage's points (KP / PQ of them)
         const int q = warp & 3;
         const int h = (warp - 2) >> 2;
         const int MT = gd.mt_modes;
@@ -790,10 +798,10 @@ __global__ void __launch_bounds__(TC_THREADS(NDR), 1)
                 const uint8_t* st = sm + s * L.stage_bytes;
                 const uint32_t col_base = lane_base + L.a_col0 + (uint32_t)a * (2u * KP);
                 if (gd.nmag == 4)
-                    produce_stage<BF16, KP, 4, 2, 1>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
+                    produce_stage<BF16, KP, 4, 2, (tc_pq<KP>() <= 2)>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
                                                      swz, col_base);
                 else
-                    produce_stage<BF16, KP, 8, 1, 1>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
+                    produce_stage<BF16, KP, 8, 1, (tc_pq<KP>() <= 2)>(st, L, zero_dv, in_tile, h, m, ml, gd.nmag, comp0, comp1, nsp,
                                                      swz, col_base);
                 tmem_wait_st();
                 tc_fence_before();
@@ -806,10 +814,10 @@ __global__ void __launch_bounds__(TC_THREADS(NDR), 1)
             }
         }
     }
-    else if (warp < 10 + ndrain)
+    else if (warp < 2 + 4 * tc_pq<KP>() + ndrain)
     {
         // ---------------- drain warps: TMEM lane quadrant warp%4, 64-column half
-        const int dw = warp - 10;
+        const int dw = warp - 2 - 4 * tc_pq<KP>();
         const int q = warp & 3;
         const int c0 = (dw >> 2) * 64;
         const int nc = min(64, NT - c0);
@@ -897,7 +905,7 @@ void lelph_launch_local_tc(const PairInfo* pairs, int npairs, const void* tmapB,
     do                                                                                                           \
     {                                                                                                            \
         cudaFuncSetAttribute(k_local_tc<BF, KPV, NDR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);        \
-        k_local_tc<BF, KPV, NDR><<<grid, TC_THREADS(NDR), smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, \
+        k_local_tc<BF, KPV, NDR><<<grid, TC_THREADS(KPV, NDR), smem, st>>>(*tB, *tP, *tV, pairs, g, chunk_pts, nchunks, \
                                                                      mtiles, (int)units, partials, status,       \
                                                                      wait_ns);                                   \
     } while (0)
