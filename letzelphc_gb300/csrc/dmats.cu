@@ -32,6 +32,7 @@
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
+#include "tc_operands.cuh"
 
 #define DM_TB 32       // D tile (bands) per CTA, both sides
 #define DM_KC 32       // plane waves per staged chunk
@@ -528,28 +529,6 @@ __host__ __device__ inline DtLayout dt_layout(int NT, int ntab)
     return L;
 }
 
-__device__ __forceinline__ uint32_t dt_swz(int r, int c) { return (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4); }
-
-__device__ __forceinline__ void dt_split4(float4 v, float4& h, float4& l)
-{
-    h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-    l = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
-}
-
-// producer barrier (id 1) that ORs a per-thread flag: the producers leave together
-template <int NTHR>
-__device__ __forceinline__ bool dt_bar_any(bool v)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)v), "n"(NTHR)
-        : "memory");
-    return r != 0;
-}
-
 struct DtUnit
 {
     int grp, spin, mt, nt;
@@ -693,7 +672,7 @@ __global__ void __launch_bounds__(DT_THREADS(NDR), 1)
             const int* mil1 = miller + 3 * pw_off[G.ik1];
             const float2* c1 = coef + coef_off[G.ik1] + (long long)w.spin * nb * NS * npw1;
             // the previous unit's stages are formed before its job data is replaced
-            if (dt_bar_any<PTH>(failed)) break;
+            if (tc_producer_bar_any<PTH>(failed)) break;
             for (int e = p; e < G.count * (1 + dg.ntab); e += PTH)
             {
                 const int j = e / (1 + dg.ntab), i = e % (1 + dg.ntab);
@@ -718,7 +697,7 @@ __global__ void __launch_bounds__(DT_THREADS(NDR), 1)
                     tab_s[j * dg.ntab + ti] = dm_phase<float2>((double)(ti - base - Nax / 2) * J.t[ax]);
                 }
             }
-            if (dt_bar_any<PTH>(failed)) break;
+            if (tc_producer_bar_any<PTH>(failed)) break;
             bool leave = false;
             int cur = 0;  // position-data buffer of the current group of stages
             for (int it = 0; it < nstage; ++it)
@@ -756,7 +735,7 @@ __global__ void __launch_bounds__(DT_THREADS(NDR), 1)
                         pii[e] = ii;
                         pc[e] = c;
                     }
-                    if (dt_bar_any<PTH>(failed))
+                    if (tc_producer_bar_any<PTH>(failed))
                     {
                         leave = true;
                         break;
@@ -803,12 +782,12 @@ __global__ void __launch_bounds__(DT_THREADS(NDR), 1)
                             r1 = make_float4(y[0].y, y[0].x, y[1].y, y[1].x);
                         }
                         float4 h, l;
-                        dt_split4(r0, h, l);
-                        *reinterpret_cast<float4*>(Ahi + dt_swz(2 * rp, c)) = h;
-                        *reinterpret_cast<float4*>(Alo + dt_swz(2 * rp, c)) = l;
-                        dt_split4(r1, h, l);
-                        *reinterpret_cast<float4*>(Ahi + dt_swz(2 * rp + 1, c)) = h;
-                        *reinterpret_cast<float4*>(Alo + dt_swz(2 * rp + 1, c)) = l;
+                        tc_split4_tf32(r0, h, l);
+                        *reinterpret_cast<float4*>(Ahi + tc_swz128(2 * rp, c)) = h;
+                        *reinterpret_cast<float4*>(Alo + tc_swz128(2 * rp, c)) = l;
+                        tc_split4_tf32(r1, h, l);
+                        *reinterpret_cast<float4*>(Ahi + tc_swz128(2 * rp + 1, c)) = h;
+                        *reinterpret_cast<float4*>(Alo + tc_swz128(2 * rp + 1, c)) = l;
                     }
                     // B: k2 rows (job j, band b), chunk c
                     const int* pii = pos_ii + cur * L.pos_n + sg * DT_G * DT_JB;
@@ -864,9 +843,9 @@ __global__ void __launch_bounds__(DT_THREADS(NDR), 1)
                                 v[e] = cmul(r, pc[j * DT_G + 2 * c + e]);
                             }
                             float4 h, l;
-                            dt_split4(make_float4(v[0].x, v[0].y, v[1].x, v[1].y), h, l);
-                            *reinterpret_cast<float4*>(Bhi + dt_swz(n, c)) = h;
-                            *reinterpret_cast<float4*>(Blo + dt_swz(n, c)) = l;
+                            tc_split4_tf32(make_float4(v[0].x, v[0].y, v[1].x, v[1].y), h, l);
+                            *reinterpret_cast<float4*>(Bhi + tc_swz128(n, c)) = h;
+                            *reinterpret_cast<float4*>(Blo + tc_swz128(n, c)) = l;
                         }
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

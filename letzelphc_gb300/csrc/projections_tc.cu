@@ -39,6 +39,7 @@
 
 #include "lelph_common.cuh"
 #include "lelph_internal.h"
+#include "tc_operands.cuh"
 #include "ylm.cuh"
 
 #define PT_G 16           // plane waves per stage
@@ -82,36 +83,6 @@ __host__ __device__ inline PtLayout pt_layout(int NTB, int nlm, int nlt, int nat
     L.bar_off = L.taup_off + (PT_MAXATOM * 3 + 12) * 8;
     L.total = L.bar_off + 256 + 1024;  // barriers, alignment slack
     return L;
-}
-
-// offset of the 16-byte chunk c of row r in a 128-byte swizzled K-major tile
-__device__ __forceinline__ uint32_t pt_swz(int r, int c) { return (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4); }
-
-__device__ __forceinline__ void pt_split4(float4 v, float4& h, float4& l)
-{
-    h.x = tf32_rn(v.x);
-    h.y = tf32_rn(v.y);
-    h.z = tf32_rn(v.z);
-    h.w = tf32_rn(v.w);
-    l.x = tf32_rn(v.x - h.x);
-    l.y = tf32_rn(v.y - h.y);
-    l.z = tf32_rn(v.z - h.z);
-    l.w = tf32_rn(v.w - h.w);
-}
-
-// barrier of the producer warps (id 1) that also ORs a per-thread flag over them:
-// every producer gets the same answer, so they leave their loops together
-template <int NTHR>
-__device__ __forceinline__ bool pt_bar_any(bool v)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)v), "n"(NTHR)
-        : "memory");
-    return r != 0;
 }
 
 __device__ __forceinline__ float2 pt_c32(double2 v) { return make_float2((float)v.x, (float)v.y); }
@@ -273,7 +244,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
             const int natom_t = a_last - a_first + 1;
             // the previous unit's stages have been formed by every producer before the
             // row table is replaced
-            if (pt_bar_any<PTH>(failed)) break;
+            if (tc_producer_bar_any<PTH>(failed)) break;
             if (p < NTB)
             {
                 const int rg = row0 + p;
@@ -314,7 +285,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                 const double* ta = nl.atom_pos + 3 * (a_first + a);
                 taup[p - 12] = S.R[x] * ta[0] + S.R[3 + x] * ta[1] + S.R[6 + x] * ta[2];
             }
-            if (pt_bar_any<PTH>(failed)) break;
+            if (tc_producer_bar_any<PTH>(failed)) break;
             const float* ylm_s = nullptr;
             const float* kx_s = nullptr;
             const float* f_s = nullptr;
@@ -400,7 +371,7 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     f_s = f_w;
                     ph_s = ph_w;
                     // tables complete; every producer leaves together when any one's wait ran out
-                    if (pt_bar_any<PTH>(failed))
+                    if (tc_producer_bar_any<PTH>(failed))
                     {
                         leave = true;
                         break;
@@ -459,9 +430,9 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                             v = make_float4(b2[0], b2[1], b2[2], b2[3]);
                         }
                         float4 h, l;
-                        pt_split4(v, h, l);
-                        *reinterpret_cast<float4*>(Bhi + pt_swz(n, c)) = h;
-                        *reinterpret_cast<float4*>(Blo + pt_swz(n, c)) = l;
+                        tc_split4_tf32(v, h, l);
+                        *reinterpret_cast<float4*>(Bhi + tc_swz128(n, c)) = h;
+                        *reinterpret_cast<float4*>(Blo + tc_swz128(n, c)) = l;
                     }
                     // A: the coefficient rows 2 sl (cr, ci) and 2 sl + 1 (-ci, cr)
 #pragma unroll
@@ -472,12 +443,12 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                         const int sl = tau >> 3, c = tau & 7;
                         const float cr0 = cv[i][0].x, ci0 = cv[i][0].y, cr1 = cv[i][1].x, ci1 = cv[i][1].y;
                         float4 h, l;
-                        pt_split4(make_float4(cr0, ci0, cr1, ci1), h, l);
-                        *reinterpret_cast<float4*>(Ahi + pt_swz(2 * sl, c)) = h;
-                        *reinterpret_cast<float4*>(Alo + pt_swz(2 * sl, c)) = l;
-                        pt_split4(make_float4(-ci0, cr0, -ci1, cr1), h, l);
-                        *reinterpret_cast<float4*>(Ahi + pt_swz(2 * sl + 1, c)) = h;
-                        *reinterpret_cast<float4*>(Alo + pt_swz(2 * sl + 1, c)) = l;
+                        tc_split4_tf32(make_float4(cr0, ci0, cr1, ci1), h, l);
+                        *reinterpret_cast<float4*>(Ahi + tc_swz128(2 * sl, c)) = h;
+                        *reinterpret_cast<float4*>(Alo + tc_swz128(2 * sl, c)) = l;
+                        tc_split4_tf32(make_float4(-ci0, cr0, -ci1, cr1), h, l);
+                        *reinterpret_cast<float4*>(Ahi + tc_swz128(2 * sl + 1, c)) = h;
+                        *reinterpret_cast<float4*>(Alo + tc_swz128(2 * sl + 1, c)) = l;
                     }
                     // generic-proxy writes -> the tensor core's async proxy
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
