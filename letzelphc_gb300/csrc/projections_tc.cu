@@ -388,11 +388,20 @@ __global__ void __launch_bounds__(PT_THREADS(NDR), 1)
                     cv[i][1] = cvn[i][1];
                 }
                 if (it + 1 < nstage) load_cv(it + 1);
-                if (!failed && !mbar_wait_bounded(&sfree[s], phs ^ 1u, wait_ns))
+                // the slot wait, decided for the whole warp: the fill below ends in a
+                // __syncwarp, which every lane must reach
+                if (!failed)
                 {
-                    failed = true;
-                    *abort_flag = 1;
-                    atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&sfree[s], phs ^ 1u, wait_ns));
+                    if (!ok)
+                    {
+                        failed = true;
+                        if (lane == 0)
+                        {
+                            *abort_flag = 1;
+                            atomicOr(status, LELPH_DEV_ERR_TIMEOUT);
+                        }
+                    }
                 }
                 if (!failed)
                 {
