@@ -49,7 +49,7 @@ WORKLOAD = "4-atom cell, 48^3 grid, npw~2500, 8x8x8 k, 8 q, 12 modes, 32 bands, 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="mixed_f16")

@@ -513,7 +513,10 @@ void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const 
                                  float2* psi32, cudaStream_t st, const BoxMask& mk)
 {
     const int inner = g.Ny * g.Nz;
-    int ich = ich_for(p.L, inner, 4096);
+    // 2048 elements a block (half the other passes' chunk): more blocks per SM to
+    // overlap one block's loads with another's transform and stores (measured
+    // 5.7 -> 5.4 ms per bench step; 1024 is slower again)
+    int ich = ich_for(p.L, inner, 2048);
     int nchunk = (inner + ich - 1) / ich;
     size_t smem = (size_t)(2 * ich * p.L + p.L) * sizeof(float2);
     long long nbox = (long long)nbox_k * g.nspin * g.nbnds * g.nspinor;
