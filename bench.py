@@ -395,6 +395,52 @@ def run_profile_case(args):
     return 0
 
 
+def path_roofline(s, value, peaks, clk_mhz):
+    """The path-level roofline of the survey's measurement contract, per pair:
+    T_roof = max(B_min / BW_HBM, F_fft / P_simt, F_gemm_eff / P_tc, F_nl / P_tc),
+    with the reference algorithm's own counts (FFTs = nspin nb nspinor + nm nspin
+    nb nspinor per pair on the reference box, each 5 [sticks Nz log2 Nz +
+    x_act Ny Nz log2 Ny + N log2 Nx] flops; F_gemm_eff = 3 split products of
+    8 nm nspin nb^2 nspinor npw; F_nl = 16 (4 P natom) npw nspin nb nspinor +
+    8 nm 3 natom nspin nb^2) and the compulsory bytes B_min (FP32 complex).
+    achieved = T_roof / T_meas, T_meas = the step's time per pair; above 1
+    means the implementation does less work than the reference's algorithm
+    (the real-space route needs no per-mode FFT)."""
+    Nx, Ny, Nz = (int(v) for v in s.fft_dims)
+    N = Nx * Ny * Nz
+    ff = []
+    npws = []
+    for m in s.miller:
+        m = np.asarray(m)
+        sticks = len({(int(a) % Nx, int(b) % Ny) for a, b in m[:, :2]})
+        xact = len({int(a) % Nx for a in m[:, 0]})
+        ff.append(5.0 * (sticks * Nz * np.log2(Nz) + xact * Ny * Nz * np.log2(Ny) + N * np.log2(Nx)))
+        npws.append(len(m))
+    f_one, npw = float(np.mean(ff)), float(np.mean(npws))
+    nm, sig, nb, ns = s.nmodes, s.nspin, s.nbnds, s.nspinor
+    lsh = np.rint(np.asarray(s.PP_table)[:, :, 0] - 1.0).astype(int)
+    P = int(max(sum(2 * l + 1 for l in lsh[:, t] if l >= 0) for t in range(lsh.shape[1])))
+    f_fft = (sig * nb * ns + nm * sig * nb * ns) * f_one
+    f_gemm = 3 * 8.0 * nm * sig * nb * nb * ns * npw
+    f_nl = 16.0 * (4 * P * s.natom) * npw * sig * nb * ns + 8.0 * nm * 3 * s.natom * sig * nb * nb
+    c = 8.0
+    b_min = 2 * sig * nb * ns * npw * c + 2 * P * npw * 4 + nm * s.nmag * N * c / s.nk_bz + nm * sig * nb * nb * c
+    p_simt = 152 * 128 * 2 * (clk_mhz or 2070.0) * 1e6
+    p_tc = (peaks.get("bf16_tflops_sustained") or 1700.0) * 1e12
+    bw = (peaks.get("hbm_gbs") or 6800.0) * 1e9
+    terms = {"hbm": b_min / bw, "fft_simt": f_fft / p_simt, "gemm_tensor": f_gemm / p_tc, "nonlocal_tensor": f_nl / p_tc}
+    bound = max(terms, key=terms.get)
+    t_roof = terms[bound]
+    t_meas = nm * sig * nb * nb / value
+    return {"definition": "T_roof = max(B_min/BW_HBM, F_fft/P_simt, F_gemm_eff/P_tc, F_nl/P_tc) per pair with the "
+                          "reference algorithm's counts; achieved = T_roof / T_meas",
+            "bound": bound, "t_roof_us": t_roof * 1e6, "t_meas_us": t_meas * 1e6, "achieved": t_roof / t_meas,
+            "per_pair": {"F_fft": f_fft, "F_gemm_eff": f_gemm, "F_nl": f_nl, "B_min": b_min},
+            "peaks": {"simt_fp32_tflops": p_simt / 1e12, "tensor_tflops": p_tc / 1e12, "hbm_gbs": bw / 1e9},
+            "peak_source": "FP32 SIMT: nominal 152 SMs x 128 lanes x 2 x median SM clock; tensor and HBM: "
+                           "MEASURED_PEAKS.json (sustained bf16, copy)"}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -625,6 +671,7 @@ def run_ours(args):
                         "ms_per_step": e2e_step_ms, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "fp64_form": fp64,
                 "cpu_baseline": cpu, "wall_s_timed": t_wall}
+        line["path_roofline"] = path_roofline(s, value / world, peaks, (clk or {}).get("sm_mhz"))
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
