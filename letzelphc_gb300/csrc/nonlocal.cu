@@ -441,14 +441,42 @@ __global__ void __launch_bounds__(256) k_finish(const PairInfo* __restrict__ pai
     }
 }
 
+// Knuth's TwoSum: s + x is added into s, its rounding error into e.  The
+// _rn intrinsics keep the compiler from contracting or reassociating.
+__device__ __forceinline__ void ff_two_sum(float& s, float& e, float x)
+{
+    const float t = __fadd_rn(s, x), z = __fsub_rn(t, s);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z)));
+    s = t;
+}
+
+// (s + e) (fh + fl) + t rounded once to float.  The product's rounding error
+// is recovered exactly with an FMA (the error-free product of Ogita, Rump and
+// Oishi), the addition of t with TwoSum; the remaining terms are summed at
+// the error's own scale, so the result carries about 2^-46 of |(s+e) fh| on
+// top of its final rounding.
+__device__ __forceinline__ float ff_scale_add(float s, float e, float fh, float fl, float t)
+{
+    const float p = __fmul_rn(s, fh);
+    float pe = __fmaf_rn(s, fh, -p);
+    pe = __fmaf_rn(s, fl, pe);
+    pe = __fmaf_rn(e, fh, pe);
+    pe = __fmaf_rn(e, fl, pe);
+    const float u = __fadd_rn(p, t), z = __fsub_rn(u, p);
+    const float ue = __fadd_rn(__fsub_rn(p, __fsub_rn(u, z)), __fsub_rn(t, z));
+    return __fadd_rn(u, __fadd_rn(pe, ue));
+}
+
 // Finish, one block per (pair, spin): the two projection sets of the pair
 // (this spin) and the pair's eigVec live in shared memory; each thread owns
 // (m, n) elements and keeps the 3*natom displacement sums in registers.
 // T is the arithmetic of the nonlocal combination and the mode transform
-// (double in the plain form, float in the mixed form); the sum of the local
-// sandwich over grid chunks and the final addition are FP64 in both.
+// (double in the plain form, float in the mixed form).  The plain form adds
+// the FP64 local term in FP64; the mixed form sums the local sandwich's K-chunk
+// partials and adds the nonlocal term with float error-free transformations
+// (three blocks per SM: 80 registers).
 template <int NJ, typename T>
-__global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const PairInfo* __restrict__ pairs, int mode_fp64,
+__global__ void __launch_bounds__(NJ <= 12 ? 256 : 128, (NJ <= 12 && sizeof(T) == 4) ? 3 : 0) k_finish_pair(const PairInfo* __restrict__ pairs, int mode_fp64,
                                                      const double2* __restrict__ glocal,
                                                      const float* __restrict__ partials, int nchunks,
                                                      const float* __restrict__ mode_scale,
@@ -472,6 +500,8 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
     C2* sE = sKp + (size_t)rows * sets;                      // [nmodes][nj]
     int* sch = reinterpret_cast<int*>(sE + (size_t)gd.nmodes * nj);  // channels: [type][8][4] = lidx, l, pbase, foff
     T* ssoc = reinterpret_cast<T*>(sch + nl.ntype * 8 * 4);
+    int* snp = reinterpret_cast<int*>(ssoc + nl.ntype * 8);  // [type] projector slots in use
+    int* styp = snp + nl.ntype;                               // [atom] type
     if (non_loc)
     {
         const double2* PK = proj + (size_t)P.kbz_kq * rows * nsets + (size_t)spin * sets;
@@ -489,6 +519,7 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
             const double2 v = E[(e / nj) * gd.nmodes + (e % nj)];
             sE[e] = mk2<C2>(v.x, v.y);
         }
+        for (int a = threadIdx.x; a < nl.natom; a += blockDim.x) styp[a] = nl.atom_type[a];
         if (threadIdx.x < nl.ntype)
         {
             const int it = threadIdx.x;
@@ -508,10 +539,63 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 ++nc;
             }
             for (; nc < 8; ++nc) sch[(it * 8 + nc) * 4 + 1] = -1;
+            snp[it] = pb;
+        }
+        __syncthreads();
+        // The channel coefficients act on the k role alone, so they are folded
+        // into its projections once per block, in place: for a channel of atom
+        // a with slots pb .. pb + tl - 1,
+        //   Z(p1, s1; m)   =  sum_{p2, s2} f(p1, p2, s1, s2) conj(Pi_0(p2, m, s2))
+        //   W_x(p1, s1; m) = -sum_{p2, s2} f(p1, p2, s1, s2) conj(Pi_x(p2, m, s2))
+        // (f diagonal, = the channel's weight, without SOC coefficients), so that
+        //   out_{a,x}(m, n) = sum_{p1, s1} K_x(p1, n, s1) Z(p1, s1; m) + K_0(p1, n, s1) W_x(p1, s1; m)
+        // with K the k+q role: the terms of src/nonloc/sum_VNL_KKp.c:8-58, regrouped.
+        // One thread owns one (atom, channel, band, component) block, reads it
+        // whole before writing it, and no other thread touches it.
+        for (int w = threadIdx.x; w < nl.natom * 8 * nb * 4; w += blockDim.x)
+        {
+            const int comp = w & 3, r = w >> 2;
+            const int a = r / (8 * nb), r2 = r - a * 8 * nb, c = r2 / nb, mm = r2 - c * nb;
+            const int it = styp[a];
+            const int* ch = sch + (it * 8 + c) * 4;
+            const int l = ch[1];
+            if (l < 0) continue;
+            const int tl = 2 * l + 1, pb = ch[2], foff = ch[3];
+            C2* blk = sKp + (size_t)(a * nl.nproj_max * 4 + pb * 4 + comp) * sets + mm * ns;  // slot stride 4 sets
+            const T sg = comp ? (T)-1 : (T)1;
+            if (foff < 0)
+            {
+                const T wgt = ssoc[it * 8 + c] * sg;
+                for (int im = 0; im < tl; ++im)
+                    for (int sp = 0; sp < ns; ++sp)
+                    {
+                        const C2 v = blk[(size_t)im * 4 * sets + sp];
+                        blk[(size_t)im * 4 * sets + sp] = mk2<C2>(wgt * v.x, -wgt * v.y);
+                    }
+            }
+            else
+            {
+                C2 vin[14];  // tl * ns <= 7 * 2 (l <= 3 is checked at context creation)
+                for (int im = 0; im < tl; ++im)
+                    for (int sp = 0; sp < ns; ++sp) vin[im * ns + sp] = cconj(blk[(size_t)im * 4 * sets + sp]);
+                for (int im1 = 0; im1 < tl; ++im1)
+                    for (int s1 = 0; s1 < ns; ++s1)
+                    {
+                        C2 acc = mk2<C2>(0.0, 0.0);
+                        for (int im2 = 0; im2 < tl; ++im2)
+                            for (int s2 = 0; s2 < ns; ++s2)
+                            {
+                                const double* fc = nl.fcoef + 2 * ((size_t)foff + (im1 * tl + im2) * ns * ns + s1 * ns + s2);
+                                acc = cadd(acc, cmul(mk2<C2>(fc[0], fc[1]), vin[im2 * ns + s2]));
+                            }
+                        blk[(size_t)im1 * 4 * sets + s1] = mk2<C2>(sg * acc.x, sg * acc.y);
+                    }
+            }
         }
         __syncthreads();
     }
     const double invN = 1.0 / ((double)gd.Nx * gd.Ny * gd.Nz);
+    const float invN_hi = (float)invN, invN_lo = (float)(invN - (double)invN_hi);  // 1/M as a float pair
     const int NT = 2 * gd.nbp;
     const double2 pre = make_double2(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
     const C2 preT = mk2<C2>(0.0, -2.0 * LELPH_PI_T * LELPH_E2);
@@ -524,57 +608,32 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
         if (non_loc)
         {
 #pragma unroll
-            for (int j = 0; j < NJ; ++j)
+            for (int a = 0; a < NJ / 3; ++a)
             {
-                if (j >= nj) continue;
-                const int a = j / 3, x = j - 3 * a;
-                const int it = nl.atom_type[a];
-                const int rb = a * nl.nproj_max * 4;
-                C2 acc = mk2<C2>(0.0, 0.0);
-                for (int c = 0; c < 8; ++c)
-                {
-                    const int* ch = sch + (it * 8 + c) * 4;
-                    const int l = ch[1];
-                    if (l < 0) break;
-                    const int tl = 2 * l + 1, pb = ch[2], foff = ch[3];
-                    const T soc = ssoc[it * 8 + c];
-                    for (int im1 = 0; im1 < tl; ++im1)
-                        for (int im2 = 0; im2 < tl; ++im2)
-                        {
-                            if (foff < 0 && im1 != im2) continue;
-                            const int p1 = pb + im1, p2 = pb + im2;
-                            for (int s1 = 0; s1 < ns; ++s1)
-                                for (int s2 = 0; s2 < ns; ++s2)
-                                {
-                                    C2 f;
-                                    if (foff >= 0)
-                                    {
-                                        const double* fc = nl.fcoef + 2 * ((size_t)foff + (im1 * tl + im2) * ns * ns + s1 * ns + s2);
-                                        f = mk2<C2>(fc[0], fc[1]);
-                                    }
-                                    else
-                                    {
-                                        if (s1 != s2) continue;
-                                        f.x = soc;
-                                        f.y = 0;
-                                    }
-                                    const C2 K0 = sK[(size_t)(rb + p1 * 4 + 0) * sets + n * ns + s1];
-                                    const C2 Kx = sK[(size_t)(rb + p1 * 4 + 1 + x) * sets + n * ns + s1];
-                                    const C2 Kp0 = cconj(sKp[(size_t)(rb + p2 * 4 + 0) * sets + m * ns + s2]);
-                                    C2 Kpx = sKp[(size_t)(rb + p2 * 4 + 1 + x) * sets + m * ns + s2];
-                                    Kpx.x = -Kpx.x;  // -conj
-                                    acc = cadd(acc, cmul(f, cadd(cmul(Kx, Kp0), cmul(K0, Kpx))));
-                                }
-                        }
-                }
-                out[j] = acc;
+                if (a >= nl.natom) break;
+                const int np = snp[styp[a]];
+                const C2* kq = sK + (size_t)a * nl.nproj_max * 4 * sets + n * ns;  // K(slot, comp; n)
+                const C2* kk = sKp + (size_t)a * nl.nproj_max * 4 * sets + m * ns;  // Z, W_x(slot; m)
+                C2 a0 = mk2<C2>(0.0, 0.0), a1 = a0, a2 = a0;
+                for (int p = 0; p < np; ++p)
+                    for (int sp = 0; sp < ns; ++sp)
+                    {
+                        const size_t o = (size_t)p * 4 * sets + sp;
+                        const C2 K0 = kq[o], Z = kk[o];
+                        a0 = cadd(a0, cadd(cmul(kq[o + sets], Z), cmul(K0, kk[o + sets])));
+                        a1 = cadd(a1, cadd(cmul(kq[o + 2 * sets], Z), cmul(K0, kk[o + 2 * sets])));
+                        a2 = cadd(a2, cadd(cmul(kq[o + 3 * sets], Z), cmul(K0, kk[o + 3 * sets])));
+                    }
+                out[3 * a] = a0;
+                out[3 * a + 1] = a1;
+                out[3 * a + 2] = a2;
             }
         }
-        for (int nu = 0; nu < gd.nmodes; ++nu)
+        if (mode_fp64)
         {
-            const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
-            if (mode_fp64)
+            for (int nu = 0; nu < gd.nmodes; ++nu)
             {
+                const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
                 double2 v = glocal[((size_t)zp * gd.nmodes * nb + nu * nb + m) * nb + n];
                 if (non_loc)
                 {
@@ -589,50 +648,58 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                 else
                     reinterpret_cast<double2*>(gout)[oidx] = v;
             }
-            else
+            continue;
+        }
+        // mixed form: the K-chunk partials are summed in FP32 with TwoSum
+        // compensation (the pair (s, e) holds the sum to about twice FP32's
+        // precision), two modes at a time so that 16 loads are in flight, then
+        // unscaled (exact inverse of the power-of-two operand scales, 1/M as a
+        // float pair) and added to the nonlocal term with error-free
+        // transformations: the complex64 result is rounded once, without FP64
+        // arithmetic (GB300's FP64 rate is 1/64 of FP32's)
+        const float bsc = band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
+                          band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
+        const float* msc = mode_scale + (size_t)P.dvslot * gd.nmodes;
+        const size_t CS = (size_t)128 * NT;  // stride of one K chunk
+        for (int nu0 = 0; nu0 < gd.nmodes; nu0 += 2)
+        {
+            // an odd mode count reads the last mode twice and stores it once
+            const int nu1 = min(nu0 + 1, gd.nmodes - 1);
+            const int mt0 = nu0 / gd.mt_modes, mt1 = nu1 / gd.mt_modes;
+            const float* pa = partials + lelph_tc_partial_offset(gd, nchunks, zp, mt0, 0, (nu0 - mt0 * gd.mt_modes) * nb + m);
+            const float* pb = partials + lelph_tc_partial_offset(gd, nchunks, zp, mt1, 0, (nu1 - mt1 * gd.mt_modes) * nb + m);
+            float sv[4] = {0.f, 0.f, 0.f, 0.f}, ev[4] = {0.f, 0.f, 0.f, 0.f};  // re, im of nu0; re, im of nu1
+            int c = 0;
+            for (; c + 4 <= nchunks; c += 4)
             {
-                // mixed form: the K-chunk partials are summed in the operand type
-                // with TwoSum compensation (the pair (s, e) holds the sum to about
-                // twice the operand precision) and combined, unscaled (exact inverse
-                // of the power-of-two operand scales, 1/M) and added to the nonlocal
-                // term in FP64: a few FP64 operations per element instead of one
-                // FP64 addition per chunk
-                const int mt = nu / gd.mt_modes, rr = (nu - mt * gd.mt_modes) * nb + m;
-                const float* pp = partials + lelph_tc_partial_offset(gd, nchunks, zp, mt, 0, rr);
-                T sre = 0, ere = 0, sim = 0, eim = 0;
-                auto two_sum = [](T& s, T& e, T x) {
-                    const T t = s + x, z = t - s;
-                    e += (s - (t - z)) + (x - z);
-                    s = t;
-                };
-                // four chunks' loads in flight before their (dependent) compensated adds
-                int c = 0;
-                for (; c + 4 <= nchunks; c += 4)
-                {
-                    T xr[4], xi[4];
+                float x[4][4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                    {
-                        xr[u] = (T)pp[(size_t)(c + u) * 128 * NT + n];
-                        xi[u] = (T)pp[(size_t)(c + u) * 128 * NT + gd.nbp + n];
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                    {
-                        two_sum(sre, ere, xr[u]);
-                        two_sum(sim, eim, xi[u]);
-                    }
-                }
-                for (; c < nchunks; ++c)
+                for (int u = 0; u < 4; ++u)
                 {
-                    two_sum(sre, ere, (T)pp[(size_t)c * 128 * NT + n]);
-                    two_sum(sim, eim, (T)pp[(size_t)c * 128 * NT + gd.nbp + n]);
+                    x[u][0] = pa[(size_t)(c + u) * CS + n];
+                    x[u][1] = pa[(size_t)(c + u) * CS + gd.nbp + n];
+                    x[u][2] = pb[(size_t)(c + u) * CS + n];
+                    x[u][3] = pb[(size_t)(c + u) * CS + gd.nbp + n];
                 }
-                const float sc = mode_scale[(size_t)P.dvslot * gd.nmodes + nu] *
-                                 band_scale[((size_t)P.kbz_k * gd.nspin + spin) * nb + m] *
-                                 band_scale[((size_t)P.kbz_kq * gd.nspin + spin) * nb + n];
-                const double f = invN * (double)(1.0f / sc);  // 1/sc: a power of two, exact
-                double vr = ((double)sre + (double)ere) * f, vi = ((double)sim + (double)eim) * f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) ff_two_sum(sv[v], ev[v], x[u][v]);
+            }
+            for (; c < nchunks; ++c)
+            {
+                ff_two_sum(sv[0], ev[0], pa[(size_t)c * CS + n]);
+                ff_two_sum(sv[1], ev[1], pa[(size_t)c * CS + gd.nbp + n]);
+                ff_two_sum(sv[2], ev[2], pb[(size_t)c * CS + n]);
+                ff_two_sum(sv[3], ev[3], pb[(size_t)c * CS + gd.nbp + n]);
+            }
+#pragma unroll
+            for (int hm = 0; hm < 2; ++hm)
+            {
+                const int nu = hm ? nu1 : nu0;
+                if (hm && nu1 == nu0) break;
+                const size_t oidx = ((((size_t)pair * gd.nmodes + nu) * gd.nspin + spin) * nb + m) * nb + n;
+                float tr = 0.f, ti = 0.f;
                 if (non_loc)
                 {
                     C2 sacc = mk2<C2>(0.0, 0.0);
@@ -640,13 +707,24 @@ __global__ void __launch_bounds__(NJ <= 12 ? 256 : 128) k_finish_pair(const Pair
                     for (int j = 0; j < NJ; ++j)
                         if (j < nj) sacc = cadd(sacc, cmul(sE[nu * nj + j], out[j]));
                     const C2 t = cmul(preT, sacc);
-                    vr += (double)t.x;
-                    vi += (double)t.y;
+                    tr = (float)t.x;
+                    ti = (float)t.y;
                 }
+                const float p2 = 1.0f / (msc[nu] * bsc);  // a power of two: exact
                 if (out_c64)
-                    reinterpret_cast<float2*>(gout)[oidx] = make_float2((float)vr, (float)vi);
+                {
+                    const float fh = invN_hi * p2, fl = invN_lo * p2;  // exact scalings
+                    reinterpret_cast<float2*>(gout)[oidx] =
+                        make_float2(ff_scale_add(sv[2 * hm], ev[2 * hm], fh, fl, tr),
+                                    ff_scale_add(sv[2 * hm + 1], ev[2 * hm + 1], fh, fl, ti));
+                }
                 else
-                    reinterpret_cast<double2*>(gout)[oidx] = make_double2(vr, vi);
+                {
+                    const double f = invN * (double)p2;
+                    reinterpret_cast<double2*>(gout)[oidx] =
+                        make_double2(((double)sv[2 * hm] + (double)ev[2 * hm]) * f + (double)tr,
+                                     ((double)sv[2 * hm + 1] + (double)ev[2 * hm + 1]) * f + (double)ti);
+                }
             }
         }
     }
@@ -657,7 +735,7 @@ static size_t finish_pair_smem(const NonlocalDesc& nl, const GeomDev& g, size_t 
     const size_t rows = (size_t)nl.natom * nl.nproj_max * 4;
     const size_t sets = (size_t)g.nbnds * g.nspinor;
     return 2 * rows * sets * csz + (size_t)g.nmodes * 3 * nl.natom * csz + (size_t)nl.ntype * 8 * 4 * sizeof(int) +
-           (size_t)nl.ntype * 8 * sizeof(double);
+           (size_t)nl.ntype * 8 * sizeof(double) + (size_t)(nl.ntype + nl.natom) * sizeof(int);
 }
 
 // Finish for many displacement components (3 natom > 24, where the

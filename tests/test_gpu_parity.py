@@ -106,6 +106,23 @@ def test_c64_output_matches_c128():
     assert np.linalg.norm((g - g_ref).ravel()) / np.linalg.norm(g_ref.ravel()) < 2e-6
 
 
+@pytest.mark.parametrize("name", ["c0", "soc_tr", "lsda"])
+def test_c64_epilogue_matches_c128_epilogue(name):
+    """The mixed form's complex64 output (float error-free epilogue: TwoSum of
+    the chunk partials, exact FMA products, 1/M as a float pair) against its
+    complex128 output (FP64 epilogue) from the same partial sums: one value
+    rounded once to float, so they differ by at most an ulp of float, plus
+    2^-40 of max|g| where the local and nonlocal terms cancel."""
+    s, _, kmq, nl = load(name)
+    g128 = run_all(s, "mixed_f16", non_loc=nl, kminusq=kmq)
+    g64 = run_all(s, "mixed_f16", non_loc=nl, kminusq=kmq, out=OUT_C64)
+    assert g64.dtype == np.complex64 and g128.dtype == np.complex128
+    ref = g128.astype(np.complex64).astype(np.complex128)
+    d = np.maximum(np.abs(g64.real - ref.real), np.abs(g64.imag - ref.imag))
+    bound = 2.0**-22 * np.maximum(np.abs(g128.real), np.abs(g128.imag)) + 2.0**-40 * np.abs(g128).max()
+    assert np.all(d <= bound), (d / bound).max()
+
+
 def test_l12_at_bench_grid_against_oracle():
     # the 4-atom cell on its 48^3 grid with npw ~2500, a few pairs of two q
     s = synth.make_system("c1", {"nbnds": 8, "qpts": [(0.125, 0, 0), (0.25, 0.125, 0.125)]})
