@@ -48,22 +48,41 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
         if (threadIdx.x == 0) nact = 0;
         __syncthreads();
         const long long ncol = (long long)mk.Nx * mk.Ny;
-        for (int j = threadIdx.x; j < nl; j += blockDim.x)
+        if (nlines <= 0x7fffffffLL)
         {
-            const long long line = l0 + j;
-            const long long box = line / ncol;
-            const long long col = line - box * ncol;
-            const long long kslot = box / mk.nbox_per_k;
-            if (mk.col[kslot * ncol + col]) act[atomicAdd(&nact, 1)] = j;
+            // 32-bit divisions (a 64-bit one is a long software sequence)
+            const unsigned nc32 = (unsigned)ncol, nbk = (unsigned)mk.nbox_per_k;
+            for (int j = threadIdx.x; j < nl; j += blockDim.x)
+            {
+                const unsigned line = (unsigned)(l0 + j);
+                const unsigned box = line / nc32;
+                const unsigned col = line - box * nc32;
+                if (mk.col[(size_t)(box / nbk) * nc32 + col]) act[atomicAdd(&nact, 1)] = j;
+            }
         }
+        else
+            for (int j = threadIdx.x; j < nl; j += blockDim.x)
+            {
+                const long long line = l0 + j;
+                const long long box = line / ncol;
+                const long long col = line - box * ncol;
+                const long long kslot = box / mk.nbox_per_k;
+                if (mk.col[kslot * ncol + col]) act[atomicAdd(&nact, 1)] = j;
+            }
         __syncthreads();
         const int na = nact;
         if (na == 0) return;
         const RecipDiv dL = recip_div(p.L);
         for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
         {
-            int e;
-            const int j = div_rem(i, dL, e);
+            int e, j;
+            if constexpr (CTL > 0)
+            {
+                j = i / CTL;  // a constant divisor: multiply and shift
+                e = i - j * CTL;
+            }
+            else
+                j = div_rem(i, dL, e);
             a[i] = g[(size_t)act[j] * p.L + e];
         }
         __syncthreads();
@@ -74,8 +93,14 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
             r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
         for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
         {
-            int e;
-            const int j = div_rem(i, dL, e);
+            int e, j;
+            if constexpr (CTL > 0)
+            {
+                j = i / CTL;  // a constant divisor: multiply and shift
+                e = i - j * CTL;
+            }
+            else
+                j = div_rem(i, dL, e);
             g[(size_t)act[j] * p.L + e] = r[i];
         }
         return;
@@ -97,11 +122,14 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
 
 // With a box mask (y pass: outer = (box, x)), empty x planes are skipped.
 // CTL as in k_fft_contig.
-template <typename T2, typename T, int CTL>
+// NLC > 0 (with CTL > 0): inner = ich = NLC, one chunk per line set, so the
+// index divisions of the load, the passes and the store are by constants.
+template <typename T2, typename T, int CTL, int NLC>
 __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long long nouter, int inner, int ich,
                                                      int nchunk, FftPlan1D p, const T2* __restrict__ tw, int sign,
                                                      BoxMask mk)
 {
+    static_assert(NLC == 0 || CTL > 0, "a compile-time line count needs a compile-time length");
     extern __shared__ __align__(16) unsigned char smraw[];
     T2* a = reinterpret_cast<T2*>(smraw);
     T2* b = a + (size_t)ich * p.L;
@@ -109,11 +137,23 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
     long long o = blockIdx.x / nchunk;
     if (mk.xpl)
     {
-        const long long box = o / mk.Nx;
-        const long long x = o - box * mk.Nx;
-        if (!mk.xpl[(box / mk.nbox_per_k) * mk.Nx + x]) return;
+        // blockIdx.x < 2^32: 32-bit divisions
+        const unsigned o32 = (unsigned)o, nx = (unsigned)mk.Nx;
+        const unsigned box = o32 / nx;
+        const unsigned x = o32 - box * nx;
+        if (!mk.xpl[(size_t)(box / (unsigned)mk.nbox_per_k) * nx + x]) return;
     }
     for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
+    if constexpr (NLC > 0)
+    {
+        // the block's CTL x NLC points are contiguous: idx = l * NLC + i
+        T2* g = data + (size_t)o * (CTL * NLC);
+        for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) a[idx] = g[idx];
+        __syncthreads();
+        T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
+        for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) g[idx] = r[idx];
+        return;
+    }
     int c = blockIdx.x - (int)(o * nchunk);
     int i0 = c * ich;
     int ic = min(ich, inner - i0);
@@ -166,13 +206,17 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t&
     }
 }
 
-template <int BF16, int CTL>
+// NLC > 0 (with CTL > 0): every chunk holds exactly NLC columns (the host
+// checks that they tile the plane), so the line count, and with it every
+// index division of the load and of the passes, is a compile-time constant.
+template <int BF16, int CTL, int NLC>
 __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ boxes, int nbox, int k0, int ich,
                                                      int nchunk, FftPlan1D p, const float2* __restrict__ tw,
                                                      int sign, GeomDev gd, const float* __restrict__ band_scale,
                                                      uint16_t* __restrict__ Bsplit, float2* __restrict__ psi32,
                                                      BoxMask mk)
 {
+    static_assert(NLC == 0 || CTL > 0, "a compile-time line count needs a compile-time length");
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* a = reinterpret_cast<float2*>(smraw);
     float2* b = a + (size_t)ich * p.L;
@@ -183,22 +227,38 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     int o = blockIdx.x / nchunk;
     int c = blockIdx.x - o * nchunk;
     int i0 = c * ich;
-    int ic = min(ich, inner - i0);
+    const int ic = NLC > 0 ? NLC : min(ich, inner - i0);
     const float2* g = boxes + (size_t)o * N + i0;
     int n = p.L * ic;
     // x planes that the sphere of this k-point does not reach are zero: not read
     const uint8_t* xpl = mk.xpl ? mk.xpl + (size_t)(o / mk.nbox_per_k) * gd.Nx : nullptr;
-    const RecipDiv dc = recip_div(ic);
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+    if constexpr (NLC > 0)
     {
-        int i;
-        const int l = div_rem(idx, dc, i);
-        a[l * ic + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : g[(size_t)l * inner + i];
+        // one column per thread, rows stepping by the rows a block covers
+        constexpr int RP = 256 / NLC;
+        const int i = threadIdx.x % NLC, l0 = threadIdx.x / NLC;
+        if (l0 < RP)
+        {
+            const float2* gi = g + i;
+#pragma unroll 4
+            for (int l = l0; l < CTL; l += RP)
+                a[l * NLC + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : gi[(size_t)l * inner];
+        }
+    }
+    else
+    {
+        const RecipDiv dc = recip_div(ic);
+        for (int idx = threadIdx.x; idx < n; idx += blockDim.x)
+        {
+            int i;
+            const int l = div_rem(idx, dc, i);
+            a[l * ic + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : g[(size_t)l * inner + i];
+        }
     }
     __syncthreads();
     float2* r;
     if constexpr (CTL > 0)
-        r = ct_fft<float2, float, CTL, 0, 1, true, 0>(a, b, ic, ic, 1, nullptr, ic, 1, tws, sign);
+        r = ct_fft<float2, float, CTL, 0, 1, true, NLC>(a, b, ic, ic, 1, nullptr, ic, 1, tws, sign);
     else
         r = fft_smem<float2, float>(a, b, ic, ic, 1, p, tws, sign);
     // box o -> (kslot, spin, band, spinor)
@@ -226,11 +286,11 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     float2* const P = psi32 + pg * npb * gd.nbp * 16 + (size_t)band * 16;
     const uint32_t kbase = (uint32_t)((long long)sp * N) + (uint32_t)i0;  // K index of (x = 0, column 0)
     // one column per thread, rows (x) stepping by the columns a block covers
-    const int rows_per = blockDim.x / ic;
+    const int rows_per = NLC > 0 ? 256 / NLC : (int)blockDim.x / ic;
     const int i = threadIdx.x % ic;
     if (rows_per > 0 && threadIdx.x < rows_per * ic)
     {
-        for (int l = threadIdx.x / ic; l < p.L; l += rows_per)
+        for (int l = threadIdx.x / ic; l < (CTL > 0 ? CTL : p.L); l += rows_per)
         {
             float2 v = r[l * ic + i];
             v.x *= sc;
@@ -408,11 +468,26 @@ static void launch_strided_l(T2* data, long long nouter, int inner, const FftPla
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaFuncSetAttribute(k_fft_strided<T2, T, CTL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_fft_strided<T2, T, CTL, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     long long nb = nouter * nchunk;
-    k_fft_strided<T2, T, CTL><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign, mk);
+    if (CTL > 0 && inner == CTL && ich == CTL)
+    {
+        // cubic planes (inner = L): a compile-time line count
+        constexpr int NLC = CTL;
+        static bool attr_n = false;
+        if (!attr_n)
+        {
+            cudaFuncSetAttribute(k_fft_strided<T2, T, CTL, NLC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024);
+            attr_n = true;
+        }
+        k_fft_strided<T2, T, CTL, NLC><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign,
+                                                                        mk);
+        return;
+    }
+    k_fft_strided<T2, T, CTL, 0><<<(unsigned)nb, 256, smem, st>>>(data, nouter, inner, ich, nchunk, p, tw, sign, mk);
 }
 
 template <typename T2, typename T>
@@ -472,8 +547,15 @@ void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const
     launch_strided<float2, float>(data, nouter, inner, p, tw, sign, st, mk);
 }
 
-template <int BF16, int CTL>
-static void launch_x_split_l(unsigned nb, size_t smem, const float2* boxes, int nbox, int k0, int ich, int nchunk,
+// columns per x-pass block for a compile-time length: ich_for(L, ., 2048)
+// before it is clipped to the plane
+__host__ __device__ constexpr int x_split_nlc(int L)
+{
+    return (2048 / L) >= 32 ? (2048 / L) / 16 * 16 : (2048 / L);
+}
+
+template <int BF16, int CTL, int NLC>
+static void launch_x_split_n(unsigned nb, size_t smem, const float2* boxes, int nbox, int k0, int ich, int nchunk,
                              const FftPlan1D& p, const float2* tw, int sign, const GeomDev& g,
                              const float* band_scale, uint16_t* Bsplit, float2* psi32, cudaStream_t st,
                              const BoxMask& mk)
@@ -481,11 +563,27 @@ static void launch_x_split_l(unsigned nb, size_t smem, const float2* boxes, int 
     static bool attr_set = false;
     if (!attr_set)
     {
-        cudaFuncSetAttribute(k_fft_x_split<BF16, CTL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_fft_x_split<BF16, CTL, NLC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    k_fft_x_split<BF16, CTL><<<nb, 256, smem, st>>>(boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
-                                                    psi32, mk);
+    k_fft_x_split<BF16, CTL, NLC><<<nb, 256, smem, st>>>(boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale,
+                                                         Bsplit, psi32, mk);
+}
+
+template <int BF16, int CTL>
+static void launch_x_split_l(unsigned nb, size_t smem, const float2* boxes, int nbox, int k0, int ich, int nchunk,
+                             const FftPlan1D& p, const float2* tw, int sign, const GeomDev& g,
+                             const float* band_scale, uint16_t* Bsplit, float2* psi32, cudaStream_t st,
+                             const BoxMask& mk)
+{
+    constexpr int NLC = CTL > 0 ? x_split_nlc(CTL) : 0;
+    const int inner = g.Ny * g.Nz;
+    if (NLC > 0 && ich == NLC && inner % NLC == 0 && 256 / NLC >= 1)
+        launch_x_split_n<BF16, CTL, NLC>(nb, smem, boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
+                                         psi32, st, mk);
+    else
+        launch_x_split_n<BF16, CTL, 0>(nb, smem, boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
+                                       psi32, st, mk);
 }
 
 template <int BF16>

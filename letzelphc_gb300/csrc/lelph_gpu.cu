@@ -1448,8 +1448,8 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
                                         chat_f32 ? 1 : 0, (const long long*)h->d_chatoff.p, nl, g,
                                         (double2*)h->d_proj.p, (unsigned*)h->d_status.p, h->wait_ns, h->st))
             return fail(h, LELPH_GPU_ERR_CUDA, "projection launch failed");
-        const int rs = check_status(h);
-        if (rs) return rs;
+        // its status is read with the preparation's final synchronisation, so
+        // that the dV windows' launches queue behind it without a host round trip
     }
     else
         lelph_launch_projections(0, d.nkpts_BZ, (const KPointSym*)h->d_ksym.p, (const double*)h->d_gvec.p,
@@ -1464,7 +1464,13 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
     if (wr) return wr;
     h->stats.windows_ms += gs_tock(h);
     h->stats.prepare_ms += tstop(h);
-    CUDA_TRY(h, cudaStreamSynchronize(h->st));
+    if (proj_tc)
+    {
+        const int rs = check_status(h);  // synchronises the stream
+        if (rs) return rs;
+    }
+    else
+        CUDA_TRY(h, cudaStreamSynchronize(h->st));
     h->prepared = true;
     return LELPH_GPU_OK;
 }
