@@ -10,12 +10,23 @@
 
 // ------------------------------------------------------------- butterflies
 
+// The direction sign is a run-time +-1: it selects between constants and
+// negations rather than multiplying (an int or double product would put a
+// conversion or an FP64 multiply on GB300's slow FP64 pipe in every butterfly).
 template <typename T2>
 __device__ __forceinline__ T2 mul_i(T2 a, int sign)  // multiply by sign * i
 {
     T2 r;
-    r.x = -sign * a.y;
-    r.y = sign * a.x;
+    if (sign > 0)
+    {
+        r.x = -a.y;
+        r.y = a.x;
+    }
+    else
+    {
+        r.x = a.y;
+        r.y = -a.x;
+    }
     return r;
 }
 
@@ -42,7 +53,7 @@ template <typename T2, typename T>
 __device__ __forceinline__ void dft3(T2* v, int sign)
 {
     const T c = (T)-0.5;
-    const T s = (T)(sign * 0.86602540378443864676);  // sin(2 pi / 3)
+    const T s = sign > 0 ? (T)0.86602540378443864676 : (T)-0.86602540378443864676;  // sign sin(2 pi / 3)
     T2 a = cadd(v[1], v[2]);
     T2 d = csub(v[1], v[2]);
     T2 t1;
@@ -61,8 +72,8 @@ __device__ __forceinline__ void dft5(T2* v, int sign)
 {
     const T c1 = (T)0.30901699437494742410;   // cos(2 pi / 5)
     const T c2 = (T)-0.80901699437494742410;  // cos(4 pi / 5)
-    const T s1 = (T)(sign * 0.95105651629515357212);  // sin(2 pi / 5)
-    const T s2 = (T)(sign * 0.58778525229247312917);  // sin(4 pi / 5)
+    const T s1 = sign > 0 ? (T)0.95105651629515357212 : (T)-0.95105651629515357212;  // sign sin(2 pi / 5)
+    const T s2 = sign > 0 ? (T)0.58778525229247312917 : (T)-0.58778525229247312917;  // sign sin(4 pi / 5)
     T2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
     T2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
     T2 x0 = v[0];
