@@ -234,15 +234,20 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     const uint8_t* xpl = mk.xpl ? mk.xpl + (size_t)(o / mk.nbox_per_k) * gd.Nx : nullptr;
     if constexpr (NLC > 0)
     {
-        // one column per thread, rows stepping by the rows a block covers
-        constexpr int RP = 256 / NLC;
-        const int i = threadIdx.x % NLC, l0 = threadIdx.x / NLC;
+        // two adjacent columns per thread (one 16-byte load: the box, the chunk
+        // start, the plane stride and the column pair are all even in points),
+        // rows stepping by the rows a block covers
+        static_assert(NLC % 2 == 0, "column pairs");
+        constexpr int NP = NLC / 2, RP = 256 / NP;
+        const int ip = threadIdx.x % NP, l0 = threadIdx.x / NP;
         if (l0 < RP)
         {
-            const float2* gi = g + i;
+            const float2* gi = g + 2 * ip;
 #pragma unroll 4
             for (int l = l0; l < CTL; l += RP)
-                a[l * NLC + i] = (xpl && !xpl[l]) ? make_float2(0.f, 0.f) : gi[(size_t)l * inner];
+                *reinterpret_cast<float4*>(a + l * NLC + 2 * ip) =
+                    (xpl && !xpl[l]) ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                     : *reinterpret_cast<const float4*>(gi + (size_t)l * inner);
         }
     }
     else
@@ -285,12 +290,42 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
     const uint32_t rot = (uint32_t)gd.nbp * 32;  // (-Im, Re) rows
     float2* const P = psi32 + pg * npb * gd.nbp * 16 + (size_t)band * 16;
     const uint32_t kbase = (uint32_t)((long long)sp * N) + (uint32_t)i0;  // K index of (x = 0, column 0)
+    if constexpr (NLC > 0)
+    {
+        // two adjacent points per thread: kc is even, so both sit in one
+        // 32-point K block (8-byte stores of the split rows) and one 16-point
+        // psi block (a 16-byte store)
+        constexpr int NP = NLC / 2, RP = 256 / NP;
+        const int ip = threadIdx.x % NP, lr = threadIdx.x / NP;
+        if (lr < RP)
+        {
+            for (int l = lr; l < CTL; l += RP)
+            {
+                const float4 w = *reinterpret_cast<const float4*>(r + l * NLC + 2 * ip);
+                const float2 v0 = make_float2(w.x * sc, w.y * sc), v1 = make_float2(w.z * sc, w.w * sc);
+                const uint32_t kc = kbase + (uint32_t)(l * inner + 2 * ip);
+                uint32_t h0a, l0a, h1a, l1a, h0b, l0b, h1b, l1b;
+                split2<BF16>(v0.x, v0.y, h0a, l0a);
+                split2<BF16>(-v0.y, v0.x, h1a, l1a);
+                split2<BF16>(v1.x, v1.y, h0b, l0b);
+                split2<BF16>(-v1.y, v1.x, h1b, l1b);
+                const uint32_t off = (kc >> 5) * (uint32_t)NT * 32u + (kc & 31u);
+                *reinterpret_cast<uint2*>(Bhi + off) = make_uint2(h0a, h0b);
+                *reinterpret_cast<uint2*>(Blo + off) = make_uint2(l0a, l0b);
+                *reinterpret_cast<uint2*>(Bhi + off + rot) = make_uint2(h1a, h1b);
+                *reinterpret_cast<uint2*>(Blo + off + rot) = make_uint2(l1a, l1b);
+                *reinterpret_cast<float4*>(P + (kc >> 4) * (uint32_t)gd.nbp * 16u + (kc & 15u)) =
+                    make_float4(v0.x, v0.y, v1.x, v1.y);
+            }
+        }
+        return;
+    }
     // one column per thread, rows (x) stepping by the columns a block covers
-    const int rows_per = NLC > 0 ? 256 / NLC : (int)blockDim.x / ic;
+    const int rows_per = (int)blockDim.x / ic;
     const int i = threadIdx.x % ic;
     if (rows_per > 0 && threadIdx.x < rows_per * ic)
     {
-        for (int l = threadIdx.x / ic; l < (CTL > 0 ? CTL : p.L); l += rows_per)
+        for (int l = threadIdx.x / ic; l < p.L; l += rows_per)
         {
             float2 v = r[l * ic + i];
             v.x *= sc;
@@ -576,7 +611,8 @@ static void launch_x_split_l(unsigned nb, size_t smem, const float2* boxes, int 
                              const float* band_scale, uint16_t* Bsplit, float2* psi32, cudaStream_t st,
                              const BoxMask& mk)
 {
-    constexpr int NLC = CTL > 0 ? x_split_nlc(CTL) : 0;
+    // an even count: the compile-time form works on column pairs
+    constexpr int NLC = (CTL > 0 && x_split_nlc(CTL) % 2 == 0) ? x_split_nlc(CTL) : 0;
     const int inner = g.Ny * g.Nz;
     if (NLC > 0 && ich == NLC && inner % NLC == 0 && 256 / NLC >= 1)
         launch_x_split_n<BF16, CTL, NLC>(nb, smem, boxes, nbox, k0, ich, nchunk, p, tw, sign, g, band_scale, Bsplit,
