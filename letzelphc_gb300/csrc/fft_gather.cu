@@ -73,36 +73,55 @@ __global__ void __launch_bounds__(256) k_fft_contig(T2* __restrict__ data, long 
         const int na = nact;
         if (na == 0) return;
         const RecipDiv dL = recip_div(p.L);
-        for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+        if constexpr (CTL > 0 && CTL % 2 == 0 && sizeof(T2) == 8)
         {
-            int e, j;
-            if constexpr (CTL > 0)
+            // two points per 16-byte load (lines start at even offsets)
+            for (int i = 2 * threadIdx.x; i < na * CTL; i += 2 * blockDim.x)
             {
-                j = i / CTL;  // a constant divisor: multiply and shift
-                e = i - j * CTL;
+                const int j = i / CTL, e = i - j * CTL;  // a constant divisor
+                *reinterpret_cast<float4*>(a + i) = *reinterpret_cast<const float4*>(g + (size_t)act[j] * CTL + e);
             }
-            else
-                j = div_rem(i, dL, e);
-            a[i] = g[(size_t)act[j] * p.L + e];
         }
+        else
+            for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+            {
+                int e, j;
+                if constexpr (CTL > 0)
+                {
+                    j = i / CTL;  // a constant divisor: multiply and shift
+                    e = i - j * CTL;
+                }
+                else
+                    j = div_rem(i, dL, e);
+                a[i] = g[(size_t)act[j] * p.L + e];
+            }
         __syncthreads();
         T2* r;
         if constexpr (CTL > 0)
             r = ct_fft<T2, T, CTL, 0, 1, false, 0>(a, b, na, 1, CTL, nullptr, 1, CTL, tws, sign);
         else
             r = fft_smem<T2, T>(a, b, na, 1, p.L, p, tws, sign);
-        for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+        if constexpr (CTL > 0 && CTL % 2 == 0 && sizeof(T2) == 8)
         {
-            int e, j;
-            if constexpr (CTL > 0)
+            for (int i = 2 * threadIdx.x; i < na * CTL; i += 2 * blockDim.x)
             {
-                j = i / CTL;  // a constant divisor: multiply and shift
-                e = i - j * CTL;
+                const int j = i / CTL, e = i - j * CTL;
+                *reinterpret_cast<float4*>(g + (size_t)act[j] * CTL + e) = *reinterpret_cast<const float4*>(r + i);
             }
-            else
-                j = div_rem(i, dL, e);
-            g[(size_t)act[j] * p.L + e] = r[i];
         }
+        else
+            for (int i = threadIdx.x; i < na * p.L; i += blockDim.x)
+            {
+                int e, j;
+                if constexpr (CTL > 0)
+                {
+                    j = i / CTL;  // a constant divisor: multiply and shift
+                    e = i - j * CTL;
+                }
+                else
+                    j = div_rem(i, dL, e);
+                g[(size_t)act[j] * p.L + e] = r[i];
+            }
         return;
     }
     int n = nl * p.L;
@@ -148,10 +167,23 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
     {
         // the block's CTL x NLC points are contiguous: idx = l * NLC + i
         T2* g = data + (size_t)o * (CTL * NLC);
-        for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) a[idx] = g[idx];
-        __syncthreads();
-        T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
-        for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) g[idx] = r[idx];
+        if constexpr (sizeof(T2) == 8 && (CTL * NLC) % 2 == 0)
+        {
+            // two points per 16-byte access (the block's start is even in points)
+            for (int idx = threadIdx.x; idx < CTL * NLC / 2; idx += blockDim.x)
+                reinterpret_cast<float4*>(a)[idx] = reinterpret_cast<const float4*>(g)[idx];
+            __syncthreads();
+            T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
+            for (int idx = threadIdx.x; idx < CTL * NLC / 2; idx += blockDim.x)
+                reinterpret_cast<float4*>(g)[idx] = reinterpret_cast<const float4*>(r)[idx];
+        }
+        else
+        {
+            for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) a[idx] = g[idx];
+            __syncthreads();
+            T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
+            for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) g[idx] = r[idx];
+        }
         return;
     }
     int c = blockIdx.x - (int)(o * nchunk);
