@@ -529,11 +529,15 @@ def run_ours(args):
     nbp = (s.nbnds + 7) // 8 * 8
     npw_k = np.array([len(s.gvec[int(ik)]) for ik in s.kmap[:, 0]], dtype=np.float64)
     box_bytes = s.nk_bz * nsets * Mp * 8.0            # FP32 boxes of every full-BZ k
+    # after the first preparation only the occupied z-columns are zeroed
+    ncols = p1.get("box_columns", 0)
+    clear_bytes = ncols * nsets * p1["product_grid"][2] * 8.0 if ncols else box_bytes
     prep_roles = {
-        "k_scatter (+ box clears)": (p1["prep_scatter_ms"] - p0["prep_scatter_ms"],
-                                     float((npw_k * (nsets * (16 + 8 + 8) + 12)).sum()) + box_bytes,
-                                     "FP64 iBZ coefficients and Miller indices read, FP32 box entries and FP32 "
-                                     "unfolded coefficients written, boxes cleared"),
+        "k_scatter (+ column clears)": (p1["prep_scatter_ms"] - p0["prep_scatter_ms"],
+                                        float((npw_k * (nsets * (16 + 8 + 8) + 12)).sum()) + clear_bytes,
+                                        "FP64 iBZ coefficients and Miller indices read, FP32 box entries and "
+                                        "FP32 unfolded coefficients written, the occupied z-columns zeroed "
+                                        f"({ncols} columns over the full-BZ k)"),
         "k_fft_x_split": (p1["prep_xsplit_ms"] - p0["prep_xsplit_ms"],
                           box_bytes + s.nk_bz * s.nspin * s.nspinor * Mp * (2 * 2 * nbp * 4 + nbp * 8.0),
                           "FP32 boxes read (an upper bound: only occupied planes are read), split k+q rows "

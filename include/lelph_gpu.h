@@ -142,6 +142,9 @@ typedef struct lelph_gpu_stats
     double prep_xsplit_ms;       /*   x pass writing the tensor-core operands, KB projections, and the */
     double prep_proj_ms;         /*   dV windows (prepare) */
     double windows_ms;
+    long long box_columns;       /* real-space route, mixed form: occupied z-columns of the wavefunction boxes
+                                    summed over the full-BZ k (known after the first preparation; the later
+                                    ones zero only these columns) */
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

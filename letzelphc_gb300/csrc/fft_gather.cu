@@ -154,13 +154,18 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
     T2* b = a + (size_t)ich * p.L;
     T2* tws = b + (size_t)ich * p.L;
     long long o = blockIdx.x / nchunk;
+    // with a box mask: this plane's column flags (y pass: line element l = y),
+    // unoccupied columns read as zero
+    const uint8_t* cflag = nullptr;
     if (mk.xpl)
     {
         // blockIdx.x < 2^32: 32-bit divisions
         const unsigned o32 = (unsigned)o, nx = (unsigned)mk.Nx;
         const unsigned box = o32 / nx;
         const unsigned x = o32 - box * nx;
-        if (!mk.xpl[(size_t)(box / (unsigned)mk.nbox_per_k) * nx + x]) return;
+        const size_t kslot = box / (unsigned)mk.nbox_per_k;
+        if (!mk.xpl[kslot * nx + x]) return;
+        if (mk.col) cflag = mk.col + (kslot * nx + x) * (size_t)mk.Ny;
     }
     for (int t = threadIdx.x; t < p.L; t += blockDim.x) tws[t] = tw[t];
     if constexpr (NLC > 0)
@@ -171,7 +176,9 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
         {
             // two points per 16-byte access (the block's start is even in points)
             for (int idx = threadIdx.x; idx < CTL * NLC / 2; idx += blockDim.x)
-                reinterpret_cast<float4*>(a)[idx] = reinterpret_cast<const float4*>(g)[idx];
+                reinterpret_cast<float4*>(a)[idx] = (cflag && !cflag[2 * idx / NLC])
+                                                        ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                        : reinterpret_cast<const float4*>(g)[idx];
             __syncthreads();
             T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
             for (int idx = threadIdx.x; idx < CTL * NLC / 2; idx += blockDim.x)
@@ -179,7 +186,8 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
         }
         else
         {
-            for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) a[idx] = g[idx];
+            for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x)
+                a[idx] = (cflag && !cflag[idx / NLC]) ? T2{} : g[idx];
             __syncthreads();
             T2* r = ct_fft<T2, T, CTL, 0, 1, true, NLC>(a, b, NLC, NLC, 1, nullptr, NLC, 1, tws, sign);
             for (int idx = threadIdx.x; idx < CTL * NLC; idx += blockDim.x) g[idx] = r[idx];
@@ -196,7 +204,7 @@ __global__ void __launch_bounds__(256) k_fft_strided(T2* __restrict__ data, long
     {
         int i;
         const int l = div_rem(idx, dc, i);
-        a[l * ic + i] = g[(size_t)l * inner + i];
+        a[l * ic + i] = (cflag && !cflag[l]) ? T2{} : g[(size_t)l * inner + i];
     }
     __syncthreads();
     T2* r;
@@ -395,6 +403,64 @@ __global__ void __launch_bounds__(256) k_fft_x_split(const float2* __restrict__ 
             P[(kc >> 4) * (uint32_t)gd.nbp * 16u + (kc & 15u)] = v;
         }
     }
+}
+
+// ------------------------------------------------------- column lists
+
+// one block per k: the occupied z-columns of its box as a list (any order)
+__global__ void __launch_bounds__(256) k_col_lists(const uint8_t* __restrict__ col, int ncol, int* __restrict__ list,
+                                                   int* __restrict__ cnt)
+{
+    __shared__ int n;
+    const int k = blockIdx.x;
+    if (threadIdx.x == 0) n = 0;
+    __syncthreads();
+    const uint8_t* ck = col + (size_t)k * ncol;
+    for (int c = threadIdx.x; c < ncol; c += blockDim.x)
+        if (ck[c]) list[(size_t)k * ncol + atomicAdd(&n, 1)] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) cnt[k] = n;
+}
+
+// one block per box of a chunk: zero the occupied columns of its k (each warp
+// one column at a time, lanes along z; 16-byte stores when Nz is even)
+__global__ void __launch_bounds__(256) k_clear_cols(float2* __restrict__ boxes, int nbox_per_k, long long N, int Nz,
+                                                    int ncol, const int* __restrict__ list,
+                                                    const int* __restrict__ cnt)
+{
+    const int box = blockIdx.x;
+    const int kslot = box / nbox_per_k;
+    const int n = cnt[kslot];
+    const int* lk = list + (size_t)kslot * ncol;
+    float2* b = boxes + (size_t)box * N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if ((Nz & 1) == 0)
+    {
+        const int h = Nz >> 1;
+        for (int j = warp; j < n; j += nw)
+        {
+            float4* c4 = reinterpret_cast<float4*>(b + (size_t)lk[j] * Nz);
+            for (int z = lane; z < h; z += 32) c4[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+    else
+        for (int j = warp; j < n; j += nw)
+        {
+            float2* c2 = b + (size_t)lk[j] * Nz;
+            for (int z = lane; z < Nz; z += 32) c2[z] = make_float2(0.f, 0.f);
+        }
+}
+
+void lelph_launch_col_lists(const uint8_t* col, int nk, int ncol, int* list, int* cnt, cudaStream_t st)
+{
+    if (nk > 0) k_col_lists<<<nk, 256, 0, st>>>(col, ncol, list, cnt);
+}
+
+void lelph_launch_clear_cols(float2* boxes, int nk, int nbox_per_k, long long N, int Nz, int ncol, const int* list,
+                             const int* cnt, cudaStream_t st)
+{
+    const long long nbox = (long long)nk * nbox_per_k;
+    if (nbox > 0) k_clear_cols<<<(unsigned)nbox, 256, 0, st>>>(boxes, nbox_per_k, N, Nz, ncol, list, cnt);
 }
 
 // ------------------------------------------------------------- scatter

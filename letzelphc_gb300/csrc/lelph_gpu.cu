@@ -84,6 +84,7 @@ struct lelph_gpu
     DevBuf d_dvr, d_eig, d_maxabs;                 // per q slot: dV_scf on the reference box (FP64), eigVec
     DevBuf d_win64, d_win32, d_winscale, d_wtmpN, d_wtmpM;  // dV windows on the product grid, per (slot, umklapp)
     DevBuf d_pairs, d_glocal, d_partials, d_gout, d_status, d_tmp;
+    std::vector<int> ulms_all;  // every q slot's umklapp list, the host side of one upload
     FftPlan1D plan[3];   // product grid (g.Nx, g.Ny, g.Nz)
     FftPlan1D planN[3];  // the reference's FFT box
     int Nbox[3] = {0, 0, 0};
@@ -98,7 +99,9 @@ struct lelph_gpu
     int chunk_pts = 0, nchunks = 0;
     // local bare potential: V_loc(|G|) table and its spline slopes per species
     DevBuf d_vl_v, d_vl_dv, d_vl_in, d_vloc;
-    DevBuf d_colmask;  // box occupancy of a chunk of k-points (z-columns, then x planes)
+    DevBuf d_colmask;  // box occupancy of every full-BZ k (z-columns of all k, then x planes of all k)
+    DevBuf d_collist, d_colcnt;  // occupied z-columns of every k as lists
+    bool boxmask_ready = false;  // occupancy and lists built (geometry only: they stay valid)
     // Dmats: Miller -> position tables of the iBZ lists, the job table and the
     // last block of representation matrices (jobs dm_first .. dm_first + dm_count - 1)
     DevBuf d_dmgtab, d_dmjobs, d_dmats, d_dmmap, d_dmcoef32, d_dmstar, d_gstar, d_qsitems;
@@ -1198,7 +1201,8 @@ extern "C" int lelph_gpu_create(const lelph_gpu_desc* desc, lelph_gpu** out)
                       &h->d_twN32[2], &h->d_dvr, &h->d_eig,
                       &h->d_maxabs, &h->d_win64, &h->d_win32, &h->d_winscale, &h->d_wtmpN, &h->d_wtmpM,
                       &h->d_pairs, &h->d_glocal, &h->d_partials, &h->d_gout, &h->d_status, &h->d_tmp,
-                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_dmgtab,
+                      &h->d_vl_v, &h->d_vl_dv, &h->d_vl_in, &h->d_vloc, &h->d_colmask, &h->d_collist, &h->d_colcnt,
+                      &h->d_dmgtab,
                       &h->d_dmjobs, &h->d_dmats, &h->d_dmmap, &h->d_dmcoef32, &h->d_dmstar, &h->d_gstar,
                       &h->d_dmgroups, &h->d_dmperm, &h->d_dmcoefT,
                       &h->d_qsitems, &h->d_dvraw, &h->d_gs_perm, &h->d_gs_kcx, &h->d_gs_cols, &h->d_gs_cst,
@@ -1398,23 +1402,41 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
         // FP32 boxes in chunks of k-points (<= ~4 GB of boxes)
         const size_t per_k = sizeof(float2) * (size_t)nbox_per_k * N;
         int nkc = (int)std::max<size_t>(1, std::min<size_t>((size_t)d.nkpts_BZ, (4ull << 30) / per_k));
+        // testing override: LELPH_PREP_CHUNK_K = at most this many k-points per chunk of boxes
+        if (const char* e = getenv("LELPH_PREP_CHUNK_K"))
+            if (atoi(e) > 0) nkc = std::min(nkc, atoi(e));
         rc = ensure(h, h->d_boxes32, per_k * nkc);
         if (rc) return rc;
-        const size_t mask_k = (size_t)g.Nx * g.Ny + g.Nx;
-        rc = ensure(h, h->d_colmask, mask_k * nkc);
+        // occupancy of every k (geometry only), built by the first preparation's
+        // scatters; afterwards a chunk's boxes need zeros only in their k's
+        // occupied columns (see BoxMask), not a clear of the whole box
+        const size_t ncol = (size_t)g.Nx * g.Ny;
+        rc = ensure(h, h->d_colmask, (ncol + g.Nx) * d.nkpts_BZ);
         if (rc) return rc;
-        BoxMask mk;
-        mk.col = (uint8_t*)h->d_colmask.p;
-        mk.xpl = mk.col + (size_t)nkc * g.Nx * g.Ny;
-        mk.Nx = g.Nx;
-        mk.Ny = g.Ny;
-        mk.nbox_per_k = nbox_per_k;
+        rc = ensure(h, h->d_collist, sizeof(int) * ncol * d.nkpts_BZ);
+        if (rc) return rc;
+        rc = ensure(h, h->d_colcnt, sizeof(int) * d.nkpts_BZ);
+        if (rc) return rc;
+        uint8_t* col_all = (uint8_t*)h->d_colmask.p;
+        uint8_t* xpl_all = col_all + ncol * d.nkpts_BZ;
+        const bool masks = h->boxmask_ready;
+        if (!masks) CUDA_TRY(h, cudaMemsetAsync(h->d_colmask.p, 0, (ncol + g.Nx) * d.nkpts_BZ, h->st));
         for (int k0 = 0; k0 < d.nkpts_BZ; k0 += nkc)
         {
             int nk = std::min(nkc, d.nkpts_BZ - k0);
+            BoxMask mk;
+            mk.col = col_all + (size_t)k0 * ncol;
+            mk.xpl = xpl_all + (size_t)k0 * g.Nx;
+            mk.Nx = g.Nx;
+            mk.Ny = g.Ny;
+            mk.nbox_per_k = nbox_per_k;
             gs_tick(h);
-            CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
-            CUDA_TRY(h, cudaMemsetAsync(h->d_colmask.p, 0, mask_k * nkc, h->st));
+            if (masks)
+                lelph_launch_clear_cols((float2*)h->d_boxes32.p, nk, nbox_per_k, N, g.Nz, (int)ncol,
+                                        (const int*)h->d_collist.p + (size_t)k0 * ncol,
+                                        (const int*)h->d_colcnt.p + k0, h->st);
+            else
+                CUDA_TRY(h, cudaMemsetAsync(h->d_boxes32.p, 0, per_k * nk, h->st));
             lelph_launch_scatter(k0, nk, (const KPointSym*)h->d_ksym.p, (const int*)h->d_miller.p,
                                  (const long long*)h->d_pwoff.p, (const int*)h->d_npw.p, npw_max,
                                  (const double2*)h->d_coef.p, (const long long*)h->d_coefoff.p, g, 0, h->d_boxes32.p,
@@ -1434,7 +1456,20 @@ extern "C" int lelph_gpu_prepare(lelph_gpu* h)
                                         (const float*)h->d_band_scale.p, h->ab_bf16, (uint16_t*)h->d_bsplit.p,
                                         (float2*)h->d_psi32.p, h->st, mk);
             h->stats.prep_xsplit_ms += gs_tock(h);
-            h->stats.kernel_launches += 4;
+            h->stats.kernel_launches += masks ? 5 : 4;
+        }
+        if (!masks)
+        {
+            lelph_launch_col_lists(col_all, d.nkpts_BZ, (int)ncol, (int*)h->d_collist.p, (int*)h->d_colcnt.p, h->st);
+            CUDA_TRY(h, cudaGetLastError());
+            std::vector<int> cnt(d.nkpts_BZ);
+            CUDA_TRY(h, cudaMemcpyAsync(cnt.data(), h->d_colcnt.p, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost,
+                                        h->st));
+            CUDA_TRY(h, cudaStreamSynchronize(h->st));
+            h->stats.box_columns = 0;
+            for (int c : cnt) h->stats.box_columns += c;
+            h->boxmask_ready = true;
+            h->stats.kernel_launches += 1;
         }
     }
     NonlocalDesc nl = nl_desc(h);
@@ -1965,8 +2000,21 @@ static int build_windows(lelph_gpu* h)
     if (rc) return rc;
     rc = ensure(h, h->d_wtmpM, sizeof(double2) * (size_t)umax * ncomp * M);
     if (rc) return rc;
-    rc = ensure(h, h->d_tmp, sizeof(int) * 3 * (size_t)umax + 16);
+    // the umklapp lists of every slot, uploaded in one copy (a pageable copy
+    // may wait for the stream, so one per slot would stall the queue per slot)
+    h->ulms_all.clear();
+    std::vector<size_t> uoff(h->qslots.size(), 0);
+    for (size_t s = 0; s < h->qslots.size(); ++s)
+        if (h->qslots[s].set)
+        {
+            uoff[s] = h->ulms_all.size();
+            h->ulms_all.insert(h->ulms_all.end(), h->qslots[s].ulms.begin(), h->qslots[s].ulms.end());
+        }
+    rc = ensure(h, h->d_tmp, sizeof(int) * h->ulms_all.size() + 16);
     if (rc) return rc;
+    if (!h->ulms_all.empty())
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->ulms_all.data(), sizeof(int) * h->ulms_all.size(),
+                                    cudaMemcpyHostToDevice, h->st));
     if (!h->mixed)
     {
         rc = ensure(h, h->d_win64, sizeof(double2) * (size_t)nwin * ncomp * M);
@@ -1999,11 +2047,9 @@ static int build_windows(lelph_gpu* h)
                                        (const float2*)h->d_twN32[1].p, -1, h->st);
             lelph_launch_fft_strided_f(tN, (long long)ncomp, h->Nbox[1] * h->Nbox[2], h->planN[0],
                                        (const float2*)h->d_twN32[0].p, -1, h->st);
-            CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->qslots[s].ulms.data(), sizeof(int) * 3 * nu,
-                                        cudaMemcpyHostToDevice, h->st));
             const int3 dm = make_int3(h->qslots[s].dmin[0], h->qslots[s].dmin[1], h->qslots[s].dmin[2]);
             k_dv_window<float2><<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
-                                                                        (const int*)h->d_tmp.p, nu, dm, g,
+                                                                        (const int*)h->d_tmp.p + uoff[s], nu, dm, g,
                                                                         1.0 / (double)NN, tM);
             lelph_launch_fft_contig_f(tM, (long long)nu * ncomp * g.Nx * g.Ny, h->plan[2],
                                       (const float2*)h->d_tw32[2].p, +1, h->st);
@@ -2043,11 +2089,10 @@ static int build_windows(lelph_gpu* h)
                                    (const double2*)h->d_twN[1].p, -1, h->st);
         lelph_launch_fft_strided_d(tN, (long long)ncomp, h->Nbox[1] * h->Nbox[2], h->planN[0],
                                    (const double2*)h->d_twN[0].p, -1, h->st);
-        CUDA_TRY(h, cudaMemcpyAsync(h->d_tmp.p, h->qslots[s].ulms.data(), sizeof(int) * 3 * nu,
-                                    cudaMemcpyHostToDevice, h->st));
         const int3 dm = make_int3(h->qslots[s].dmin[0], h->qslots[s].dmin[1], h->qslots[s].dmin[2]);
         k_dv_window<double2><<<dim3(64, ncomp, nu), 256, 0, h->st>>>(tN, ncomp, h->Nbox[0], h->Nbox[1], h->Nbox[2],
-                                                             (const int*)h->d_tmp.p, nu, dm, g, 1.0 / (double)NN, tM);
+                                                             (const int*)h->d_tmp.p + uoff[s], nu, dm, g,
+                                                             1.0 / (double)NN, tM);
         // inverse transform on the product grid
         lelph_launch_fft_contig_d(tM, (long long)nu * ncomp * g.Nx * g.Ny, h->plan[2], (const double2*)h->d_tw64[2].p,
                                   +1, h->st);

@@ -76,7 +76,11 @@ inline size_t lelph_tc_partials_per_pair(const GeomDev& g, int nchunks)
 // Occupancy of the boxes of a chunk of k-points after the sphere -> box
 // scatter: col[(kslot*Nx + x)*Ny + y] != 0 when the z-column (x, y) holds a
 // plane wave of k, xpl[kslot*Nx + x] != 0 when the plane x does.  Every band
-// of a k-point shares its sphere.  col == nullptr: no masking.
+// of a k-point shares its sphere.  col == nullptr: no masking.  With masks the
+// passes never read a point outside the sphere's columns and planes: the z
+// pass reads the occupied columns, the y pass reads unoccupied columns as
+// zero, the x pass unoccupied planes; only the occupied columns need zeros
+// (off the sphere) before a scatter.
 struct BoxMask
 {
     uint8_t* col = nullptr;
@@ -97,6 +101,12 @@ void lelph_launch_fft_strided_f(float2* data, long long nouter, int inner, const
 void lelph_launch_fft_x_to_split(const float2* boxes, int nbox_k, int k0, const FftPlan1D& p, const float2* tw,
                                  int sign, const GeomDev& g, const float* band_scale, int ab_bf16, uint16_t* Bsplit,
                                  float2* psi32, cudaStream_t st, const BoxMask& mk = BoxMask());
+
+// occupied columns of each k as a list (col[k*ncol + c] != 0 -> list[k*ncol + i] = c,
+// i < cnt[k], any order), and the zeroing of those columns in a chunk's boxes
+void lelph_launch_col_lists(const uint8_t* col, int nk, int ncol, int* list, int* cnt, cudaStream_t st);
+void lelph_launch_clear_cols(float2* boxes, int nk, int nbox_per_k, long long N, int Nz, int ncol, const int* list,
+                             const int* cnt, cudaStream_t st);
 
 // sphere -> box scatter with su2, fractional-translation phase and conj
 void lelph_launch_scatter(int k0, int nk, const KPointSym* ksym_dev, const int* miller, const long long* pw_off,

@@ -63,7 +63,7 @@ class Stats(C.Structure):
         ("qstar_ms", C.c_double), ("dvscf_ms", C.c_double), ("route", C.c_int),
         ("gs_plane_ms", C.c_double), ("gs_xpass_ms", C.c_double), ("gs_gemm_ms", C.c_double),
         ("prep_scatter_ms", C.c_double), ("prep_fft_ms", C.c_double), ("prep_xsplit_ms", C.c_double),
-        ("prep_proj_ms", C.c_double), ("windows_ms", C.c_double),
+        ("prep_proj_ms", C.c_double), ("windows_ms", C.c_double), ("box_columns", C.c_longlong),
     ]
 
 
