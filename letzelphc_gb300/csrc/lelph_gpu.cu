@@ -2278,28 +2278,57 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     }
     const lelph_gpu_desc& d = h->d;
     const GeomDev& g = h->g;
-    // pairs (src/elph/compute_elph_matq.c:65-128)
+    // pairs (src/elph/compute_elph_matq.c:65-128): per pair the k+q search, the
+    // umklapp vector and the dV window; large batches are split over the host
+    // cores (the GPU waits for this table), and the error reported is that of
+    // the first failing pair, as in a serial loop
     std::vector<PairInfo> pairs(n);
-    for (int i = 0; i < n; ++i)
+    if (h->khash.empty())
+        for (int i = 0; i < d.nkpts_BZ; ++i) h->khash.emplace(k_hash_key(&h->kbz_crys[3 * i]), i);
+    struct PairErr
     {
-        if (qslot[i] < 0 || qslot[i] >= (int)h->qslots.size() || !h->qslots[qslot[i]].set)
-            return fail(h, LELPH_GPU_ERR_STATE, "q slot not loaded");
-        if (kbz[i] < 0 || kbz[i] >= d.nkpts_BZ) return fail(h, LELPH_GPU_ERR_INVALID, "k index out of range");
-        const double* q = h->qslots[qslot[i]].q;
-        double qt[3], kq[3];
-        for (int x = 0; x < 3; ++x) qt[x] = kminusq ? -q[x] : q[x];
-        for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * kbz[i] + x] + qt[x];
-        int ikq = find_k_fast(h, kq);
-        if (ikq < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
-        int idx_k = kbz[i], idx_kq = ikq;
-        if (kminusq) std::swap(idx_k, idx_kq);
-        PairInfo& P = pairs[i];
-        P.kbz_k = idx_k;
-        P.kbz_kq = idx_kq;
-        P.qslot = qslot[i];
-        if (umklapp(h, idx_k, idx_kq, q, P.ulm)) return fail(h, LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
-        P.dvslot = window_of(h, qslot[i], P.ulm);
-        if (P.dvslot < 0) return fail(h, LELPH_GPU_ERR_GEOMETRY, "umklapp vector outside the q slot's set");
+        int at = -1, code = 0;
+        const char* msg = "";
+    };
+    auto make_pairs = [&](int i0, int i1, PairErr& e) {
+        for (int i = i0; i < i1; ++i)
+        {
+            auto bad = [&](int code, const char* msg) {
+                e.at = i;
+                e.code = code;
+                e.msg = msg;
+            };
+            if (qslot[i] < 0 || qslot[i] >= (int)h->qslots.size() || !h->qslots[qslot[i]].set)
+                return bad(LELPH_GPU_ERR_STATE, "q slot not loaded");
+            if (kbz[i] < 0 || kbz[i] >= d.nkpts_BZ) return bad(LELPH_GPU_ERR_INVALID, "k index out of range");
+            const double* q = h->qslots[qslot[i]].q;
+            double qt[3], kq[3];
+            for (int x = 0; x < 3; ++x) qt[x] = kminusq ? -q[x] : q[x];
+            for (int x = 0; x < 3; ++x) kq[x] = h->kbz_crys[3 * kbz[i] + x] + qt[x];
+            int ikq = find_k_fast(h, kq);
+            if (ikq < 0) return bad(LELPH_GPU_ERR_GEOMETRY, "K+Q point cannot be found in kgrid");
+            int idx_k = kbz[i], idx_kq = ikq;
+            if (kminusq) std::swap(idx_k, idx_kq);
+            PairInfo& P = pairs[i];
+            P.kbz_k = idx_k;
+            P.kbz_kq = idx_kq;
+            P.qslot = qslot[i];
+            if (umklapp(h, idx_k, idx_kq, q, P.ulm)) return bad(LELPH_GPU_ERR_GEOMETRY, "non-integral umklapp vector");
+            P.dvslot = window_of(h, qslot[i], P.ulm);
+            if (P.dvslot < 0) return bad(LELPH_GPU_ERR_GEOMETRY, "umklapp vector outside the q slot's set");
+        }
+    };
+    {
+        const int nthr = n >= 1024 ? std::max(1, std::min<int>(8, (int)std::thread::hardware_concurrency())) : 1;
+        std::vector<PairErr> errs(nthr);
+        const int per = (n + nthr - 1) / nthr;
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nthr; ++t)
+            pool.emplace_back(make_pairs, std::min(n, t * per), std::min(n, (t + 1) * per), std::ref(errs[t]));
+        make_pairs(0, std::min(n, per), errs[0]);
+        for (auto& th : pool) th.join();
+        for (const PairErr& e : errs)
+            if (e.at >= 0) return fail(h, e.code, e.msg);  // ranges are in order: the first is the earliest pair
     }
     int rc = upload(h, h->d_pairs, pairs.data(), sizeof(PairInfo) * n);
     if (rc) return rc;
