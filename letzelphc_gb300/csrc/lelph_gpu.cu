@@ -17,6 +17,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -150,6 +151,31 @@ int fail(lelph_gpu* h, int code, const std::string& msg)
             return fail((h), e__ == cudaErrorMemoryAllocation ? LELPH_GPU_ERR_ALLOC : LELPH_GPU_ERR_CUDA, \
                         std::string(#call) + ": " + cudaGetErrorString(e__));                              \
     } while (0)
+
+// Runs work(w) for every w in [0, nthr): worker 0 on the calling thread, the
+// others on new threads.  A worker whose thread cannot be started (a limit on
+// threads) runs on the calling thread instead, so the limit costs time, not
+// the call.
+template <typename F>
+void run_workers(int nthr, F&& work)
+{
+    std::vector<std::thread> pool;
+    std::vector<int> here;
+    for (int w = 1; w < nthr; ++w)
+    {
+        try
+        {
+            pool.emplace_back(work, w);
+        }
+        catch (const std::system_error&)
+        {
+            here.push_back(w);
+        }
+    }
+    work(0);
+    for (int w : here) work(w);
+    for (auto& t : pool) t.join();
+}
 
 int ensure(lelph_gpu* h, DevBuf& b, size_t bytes)
 {
@@ -697,13 +723,9 @@ static int upload_wfc(lelph_gpu* h, const double* const* wfc)
     };
     {
         const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), d.nkpts_iBZ));
-        std::vector<std::thread> pool;
-        for (int w = 1; w < nthr; ++w)
-            pool.emplace_back([&, w]() {
-                for (int ik = w; ik < d.nkpts_iBZ; ik += nthr) scales_of(ik);
-            });
-        for (int ik = 0; ik < d.nkpts_iBZ; ik += nthr) scales_of(ik);
-        for (auto& t : pool) t.join();
+        run_workers(nthr, [&](int w) {
+            for (int ik = w; ik < d.nkpts_iBZ; ik += nthr) scales_of(ik);
+        });
     }
     h->band_scale.resize((size_t)d.nkpts_BZ * d.nspin * nb);
     for (int i = 0; i < d.nkpts_BZ; ++i)
@@ -789,13 +811,9 @@ static int gs_tables(lelph_gpu* h)
     };
     {
         const int nthr = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), nk));
-        std::vector<std::thread> pool;
-        for (int w = 1; w < nthr; ++w)
-            pool.emplace_back([&, w]() {
-                for (int k = w; k < nk; k += nthr) one(k);
-            });
-        for (int k = 0; k < nk; k += nthr) one(k);
-        for (auto& t : pool) t.join();
+        run_workers(nthr, [&](int w) {
+            for (int k = w; k < nk; k += nthr) one(k);
+        });
     }
     for (int k = 0; k < nk; ++k)
         if (bad[k]) return fail(h, LELPH_GPU_ERR_GEOMETRY, "G-space route: two plane waves share a product-grid point");
@@ -2322,11 +2340,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         const int nthr = n >= 1024 ? std::max(1, std::min<int>(8, (int)std::thread::hardware_concurrency())) : 1;
         std::vector<PairErr> errs(nthr);
         const int per = (n + nthr - 1) / nthr;
-        std::vector<std::thread> pool;
-        for (int t = 1; t < nthr; ++t)
-            pool.emplace_back(make_pairs, std::min(n, t * per), std::min(n, (t + 1) * per), std::ref(errs[t]));
-        make_pairs(0, std::min(n, per), errs[0]);
-        for (auto& th : pool) th.join();
+        run_workers(nthr, [&](int t) { make_pairs(std::min(n, t * per), std::min(n, (t + 1) * per), errs[t]); });
         for (const PairErr& e : errs)
             if (e.at >= 0) return fail(h, e.code, e.msg);  // ranges are in order: the first is the earliest pair
     }
@@ -2674,17 +2688,14 @@ static int dmats_run(lelph_gpu* h, int nsym, const double* Rmat, const double* t
     }
     else
     {
-        std::vector<std::thread> pool;
-        for (int w = 0; w < nthr; ++w)
-            pool.emplace_back([&, w]() {
-                for (long long i = count * w / nthr; i < count * (w + 1) / nthr; ++i)
-                    if (build(i).first != 0)
-                    {
-                        bad_job[(size_t)w] = i;
-                        return;
-                    }
-            });
-        for (auto& t : pool) t.join();
+        run_workers(nthr, [&](int w) {
+            for (long long i = count * w / nthr; i < count * (w + 1) / nthr; ++i)
+                if (build(i).first != 0)
+                {
+                    bad_job[(size_t)w] = i;
+                    return;
+                }
+        });
         for (long long b : bad_job)
             if (b >= 0)
             {
