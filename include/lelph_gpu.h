@@ -145,6 +145,9 @@ typedef struct lelph_gpu_stats
     long long box_columns;       /* real-space route, mixed form: occupied z-columns of the wavefunction boxes
                                     summed over the full-BZ k (known after the first preparation; the later
                                     ones zero only these columns) */
+    double local_live_ms;        /* device time of the local-sandwich launches of every run, from events recorded
+                                    around them always (no profiling synchronisations), read after the run */
+    long long local_live_launches;
 } lelph_gpu_stats;
 
 /* Create a context: validates the inputs, derives the integer symmetry maps,

@@ -55,6 +55,10 @@ struct lelph_gpu
     cudaEvent_t evc[2] = {nullptr, nullptr};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evg0 = nullptr, evg1 = nullptr;  // per-kernel timing of the G-space route (profiling on)
+    // always-on events around each local-sandwich launch of a run (one pair per
+    // batch), read after the run's own synchronisation: the kernel's time in
+    // back-to-back work, without the synchronisations of the profiling mode
+    std::vector<cudaEvent_t> evlive;
     bool profiling = false;
     std::string err;
     lelph_gpu_stats stats;
@@ -689,6 +693,8 @@ extern "C" void lelph_gpu_destroy(lelph_gpu* h)
     if (h->evg1) cudaEventDestroy(h->evg1);
     if (h->st_copy) cudaStreamSynchronize(h->st_copy);
     for (cudaEvent_t e : h->evc)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->evlive)
         if (e) cudaEventDestroy(e);
     if (h->st_copy) cudaStreamDestroy(h->st_copy);
     if (h->st) cudaStreamDestroy(h->st);
@@ -2394,6 +2400,13 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
     {
         int nb = std::min(batch, n - p0);
         const PairInfo* dp = (const PairInfo*)h->d_pairs.p + p0;
+        while ((int)h->evlive.size() < 2 * (ib + 1))
+        {
+            cudaEvent_t e = nullptr;
+            CUDA_TRY(h, cudaEventCreate(&e));
+            h->evlive.push_back(e);
+        }
+        CUDA_TRY(h, cudaEventRecord(h->evlive[2 * ib], h->st));
         tstart(h);
         if (h->gspace)
         {
@@ -2406,6 +2419,7 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         else
             lelph_launch_local_tc(dp, nb, &h->tmapB, &h->tmapP, &h->tmapV, g, h->ab_bf16, h->chunk_pts, h->nchunks,
                                   (float*)h->d_partials.p, (unsigned*)h->d_status.p, h->st, h->wait_ns);
+        CUDA_TRY(h, cudaEventRecord(h->evlive[2 * ib + 1], h->st));
         h->stats.local_ms += tstop(h);
         h->stats.local_launches += 1;
         tstart(h);
@@ -2439,6 +2453,15 @@ static int run_impl(lelph_gpu* h, int n, const int* qslot, const int* kbz, int n
         CUDA_TRY(h, cudaMemcpyAsync(g_out, gdev, esz * gsz * n, cudaMemcpyDeviceToHost, h->st));
     rc = check_status(h);
     if (rc) return rc;
+    for (int b = 0; b < ib; ++b)
+    {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->evlive[2 * b], h->evlive[2 * b + 1]) == cudaSuccess)
+        {
+            h->stats.local_live_ms += ms;
+            h->stats.local_live_launches += 1;
+        }
+    }
     h->stats.pairs_done += n;
     return LELPH_GPU_OK;
 }

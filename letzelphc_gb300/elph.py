@@ -64,6 +64,7 @@ class Stats(C.Structure):
         ("gs_plane_ms", C.c_double), ("gs_xpass_ms", C.c_double), ("gs_gemm_ms", C.c_double),
         ("prep_scatter_ms", C.c_double), ("prep_fft_ms", C.c_double), ("prep_xsplit_ms", C.c_double),
         ("prep_proj_ms", C.c_double), ("windows_ms", C.c_double), ("box_columns", C.c_longlong),
+        ("local_live_ms", C.c_double), ("local_live_launches", C.c_longlong),
     ]
 
 
